@@ -1,0 +1,358 @@
+"""Benchmark: flip attempts/s of coupled-from-the-past domino chains on one GB300.
+
+Workload: the weighted Aztec diamond of order 1024 (tiling side N = 2054) with 2x2-periodic
+weights a = 1.0, b = 0.5 (fp32 values), the monotone two-periodic CFTP rule, coupled max and
+min chains on one shared random stream.  One step is one CFTP attempt at the first look-back
+of 2^10 sweeps: both chains reset to the extremal tilings, 2048 half-sweeps, then the device
+XOR-popcount coalescence test.  In TinyMT mode (the default) each step is an epoch of the
+reference's CFTP driver (generators seeded from the epoch seed, colours from mt19937 of it).
+
+`value` times steps on chains resident in HBM; `e2e` times the same attempt through the C ABI
+(rt_domino_cftp) from pinned host buffers, copies included.  The CPU baseline and the
+`--impl reference` arm run the reference's sweep logic (the oracle's restatement of its
+OpenCL kernels) on all host threads over a bounded sample of the same attempt.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+ORDER = 1024
+WEIGHT_A, WEIGHT_B = 1.0, 0.5
+HALF_SWEEPS = 2048  # look-back of 2^10 sweeps
+DRIVER_SEED = 1
+METRIC = "flip attempts/sec/GPU (coupled CFTP chains, weighted Aztec diamond n=1024)"
+L2_FLUSH_BYTES = 256 << 20
+
+
+def _peaks() -> dict:
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return {"hbm_gbs": float(d["hbm_gbs"]), "source": "measured"}
+    return {"hbm_gbs": 6800.0, "source": "fallback"}
+
+
+def _interior_by_colour(rt, d) -> tuple[int, int]:
+    v = rt.DominoTiler.DomainToVertices(d)
+    n = int(np.sqrt(v.size))
+    ii, jj = np.divmod(np.arange(v.size), n)
+    inter = v == 1
+    black = int(np.count_nonzero(inter & ((ii + jj) % 2 == 0)))
+    return int(np.count_nonzero(inter)) - black, black  # (white, black)
+
+
+def _attempts(colours: np.ndarray, interior: tuple[int, int], chains: int = 2) -> int:
+    nb = int(np.count_nonzero(colours))
+    return chains * (nb * interior[1] + (colours.size - nb) * interior[0])
+
+
+class Clocks:
+    """Samples SM clocks and throttle reasons with nvidia-smi during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu: int):
+        self.gpu = gpu
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except (FileNotFoundError, OSError):
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            self.proc.wait()
+
+    def summary(self):
+        if not self.proc or not self.path:
+            return None
+        rows = []
+        for line in Path(self.path).read_text().splitlines():
+            f = [x.strip() for x in line.split(",")]
+            if len(f) >= 9:
+                rows.append(f)
+        os.unlink(self.path)
+        if not rows:
+            return None
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        reasons = set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            for k, name in enumerate(names):
+                if r[5 + k].lower().startswith("active"):
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": float(rows[0][2]) if rows[0][2].replace(".", "").isdigit() else None,
+                "samples": len(rows), "reasons": sorted(reasons)}
+
+
+def _dist():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    if ws <= 1:
+        return 0, 1, 0, None
+    import torch
+    import torch.distributed as dist
+
+    rank, local = int(os.environ["RANK"]), int(os.environ.get("LOCAL_RANK", "0"))
+    backend = "nccl" if torch.cuda.is_available() else "gloo"
+    if backend == "nccl":
+        torch.cuda.set_device(local)
+    dist.init_process_group(backend)
+    return rank, ws, local, dist
+
+
+def _max_over_ranks(x: float, dist, device) -> float:
+    if dist is None:
+        return x
+    import torch
+
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def _sum_over_ranks(x: float, dist, device) -> float:
+    if dist is None:
+        return x
+    import torch
+
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.SUM)
+    return float(t.item())
+
+
+def cpu_leg(rt, orc, tmax, tmin, interior, steps_per_sample: int, samples: int, threads: int):
+    """Oracle (the reference's sweep logic restated) on `threads` host threads: `samples`
+    coupled attempts of `steps_per_sample` TinyMT steps each; returns attempts/s per sample."""
+    n = int(np.sqrt(tmax.size))
+    rates = []
+    drv = rt.mt19937_draws(DRIVER_SEED, samples)
+    for k in range(samples):
+        driver = int(drv[k]) ^ 0x5EED
+        epoch_seed = int(rt.mt19937_draws(driver, 1)[0])  # the driver's first draw seeds the epoch
+        cols = rt.mt19937_colours(epoch_seed, steps_per_sample)
+        t0 = time.perf_counter()
+        # One attempt (max_attempts=1) at a look-back of steps_per_sample: the same work
+        # pattern as a GPU step, shortened.
+        orc.cftp_tinymt(tmax, tmin, n, driver, steps_per_sample, 0, 1, rule=3, a=WEIGHT_A,
+                        b=WEIGHT_B, threads=threads)
+        dt = time.perf_counter() - t0
+        rates.append(_attempts(cols, interior) / dt)
+    return rates
+
+
+def run_reference(args) -> None:
+    rank, ws, local, dist = _dist()
+    if rank != 0:
+        return
+    import randomtilingspublic_gb300 as rt
+    from tests import oracle_py as orc
+
+    D = rt.DominoTiler
+    d = D.AztecDiamond(ORDER)
+    tmax, tmin = D.MaxTiling(d), D.MinTiling(d)
+    interior = _interior_by_colour(rt, d)
+    threads = os.cpu_count() or 1
+    sample = 32
+    orc.lib()
+    cpu_leg(rt, orc, tmax, tmin, interior, sample, max(args.warmup, 1), threads)
+    t0 = time.perf_counter()
+    rates = cpu_leg(rt, orc, tmax, tmin, interior, sample, args.steps, threads)
+    wall = time.perf_counter() - t0
+    value = statistics.mean(rates)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "flip attempts/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * wall / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u8", "data": "synthetic",
+        "config": {"workload": f"aztec{ORDER}_twoperiodic_a1.0_b0.5_cftp_coupled_maxmin",
+                   "sample": f"{sample} of the {HALF_SWEEPS} half-sweeps of one attempt per step",
+                   "l2": "n/a (host)"},
+        "cpu_baseline": {"value": value, "unit": "flip attempts/s", "cores": threads, "kind": "port",
+                         "sample": f"{sample} TinyMT half-sweeps of the coupled max/min chains per step, "
+                                   f"order {ORDER}, {threads} host threads"},
+        "e2e": {"value": value, "unit": "flip attempts/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+
+
+def run_ours(args) -> None:
+    import torch
+
+    rank, ws, local, dist = _dist()
+    dev = torch.device("cuda", local)
+    torch.cuda.set_device(dev)
+    import randomtilingspublic_gb300 as rt
+
+    D = rt.DominoTiler
+    d = D.AztecDiamond(ORDER)
+    tmax, tmin = D.MaxTiling(d), D.MinTiling(d)
+    n = int(np.sqrt(tmax.size))
+    interior = _interior_by_colour(rt, d)
+    tiler = rt.DominoTiler(rule="cftp_twoperiodic", rng=args.mode, a=WEIGHT_A, b=WEIGHT_B, fast_stream=rank,
+                           engine=args.engine)
+    stream = torch.cuda.Stream(device=dev)
+    s = rt.DominoSampler(n, 4, tiler, cuda_stream=stream.cuda_stream)
+    s.load(0, tmin)
+    s.load(1, tmax)
+    s.load(2, tmin)
+    s.load(3, tmax)
+    s.sync()
+    lib = rt.lib()
+    flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device=dev)
+    seeds = rt.mt19937_draws(DRIVER_SEED + 7919 * rank, args.warmup + args.steps)
+
+    # Chains 0, 1 are swept; chains 2, 3 keep the extremal start states.
+    s.set_active(2)
+
+    def one_step(k: int) -> tuple[int, int]:
+        s.copy_chain(0, 2)
+        s.copy_chain(1, 3)
+        if args.mode == "tinymt":
+            cols = rt.mt19937_colours(int(seeds[k]), HALF_SWEEPS)
+            s.seed(int(seeds[k]))
+            s.run(cols)
+        else:
+            cols = np.array([1, 0] * (HALF_SWEEPS // 2), np.uint8)
+            s.run_fast(int(seeds[k]), -HALF_SWEEPS, HALF_SWEEPS)
+        return _attempts(cols, interior), int(np.count_nonzero(cols))
+
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    for k in range(args.warmup):
+        one_step(k)
+        s.diff(0, 1)
+    torch.cuda.synchronize()
+    if dist is not None:
+        dist.barrier()
+    attempts = 0
+    launches0 = s.launches
+    with Clocks(local) as clk:
+        for k in range(args.steps):
+            flush.zero_()  # L2 flush between timed steps (outside the events)
+            torch.cuda.current_stream(dev).synchronize()
+            with torch.cuda.stream(stream):
+                ev[k][0].record(stream)
+                a, _ = one_step(args.warmup + k)
+                ev[k][1].record(stream)
+            attempts += a
+            s.diff(0, 1)
+        torch.cuda.synchronize()
+    launches = s.launches - launches0 - args.steps  # minus the diff kernels outside the events
+    ms = sum(e0.elapsed_time(e1) for e0, e1 in ev)
+    sec = _max_over_ranks(ms / 1e3, dist, dev)
+    total_attempts = _sum_over_ranks(attempts, dist, dev)
+    value = total_attempts / sec
+    clocks = clk.summary()
+
+    # Roofline of the half-sweep: algorithmic bytes per half-sweep over its average time.
+    half_sweeps = args.steps * HALF_SWEEPS
+    t_half = (ms / 1e3) / half_sweeps
+    cells = (n - 2) * (n // 2 - 2)
+    tiling_bytes = 3 * (attempts / half_sweeps)  # 3 B per flip attempt (u8 state), both chains
+    gen_bytes = 32 * cells if args.mode == "tinymt" else 0  # generator state read + write
+    algo_bytes = tiling_bytes + gen_bytes
+    peaks = _peaks()
+    achieved = algo_bytes / t_half / 1e9
+    traffic = _traffic_from_profile(args.mode)
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
+                "frac": achieved / peaks["hbm_gbs"], "traffic": traffic, "peak_source": peaks["source"],
+                "kernel": "domino half-sweep (rotate + update)", "algorithmic_bytes_per_launch": algo_bytes,
+                "launch_us": t_half * 1e6}
+
+    # e2e: one attempt through the C ABI from pinned host buffers, copies included.
+    if True:
+        pin_max = torch.from_numpy(tmax).pin_memory()
+        pin_min = torch.from_numpy(tmin).pin_memory()
+        pin_out = torch.empty_like(pin_max).pin_memory()
+        o = tiler.opts()
+        stats = rt.CftpStats()
+        e2e_rates = []
+        for k in range(max(2, min(args.steps, 3))):
+            t0 = time.perf_counter()
+            st = lib.rt_domino_cftp(pin_max.data_ptr(), pin_min.data_ptr(), n, int(seeds[k]), HALF_SWEEPS, 0, 1,
+                                    C.byref(o), pin_out.data_ptr(), C.byref(stats))
+            dt = time.perf_counter() - t0
+            if st not in (rt.RT_OK, rt.RT_ERR_NOT_COALESCED):
+                raise rt.RTError(st, lib.rt_last_error().decode())
+            e2e_rates.append(stats.flip_attempts / dt)
+        nbytes = n * n * 4
+        e2e = {"value": _sum_over_ranks(statistics.median(e2e_rates[1:]), dist, dev), "unit": "flip attempts/s",
+               "h2d_bytes_per_step": 3 * nbytes, "d2h_bytes_per_step": nbytes + 8,
+               "api": "rt_domino_cftp (one attempt, look-back 2048 half-sweeps)"}
+
+    cpu = None
+    if rank == 0 and ws == 1 and not args.no_cpu:
+        from tests import oracle_py as orc
+
+        threads = os.cpu_count() or 1
+        sample = 32
+        rates = cpu_leg(rt, orc, tmax, tmin, interior, sample, 2, threads)
+        cpu = {"value": statistics.mean(rates), "unit": "flip attempts/s", "cores": threads, "kind": "port",
+               "sample": f"{sample} TinyMT half-sweeps of the coupled max/min chains (order {ORDER}) per attempt, "
+                         f"2 attempts, {threads} host threads"}
+    s.close()
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": "flip attempts/s", "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "u8", "data": "synthetic",
+            "config": {"workload": f"aztec{ORDER}_twoperiodic_a1.0_b0.5_cftp_coupled_maxmin",
+                       "rng": args.mode, "engine": args.engine, "half_sweeps_per_step": HALF_SWEEPS,
+                       "l2": "flushed between timed steps (256 MiB write)", "parallelism": f"replicas{ws}"},
+            "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches, "clocks": clocks,
+        }
+        print(json.dumps(line))
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+def main() -> None:
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--mode", choices=["tinymt", "fast"], default="tinymt")
+    ap.add_argument("--engine", type=int, default=0)
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+def _traffic_from_profile(mode: str):
+    """DRAM bytes per half-sweep from the committed ncu summary, when one exists."""
+    p = ROOT / "profiles" / f"domino_halfsweep_{mode}_traffic.json"
+    if p.exists():
+        return json.loads(p.read_text()).get("dram_bytes_per_half_sweep")
+    return None
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,186 @@
+/*
+ * rt_tilings.h - C ABI of librt_tilings.so, the GB300 (sm_103a) random-tiling sampler.
+ *
+ * The entry points replace the domino tiler of the reference library
+ * (src/Domino/DominoTiler.h:78-130) for callers that bind it over an FFI: plain pointers,
+ * sizes and status codes, no C++ or CUDA types.  include/rt_tilings.hpp keeps the
+ * reference's C++ class shape (DominoTiler::Walk, MaxTiling, ...) on top of this ABI.
+ *
+ * Conventions shared by every entry point
+ *  - A domain is an M x M int32 0/1 array of squares, a tiling an N x N int32 array of
+ *    vertex edge-indicator masks with N = M + 1 (src/Domino/DominoTiler.h:19-37): bit 1 for
+ *    the edge toward row i-1, 2 toward row i+1, 4 toward column j-1, 8 toward column j+1.
+ *  - The caller owns every buffer; tilings are updated in place, as the reference's
+ *    Walk(tiling&, ...) does (DominoTiler.cpp:18-122).
+ *  - Errors are returned, never exit(): the reference prints and calls exit() from
+ *    checkCudaErrors (src/common/helper_cuda.h:566-579).  rt_last_error() gives the
+ *    message of the last failing call on the calling thread.
+ *  - Sweeps run on the GPU only.  There is no CPU fallback: without a usable CUDA device
+ *    every sweep entry point returns RT_ERR_CUDA.
+ */
+#ifndef RT_TILINGS_H_
+#define RT_TILINGS_H_
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#if defined(__GNUC__)
+#define RT_API __attribute__((visibility("default")))
+#else
+#define RT_API
+#endif
+
+typedef int32_t rt_status;
+#define RT_OK 0
+#define RT_ERR_INVALID_ARGUMENT 1
+#define RT_ERR_CUDA 2
+#define RT_ERR_NOT_TILEABLE 3
+#define RT_ERR_TIMEOUT 4
+#define RT_ERR_OUT_OF_MEMORY 5
+#define RT_ERR_NOT_COALESCED 6
+#define RT_ERR_BUFFER_TOO_SMALL 7
+
+/* Random-number modes of the sweep. */
+#define RT_RNG_TINYMT 0 /* one TinyMT32 generator per site, the reference's OpenCL path
+                           (src/TinyMT/tinymt32.clh, dominokernel.cl:4-40): bit-exact with it */
+#define RT_RNG_FAST 1   /* counter-based Philox4x32-10 keyed by (seed, stream, half-sweep,
+                           site); no generator state in memory */
+
+/* Flip rules: the reference picks one by compiling one of four kernel files. */
+#define RT_DOMINO_PLAIN 0            /* src/Domino/dominokernel.cl:4-18 (propose 0.8) */
+#define RT_DOMINO_CFTP 1             /* src/Domino/dominokernelCFTP.cl:51-71 (monotone 1/2-1/2) */
+#define RT_DOMINO_TWOPERIODIC 2      /* src/Domino/dominokerneltwoperiodic.cl:7-35 */
+#define RT_DOMINO_CFTP_TWOPERIODIC 3 /* src/Domino/dominokernelCFTPtwoperiodic.cl:72-101 */
+
+typedef struct rt_walk_opts {
+  int32_t rng_mode;  /* RT_RNG_* */
+  int32_t rule;      /* RT_DOMINO_* */
+  double weight_a;   /* two-periodic weights; the reference hard-codes a = 0.7, b = 1. */
+  double weight_b;   /* (dominokerneltwoperiodic.cl:3-4).  Both must be > 0. */
+  /* Optional TinyMT parameter table: count triples (mat1, mat2, tmat), one per generator
+     in the order of the reference's parameter file (LoadTinyMT, DominoTiler.cpp:235-237).
+     NULL selects the TinyMT32 jump parameters for every generator. */
+  const uint32_t* tinymt_params;
+  int64_t tinymt_params_count;
+  uint32_t fast_stream; /* RT_RNG_FAST: stream id (< 65536), e.g. the instance number */
+  int32_t engine;       /* 0: automatic; 1: per-half-sweep kernels; 2: resident persistent kernel */
+  void* cuda_stream;    /* cudaStream_t to run on; NULL = the library's own stream */
+} rt_walk_opts;
+
+/* Fills *o with the reference's defaults: TinyMT, RT_DOMINO_PLAIN, a = 0.7, b = 1. */
+RT_API void rt_walk_opts_default(rt_walk_opts* o);
+
+RT_API const char* rt_status_string(rt_status s);
+RT_API const char* rt_last_error(void);
+RT_API const char* rt_version(void);
+
+/* ---- domino host utilities (no GPU needed) ------------------------------------------- */
+
+/* DominoTiler::AztecRectangle (DominoTiler.cpp:267-324) / AztecDiamond (:262-265).
+   Writes the padded side^2 domain into out (capacity cap ints); *side receives M. */
+RT_API rt_status rt_domino_aztec_rectangle(int32_t n, const int32_t* remove, int32_t n_remove, int32_t* out,
+                                           int64_t cap, int32_t* side);
+RT_API rt_status rt_domino_aztec_diamond(int32_t n, int32_t* out, int64_t cap, int32_t* side);
+/* DominoTiler::Rectangle (DominoTiler.cpp:249-260). */
+RT_API rt_status rt_domino_rectangle(int32_t rows, int32_t cols, int32_t* out, int64_t cap, int32_t* side);
+/* DominoTiler::DomainToVertices (DominoTiler.cpp:611-631): out is (M+1)^2. */
+RT_API rt_status rt_domino_domain_to_vertices(const int32_t* domain, int32_t m_side, int32_t* out);
+/* DominoTiler::MaxTiling / MinTiling, Thurston's algorithm (DominoTiler.cpp:345-531).
+   RT_ERR_NOT_TILEABLE when the boundary or bulk height check fails (the reference prints
+   "NOT tileable" and returns a height function in that case). */
+RT_API rt_status rt_domino_max_tiling(const int32_t* domain, int32_t m_side, int32_t* out);
+RT_API rt_status rt_domino_min_tiling(const int32_t* domain, int32_t m_side, int32_t* out);
+/* DominoTiler::TilingToHeightfunc / HeightfuncToTiling / TilingToDomain
+   (DominoTiler.cpp:555-593, 534-553, 595-609).  Heights outside the domain are INT32_MAX. */
+RT_API rt_status rt_domino_tiling_to_heightfunc(const int32_t* tiling, const int32_t* domain, int32_t n_side,
+                                                int32_t* out);
+RT_API rt_status rt_domino_heightfunc_to_tiling(const int32_t* hf, const int32_t* domain, int32_t n_side,
+                                                int32_t* out);
+RT_API rt_status rt_domino_tiling_to_domain(const int32_t* tiling, int32_t n_side, int32_t* out);
+
+/* ---- domino sweeps (GPU) ---------------------------------------------------------------- */
+
+/* DominoTiler::Walk(tiling&, long steps, long seed) (DominoTiler.cpp:18-122).  One step is
+   one half-sweep: a colour drawn from mt19937(seed) (TinyMT mode; the generators are seeded
+   with the first draw, as on the reference's OpenCL path) or alternating black/white
+   (fast mode), a flip attempt at every site of that colour, then the other colour rebuilt.
+   n_side = N must be even and >= 6; the outermost two rings must be empty (padded). */
+RT_API rt_status rt_domino_walk(int32_t* tiling, int32_t n_side, int64_t steps, int64_t seed,
+                                const rt_walk_opts* opts);
+
+/* DominoTiler::Walk(tiling&, vector steps, vector seeds) (DominoTiler.cpp:125-231): epoch k
+   re-seeds the generators with seeds[k] and draws its colours from mt19937(seeds[k]). */
+RT_API rt_status rt_domino_walk_epochs(int32_t* tiling, int32_t n_side, const int64_t* steps, const int64_t* seeds,
+                                       int32_t n_epochs, const rt_walk_opts* opts);
+
+/* Coupling from the past for the monotone rules (RT_DOMINO_CFTP, RT_DOMINO_CFTP_TWOPERIODIC).
+   TinyMT mode follows Examples/AztecDiamondCftpEx.cpp:51-77: epoch seeds from
+   mt19937(driver_seed); the first epoch has first_steps steps; each failed attempt prepends
+   an epoch of 2*steps.back() steps (schedule 0, the reference's rule) or 2*steps.front()
+   (schedule 1, doubling).  Fast mode: attempt j runs half-sweeps [-2T, 0) with
+   T = first_steps * 2^j sweeps, randomness keyed by (driver_seed, fast_stream, half-sweep).
+   The coupled max/min chains run in one kernel on the shared stream and coalescence is a
+   device XOR-popcount.  RT_ERR_NOT_COALESCED after max_attempts attempts; out then holds the
+   top chain after the last attempt and *stats is filled. */
+typedef struct rt_cftp_stats {
+  int32_t attempts;     /* attempts run (the last one coalesced on success) */
+  int64_t total_steps;  /* half-sweeps run per chain over all attempts */
+  int64_t final_steps;  /* half-sweeps of the coalesced attempt (its look-back) */
+  int64_t flip_attempts;/* interior-site evaluations over both chains and all attempts */
+  double seconds;       /* device time of the sweeps */
+} rt_cftp_stats;
+
+RT_API rt_status rt_domino_cftp(const int32_t* tmax, const int32_t* tmin, int32_t n_side, int64_t driver_seed,
+                                int64_t first_steps, int32_t schedule, int32_t max_attempts,
+                                const rt_walk_opts* opts, int32_t* out, rt_cftp_stats* stats);
+
+/* ---- device-resident chains --------------------------------------------------------------
+   A sampler keeps n_chains coupled chains of one N x N domain on the GPU; all chains see
+   the same random stream (CFTP couples the max and min chains this way).  The building
+   block of the entry points above, exposed for callers that keep state on the device. */
+typedef struct rt_dm_sampler rt_dm_sampler;
+
+RT_API rt_status rt_dm_sampler_create(int32_t n_side, int32_t n_chains, const rt_walk_opts* opts,
+                                      rt_dm_sampler** out);
+RT_API rt_status rt_dm_sampler_destroy(rt_dm_sampler* s);
+/* Host int32 N x N tiling -> chain (copy and colour split run on the device). */
+RT_API rt_status rt_dm_sampler_load(rt_dm_sampler* s, int32_t chain, const int32_t* tiling);
+/* Chain -> host int32 N x N tiling. */
+RT_API rt_status rt_dm_sampler_store(rt_dm_sampler* s, int32_t chain, int32_t* tiling);
+/* Copies chain src onto chain dst on the device. */
+RT_API rt_status rt_dm_sampler_copy_chain(rt_dm_sampler* s, int32_t dst, int32_t src);
+/* Only chains [0, k) are swept by later runs (the others keep their state), 1 <= k <= n_chains. */
+RT_API rt_status rt_dm_sampler_set_active(rt_dm_sampler* s, int32_t k);
+/* TinyMT mode: InitTinyMT (dominokernel.cl:33-40): generator k <- seed + k. */
+RT_API rt_status rt_dm_sampler_seed(rt_dm_sampler* s, uint32_t seed);
+/* TinyMT mode: runs steps half-sweeps, colours[s] = 1 rotates black (t = 1), 0 white. */
+RT_API rt_status rt_dm_sampler_run(rt_dm_sampler* s, const uint8_t* colours, int64_t steps);
+/* Fast mode: runs half-sweeps h0 .. h0+steps-1 (even h black, odd h white). */
+RT_API rt_status rt_dm_sampler_run_fast(rt_dm_sampler* s, uint64_t seed, int64_t h0, int64_t steps);
+/* Number of sites where chains a and b differ (device XOR-popcount). */
+RT_API rt_status rt_dm_sampler_diff(rt_dm_sampler* s, int32_t a, int32_t b, int64_t* ndiff);
+/* Waits for the sampler's stream. */
+RT_API rt_status rt_dm_sampler_sync(rt_dm_sampler* s);
+/* The cudaStream_t the sampler launches on. */
+RT_API void* rt_dm_sampler_stream(rt_dm_sampler* s);
+/* Flip attempts (interior sites of one colour class) per half-sweep of one chain: the
+   average over the two colours is interior_vertices / 2. */
+RT_API int64_t rt_dm_sampler_interior_vertices(rt_dm_sampler* s);
+/* Kernels launched by this sampler since creation. */
+RT_API int64_t rt_dm_sampler_launches(rt_dm_sampler* s);
+
+/* ---- diagnostics ---------------------------------------------------------------------
+   The acceptance intervals a rule compiles to: for c = (row & 1) | (colour << 1),
+   out16[4c .. 4c+3] = {lo_up, width_up, lo_down, width_down}; a site in state 3 flips to 12
+   when (u - lo_up) < width_up, a site in state 12 flips to 3 when (u - lo_down) < width_down,
+   u the 23-bit TinyMT draw or the 32-bit fast draw.  No reference counterpart: the
+   reference evaluates its float thresholds per draw (dominokernel*.cl). */
+RT_API rt_status rt_domino_rule_table(int32_t rule, int32_t rng_mode, double a, double b, uint32_t* out16);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* RT_TILINGS_H_ */

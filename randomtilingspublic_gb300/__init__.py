@@ -1,0 +1,408 @@
+"""GB300-native random-tiling sampler: Python mirror of the reference's domino tiler API.
+
+The reference exposes one C++ class per model (src/Domino/DominoTiler.h:46-131).  This
+module keeps that shape - ``DominoTiler().Walk(t, steps, seed)``, ``DominoTiler.MaxTiling(d)``,
+... - on top of the C ABI of ``librt_tilings.so`` (include/rt_tilings.h).  Domains, tilings
+and height functions are flat int32 arrays of a square side, as the reference's
+``std::vector<int>`` typedefs are (src/common/common.h:50-52).
+
+Sweeps run on the GPU only; if the shared library is missing this module raises instead of
+falling back to anything else.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import math
+import os
+from dataclasses import dataclass
+from pathlib import Path
+from typing import Sequence
+
+import numpy as np
+
+_PKG = Path(__file__).resolve().parent
+LIB_PATH = _PKG / "librt_tilings.so"
+
+RT_OK = 0
+RT_ERR_INVALID_ARGUMENT = 1
+RT_ERR_CUDA = 2
+RT_ERR_NOT_TILEABLE = 3
+RT_ERR_TIMEOUT = 4
+RT_ERR_OUT_OF_MEMORY = 5
+RT_ERR_NOT_COALESCED = 6
+RT_ERR_BUFFER_TOO_SMALL = 7
+
+RNG_MODES = {"tinymt": 0, "fast": 1}
+DOMINO_RULES = {"plain": 0, "cftp": 1, "twoperiodic": 2, "cftp_twoperiodic": 3}
+
+
+class RTError(RuntimeError):
+    def __init__(self, status: int, message: str):
+        super().__init__(f"{message} (status {status})")
+        self.status = status
+
+
+class _WalkOpts(C.Structure):
+    _fields_ = [
+        ("rng_mode", C.c_int32),
+        ("rule", C.c_int32),
+        ("weight_a", C.c_double),
+        ("weight_b", C.c_double),
+        ("tinymt_params", C.c_void_p),
+        ("tinymt_params_count", C.c_int64),
+        ("fast_stream", C.c_uint32),
+        ("engine", C.c_int32),
+        ("cuda_stream", C.c_void_p),
+    ]
+
+
+class CftpStats(C.Structure):
+    _fields_ = [
+        ("attempts", C.c_int32),
+        ("total_steps", C.c_int64),
+        ("final_steps", C.c_int64),
+        ("flip_attempts", C.c_int64),
+        ("seconds", C.c_double),
+    ]
+
+    def as_dict(self) -> dict:
+        return {f: getattr(self, f) for f, _ in self._fields_}
+
+
+_P = C.c_void_p
+_SIGNATURES = {
+    "rt_walk_opts_default": (None, [_P]),
+    "rt_status_string": (C.c_char_p, [C.c_int32]),
+    "rt_last_error": (C.c_char_p, []),
+    "rt_version": (C.c_char_p, []),
+    "rt_domino_aztec_rectangle": (C.c_int32, [C.c_int32, _P, C.c_int32, _P, C.c_int64, _P]),
+    "rt_domino_aztec_diamond": (C.c_int32, [C.c_int32, _P, C.c_int64, _P]),
+    "rt_domino_rectangle": (C.c_int32, [C.c_int32, C.c_int32, _P, C.c_int64, _P]),
+    "rt_domino_domain_to_vertices": (C.c_int32, [_P, C.c_int32, _P]),
+    "rt_domino_max_tiling": (C.c_int32, [_P, C.c_int32, _P]),
+    "rt_domino_min_tiling": (C.c_int32, [_P, C.c_int32, _P]),
+    "rt_domino_tiling_to_heightfunc": (C.c_int32, [_P, _P, C.c_int32, _P]),
+    "rt_domino_heightfunc_to_tiling": (C.c_int32, [_P, _P, C.c_int32, _P]),
+    "rt_domino_tiling_to_domain": (C.c_int32, [_P, C.c_int32, _P]),
+    "rt_domino_walk": (C.c_int32, [_P, C.c_int32, C.c_int64, C.c_int64, _P]),
+    "rt_domino_walk_epochs": (C.c_int32, [_P, C.c_int32, _P, _P, C.c_int32, _P]),
+    "rt_domino_cftp": (C.c_int32, [_P, _P, C.c_int32, C.c_int64, C.c_int64, C.c_int32, C.c_int32, _P, _P, _P]),
+    "rt_dm_sampler_create": (C.c_int32, [C.c_int32, C.c_int32, _P, _P]),
+    "rt_dm_sampler_destroy": (C.c_int32, [_P]),
+    "rt_dm_sampler_load": (C.c_int32, [_P, C.c_int32, _P]),
+    "rt_dm_sampler_store": (C.c_int32, [_P, C.c_int32, _P]),
+    "rt_dm_sampler_copy_chain": (C.c_int32, [_P, C.c_int32, C.c_int32]),
+    "rt_dm_sampler_set_active": (C.c_int32, [_P, C.c_int32]),
+    "rt_dm_sampler_seed": (C.c_int32, [_P, C.c_uint32]),
+    "rt_dm_sampler_run": (C.c_int32, [_P, _P, C.c_int64]),
+    "rt_dm_sampler_run_fast": (C.c_int32, [_P, C.c_uint64, C.c_int64, C.c_int64]),
+    "rt_dm_sampler_diff": (C.c_int32, [_P, C.c_int32, C.c_int32, _P]),
+    "rt_dm_sampler_sync": (C.c_int32, [_P]),
+    "rt_dm_sampler_stream": (C.c_void_p, [_P]),
+    "rt_dm_sampler_interior_vertices": (C.c_int64, [_P]),
+    "rt_dm_sampler_launches": (C.c_int64, [_P]),
+    "rt_domino_rule_table": (C.c_int32, [C.c_int32, C.c_int32, C.c_double, C.c_double, _P]),
+}
+
+_lib_handle = None
+
+
+def lib() -> C.CDLL:
+    """Loads librt_tilings.so (built by ``randomtilingspublic_gb300.build``)."""
+    global _lib_handle
+    if _lib_handle is None:
+        path = Path(os.environ.get("RT_TILINGS_LIB", LIB_PATH))
+        if not path.exists():
+            raise RuntimeError(
+                f"{path} is missing: build it with `python -m randomtilingspublic_gb300.build` "
+                "(the sampler has no non-CUDA implementation)")
+        h = C.CDLL(str(path))
+        for name, (res, args) in _SIGNATURES.items():
+            fn = getattr(h, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib_handle = h
+    return _lib_handle
+
+
+def _check(status: int) -> None:
+    if status != RT_OK:
+        msg = lib().rt_last_error().decode() or lib().rt_status_string(status).decode()
+        raise RTError(status, msg)
+
+
+def _i32(a) -> np.ndarray:
+    return np.ascontiguousarray(np.asarray(a, dtype=np.int32).ravel())
+
+
+def _ptr(a: np.ndarray) -> int:
+    return a.ctypes.data
+
+
+def side_of(a) -> int:
+    n = math.isqrt(len(a))
+    if n * n != len(a):
+        raise ValueError("expected a square array")
+    return n
+
+
+def _write_back(dst, src: np.ndarray) -> None:
+    """In-place update of the caller's tiling, as Walk(tiling&, ...) does."""
+    if isinstance(dst, np.ndarray):
+        dst.reshape(-1)[:] = src
+    elif isinstance(dst, list):
+        dst[:] = src.tolist()
+    else:
+        raise TypeError("tiling must be a numpy array or a list to be updated in place")
+
+
+def read_tinymt_params(path: str | os.PathLike, count: int) -> np.ndarray:
+    """Parameter file of TinyMTDC as LoadTinyMT reads it (src/TinyMT/file_reader.cpp:22-38,
+    :142-158): lines starting with '#' are skipped; mat1, mat2, tmat are the hex fields after
+    the 3rd, 4th and 5th comma.  Returns a (count, 3) uint32 array."""
+    out = np.zeros((count, 3), dtype=np.uint32)
+    k = 0
+    with open(path) as f:
+        for line in f:
+            if k >= count:
+                break
+            if line.startswith("#") or not line.strip():
+                continue
+            fields = line.split(",")
+            out[k] = [int(fields[3], 16), int(fields[4], 16), int(fields[5], 16)]
+            k += 1
+    if k < count:
+        raise ValueError(f"{path} holds {k} parameter sets, {count} needed")
+    return out
+
+
+class DominoTiler:
+    """Domino tilings (src/Domino/DominoTiler.h:46-131).
+
+    ``rule`` selects what the reference selects by compiling one of its kernel files:
+    'plain' (dominokernel), 'cftp' (dominokernelCFTP), 'twoperiodic', 'cftp_twoperiodic';
+    ``a``, ``b`` are the two-periodic weights the reference hard-codes (0.7, 1.0).
+    ``rng`` is 'tinymt' (bit-exact with the reference's OpenCL path) or 'fast' (Philox).
+    """
+
+    def __init__(self, rule: str = "plain", rng: str = "tinymt", a: float = 0.7, b: float = 1.0,
+                 fast_stream: int = 0, engine: int = 0):
+        self.rule = rule
+        self.rng = rng
+        self.a = float(a)
+        self.b = float(b)
+        self.fast_stream = int(fast_stream)
+        self.engine = int(engine)
+        self._params: np.ndarray | None = None
+
+    # -- reference: LoadTinyMT(params, size) / LoadMTGP() ----------------------------------
+    def LoadTinyMT(self, params, size: int | None = None) -> None:
+        """Loads per-generator TinyMT parameters: a TinyMTDC file path (with ``size`` sets,
+        DominoTiler.cpp:235-237) or an (n, 3) array of (mat1, mat2, tmat)."""
+        if isinstance(params, (str, os.PathLike)):
+            if size is None:
+                raise ValueError("size is required with a parameter file")
+            self._params = read_tinymt_params(params, size)
+        else:
+            self._params = np.ascontiguousarray(np.asarray(params, dtype=np.uint32).reshape(-1, 3))
+
+    def opts(self, cuda_stream: int | None = None) -> _WalkOpts:
+        o = _WalkOpts()
+        lib().rt_walk_opts_default(C.byref(o))
+        o.rng_mode = RNG_MODES[self.rng]
+        o.rule = DOMINO_RULES[self.rule]
+        o.weight_a = self.a
+        o.weight_b = self.b
+        o.fast_stream = self.fast_stream
+        o.engine = self.engine
+        if self._params is not None:
+            o.tinymt_params = self._params.ctypes.data
+            o.tinymt_params_count = self._params.shape[0]
+        if cuda_stream:
+            o.cuda_stream = cuda_stream
+        return o
+
+    # -- reference: Walk(t, steps, seed) and Walk(t, vector steps, vector seeds) -------------
+    def Walk(self, t, steps, seeds) -> None:
+        tt = _i32(t)
+        n = side_of(tt)
+        o = self.opts()
+        if isinstance(steps, (list, tuple, np.ndarray)):
+            st = np.ascontiguousarray(np.asarray(steps, dtype=np.int64))
+            sd = np.ascontiguousarray(np.asarray(seeds, dtype=np.int64))
+            if st.shape != sd.shape:
+                raise ValueError("steps and seeds must have the same length")
+            _check(lib().rt_domino_walk_epochs(_ptr(tt), n, _ptr(st), _ptr(sd), len(st), C.byref(o)))
+        else:
+            _check(lib().rt_domino_walk(_ptr(tt), n, int(steps), int(seeds), C.byref(o)))
+        _write_back(t, tt)
+
+    def cftp(self, tmax, tmin, driver_seed: int, first_steps: int = 128, schedule: int = 0,
+             max_attempts: int = 20):
+        """Coupling from the past (Examples/AztecDiamondCftpEx.cpp:51-77); returns
+        (tiling, stats dict).  Needs rule 'cftp' or 'cftp_twoperiodic'."""
+        a, b = _i32(tmax), _i32(tmin)
+        n = side_of(a)
+        out = np.zeros_like(a)
+        stats = CftpStats()
+        o = self.opts()
+        _check(lib().rt_domino_cftp(_ptr(a), _ptr(b), n, int(driver_seed), int(first_steps), int(schedule),
+                                    int(max_attempts), C.byref(o), _ptr(out), C.byref(stats)))
+        return out, stats.as_dict()
+
+    # -- static utilities (DominoTiler.cpp:249-631) -----------------------------------------
+    @staticmethod
+    def AztecRectangle(n: int, remove: Sequence[int] = ()) -> np.ndarray:
+        rm = _i32(list(remove)) if len(remove) else None
+        side = C.c_int32()
+        m = 2 * n - len(remove) + 5
+        buf = np.zeros(m * m, dtype=np.int32)
+        _check(lib().rt_domino_aztec_rectangle(n, _ptr(rm) if rm is not None else None, len(remove), _ptr(buf),
+                                               buf.size, C.byref(side)))
+        return buf[: side.value * side.value].copy()
+
+    @staticmethod
+    def AztecDiamond(n: int) -> np.ndarray:
+        return DominoTiler.AztecRectangle(n, ())
+
+    @staticmethod
+    def Rectangle(rows: int, cols: int) -> np.ndarray:
+        m = max(rows, cols) + 5
+        buf = np.zeros(m * m, dtype=np.int32)
+        side = C.c_int32()
+        _check(lib().rt_domino_rectangle(rows, cols, _ptr(buf), buf.size, C.byref(side)))
+        return buf[: side.value * side.value].copy()
+
+    @staticmethod
+    def DomainToVertices(d) -> np.ndarray:
+        dd = _i32(d)
+        m = side_of(dd)
+        out = np.zeros((m + 1) ** 2, dtype=np.int32)
+        _check(lib().rt_domino_domain_to_vertices(_ptr(dd), m, _ptr(out)))
+        return out
+
+    @staticmethod
+    def MaxTiling(d) -> np.ndarray:
+        dd = _i32(d)
+        m = side_of(dd)
+        out = np.zeros((m + 1) ** 2, dtype=np.int32)
+        _check(lib().rt_domino_max_tiling(_ptr(dd), m, _ptr(out)))
+        return out
+
+    @staticmethod
+    def MinTiling(d) -> np.ndarray:
+        dd = _i32(d)
+        m = side_of(dd)
+        out = np.zeros((m + 1) ** 2, dtype=np.int32)
+        _check(lib().rt_domino_min_tiling(_ptr(dd), m, _ptr(out)))
+        return out
+
+    @staticmethod
+    def TilingToHeightfunc(t, d) -> np.ndarray:
+        tt, dd = _i32(t), _i32(d)
+        n = side_of(tt)
+        out = np.zeros(n * n, dtype=np.int32)
+        _check(lib().rt_domino_tiling_to_heightfunc(_ptr(tt), _ptr(dd), n, _ptr(out)))
+        return out
+
+    @staticmethod
+    def HeightfuncToTiling(hf, d) -> np.ndarray:
+        hh, dd = _i32(hf), _i32(d)
+        n = side_of(hh)
+        out = np.zeros(n * n, dtype=np.int32)
+        _check(lib().rt_domino_heightfunc_to_tiling(_ptr(hh), _ptr(dd), n, _ptr(out)))
+        return out
+
+    @staticmethod
+    def TilingToDomain(t) -> np.ndarray:
+        tt = _i32(t)
+        n = side_of(tt)
+        out = np.zeros((n - 1) ** 2, dtype=np.int32)
+        _check(lib().rt_domino_tiling_to_domain(_ptr(tt), n, _ptr(out)))
+        return out
+
+
+class DominoSampler:
+    """Device-resident coupled chains (rt_dm_sampler_*): the chains stay in HBM between
+    calls; all chains share one random stream."""
+
+    def __init__(self, n_side: int, n_chains: int, tiler: DominoTiler, cuda_stream: int | None = None):
+        self._tiler = tiler
+        self._o = tiler.opts(cuda_stream)
+        h = C.c_void_p()
+        _check(lib().rt_dm_sampler_create(n_side, n_chains, C.byref(self._o), C.byref(h)))
+        self.h = h
+        self.n = n_side
+
+    def close(self) -> None:
+        if self.h:
+            lib().rt_dm_sampler_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def load(self, chain: int, t) -> None:
+        tt = _i32(t)
+        _check(lib().rt_dm_sampler_load(self.h, chain, _ptr(tt)))
+
+    def store(self, chain: int) -> np.ndarray:
+        out = np.zeros(self.n * self.n, dtype=np.int32)
+        _check(lib().rt_dm_sampler_store(self.h, chain, _ptr(out)))
+        return out
+
+    def set_active(self, k: int) -> None:
+        _check(lib().rt_dm_sampler_set_active(self.h, k))
+
+    def copy_chain(self, dst: int, src: int) -> None:
+        _check(lib().rt_dm_sampler_copy_chain(self.h, dst, src))
+
+    def seed(self, seed: int) -> None:
+        _check(lib().rt_dm_sampler_seed(self.h, seed & 0xFFFFFFFF))
+
+    def run(self, colours: np.ndarray) -> None:
+        c = np.ascontiguousarray(np.asarray(colours, dtype=np.uint8))
+        _check(lib().rt_dm_sampler_run(self.h, _ptr(c), c.size))
+
+    def run_fast(self, seed: int, h0: int, steps: int) -> None:
+        _check(lib().rt_dm_sampler_run_fast(self.h, seed, h0, steps))
+
+    def diff(self, a: int, b: int) -> int:
+        n = C.c_int64()
+        _check(lib().rt_dm_sampler_diff(self.h, a, b, C.byref(n)))
+        return n.value
+
+    def sync(self) -> None:
+        _check(lib().rt_dm_sampler_sync(self.h))
+
+    @property
+    def stream(self) -> int:
+        return lib().rt_dm_sampler_stream(self.h) or 0
+
+    @property
+    def interior_vertices(self) -> int:
+        return lib().rt_dm_sampler_interior_vertices(self.h)
+
+    @property
+    def launches(self) -> int:
+        return lib().rt_dm_sampler_launches(self.h)
+
+
+def mt19937_colours(seed: int, steps: int, skip: int = 0) -> np.ndarray:
+    """Colour stream of the reference's host loop: mt19937(seed)() % 2 per step, after
+    ``skip`` draws (DominoTiler.cpp:51,70)."""
+    return (mt19937_draws(seed, skip + steps)[skip:] % 2).astype(np.uint8)
+
+
+def mt19937_draws(seed: int, count: int) -> np.ndarray:
+    """First ``count`` outputs of std::mt19937(seed) (numpy's legacy MT19937 uses the same
+    integer seeding and returns raw 32-bit outputs for the full uint32 range)."""
+    rs = np.random.RandomState(seed & 0xFFFFFFFF)
+    return rs.randint(0, 2**32, size=count, dtype=np.uint32)
+
+
+__all__ = ["DominoTiler", "DominoSampler", "RTError", "lib", "read_tinymt_params", "mt19937_colours",
+           "mt19937_draws", "CftpStats"]

@@ -1,0 +1,571 @@
+// The domino checkerboard sweep on the GPU: colour split/merge, per-half-sweep kernels,
+// the sampler object behind the C ABI, and the walk / epoch / CFTP entry points.
+//
+// Device layout of one chain: two colour arrays, black (t = 1, (i + j) even) and white
+// (t = 0), each N rows x P bytes (P = N/2 rounded up to 16; column m of row i holds vertex
+// (i, 2m + ((i + 1 - t) & 1))), one uint8 edge mask per vertex as in the reference
+// (DominoTiler.cpp:24-33).  Chains of a sampler are consecutive; all see one random stream.
+// Site (i, m) for i in [1, N-2], m in [1, N/2-2] is a flip candidate; its TinyMT generator
+// is number (i-1)*(N/2-2) + (m-1), the reference's work-item order (tinymt.clh:24).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstring>
+#include <memory>
+#include <random>
+#include <string>
+#include <vector>
+
+#include "domino_rules.h"
+#include "domino_sweep.h"
+#include "rng.cuh"
+#include "rt_internal.h"
+
+namespace rt {
+
+// -----------------------------------------------------------------------------------------
+// Kernels
+// -----------------------------------------------------------------------------------------
+
+__device__ __forceinline__ uint8_t dm_flip(uint32_t e, uint32_t u, uint32_t lo_up, uint32_t w_up, uint32_t lo_dn,
+                                           uint32_t w_dn) {
+  if (e == 3u) return (u - lo_up) < w_up ? 12 : 3;
+  if (e == 12u) return (u - lo_dn) < w_dn ? 3 : 12;
+  return (uint8_t)e;
+}
+
+// Passive site (i, m) rebuilt from the four active neighbours (dominokernel.cl:22-31):
+// its up edge from the site above's down edge, down from below's up, and the two
+// horizontal edges from the active sites left and right of it.
+__device__ __forceinline__ uint8_t dm_passive(const uint8_t* A, int P, int i, int m, int t) {
+  const uint8_t* row = A + (size_t)i * P;
+  const int left = m - ((i + t + 1) & 1), right = m + ((i + t) & 1);
+  return (uint8_t)(((A[(size_t)(i - 1) * P + m] & 2) >> 1) | ((A[(size_t)(i + 1) * P + m] & 1) << 1) |
+                   ((row[left] & 8) >> 1) | ((row[right] & 4) << 1));
+}
+
+__global__ void k_tmt_seed(uint4* st, const uint4* params, int64_t count, uint32_t seed) {
+  int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= count) return;
+  uint32_t m1 = kTmtMat1, m2 = kTmtMat2, tm = kTmtTmat;
+  if (params) {
+    uint4 p = params[k];
+    m1 = p.x; m2 = p.y; tm = p.z;
+  }
+  st[k] = tmt_seed(seed + (uint32_t)k, m1, m2, tm);
+}
+
+// One half-sweep's rotation, TinyMT mode: every generator of the grid advances once (as
+// the reference's NDRange does) and the draw decides the flip of site (i, m) of colour t
+// in every chain.
+template <bool kParams>
+__global__ void k_rotate_tmt(DmView v, int t, DmRule rule) {
+  const int m = blockIdx.x * blockDim.x + threadIdx.x + 1;
+  const int i = blockIdx.y * blockDim.y + threadIdx.y + 1;
+  if (m > v.cols || i > v.rows) return;
+  const int64_t k = (int64_t)(i - 1) * v.cols + (m - 1);
+  uint32_t m1 = kTmtMat1, m2 = kTmtMat2, tm = kTmtTmat;
+  if (kParams) {
+    uint4 p = v.tmt_params[k];
+    m1 = p.x; m2 = p.y; tm = p.z;
+  }
+  uint4 s = v.tmt[k];
+  const uint32_t u = tmt_next_u23(s, m1, m2, tm);
+  v.tmt[k] = s;
+  const int c = (i & 1) | (t << 1);
+  const uint32_t lo_up = rule.lo_up[c], w_up = rule.w_up[c], lo_dn = rule.lo_dn[c], w_dn = rule.w_dn[c];
+  for (int ch = 0; ch < v.active; ++ch) {
+    uint8_t* A = v.colour(ch, t);
+    const size_t off = (size_t)i * v.P + m;
+    const uint32_t e = A[off];
+    const uint8_t n = dm_flip(e, u, lo_up, w_up, lo_dn, w_dn);
+    if (n != e) A[off] = n;
+  }
+}
+
+// Fast mode: one Philox call per column quad of a row gives the draws of its four sites.
+__global__ void k_rotate_fast(DmView v, int t, DmRule rule, uint64_t seed, uint32_t stream, int64_t h) {
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  const int i = blockIdx.y * blockDim.y + threadIdx.y + 1;
+  if (4 * q > v.cols || i > v.rows) return;
+  const uint4 r = fast_quad(seed, stream, h, (uint32_t)i, (uint32_t)q);
+  const uint32_t u4[4] = {r.x, r.y, r.z, r.w};
+  const int c = (i & 1) | (t << 1);
+  const uint32_t lo_up = rule.lo_up[c], w_up = rule.w_up[c], lo_dn = rule.lo_dn[c], w_dn = rule.w_dn[c];
+  for (int ch = 0; ch < v.active; ++ch) {
+    uint8_t* A = v.colour(ch, t) + (size_t)i * v.P;
+#pragma unroll
+    for (int r4 = 0; r4 < 4; ++r4) {
+      const int m = 4 * q + r4;
+      if (m < 1 || m > v.cols) continue;
+      const uint32_t e = A[m];
+      const uint8_t n = dm_flip(e, u4[r4], lo_up, w_up, lo_dn, w_dn);
+      if (n != e) A[m] = n;
+    }
+  }
+}
+
+__global__ void k_update(DmView v, int t) {
+  const int m = blockIdx.x * blockDim.x + threadIdx.x + 1;
+  const int i = blockIdx.y * blockDim.y + threadIdx.y + 1;
+  if (m > v.cols || i > v.rows) return;
+  for (int ch = 0; ch < v.active; ++ch) {
+    const uint8_t* A = v.colour(ch, t);
+    uint8_t* Pa = v.colour(ch, 1 - t);
+    Pa[(size_t)i * v.P + m] = dm_passive(A, v.P, i, m, t);
+  }
+}
+
+// Host-layout int32 tiling (N x N) <-> colour arrays of one chain.
+__global__ void k_split(DmView v, int ch, const int32_t* tiling) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  const int i = blockIdx.y;
+  if (j >= v.N) return;
+  const int t = ((i + j) & 1) == 0 ? 1 : 0;
+  v.colour(ch, t)[(size_t)i * v.P + (j >> 1)] = (uint8_t)tiling[(size_t)i * v.N + j];
+}
+
+__global__ void k_merge(DmView v, int ch, int32_t* tiling) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  const int i = blockIdx.y;
+  if (j >= v.N) return;
+  const int t = ((i + j) & 1) == 0 ? 1 : 0;
+  tiling[(size_t)i * v.N + j] = v.colour(ch, t)[(size_t)i * v.P + (j >> 1)];
+}
+
+// Sites where chains a and b differ: per 4-byte word, XOR then count the non-zero bytes
+// (masks are < 16, so byte b is non-zero iff bit 4 of (b + 15) is set).
+__global__ void k_diff(DmView v, int a, int b, unsigned long long* out) {
+  const size_t words = (size_t)v.chain_stride / 4;
+  const uint32_t* x = reinterpret_cast<const uint32_t*>(v.base + (size_t)a * v.chain_stride);
+  const uint32_t* y = reinterpret_cast<const uint32_t*>(v.base + (size_t)b * v.chain_stride);
+  unsigned long long local = 0;
+  for (size_t w = (size_t)blockIdx.x * blockDim.x + threadIdx.x; w < words; w += (size_t)gridDim.x * blockDim.x) {
+    uint32_t d = (x[w] ^ y[w]) & 0x0f0f0f0fu;
+    local += __popc((d + 0x0f0f0f0fu) & 0x10101010u);
+  }
+  for (int o = 16; o > 0; o >>= 1) local += __shfl_down_sync(0xffffffffu, local, o);
+  if ((threadIdx.x & 31) == 0 && local) atomicAdd(out, local);
+}
+
+// -----------------------------------------------------------------------------------------
+// Sampler
+// -----------------------------------------------------------------------------------------
+
+#define RT_CUDA(expr)                                                                   \
+  do {                                                                                  \
+    cudaError_t _e = (expr);                                                            \
+    if (_e != cudaSuccess)                                                              \
+      return fail(RT_ERR_CUDA, std::string(#expr) + ": " + cudaGetErrorString(_e));     \
+  } while (0)
+
+DmSampler::~DmSampler() {
+  if (tmt) cudaFree(tmt);
+  if (tmt_params) cudaFree(tmt_params);
+  if (base) cudaFree(base);
+  if (scratch) cudaFree(scratch);
+  if (counter) cudaFree(counter);
+  if (ev0) cudaEventDestroy(ev0);
+  if (ev1) cudaEventDestroy(ev1);
+  if (own_stream && stream) cudaStreamDestroy(stream);
+}
+
+DmView DmSampler::view() const {
+  DmView v;
+  v.base = base;
+  v.N = N;
+  v.P = P;
+  v.rows = N - 2;
+  v.cols = N / 2 - 2;
+  v.active = active;
+  v.chain_stride = chain_stride;
+  v.colour_stride = colour_stride;
+  v.tmt = tmt;
+  v.tmt_params = tmt_params;
+  return v;
+}
+
+rt_status DmSampler::create(int n_side, int n_chains, const rt_walk_opts& o, std::unique_ptr<DmSampler>* out) {
+  if (n_side < 6 || n_side % 2) return fail(RT_ERR_INVALID_ARGUMENT, "tiling side must be even and >= 6");
+  if (n_side > 65536) return fail(RT_ERR_INVALID_ARGUMENT, "tiling side must be <= 65536");
+  if (n_chains < 1 || n_chains > 64) return fail(RT_ERR_INVALID_ARGUMENT, "n_chains must be in [1, 64]");
+  if (o.rng_mode == RT_RNG_FAST && o.fast_stream >= 65536u)
+    return fail(RT_ERR_INVALID_ARGUMENT, "fast_stream must be < 65536");
+  DmRule rule{};
+  const char* err = nullptr;
+  if (!dm_rule_build(o.rule, o.rng_mode, o.weight_a, o.weight_b, &rule, &err)) return fail(RT_ERR_INVALID_ARGUMENT, err);
+  if (o.tinymt_params && o.tinymt_params_count < 0) return fail(RT_ERR_INVALID_ARGUMENT, "negative parameter count");
+  int dev_count = 0;
+  if (cudaGetDeviceCount(&dev_count) != cudaSuccess || dev_count == 0) {
+    cudaGetLastError();
+    return fail(RT_ERR_CUDA, "no CUDA device: the sweep has no CPU fallback");
+  }
+  auto s = std::make_unique<DmSampler>();
+  s->N = n_side;
+  s->P = ((n_side / 2) + 15) / 16 * 16;
+  s->n_chains = n_chains;
+  s->active = n_chains;
+  s->opts = o;
+  s->rule = rule;
+  s->colour_stride = (size_t)s->N * s->P;
+  s->chain_stride = 2 * s->colour_stride;
+  if (o.cuda_stream) {
+    s->stream = (cudaStream_t)o.cuda_stream;
+  } else {
+    RT_CUDA(cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking));
+    s->own_stream = true;
+  }
+  RT_CUDA(cudaEventCreate(&s->ev0));
+  RT_CUDA(cudaEventCreate(&s->ev1));
+  RT_CUDA(cudaMalloc(&s->base, s->chain_stride * n_chains));
+  RT_CUDA(cudaMemsetAsync(s->base, 0, s->chain_stride * n_chains, s->stream));
+  RT_CUDA(cudaMalloc(&s->scratch, (size_t)s->N * s->N * sizeof(int32_t)));
+  RT_CUDA(cudaMalloc(&s->counter, sizeof(unsigned long long)));
+  const int64_t cells = (int64_t)(s->N - 2) * (s->N / 2 - 2);
+  if (o.rng_mode == RT_RNG_TINYMT) {
+    RT_CUDA(cudaMalloc(&s->tmt, cells * sizeof(uint4)));
+    if (o.tinymt_params) {
+      // Generators beyond the table keep the default set, as the oracle does.
+      std::vector<uint4> p((size_t)cells);
+      for (int64_t k = 0; k < cells; ++k) {
+        if (k < o.tinymt_params_count)
+          p[k] = make_uint4(o.tinymt_params[3 * k], o.tinymt_params[3 * k + 1], o.tinymt_params[3 * k + 2], 0);
+        else
+          p[k] = make_uint4(kTmtMat1, kTmtMat2, kTmtTmat, 0);
+      }
+      RT_CUDA(cudaMalloc(&s->tmt_params, cells * sizeof(uint4)));
+      RT_CUDA(cudaMemcpyAsync(s->tmt_params, p.data(), cells * sizeof(uint4), cudaMemcpyHostToDevice, s->stream));
+      RT_CUDA(cudaStreamSynchronize(s->stream));
+    }
+  }
+  *out = std::move(s);
+  return RT_OK;
+}
+
+rt_status DmSampler::check_launch() {
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return fail(RT_ERR_CUDA, std::string("kernel launch: ") + cudaGetErrorString(e));
+  return RT_OK;
+}
+
+rt_status DmSampler::load(int ch, const int32_t* tiling) {
+  if (ch < 0 || ch >= n_chains || !tiling) return fail(RT_ERR_INVALID_ARGUMENT, "load: bad chain or NULL tiling");
+  for (size_t p = 0; p < (size_t)N * N; ++p)
+    if ((uint32_t)tiling[p] > 15u) return fail(RT_ERR_INVALID_ARGUMENT, "tiling values must be edge masks in [0, 15]");
+  if (ch == 0) {
+    // Interior vertices per colour: the flip attempts of one half-sweep.
+    const int M = N - 1;
+    std::vector<uint8_t> sq((size_t)M * M);
+    for (int i = 0; i < M; ++i)
+      for (int j = 0; j < M; ++j)
+        sq[(size_t)i * M + j] = ((tiling[(size_t)i * N + j] & 10) != 0) || ((tiling[(size_t)(i + 1) * N + j + 1] & 5) != 0);
+    interior[0] = interior[1] = 0;
+    for (int i = 1; i < M; ++i)
+      for (int j = 1; j < M; ++j)
+        if (sq[(size_t)(i - 1) * M + j - 1] && sq[(size_t)(i - 1) * M + j] && sq[(size_t)i * M + j - 1] && sq[(size_t)i * M + j])
+          interior[((i + j) & 1) == 0 ? 1 : 0]++;
+  }
+  RT_CUDA(cudaMemcpyAsync(scratch, tiling, (size_t)N * N * sizeof(int32_t), cudaMemcpyHostToDevice, stream));
+  DmView v = view();
+  k_split<<<dim3((N + 255) / 256, N), 256, 0, stream>>>(v, ch, scratch);
+  launches++;
+  return check_launch();
+}
+
+rt_status DmSampler::store(int ch, int32_t* tiling) {
+  if (ch < 0 || ch >= n_chains || !tiling) return fail(RT_ERR_INVALID_ARGUMENT, "store: bad chain or NULL tiling");
+  DmView v = view();
+  k_merge<<<dim3((N + 255) / 256, N), 256, 0, stream>>>(v, ch, scratch);
+  launches++;
+  if (rt_status s = check_launch()) return s;
+  RT_CUDA(cudaMemcpyAsync(tiling, scratch, (size_t)N * N * sizeof(int32_t), cudaMemcpyDeviceToHost, stream));
+  RT_CUDA(cudaStreamSynchronize(stream));
+  return RT_OK;
+}
+
+rt_status DmSampler::copy_chain(int dst, int src) {
+  if (dst < 0 || src < 0 || dst >= n_chains || src >= n_chains) return fail(RT_ERR_INVALID_ARGUMENT, "copy_chain: bad chain");
+  if (dst == src) return RT_OK;
+  RT_CUDA(cudaMemcpyAsync(base + (size_t)dst * chain_stride, base + (size_t)src * chain_stride, chain_stride,
+                          cudaMemcpyDeviceToDevice, stream));
+  return RT_OK;
+}
+
+rt_status DmSampler::seed(uint32_t s) {
+  if (opts.rng_mode != RT_RNG_TINYMT) return fail(RT_ERR_INVALID_ARGUMENT, "seed: sampler is not in TinyMT mode");
+  const int64_t cells = (int64_t)(N - 2) * (N / 2 - 2);
+  k_tmt_seed<<<(unsigned)((cells + 255) / 256), 256, 0, stream>>>(tmt, tmt_params, cells, s);
+  launches++;
+  return check_launch();
+}
+
+rt_status DmSampler::run(const uint8_t* colours, int64_t steps) {
+  if (opts.rng_mode != RT_RNG_TINYMT) return fail(RT_ERR_INVALID_ARGUMENT, "run: sampler is not in TinyMT mode");
+  if (steps < 0 || (steps > 0 && !colours)) return fail(RT_ERR_INVALID_ARGUMENT, "run: bad colours / steps");
+  DmView v = view();
+  const dim3 blk(128, 2), grd((v.cols + 127) / 128, (v.rows + 1) / 2);
+  for (int64_t s = 0; s < steps; ++s) {
+    const int t = colours[s] ? 1 : 0;
+    if (tmt_params) k_rotate_tmt<true><<<grd, blk, 0, stream>>>(v, t, rule);
+    else k_rotate_tmt<false><<<grd, blk, 0, stream>>>(v, t, rule);
+    k_update<<<grd, blk, 0, stream>>>(v, t);
+    launches += 2;
+    half_sweeps[t]++;
+  }
+  return check_launch();
+}
+
+rt_status DmSampler::run_fast(uint64_t seed_value, int64_t h0, int64_t steps) {
+  if (opts.rng_mode != RT_RNG_FAST) return fail(RT_ERR_INVALID_ARGUMENT, "run_fast: sampler is not in fast mode");
+  if (steps < 0) return fail(RT_ERR_INVALID_ARGUMENT, "run_fast: negative steps");
+  const int64_t lim = (int64_t)1 << 47;
+  if (h0 < -lim || h0 + steps > lim) return fail(RT_ERR_INVALID_ARGUMENT, "run_fast: half-sweep index out of range");
+  DmView v = view();
+  const int quads = v.cols / 4 + 1;
+  const dim3 blk(64, 4), grd_r((quads + 63) / 64, (v.rows + 3) / 4);
+  const dim3 blk_u(128, 2), grd_u((v.cols + 127) / 128, (v.rows + 1) / 2);
+  for (int64_t s = 0; s < steps; ++s) {
+    const int64_t h = h0 + s;
+    const int t = (h & 1) ? 0 : 1;
+    k_rotate_fast<<<grd_r, blk, 0, stream>>>(v, t, rule, seed_value, opts.fast_stream, h);
+    k_update<<<grd_u, blk_u, 0, stream>>>(v, t);
+    launches += 2;
+    half_sweeps[t]++;
+  }
+  return check_launch();
+}
+
+rt_status DmSampler::diff(int a, int b, int64_t* ndiff) {
+  if (a < 0 || b < 0 || a >= n_chains || b >= n_chains || !ndiff) return fail(RT_ERR_INVALID_ARGUMENT, "diff: bad arguments");
+  RT_CUDA(cudaMemsetAsync(counter, 0, sizeof(unsigned long long), stream));
+  DmView v = view();
+  const size_t words = chain_stride / 4;
+  const unsigned blocks = (unsigned)std::min<size_t>((words + 255) / 256, 1024);
+  k_diff<<<blocks, 256, 0, stream>>>(v, a, b, counter);
+  launches++;
+  if (rt_status s = check_launch()) return s;
+  unsigned long long h = 0;
+  RT_CUDA(cudaMemcpyAsync(&h, counter, sizeof h, cudaMemcpyDeviceToHost, stream));
+  RT_CUDA(cudaStreamSynchronize(stream));
+  *ndiff = (int64_t)h;
+  return RT_OK;
+}
+
+rt_status DmSampler::sync() {
+  RT_CUDA(cudaStreamSynchronize(stream));
+  return RT_OK;
+}
+
+}  // namespace rt
+
+// -----------------------------------------------------------------------------------------
+// C ABI
+// -----------------------------------------------------------------------------------------
+using namespace rt;
+
+struct rt_dm_sampler {
+  std::unique_ptr<DmSampler> impl;
+};
+
+static rt_walk_opts opts_or_default(const rt_walk_opts* o) {
+  rt_walk_opts d;
+  rt_walk_opts_default(&d);
+  return o ? *o : d;
+}
+
+extern "C" {
+
+RT_API rt_status rt_dm_sampler_create(int32_t n_side, int32_t n_chains, const rt_walk_opts* opts, rt_dm_sampler** out) {
+  clear_error();
+  if (!out) return fail(RT_ERR_INVALID_ARGUMENT, "out is NULL");
+  *out = nullptr;
+  auto h = std::make_unique<rt_dm_sampler>();
+  if (rt_status s = DmSampler::create(n_side, n_chains, opts_or_default(opts), &h->impl)) return s;
+  *out = h.release();
+  return RT_OK;
+}
+
+RT_API rt_status rt_dm_sampler_destroy(rt_dm_sampler* s) {
+  clear_error();
+  delete s;
+  return RT_OK;
+}
+
+#define RT_SAMPLER(s) \
+  clear_error();      \
+  if (!(s) || !(s)->impl) return fail(RT_ERR_INVALID_ARGUMENT, "sampler is NULL")
+
+RT_API rt_status rt_dm_sampler_load(rt_dm_sampler* s, int32_t chain, const int32_t* tiling) {
+  RT_SAMPLER(s);
+  return s->impl->load(chain, tiling);
+}
+RT_API rt_status rt_dm_sampler_store(rt_dm_sampler* s, int32_t chain, int32_t* tiling) {
+  RT_SAMPLER(s);
+  return s->impl->store(chain, tiling);
+}
+RT_API rt_status rt_dm_sampler_copy_chain(rt_dm_sampler* s, int32_t dst, int32_t src) {
+  RT_SAMPLER(s);
+  return s->impl->copy_chain(dst, src);
+}
+RT_API rt_status rt_dm_sampler_set_active(rt_dm_sampler* s, int32_t k) {
+  RT_SAMPLER(s);
+  if (k < 1 || k > s->impl->n_chains) return fail(RT_ERR_INVALID_ARGUMENT, "set_active: k must be in [1, n_chains]");
+  s->impl->active = k;
+  return RT_OK;
+}
+RT_API rt_status rt_dm_sampler_seed(rt_dm_sampler* s, uint32_t seed) {
+  RT_SAMPLER(s);
+  return s->impl->seed(seed);
+}
+RT_API rt_status rt_dm_sampler_run(rt_dm_sampler* s, const uint8_t* colours, int64_t steps) {
+  RT_SAMPLER(s);
+  return s->impl->run(colours, steps);
+}
+RT_API rt_status rt_dm_sampler_run_fast(rt_dm_sampler* s, uint64_t seed, int64_t h0, int64_t steps) {
+  RT_SAMPLER(s);
+  return s->impl->run_fast(seed, h0, steps);
+}
+RT_API rt_status rt_dm_sampler_diff(rt_dm_sampler* s, int32_t a, int32_t b, int64_t* ndiff) {
+  RT_SAMPLER(s);
+  return s->impl->diff(a, b, ndiff);
+}
+RT_API rt_status rt_dm_sampler_sync(rt_dm_sampler* s) {
+  RT_SAMPLER(s);
+  return s->impl->sync();
+}
+RT_API void* rt_dm_sampler_stream(rt_dm_sampler* s) { return (s && s->impl) ? (void*)s->impl->stream : nullptr; }
+RT_API int64_t rt_dm_sampler_interior_vertices(rt_dm_sampler* s) {
+  return (s && s->impl) ? s->impl->interior[0] + s->impl->interior[1] : -1;
+}
+RT_API int64_t rt_dm_sampler_launches(rt_dm_sampler* s) { return (s && s->impl) ? s->impl->launches : -1; }
+
+// ---- walks ---------------------------------------------------------------------------------
+
+static std::vector<uint8_t> colour_draws(std::mt19937& mt, int64_t steps) {
+  std::vector<uint8_t> c((size_t)steps);
+  for (int64_t s = 0; s < steps; ++s) c[(size_t)s] = (uint8_t)(mt() % 2);
+  return c;
+}
+
+RT_API rt_status rt_domino_walk(int32_t* tiling, int32_t n_side, int64_t steps, int64_t seed, const rt_walk_opts* opts) {
+  clear_error();
+  if (!tiling || steps < 0) return fail(RT_ERR_INVALID_ARGUMENT, "walk: NULL tiling or negative steps");
+  rt_walk_opts o = opts_or_default(opts);
+  std::unique_ptr<DmSampler> s;
+  if (rt_status st = DmSampler::create(n_side, 1, o, &s)) return st;
+  if (rt_status st = s->load(0, tiling)) return st;
+  if (o.rng_mode == RT_RNG_TINYMT) {
+    // DominoTiler.cpp:50-53 (OpenCL branch): generators seeded by the first draw, colours
+    // from the following draws (:69-70).
+    std::mt19937 mt((uint32_t)seed);
+    if (rt_status st = s->seed((uint32_t)mt())) return st;
+    std::vector<uint8_t> col = colour_draws(mt, steps);
+    if (rt_status st = s->run(col.data(), steps)) return st;
+  } else {
+    if (rt_status st = s->run_fast((uint64_t)seed, 0, steps)) return st;
+  }
+  return s->store(0, tiling);
+}
+
+RT_API rt_status rt_domino_walk_epochs(int32_t* tiling, int32_t n_side, const int64_t* steps, const int64_t* seeds,
+                                       int32_t n_epochs, const rt_walk_opts* opts) {
+  clear_error();
+  if (!tiling || n_epochs < 0 || (n_epochs > 0 && (!steps || !seeds)))
+    return fail(RT_ERR_INVALID_ARGUMENT, "walk_epochs: bad arguments");
+  for (int k = 0; k < n_epochs; ++k)
+    if (steps[k] < 0) return fail(RT_ERR_INVALID_ARGUMENT, "walk_epochs: negative steps");
+  rt_walk_opts o = opts_or_default(opts);
+  std::unique_ptr<DmSampler> s;
+  if (rt_status st = DmSampler::create(n_side, 1, o, &s)) return st;
+  if (rt_status st = s->load(0, tiling)) return st;
+  int64_t h = 0;
+  for (int k = 0; k < n_epochs; ++k) {
+    if (o.rng_mode == RT_RNG_TINYMT) {
+      // DominoTiler.cpp:155-175: mt19937(seeds[k]) for the colours, generators from seeds[k].
+      std::mt19937 mt((uint32_t)seeds[k]);
+      if (rt_status st = s->seed((uint32_t)seeds[k])) return st;
+      std::vector<uint8_t> col = colour_draws(mt, steps[k]);
+      if (rt_status st = s->run(col.data(), steps[k])) return st;
+    } else {
+      // Fast mode: epoch k is keyed by seeds[k] and restarts at half-sweep 0.
+      if (rt_status st = s->run_fast((uint64_t)seeds[k], 0, steps[k])) return st;
+      h += steps[k];
+    }
+  }
+  return s->store(0, tiling);
+}
+
+RT_API rt_status rt_domino_cftp(const int32_t* tmax, const int32_t* tmin, int32_t n_side, int64_t driver_seed,
+                                int64_t first_steps, int32_t schedule, int32_t max_attempts, const rt_walk_opts* opts,
+                                int32_t* out, rt_cftp_stats* stats) {
+  clear_error();
+  if (!tmax || !tmin || !out) return fail(RT_ERR_INVALID_ARGUMENT, "cftp: NULL tiling");
+  if (first_steps < 1 || max_attempts < 1 || max_attempts > 40 || (schedule != 0 && schedule != 1))
+    return fail(RT_ERR_INVALID_ARGUMENT, "cftp: first_steps >= 1, 1 <= max_attempts <= 40, schedule 0 or 1");
+  rt_walk_opts o = opts_or_default(opts);
+  if (o.rule != RT_DOMINO_CFTP && o.rule != RT_DOMINO_CFTP_TWOPERIODIC)
+    return fail(RT_ERR_INVALID_ARGUMENT, "cftp needs a monotone rule (RT_DOMINO_CFTP or RT_DOMINO_CFTP_TWOPERIODIC)");
+  std::unique_ptr<DmSampler> s;
+  // chains 0 (bottom) and 1 (top) are swept; 2 and 3 keep the min and max start states.
+  if (rt_status st = DmSampler::create(n_side, 4, o, &s)) return st;
+  if (rt_status st = s->load(0, tmin)) return st;
+  if (rt_status st = s->load(2, tmin)) return st;
+  if (rt_status st = s->load(3, tmax)) return st;
+  s->active = 2;
+  rt_cftp_stats st_out{};
+  std::mt19937 drv((uint32_t)driver_seed);
+  std::vector<int64_t> steps{first_steps};
+  std::vector<uint32_t> seeds{(uint32_t)drv()};
+  std::vector<std::vector<uint8_t>> colours;  // colour draws per epoch, in the order of steps
+  float ms_total = 0.f;
+  for (int attempt = 1; attempt <= max_attempts; ++attempt) {
+    if (rt_status st = s->copy_chain(0, 2)) return st;
+    if (rt_status st = s->copy_chain(1, 3)) return st;
+    int64_t before0 = s->half_sweeps[0], before1 = s->half_sweeps[1];
+    cudaEventRecord(s->ev0, s->stream);
+    int64_t look_back = 0;
+    if (o.rng_mode == RT_RNG_TINYMT) {
+      while (colours.size() < steps.size()) colours.insert(colours.begin(), std::vector<uint8_t>());  // prepended epochs
+      for (size_t k = 0; k < steps.size(); ++k) {
+        if (colours[k].empty() && steps[k] > 0) {
+          std::mt19937 mt(seeds[k]);
+          colours[k] = colour_draws(mt, steps[k]);
+        }
+        if (rt_status st = s->seed(seeds[k])) return st;
+        if (rt_status st = s->run(colours[k].data(), steps[k])) return st;
+        look_back += steps[k];
+      }
+    } else {
+      const int64_t T = first_steps << (attempt - 1);
+      if (rt_status st = s->run_fast((uint64_t)driver_seed, -2 * T, 2 * T)) return st;
+      look_back = 2 * T;
+    }
+    cudaEventRecord(s->ev1, s->stream);
+    int64_t nd = -1;
+    if (rt_status st = s->diff(0, 1, &nd)) return st;
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, s->ev0, s->ev1);
+    ms_total += ms;
+    st_out.attempts = attempt;
+    st_out.total_steps += look_back;
+    st_out.final_steps = look_back;
+    st_out.flip_attempts += 2 * ((s->half_sweeps[0] - before0) * s->interior[0] + (s->half_sweeps[1] - before1) * s->interior[1]);
+    st_out.seconds = ms_total * 1e-3;
+    if (nd == 0) {
+      if (stats) *stats = st_out;
+      return s->store(1, out);
+    }
+    if (o.rng_mode == RT_RNG_TINYMT) {
+      // AztecDiamondCftpEx.cpp:76 prepends 2 * steps.back(); schedule 1 doubles the oldest.
+      int64_t next = schedule == 0 ? steps.back() * 2 : steps.front() * 2;
+      steps.insert(steps.begin(), next);
+      seeds.insert(seeds.begin(), (uint32_t)drv());
+    }
+  }
+  if (stats) *stats = st_out;
+  // out receives the top chain of the last attempt, so a caller can resume or inspect it.
+  if (rt_status st = s->store(1, out)) return st;
+  return fail(RT_ERR_NOT_COALESCED, "cftp: chains did not coalesce within max_attempts");
+}
+
+}  // extern "C"

@@ -1,0 +1,57 @@
+// Device-side state of the domino sweep (see domino_sweep.cu for the layout).
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <memory>
+
+#include "domino_rules.h"
+#include "rt_internal.h"
+
+namespace rt {
+
+// Plain-data view of a sampler passed to the kernels by value.
+struct DmView {
+  uint8_t* base;
+  int N, P, rows, cols, active;
+  size_t chain_stride, colour_stride;
+  uint4* tmt;
+  const uint4* tmt_params;
+  // Colour array t (1 black, 0 white) of chain ch.
+  __host__ __device__ uint8_t* colour(int ch, int t) const {
+    return base + (size_t)ch * chain_stride + (size_t)t * colour_stride;
+  }
+};
+
+struct DmSampler {
+  int N = 0, P = 0, n_chains = 0, active = 0;
+  size_t chain_stride = 0, colour_stride = 0;
+  rt_walk_opts opts{};
+  DmRule rule{};
+  uint8_t* base = nullptr;
+  uint4* tmt = nullptr;
+  uint4* tmt_params = nullptr;
+  int32_t* scratch = nullptr;
+  unsigned long long* counter = nullptr;
+  cudaStream_t stream = nullptr;
+  bool own_stream = false;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  int64_t interior[2] = {0, 0};     // interior vertices of colour 0 (white) and 1 (black)
+  int64_t half_sweeps[2] = {0, 0};  // half-sweeps run per colour
+  int64_t launches = 0;
+
+  static rt_status create(int n_side, int n_chains, const rt_walk_opts& o, std::unique_ptr<DmSampler>* out);
+  ~DmSampler();
+  DmView view() const;
+  rt_status check_launch();
+  rt_status load(int ch, const int32_t* tiling);
+  rt_status store(int ch, int32_t* tiling);
+  rt_status copy_chain(int dst, int src);
+  rt_status seed(uint32_t s);
+  rt_status run(const uint8_t* colours, int64_t steps);
+  rt_status run_fast(uint64_t seed, int64_t h0, int64_t steps);
+  rt_status diff(int a, int b, int64_t* ndiff);
+  rt_status sync();
+};
+
+}  // namespace rt

@@ -1,0 +1,150 @@
+"""Generates tests/golden/domino_ref_cases.json from the reference's own code.
+
+Runs where the reference tree exists (it is not on the GPU machine): builds oracle/_ref
+(`make -C oracle ref`), which compiles the reference's domino .cl kernel files and its host
+code (src/Domino/DominoTiler.cpp) from the reference tree, and records for a set of small
+cases the start tiling and the tiling after the reference's own sweep code ran (TinyMT
+generators with the default parameter set, or with a seeded synthetic parameter table where
+noted; the reference's own table file is absent from its tree).  Also pins the committed
+fixture Examples/ExampleOuts/WeightedAztecDiamond/TilingStart.txt against the reference's
+MinTiling(AztecDiamond(16)).
+
+    python tests/golden/make_golden.py [--ref /root/reference]
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import json
+import subprocess
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+ROOT = HERE.parent.parent
+RULES = ["plain", "CFTP", "twoperiodic", "CFTPtwoperiodic"]
+
+
+def main() -> None:
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--ref", default="/root/reference")
+    args = ap.parse_args()
+    subprocess.run(["make", "-s", "-C", str(ROOT / "oracle"), "ref", f"REF={args.ref}"], check=True)
+    host = C.CDLL(str(ROOT / "oracle/_ref/libref_domino_host.so"))
+    cl = C.CDLL(str(ROOT / "oracle/_ref/libref_domino_cl.so"))
+    P = lambda a: None if a is None else a.ctypes.data_as(C.c_void_p)
+
+    def domain(n):
+        buf = np.zeros((2 * n + 6) ** 2, np.int32)
+        side = host.refh_dm_aztec_rectangle(n, None, 0, P(buf), buf.size)
+        return buf[: side * side].copy(), side
+
+    def extremal(n, which):
+        d, m = domain(n)
+        out = np.zeros((m + 1) ** 2, np.int32)
+        getattr(host, f"refh_dm_{which}_tiling")(P(d), m, P(out))
+        return out, m + 1
+
+    for nm in RULES:
+        for suffix in ("_walk", "_walk_epochs"):
+            f = getattr(cl, f"ref_{nm}{suffix}")
+            f.restype = C.c_int
+        getattr(cl, f"ref_{nm}_walk").argtypes = [C.c_void_p, C.c_int, C.c_long, C.c_long, C.c_void_p, C.c_long]
+        getattr(cl, f"ref_{nm}_walk_epochs").argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_int,
+                                                         C.c_void_p, C.c_long]
+
+    def walk(nm, t, n, steps, seed, params=None):
+        t = t.copy()
+        getattr(cl, f"ref_{nm}_walk")(P(t), n, steps, seed, P(params), 0 if params is None else params.shape[0])
+        return t
+
+    def walk_epochs(nm, t, n, steps, seeds, params=None):
+        t = t.copy()
+        st = np.asarray(steps, np.int64)
+        sd = np.asarray(seeds, np.int64)
+        getattr(cl, f"ref_{nm}_walk_epochs")(P(t), n, P(st), P(sd), len(st), P(params),
+                                             0 if params is None else params.shape[0])
+        return t
+
+    cases = []
+
+    def add(name, kind, rule, start, n, expected, **kw):
+        cases.append({"name": name, "kind": kind, "rule": rule, "N": n, "start": start.tolist(),
+                      "expected": expected.tolist(), **kw})
+
+    # Single walks, every rule, from the max and the min tiling.
+    for r, nm in enumerate(RULES):
+        for order, which, steps, seed in [(6, "max", 57, 34893), (11, "min", 131, 1)]:
+            start, n = extremal(order, which)
+            add(f"walk_{nm}_aztec{order}_{which}", "walk", r, start, n, walk(nm, start, n, steps, seed),
+                steps=steps, seed=seed)
+    # Epoch walks (the vector overload).
+    for r, nm in enumerate(RULES):
+        start, n = extremal(7, "min")
+        steps, seeds = [40, 23, 17], [11, 2024, 4294967295]
+        add(f"epochs_{nm}_aztec7", "epochs", r, start, n, walk_epochs(nm, start, n, steps, seeds),
+            steps=steps, seeds=seeds)
+    # A per-generator parameter table (synthetic, seeded) in place of the missing file.
+    start, n = extremal(5, "max")
+    rng = np.random.default_rng(20261203)
+    params = rng.integers(0, 2**32, size=(n * n // 2, 3), dtype=np.uint64).astype(np.uint32)
+    add("walk_plain_aztec5_paramtable", "walk", 0, start, n, walk("plain", start, n, 73, 99, params),
+        steps=73, seed=99, params=params.tolist())
+    # The MinimalDomino example tiling (Examples/MinimalDominoEx.cpp:33-42, 10 x 10), 100 steps, seed 34893.
+    t10 = np.zeros(100, np.int32)
+    rows = {2: {4: 2}, 3: {2: 8, 3: 4, 4: 1, 5: 8, 6: 4}, 4: {3: 8, 4: 12, 5: 4}, 5: {2: 8, 3: 4, 4: 2, 5: 8, 6: 4},
+            6: {4: 1}}
+    for i, row in rows.items():
+        for j, v in row.items():
+            t10[i * 10 + j] = v
+    add("walk_plain_minimal_domino", "walk", 0, t10, 10, walk("plain", t10, 10, 100, 34893), steps=100, seed=34893)
+    # The CFTP example (Examples/AztecDiamondCftpEx.cpp:13,51-77): order 5, driver seed 345903,
+    # first epoch 128 steps, epochs prepended at 2 * steps.back(); both chains through the
+    # reference's epoch walk.
+    tmax, n = extremal(5, "max")
+    tmin, _ = extremal(5, "min")
+    drv = np.random.RandomState(345903)
+    draw = lambda: int(drv.randint(0, 2**32, dtype=np.uint32))
+    steps, seeds = [128], [draw()]
+    attempts = 0
+    while True:
+        attempts += 1
+        top = walk_epochs("CFTP", tmax, n, steps, seeds)
+        bot = walk_epochs("CFTP", tmin, n, steps, seeds)
+        if np.array_equal(top, bot):
+            break
+        steps.insert(0, steps[-1] * 2)
+        seeds.insert(0, draw())
+        assert attempts < 30
+    cases.append({"name": "cftp_example_aztec5", "kind": "cftp", "rule": 1, "N": n, "tmax": tmax.tolist(),
+                  "tmin": tmin.tolist(), "driver_seed": 345903, "first_steps": 128, "schedule": 0,
+                  "attempts": attempts, "expected": top.tolist()})
+
+    # Pin: the committed start tiling of the weighted example equals MinTiling(AztecDiamond(16)).
+    fixture = np.loadtxt(Path(args.ref) / "Examples/ExampleOuts/WeightedAztecDiamond/TilingStart.txt", dtype=np.int32)
+    mint, _ = extremal(16, "min")
+    assert np.array_equal(fixture.ravel(), mint), "reference MinTiling differs from its committed fixture"
+    pins = {"min_tiling_aztec16": mint.tolist()}
+    # Reference host utilities on a few domains for the host-side restatement.
+    host_cases = []
+    for order in (1, 2, 3, 9):
+        d, m = domain(order)
+        tmx = np.zeros((m + 1) ** 2, np.int32)
+        tmn = np.zeros((m + 1) ** 2, np.int32)
+        host.refh_dm_max_tiling(P(d), m, P(tmx))
+        host.refh_dm_min_tiling(P(d), m, P(tmn))
+        hf = np.zeros((m + 1) ** 2, np.int32)
+        host.refh_dm_tiling_to_heightfunc(P(tmx), P(d), m + 1, P(hf))
+        host_cases.append({"order": order, "domain": d.tolist(), "max": tmx.tolist(), "min": tmn.tolist(),
+                           "hf_max": hf.tolist()})
+    rect = np.zeros(30 * 30, np.int32)
+    side = host.refh_dm_rectangle(6, 9, P(rect), rect.size)
+    pins["rectangle_6x9"] = rect[: side * side].tolist()
+    out = {"generator": "tests/golden/make_golden.py", "cases": cases, "pins": pins, "host_cases": host_cases}
+    (HERE / "domino_ref_cases.json").write_text(json.dumps(out, separators=(",", ":")))
+    print(f"wrote {len(cases)} sweep cases, {len(host_cases)} host cases")
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,192 @@
+"""ctypes bindings of the oracle (oracle/_build/liboracle.so), the CPU checker of the
+library.  Test infrastructure: imported only by tests/, __graft_entry__.smoke() and the
+CPU-baseline leg of bench.py."""
+from __future__ import annotations
+
+import ctypes as C
+import subprocess
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent.parent
+ORACLE_DIR = ROOT / "oracle"
+ORACLE_LIB = ORACLE_DIR / "_build" / "liboracle.so"
+REF_DIR = ORACLE_DIR / "_ref"
+
+_P = C.c_void_p
+_L = C.c_long
+_SIG = {
+    "orc_dm_aztec_rectangle": (C.c_int, [C.c_int, _P, C.c_int, _P, _L]),
+    "orc_dm_rectangle": (C.c_int, [C.c_int, C.c_int, _P, _L]),
+    "orc_dm_domain_to_vertices": (None, [_P, C.c_int, _P]),
+    "orc_dm_max_tiling": (C.c_int, [_P, C.c_int, _P]),
+    "orc_dm_min_tiling": (C.c_int, [_P, C.c_int, _P]),
+    "orc_dm_heightfunc_to_tiling": (None, [_P, _P, C.c_int, _P]),
+    "orc_dm_tiling_to_heightfunc": (None, [_P, _P, C.c_int, _P]),
+    "orc_dm_tiling_to_domain": (None, [_P, C.c_int, _P]),
+    "orc_dm_walk_tinymt": (C.c_int, [_P, C.c_int, _L, _L, C.c_int, C.c_double, C.c_double, _P, _L, C.c_int]),
+    "orc_dm_walk_epochs_tinymt": (C.c_int, [_P, C.c_int, _P, _P, C.c_int, C.c_int, C.c_double, C.c_double, _P, _L,
+                                            C.c_int]),
+    "orc_dm_cftp_tinymt": (C.c_int, [_P, _P, C.c_int, _L, _L, C.c_int, C.c_int, C.c_int, C.c_double, C.c_double, _P,
+                                     _L, C.c_int, _P, _P]),
+    "orc_dm_walk_fast": (C.c_int, [_P, C.c_int, _L, _L, C.c_ulong, C.c_uint, C.c_int, C.c_double, C.c_double,
+                                   C.c_int]),
+    "orc_dm_cftp_fast": (C.c_int, [_P, _P, C.c_int, C.c_ulong, C.c_uint, _L, C.c_int, C.c_int, C.c_double,
+                                   C.c_double, C.c_int, _P, _P]),
+    "orc_tinymt_u32": (C.c_uint, [C.c_uint, C.c_uint, C.c_uint, C.c_uint, C.c_int]),
+    "orc_philox4x32_10": (None, [_P, _P, _P]),
+}
+
+_lib = None
+
+
+def lib() -> C.CDLL:
+    global _lib
+    if _lib is None:
+        if not ORACLE_LIB.exists():
+            subprocess.run(["make", "-s", "-C", str(ORACLE_DIR)], check=True)
+        h = C.CDLL(str(ORACLE_LIB))
+        for name, (res, args) in _SIG.items():
+            f = getattr(h, name)
+            f.restype = res
+            f.argtypes = args
+        _lib = h
+    return _lib
+
+
+def _i32(a) -> np.ndarray:
+    return np.ascontiguousarray(np.asarray(a, dtype=np.int32).ravel())
+
+
+def _p(a: np.ndarray | None):
+    return None if a is None else a.ctypes.data
+
+
+def _params(params):
+    if params is None:
+        return None, 0
+    p = np.ascontiguousarray(np.asarray(params, dtype=np.uint32).reshape(-1, 3))
+    return p, p.shape[0]
+
+
+def aztec_rectangle(n: int, remove=()) -> np.ndarray:
+    m = 2 * n - len(remove) + 6
+    buf = np.zeros(m * m, np.int32)
+    rm = _i32(list(remove)) if len(remove) else None
+    side = lib().orc_dm_aztec_rectangle(n, _p(rm), len(remove), _p(buf), buf.size)
+    return buf[: side * side].copy()
+
+
+def rectangle(rows: int, cols: int) -> np.ndarray:
+    m = max(rows, cols) + 6
+    buf = np.zeros(m * m, np.int32)
+    side = lib().orc_dm_rectangle(rows, cols, _p(buf), buf.size)
+    return buf[: side * side].copy()
+
+
+def _side(a) -> int:
+    import math
+    return math.isqrt(len(a))
+
+
+def domain_to_vertices(d) -> np.ndarray:
+    d = _i32(d)
+    m = _side(d)
+    out = np.zeros((m + 1) ** 2, np.int32)
+    lib().orc_dm_domain_to_vertices(_p(d), m, _p(out))
+    return out
+
+
+def max_tiling(d):
+    d = _i32(d)
+    m = _side(d)
+    out = np.zeros((m + 1) ** 2, np.int32)
+    rc = lib().orc_dm_max_tiling(_p(d), m, _p(out))
+    return rc, out
+
+
+def min_tiling(d):
+    d = _i32(d)
+    m = _side(d)
+    out = np.zeros((m + 1) ** 2, np.int32)
+    rc = lib().orc_dm_min_tiling(_p(d), m, _p(out))
+    return rc, out
+
+
+def tiling_to_heightfunc(t, d) -> np.ndarray:
+    t, d = _i32(t), _i32(d)
+    n = _side(t)
+    out = np.zeros(n * n, np.int32)
+    lib().orc_dm_tiling_to_heightfunc(_p(t), _p(d), n, _p(out))
+    return out
+
+
+def heightfunc_to_tiling(h, d) -> np.ndarray:
+    h, d = _i32(h), _i32(d)
+    n = _side(h)
+    out = np.zeros(n * n, np.int32)
+    lib().orc_dm_heightfunc_to_tiling(_p(h), _p(d), n, _p(out))
+    return out
+
+
+def tiling_to_domain(t) -> np.ndarray:
+    t = _i32(t)
+    n = _side(t)
+    out = np.zeros((n - 1) ** 2, np.int32)
+    lib().orc_dm_tiling_to_domain(_p(t), n, _p(out))
+    return out
+
+
+def walk_tinymt(t: np.ndarray, n: int, steps: int, seed: int, rule: int = 0, a=0.7, b=1.0, params=None,
+                threads: int = 1) -> None:
+    p, cnt = _params(params)
+    rc = lib().orc_dm_walk_tinymt(_p(t), n, steps, seed, rule, a, b, _p(p), cnt, threads)
+    assert rc == 0
+
+
+def walk_epochs_tinymt(t: np.ndarray, n: int, steps, seeds, rule: int = 0, a=0.7, b=1.0, params=None,
+                       threads: int = 1) -> None:
+    st = np.ascontiguousarray(np.asarray(steps, np.int64))
+    sd = np.ascontiguousarray(np.asarray(seeds, np.int64))
+    p, cnt = _params(params)
+    rc = lib().orc_dm_walk_epochs_tinymt(_p(t), n, _p(st), _p(sd), len(st), rule, a, b, _p(p), cnt, threads)
+    assert rc == 0
+
+
+def cftp_tinymt(tmax, tmin, n, driver_seed, first_steps, schedule, max_attempts, rule=1, a=0.7, b=1.0, params=None,
+                threads: int = 1):
+    tmax, tmin = _i32(tmax), _i32(tmin)
+    out = np.zeros_like(tmax)
+    total = C.c_long()
+    p, cnt = _params(params)
+    att = lib().orc_dm_cftp_tinymt(_p(tmax), _p(tmin), n, driver_seed, first_steps, schedule, max_attempts, rule, a,
+                                   b, _p(p), cnt, threads, _p(out), C.addressof(total))
+    return out, att, total.value
+
+
+def walk_fast(t: np.ndarray, n: int, h0: int, steps: int, seed: int, stream: int = 0, rule: int = 0, a=0.7, b=1.0,
+              threads: int = 1) -> None:
+    rc = lib().orc_dm_walk_fast(_p(t), n, h0, steps, seed, stream, rule, a, b, threads)
+    assert rc == 0
+
+
+def cftp_fast(tmax, tmin, n, seed, stream, first_sweeps, max_attempts, rule=1, a=0.7, b=1.0, threads: int = 1):
+    tmax, tmin = _i32(tmax), _i32(tmin)
+    out = np.zeros_like(tmax)
+    used = C.c_long()
+    att = lib().orc_dm_cftp_fast(_p(tmax), _p(tmin), n, seed, stream, first_sweeps, max_attempts, rule, a, b, threads,
+                                 _p(out), C.addressof(used))
+    return out, att, used.value
+
+
+def tinymt_u32(seed, mat1, mat2, tmat, skip=0) -> int:
+    return lib().orc_tinymt_u32(seed, mat1, mat2, tmat, skip)
+
+
+def philox4x32_10(ctr, key):
+    c = np.ascontiguousarray(np.asarray(ctr, np.uint32))
+    k = np.ascontiguousarray(np.asarray(key, np.uint32))
+    out = np.zeros(4, np.uint32)
+    lib().orc_philox4x32_10(_p(c), _p(k), _p(out))
+    return out
