@@ -187,7 +187,7 @@ DmView DmSampler::view() const {
 
 rt_status DmSampler::create(int n_side, int n_chains, const rt_walk_opts& o, std::unique_ptr<DmSampler>* out) {
   if (n_side < 6 || n_side % 2) return fail(RT_ERR_INVALID_ARGUMENT, "tiling side must be even and >= 6");
-  if (n_side > 65536) return fail(RT_ERR_INVALID_ARGUMENT, "tiling side must be <= 65536");
+  if (n_side > 32768) return fail(RT_ERR_INVALID_ARGUMENT, "tiling side must be <= 32768");
   if (n_chains < 1 || n_chains > 64) return fail(RT_ERR_INVALID_ARGUMENT, "n_chains must be in [1, 64]");
   if (o.rng_mode == RT_RNG_FAST && o.fast_stream >= 65536u)
     return fail(RT_ERR_INVALID_ARGUMENT, "fast_stream must be < 65536");
