@@ -143,9 +143,11 @@ def test_tinymt_cftp_doubling_schedule_matches_oracle(rt, orc):
     tmax, tmin = D.MaxTiling(d), D.MinTiling(d)
     n = int(np.sqrt(tmax.size))
     for schedule in (0, 1):
-        out, stats = rt.DominoTiler(rule="cftp_twoperiodic", a=1.0, b=0.5).cftp(tmax, tmin, 99, 32, schedule, 20)
-        ref, attempts, total = orc.cftp_tinymt(tmax, tmin, n, 99, 32, schedule, 20, rule=3, a=1.0, b=0.5)
-        assert attempts == stats["attempts"] and np.array_equal(out, ref)
+        # schedule 0 (the reference's 128 + 256k look-back) coalesces here after 13 attempts,
+        # schedule 1 (doubling) after 4.
+        out, stats = rt.DominoTiler(rule="cftp_twoperiodic", a=1.0, b=0.5).cftp(tmax, tmin, 99, 128, schedule, 25)
+        ref, attempts, total = orc.cftp_tinymt(tmax, tmin, n, 99, 128, schedule, 25, rule=3, a=1.0, b=0.5)
+        assert attempts == stats["attempts"] and total == stats["total_steps"] and np.array_equal(out, ref)
 
 
 def test_sampler_api(rt):
