@@ -656,7 +656,7 @@ int orc_dm_cftp_tinymt(const int* tmax, const int* tmin, int N, long driver_seed
       init_generators(g, (size_t)J.rows * J.cols, (uint32_t)seeds[k], params, nparams);
       std::vector<uint8_t> col = colour_stream(mt, steps[k]);
       run_tinymt(J, g, col, threads);
-      total += 2 * steps[k];
+      total += steps[k];  // half-sweeps per chain
     }
     if (top.B == bot.B && top.W == bot.W) {
       merge_tiling(top, out);
