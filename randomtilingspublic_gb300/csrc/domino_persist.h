@@ -1,0 +1,80 @@
+// Resident persistent engine of the domino sweep (see domino_persist.cu).
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "domino_rules.h"
+#include "rt_internal.h"
+
+namespace rt {
+
+struct DmSampler;
+
+// One CTA's share: colour-array rows [r0, r1), shared-memory column window [wlo, whi)
+// (bytes, multiples of 4), and its number of units (flip-candidate sites or quads).
+struct DmBand {
+  int r0, r1, wlo, whi, units, pad0, pad1, pad2;
+};
+
+struct PersistArgs {
+  uint8_t* base;
+  int P, cols, nch, nbands;
+  size_t chain_stride, colour_stride;
+  uint4* tmt;
+  const uint4* tmt_params;
+  const DmBand* bands;
+  const int* row_lo;      // first unit of each row
+  const int* row_prefix;  // unit index of that first unit within the row's band
+  DmRule rule;
+  uint8_t* xbuf;          // [2 slots][band][top, bottom][chain][P]
+  unsigned* flags;        // per band: half-sweeps published; flags[nbands] is the error word
+  int* error;
+  long max_spin;
+  int64_t steps, h0;
+  uint64_t fast_seed;
+  uint32_t fast_stream;
+  const uint8_t* colours;
+};
+
+struct PersistPlan {
+  bool ok = false;
+  std::string why;
+  std::vector<DmBand> bands;
+  std::vector<int> row_lo, row_cnt, row_prefix;
+  int max_units = 0, K = 0;
+  size_t smem_bytes = 0;
+  rt_status build(const std::vector<uint8_t>& candidates, int N, int P, int mode, int nch, int nbands_max,
+                  size_t smem_limit);
+};
+
+struct PersistEngine {
+  PersistPlan plan;
+  bool ready = false;
+  int nch = 0;
+  void* kernel = nullptr;
+  DmBand* d_bands = nullptr;
+  int* d_rows = nullptr;
+  uint8_t* d_xbuf = nullptr;
+  unsigned* d_flags = nullptr;
+  uint8_t* d_colours = nullptr;
+  int64_t colours_cap = 0;
+  size_t xbuf_bytes = 0;
+  bool pending_error_check = false;
+
+  ~PersistEngine();
+  rt_status prepare(DmSampler& s);
+  rt_status launch(DmSampler& s, const uint8_t* colours_host, int64_t steps, uint64_t fast_seed, int64_t h0);
+  rt_status check_error(DmSampler& s);
+};
+
+// True when every edge bit agrees with the bit of the vertex across it and no edge leaves
+// the array: then rebuilding a colour from the other reproduces it, which the persistent
+// engine relies on outside its windows.
+bool dm_tiling_consistent(const int32_t* t, int N);
+// Marks cells (i, N/2 * i + m) holding an interior vertex of the tiling's domain.
+void dm_mark_candidates(const int32_t* t, int N, std::vector<uint8_t>& cand);
+
+}  // namespace rt

@@ -252,6 +252,9 @@ rt_status DmSampler::load(int ch, const int32_t* tiling) {
   if (ch < 0 || ch >= n_chains || !tiling) return fail(RT_ERR_INVALID_ARGUMENT, "load: bad chain or NULL tiling");
   for (size_t p = 0; p < (size_t)N * N; ++p)
     if ((uint32_t)tiling[p] > 15u) return fail(RT_ERR_INVALID_ARGUMENT, "tiling values must be edge masks in [0, 15]");
+  consistent = consistent && dm_tiling_consistent(tiling, N);
+  dm_mark_candidates(tiling, N, candidates);
+  plan_dirty = true;
   if (ch == 0) {
     // Interior vertices per colour: the flip attempts of one half-sweep.
     const int M = N - 1;
@@ -274,6 +277,9 @@ rt_status DmSampler::load(int ch, const int32_t* tiling) {
 
 rt_status DmSampler::store(int ch, int32_t* tiling) {
   if (ch < 0 || ch >= n_chains || !tiling) return fail(RT_ERR_INVALID_ARGUMENT, "store: bad chain or NULL tiling");
+  if (persist) {
+    if (rt_status st = persist->check_error(*this)) return st;
+  }
   DmView v = view();
   k_merge<<<dim3((N + 255) / 256, N), 256, 0, stream>>>(v, ch, scratch);
   launches++;
@@ -302,6 +308,15 @@ rt_status DmSampler::seed(uint32_t s) {
 rt_status DmSampler::run(const uint8_t* colours, int64_t steps) {
   if (opts.rng_mode != RT_RNG_TINYMT) return fail(RT_ERR_INVALID_ARGUMENT, "run: sampler is not in TinyMT mode");
   if (steps < 0 || (steps > 0 && !colours)) return fail(RT_ERR_INVALID_ARGUMENT, "run: bad colours / steps");
+  if (steps == 0) return RT_OK;
+  bool pers = false;
+  if (rt_status st = use_persistent(&pers)) return st;
+  if (pers) {
+    last_engine = 2;
+    for (int64_t q = 0; q < steps; ++q) half_sweeps[colours[q] ? 1 : 0]++;
+    return persist->launch(*this, colours, steps, 0, 0);
+  }
+  last_engine = 1;
   DmView v = view();
   const dim3 blk(128, 2), grd((v.cols + 127) / 128, (v.rows + 1) / 2);
   for (int64_t s = 0; s < steps; ++s) {
@@ -320,6 +335,15 @@ rt_status DmSampler::run_fast(uint64_t seed_value, int64_t h0, int64_t steps) {
   if (steps < 0) return fail(RT_ERR_INVALID_ARGUMENT, "run_fast: negative steps");
   const int64_t lim = (int64_t)1 << 47;
   if (h0 < -lim || h0 + steps > lim) return fail(RT_ERR_INVALID_ARGUMENT, "run_fast: half-sweep index out of range");
+  if (steps == 0) return RT_OK;
+  bool pers = false;
+  if (rt_status st = use_persistent(&pers)) return st;
+  if (pers) {
+    last_engine = 2;
+    for (int64_t q = 0; q < steps; ++q) half_sweeps[((h0 + q) & 1) ? 0 : 1]++;
+    return persist->launch(*this, nullptr, steps, seed_value, h0);
+  }
+  last_engine = 1;
   DmView v = view();
   const int quads = v.cols / 4 + 1;
   const dim3 blk(64, 4), grd_r((quads + 63) / 64, (v.rows + 3) / 4);
@@ -344,6 +368,9 @@ rt_status DmSampler::diff(int a, int b, int64_t* ndiff) {
   k_diff<<<blocks, 256, 0, stream>>>(v, a, b, counter);
   launches++;
   if (rt_status s = check_launch()) return s;
+  if (persist) {
+    if (rt_status st = persist->check_error(*this)) return st;
+  }
   unsigned long long h = 0;
   RT_CUDA(cudaMemcpyAsync(&h, counter, sizeof h, cudaMemcpyDeviceToHost, stream));
   RT_CUDA(cudaStreamSynchronize(stream));
@@ -353,6 +380,27 @@ rt_status DmSampler::diff(int a, int b, int64_t* ndiff) {
 
 rt_status DmSampler::sync() {
   RT_CUDA(cudaStreamSynchronize(stream));
+  if (persist) return persist->check_error(*this);
+  return RT_OK;
+}
+
+rt_status DmSampler::use_persistent(bool* yes) {
+  *yes = false;
+  if (opts.engine == 1) return RT_OK;
+  if (!consistent || candidates.empty()) {
+    if (opts.engine == 2) return fail(RT_ERR_INVALID_ARGUMENT, "persistent engine needs consistent loaded tilings");
+    return RT_OK;
+  }
+  if (plan_dirty || !persist || persist->nch != active) {
+    if (!persist) persist = std::make_unique<PersistEngine>();
+    if (rt_status st = persist->prepare(*this)) return st;
+    plan_dirty = false;
+  }
+  if (!persist->ready) {
+    if (opts.engine == 2) return fail(RT_ERR_INVALID_ARGUMENT, "persistent engine unavailable: " + persist->plan.why);
+    return RT_OK;
+  }
+  *yes = true;
   return RT_OK;
 }
 
@@ -411,6 +459,7 @@ RT_API rt_status rt_dm_sampler_set_active(rt_dm_sampler* s, int32_t k) {
   RT_SAMPLER(s);
   if (k < 1 || k > s->impl->n_chains) return fail(RT_ERR_INVALID_ARGUMENT, "set_active: k must be in [1, n_chains]");
   s->impl->active = k;
+  s->impl->plan_dirty = true;
   return RT_OK;
 }
 RT_API rt_status rt_dm_sampler_seed(rt_dm_sampler* s, uint32_t seed) {
@@ -512,6 +561,7 @@ RT_API rt_status rt_domino_cftp(const int32_t* tmax, const int32_t* tmin, int32_
   if (rt_status st = s->load(2, tmin)) return st;
   if (rt_status st = s->load(3, tmax)) return st;
   s->active = 2;
+  s->plan_dirty = true;
   rt_cftp_stats st_out{};
   std::mt19937 drv((uint32_t)driver_seed);
   std::vector<int64_t> steps{first_steps};

@@ -5,6 +5,7 @@
 #include <cstdint>
 #include <memory>
 
+#include "domino_persist.h"
 #include "domino_rules.h"
 #include "rt_internal.h"
 
@@ -39,6 +40,13 @@ struct DmSampler {
   int64_t interior[2] = {0, 0};     // interior vertices of colour 0 (white) and 1 (black)
   int64_t half_sweeps[2] = {0, 0};  // half-sweeps run per colour
   int64_t launches = 0;
+  // Persistent engine state: flip-candidate cells over all loaded chains, whether every
+  // loaded tiling is consistent, and the engine (re)planned when either changes.
+  std::vector<uint8_t> candidates;
+  bool consistent = true;
+  bool plan_dirty = true;
+  std::unique_ptr<PersistEngine> persist;
+  int last_engine = 0;  // engine of the last run: 1 per-half-sweep kernels, 2 persistent
 
   static rt_status create(int n_side, int n_chains, const rt_walk_opts& o, std::unique_ptr<DmSampler>* out);
   ~DmSampler();
@@ -52,6 +60,8 @@ struct DmSampler {
   rt_status run_fast(uint64_t seed, int64_t h0, int64_t steps);
   rt_status diff(int a, int b, int64_t* ndiff);
   rt_status sync();
+  // Picks the engine for the next run: true when the persistent kernel will run it.
+  rt_status use_persistent(bool* yes);
 };
 
 }  // namespace rt

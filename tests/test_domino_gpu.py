@@ -36,7 +36,7 @@ def _is_valid_tiling(rt, t, d) -> bool:
     return bool(np.all(cover[D == 1] == 1) and np.all(cover[D == 0] == 0))
 
 
-@pytest.mark.parametrize("engine", [0, 1])
+@pytest.mark.parametrize("engine", [1, 2])
 def test_golden_reference_vectors(rt, golden, engine):
     for case in golden["cases"]:
         n = case["N"]
@@ -56,7 +56,7 @@ def test_golden_reference_vectors(rt, golden, engine):
         assert np.array_equal(t, np.array(case["expected"], np.int32)), case["name"]
 
 
-@pytest.mark.parametrize("engine", [0, 1])
+@pytest.mark.parametrize("engine", [1, 2])
 def test_tinymt_walk_random_cases_match_oracle(rt, orc, engine):
     rng = np.random.default_rng(11)
     D = rt.DominoTiler
@@ -76,15 +76,16 @@ def test_tinymt_walk_random_cases_match_oracle(rt, orc, engine):
         assert np.array_equal(g, o), (order, rule, steps, seed)
 
 
-def test_tinymt_walk_with_parameter_table_and_rectangles(rt, orc):
+@pytest.mark.parametrize("engine", [1, 2])
+def test_tinymt_walk_with_parameter_table_and_rectangles(rt, orc, engine):
     D = rt.DominoTiler
     rng = np.random.default_rng(3)
-    for rows, cols in [(4, 6), (13, 8), (30, 31)]:
+    for rows, cols in [(4, 6), (13, 8), (30, 31), (200, 90)]:
         d = D.Rectangle(rows, cols) if (rows * cols) % 2 == 0 else D.Rectangle(rows, cols + 1)
         t0 = D.MaxTiling(d)
         n = int(np.sqrt(t0.size))
         params = rng.integers(0, 2**32, size=(n * n // 2, 3), dtype=np.uint64).astype(np.uint32)
-        tiler = rt.DominoTiler(rule="plain")
+        tiler = rt.DominoTiler(rule="plain", engine=engine)
         tiler.LoadTinyMT(params)
         g = t0.copy()
         tiler.Walk(g, 150, 77)
@@ -93,7 +94,8 @@ def test_tinymt_walk_with_parameter_table_and_rectangles(rt, orc):
         assert np.array_equal(g, o)
 
 
-def test_tinymt_epochs_match_oracle(rt, orc):
+@pytest.mark.parametrize("engine", [1, 2])
+def test_tinymt_epochs_match_oracle(rt, orc, engine):
     D = rt.DominoTiler
     d = D.AztecDiamond(33)
     t0 = D.MinTiling(d)
@@ -101,20 +103,21 @@ def test_tinymt_epochs_match_oracle(rt, orc):
     steps, seeds = [100, 0, 37, 256], [5, 6, 2**32 + 7, -3]
     for rule in range(4):
         g = t0.copy()
-        _tiler(rt, rule).Walk(g, steps, seeds)
+        _tiler(rt, rule, engine=engine).Walk(g, steps, seeds)
         o = t0.copy()
         orc.walk_epochs_tinymt(o, n, steps, seeds, rule=rule)
         assert np.array_equal(g, o), rule
 
 
+@pytest.mark.parametrize("engine", [1, 2])
 @pytest.mark.parametrize("rule", [0, 1, 2, 3])
-def test_fast_walk_matches_oracle(rt, orc, rule):
+def test_fast_walk_matches_oracle(rt, orc, rule, engine):
     D = rt.DominoTiler
     for order, steps, seed, stream in [(3, 50, 1, 0), (20, 301, 2**40 + 5, 17), (47, 200, 9, 65535)]:
         d = D.AztecDiamond(order)
         t0 = D.MaxTiling(d)
         n = int(np.sqrt(t0.size))
-        tiler = rt.DominoTiler(rule=RULE_NAMES[rule], rng="fast", a=1.0, b=0.5, fast_stream=stream)
+        tiler = rt.DominoTiler(rule=RULE_NAMES[rule], rng="fast", a=1.0, b=0.5, fast_stream=stream, engine=engine)
         g = t0.copy()
         tiler.Walk(g, steps, seed)
         o = t0.copy()
@@ -122,14 +125,15 @@ def test_fast_walk_matches_oracle(rt, orc, rule):
         assert np.array_equal(g, o), (order, steps)
 
 
+@pytest.mark.parametrize("engine", [1, 2])
 @pytest.mark.parametrize("rule,a,b", [(1, 1.0, 1.0), (3, 1.0, 0.5)])
-def test_fast_cftp_matches_oracle(rt, orc, rule, a, b):
+def test_fast_cftp_matches_oracle(rt, orc, rule, a, b, engine):
     D = rt.DominoTiler
     for order, seed in [(4, 3), (10, 12345)]:
         d = D.AztecDiamond(order)
         tmax, tmin = D.MaxTiling(d), D.MinTiling(d)
         n = int(np.sqrt(tmax.size))
-        tiler = rt.DominoTiler(rule=RULE_NAMES[rule], rng="fast", a=a, b=b)
+        tiler = rt.DominoTiler(rule=RULE_NAMES[rule], rng="fast", a=a, b=b, engine=engine)
         out, stats = tiler.cftp(tmax, tmin, seed, first_steps=8, max_attempts=16)
         ref, attempts, used = orc.cftp_fast(tmax, tmin, n, seed, 0, 8, 16, rule=rule, a=a, b=b)
         assert attempts == stats["attempts"] and 2 * used == stats["final_steps"]
@@ -137,7 +141,8 @@ def test_fast_cftp_matches_oracle(rt, orc, rule, a, b):
         assert _is_valid_tiling(rt, out, d)
 
 
-def test_tinymt_cftp_doubling_schedule_matches_oracle(rt, orc):
+@pytest.mark.parametrize("engine", [1, 2])
+def test_tinymt_cftp_doubling_schedule_matches_oracle(rt, orc, engine):
     D = rt.DominoTiler
     d = D.AztecDiamond(8)
     tmax, tmin = D.MaxTiling(d), D.MinTiling(d)
@@ -145,7 +150,8 @@ def test_tinymt_cftp_doubling_schedule_matches_oracle(rt, orc):
     for schedule in (0, 1):
         # schedule 0 (the reference's 128 + 256k look-back) coalesces here after 13 attempts,
         # schedule 1 (doubling) after 4.
-        out, stats = rt.DominoTiler(rule="cftp_twoperiodic", a=1.0, b=0.5).cftp(tmax, tmin, 99, 128, schedule, 25)
+        tiler = rt.DominoTiler(rule="cftp_twoperiodic", a=1.0, b=0.5, engine=engine)
+        out, stats = tiler.cftp(tmax, tmin, 99, 128, schedule, 25)
         ref, attempts, total = orc.cftp_tinymt(tmax, tmin, n, 99, 128, schedule, 25, rule=3, a=1.0, b=0.5)
         assert attempts == stats["attempts"] and total == stats["total_steps"] and np.array_equal(out, ref)
 
@@ -172,18 +178,35 @@ def test_sampler_api(rt):
     s.close()
 
 
-def test_full_size_order_1024_matches_threaded_oracle(rt, orc):
-    """Order-1024 Aztec diamond (N = 2054): 24 TinyMT steps of the two-periodic CFTP rule
+@pytest.mark.parametrize("engine", [1, 2])
+def test_full_size_order_1024_matches_threaded_oracle(rt, orc, engine):
+    """Order-1024 Aztec diamond (N = 2054): 40 TinyMT steps of the two-periodic CFTP rule
     equal the oracle bit for bit."""
     D = rt.DominoTiler
     d = D.AztecDiamond(1024)
     t0 = D.MaxTiling(d)
     n = int(np.sqrt(t0.size))
     g = t0.copy()
-    rt.DominoTiler(rule="cftp_twoperiodic", a=1.0, b=0.5).Walk(g, 24, 1)
+    rt.DominoTiler(rule="cftp_twoperiodic", a=1.0, b=0.5, engine=engine).Walk(g, 40, 1)
     o = t0.copy()
-    orc.walk_tinymt(o, n, 24, 1, rule=3, a=1.0, b=0.5, threads=8)
+    orc.walk_tinymt(o, n, 40, 1, rule=3, a=1.0, b=0.5, threads=8)
     assert np.array_equal(g, o)
+
+
+def test_inconsistent_tiling_takes_the_per_half_sweep_path(rt, orc):
+    """A tiling whose edge bits disagree is swept exactly as the reference does (its
+    rebuild overwrites such sites); the resident engine declines it."""
+    D = rt.DominoTiler
+    t0 = D.MaxTiling(D.AztecDiamond(12))
+    n = int(np.sqrt(t0.size))
+    t0[5 * n + 5] ^= 8
+    g = t0.copy()
+    rt.DominoTiler(rule="plain").Walk(g, 31, 4)
+    o = t0.copy()
+    orc.walk_tinymt(o, n, 31, 4, rule=0)
+    assert np.array_equal(g, o)
+    with pytest.raises(rt.RTError):
+        rt.DominoTiler(rule="plain", engine=2).Walk(t0.copy(), 3, 4)
 
 
 def test_full_size_order_1024_properties(rt):
