@@ -229,19 +229,28 @@ def run_ours(args) -> None:
     # Chains 0, 1 are swept; chains 2, 3 keep the extremal start states.
     s.set_active(2)
 
-    def one_step(k: int) -> tuple[int, int]:
+    info = s.engine_info()
+
+    def one_step(k: int, kev=None) -> tuple[int, int]:
         s.copy_chain(0, 2)
         s.copy_chain(1, 3)
         if args.mode == "tinymt":
             cols = rt.mt19937_colours(int(seeds[k]), HALF_SWEEPS)
             s.seed(int(seeds[k]))
+            if kev:
+                kev[0].record(stream)
             s.run(cols)
         else:
             cols = np.array([1, 0] * (HALF_SWEEPS // 2), np.uint8)
+            if kev:
+                kev[0].record(stream)
             s.run_fast(int(seeds[k]), -HALF_SWEEPS, HALF_SWEEPS)
+        if kev:
+            kev[1].record(stream)
         return _attempts(cols, interior), int(np.count_nonzero(cols))
 
     ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    kev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
     for k in range(args.warmup):
         one_step(k)
         s.diff(0, 1)
@@ -256,7 +265,7 @@ def run_ours(args) -> None:
             torch.cuda.current_stream(dev).synchronize()
             with torch.cuda.stream(stream):
                 ev[k][0].record(stream)
-                a, _ = one_step(args.warmup + k)
+                a, _ = one_step(args.warmup + k, kev[k])
                 ev[k][1].record(stream)
             attempts += a
             s.diff(0, 1)
@@ -268,20 +277,33 @@ def run_ours(args) -> None:
     value = total_attempts / sec
     clocks = clk.summary()
 
-    # Roofline of the half-sweep: algorithmic bytes per half-sweep over its average time.
+    # Roofline of the sweep kernel.  Algorithmic bytes: 3 B per flip attempt (read and write
+    # the active u8 site, write the passive one), plus TinyMT generator state where it moves
+    # through memory: 32 B per generator per half-sweep on the per-half-sweep engine (every
+    # generator of the grid), 32 B per flip-candidate generator per launch on the resident
+    # engine (loaded once, stored once).
+    kms = sum(e0.elapsed_time(e1) for e0, e1 in kev)
     half_sweeps = args.steps * HALF_SWEEPS
-    t_half = (ms / 1e3) / half_sweeps
     cells = (n - 2) * (n // 2 - 2)
-    tiling_bytes = 3 * (attempts / half_sweeps)  # 3 B per flip attempt (u8 state), both chains
-    gen_bytes = 32 * cells if args.mode == "tinymt" else 0  # generator state read + write
-    algo_bytes = tiling_bytes + gen_bytes
+    tiling_bytes_per_half = 3 * (attempts / half_sweeps)
     peaks = _peaks()
-    achieved = algo_bytes / t_half / 1e9
-    traffic = _traffic_from_profile(args.mode)
+    if info["engine"] == 2:
+        kernel = "k_persist (resident cooperative sweep, one launch per step)"
+        launches_timed = args.steps
+        gen = 32 * info["units"] if args.mode == "tinymt" else 0
+        algo_bytes = tiling_bytes_per_half * HALF_SWEEPS + gen
+    else:
+        kernel = "k_rotate_tmt + k_update (one pair per half-sweep)"
+        launches_timed = half_sweeps
+        gen = 32 * cells if args.mode == "tinymt" else 0
+        algo_bytes = tiling_bytes_per_half + gen
+    t_launch = (kms / 1e3) / launches_timed
+    achieved = algo_bytes / t_launch / 1e9
+    traffic = _traffic_from_profile(args.mode, info["engine"])
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
                 "frac": achieved / peaks["hbm_gbs"], "traffic": traffic, "peak_source": peaks["source"],
-                "kernel": "domino half-sweep (rotate + update)", "algorithmic_bytes_per_launch": algo_bytes,
-                "launch_us": t_half * 1e6}
+                "kernel": kernel, "algorithmic_bytes_per_launch": algo_bytes, "launch_us": t_launch * 1e6,
+                "half_sweep_us": (kms / 1e3) / half_sweeps * 1e6, "engine": info}
 
     # e2e: one attempt through the C ABI from pinned host buffers, copies included.
     if True:
@@ -346,11 +368,11 @@ def main() -> None:
         run_ours(args)
 
 
-def _traffic_from_profile(mode: str):
-    """DRAM bytes per half-sweep from the committed ncu summary, when one exists."""
-    p = ROOT / "profiles" / f"domino_halfsweep_{mode}_traffic.json"
+def _traffic_from_profile(mode: str, engine: int):
+    """DRAM bytes per launch of the sweep kernel from the committed ncu summary, if any."""
+    p = ROOT / "profiles" / "traffic.json"
     if p.exists():
-        return json.loads(p.read_text()).get("dram_bytes_per_half_sweep")
+        return json.loads(p.read_text()).get(f"{mode}_engine{engine}")
     return None
 
 

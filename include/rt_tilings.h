@@ -171,6 +171,10 @@ RT_API void* rt_dm_sampler_stream(rt_dm_sampler* s);
 RT_API int64_t rt_dm_sampler_interior_vertices(rt_dm_sampler* s);
 /* Kernels launched by this sampler since creation. */
 RT_API int64_t rt_dm_sampler_launches(rt_dm_sampler* s);
+/* The engine the next run will use: out4 = {engine (1 per-half-sweep kernels, 2 resident
+   persistent kernel), flip-candidate units held by the persistent kernel, CTAs (bands),
+   units per thread}. */
+RT_API rt_status rt_dm_sampler_engine_info(rt_dm_sampler* s, int64_t* out4);
 
 /* ---- diagnostics ---------------------------------------------------------------------
    The acceptance intervals a rule compiles to: for c = (row & 1) | (colour << 1),

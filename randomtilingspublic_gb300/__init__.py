@@ -101,6 +101,7 @@ _SIGNATURES = {
     "rt_dm_sampler_stream": (C.c_void_p, [_P]),
     "rt_dm_sampler_interior_vertices": (C.c_int64, [_P]),
     "rt_dm_sampler_launches": (C.c_int64, [_P]),
+    "rt_dm_sampler_engine_info": (C.c_int32, [_P, _P]),
     "rt_domino_rule_table": (C.c_int32, [C.c_int32, C.c_int32, C.c_double, C.c_double, _P]),
 }
 
@@ -389,6 +390,11 @@ class DominoSampler:
     @property
     def launches(self) -> int:
         return lib().rt_dm_sampler_launches(self.h)
+
+    def engine_info(self) -> dict:
+        out = np.zeros(4, np.int64)
+        _check(lib().rt_dm_sampler_engine_info(self.h, _ptr(out)))
+        return {"engine": int(out[0]), "units": int(out[1]), "bands": int(out[2]), "units_per_thread": int(out[3])}
 
 
 def mt19937_colours(seed: int, steps: int, skip: int = 0) -> np.ndarray:

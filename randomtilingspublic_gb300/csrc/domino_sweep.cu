@@ -487,6 +487,21 @@ RT_API int64_t rt_dm_sampler_interior_vertices(rt_dm_sampler* s) {
   return (s && s->impl) ? s->impl->interior[0] + s->impl->interior[1] : -1;
 }
 RT_API int64_t rt_dm_sampler_launches(rt_dm_sampler* s) { return (s && s->impl) ? s->impl->launches : -1; }
+RT_API rt_status rt_dm_sampler_engine_info(rt_dm_sampler* s, int64_t* out4) {
+  RT_SAMPLER(s);
+  if (!out4) return fail(RT_ERR_INVALID_ARGUMENT, "engine_info: out is NULL");
+  DmSampler& d = *s->impl;
+  bool pers = false;
+  if (rt_status st = d.use_persistent(&pers)) return st;
+  int64_t units = 0;
+  if (pers)
+    for (const DmBand& b : d.persist->plan.bands) units += b.units;
+  out4[0] = pers ? 2 : 1;
+  out4[1] = units;
+  out4[2] = pers ? (int64_t)d.persist->plan.bands.size() : 0;
+  out4[3] = pers ? d.persist->plan.K : 0;
+  return RT_OK;
+}
 
 // ---- walks ---------------------------------------------------------------------------------
 

@@ -136,3 +136,23 @@ def test_tinymt_parameter_file_reader(rt, tmp_path):
     assert got.tolist() == [[0x8F7011EE, 0xFC78FF1F, 0x3793FDFF], [1, 2, 3]]
     with pytest.raises(ValueError):
         rt.read_tinymt_params(p, 3)
+
+
+def test_cpp_dropin_header_compiles_and_runs(rt, tmp_path):
+    """include/rt_tilings.hpp used as the reference's own examples use DominoTiler."""
+    import shutil
+    import subprocess
+
+    if not shutil.which("g++"):
+        pytest.skip("no g++")
+    exe = tmp_path / "dropin"
+    libdir = str(rt.LIB_PATH.parent)
+    subprocess.run(["g++", "-std=c++17", "-O1", f"-I{ROOT / 'include'}", str(ROOT / "tests/cpp/dropin_host.cpp"),
+                    f"-L{libdir}", "-l:librt_tilings.so", f"-Wl,-rpath,{libdir}", "-o", str(exe)], check=True)
+    out = subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout
+    D = rt.DominoTiler
+    d = D.AztecDiamond(5)
+    tmax, tmin = D.MaxTiling(d), D.MinTiling(d)
+    n = int(np.sqrt(tmax.size))
+    assert f"side {n} max {int(tmax.sum())} min {int(tmin.sum())} roundtrip 1" in out
+    assert f"untileable status {rt.RT_ERR_NOT_TILEABLE}" in out
