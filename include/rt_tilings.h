@@ -176,6 +176,32 @@ RT_API int64_t rt_dm_sampler_launches(rt_dm_sampler* s);
    units per thread}. */
 RT_API rt_status rt_dm_sampler_engine_info(rt_dm_sampler* s, int64_t* out4);
 
+/* ---- allocation-free sweep -------------------------------------------------------------
+   No counterpart in the reference.  For callers that cannot allocate device memory (a
+   host application that hands the library a fixed device arena up front, or code that must
+   not allocate inside a latency-critical loop or under a hard memory cap): runs steps
+   half-sweeps of the resident sweep kernel on chains the caller already holds on the
+   device, and allocates nothing - no cudaMalloc, cudaFree or allocating library call.
+   The kernel's scratch (neighbour exchange rows, flags, band plan, colours) is a fixed
+   static device array of about 1.2 MiB that every GPU loading the library keeps until the
+   process exits.
+   Layout: dev_chains holds n_chains chains, each two colour arrays (white then black, black
+   being the vertices with i + j even) of N rows x P bytes, P = N/2 rounded up to a multiple
+   of 16, column m of row i holding vertex (i, 2m + ((i + colour + 1) & 1))... i.e. the
+   vertex of that colour in columns 2m, 2m+1.  dev_generators (TinyMT mode) holds one uint4
+   state per site (i, m), i in [1, N-2], m in [1, N/2-2], index (i-1)*(N/2-2) + (m-1),
+   advanced in place; colours (host) gives the colour of each half-sweep (1 black, 0 white).
+   Fast mode ignores both and runs half-sweeps h0 .. h0+steps-1 keyed by fast_seed.
+   Limits: N <= 1024, n_chains <= 2, steps <= 65536 per call; larger requests return
+   RT_ERR_INVALID_ARGUMENT.  Per-generator parameter tables are not supported here.
+   The first call on a device takes the array's device address (cudaGetSymbolAddress) with
+   that device current, so make it before any stream capture.  Every call shares the array
+   and clears the flags it relies on; calls that overlap on the GPU race on it, so order them
+   (one stream, or synchronise between calls).  Synchronous: returns after the sweep ends. */
+RT_API rt_status rt_dm_sweep_noalloc(uint8_t* dev_chains, void* dev_generators, int32_t n_side, int32_t n_chains,
+                                     const uint8_t* colours, int64_t steps, uint64_t fast_seed, int64_t h0,
+                                     const rt_walk_opts* opts);
+
 /* ---- diagnostics ---------------------------------------------------------------------
    The acceptance intervals a rule compiles to: for c = (row & 1) | (colour << 1),
    out16[4c .. 4c+3] = {lo_up, width_up, lo_down, width_down}; a site in state 3 flips to 12

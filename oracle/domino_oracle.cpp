@@ -756,3 +756,20 @@ int orc_dm_rotate_fast(int e, uint32_t u, int rule, int i, int t, double a, doub
 }
 
 }  // extern "C"
+
+extern "C" {
+
+// Seeded TinyMT generator states (default parameters) for generators 0 .. count-1 seeded
+// with seed + k, as InitTinyMT does (dominokernel.cl:33-40): out is count x {s0, s1, s2, s3}.
+void orc_tmt_seed_states(uint32_t seed, long count, uint32_t* out) {
+  for (long k = 0; k < count; ++k) {
+    oracle::TinyMT32 g{0, 0, 0, 0, oracle::kTmtMat1, oracle::kTmtMat2, oracle::kTmtTmat};
+    oracle::tmt_init(g, seed + (uint32_t)k);
+    out[4 * k] = g.s0;
+    out[4 * k + 1] = g.s1;
+    out[4 * k + 2] = g.s2;
+    out[4 * k + 3] = g.s3;
+  }
+}
+
+}  // extern "C"

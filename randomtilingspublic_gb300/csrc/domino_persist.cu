@@ -513,3 +513,12 @@ rt_status PersistEngine::check_error(DmSampler& s) {
 }
 
 }  // namespace rt
+
+namespace rt {
+
+void* dm_persist_kernel_ptr(int mode, int K, bool params) {
+  if (mode == RT_RNG_TINYMT) return params ? kernel_for<RT_RNG_TINYMT, true>(K) : kernel_for<RT_RNG_TINYMT, false>(K);
+  return kernel_for<RT_RNG_FAST, false>(K);
+}
+
+}  // namespace rt

@@ -70,6 +70,11 @@ struct PersistEngine {
   rt_status check_error(DmSampler& s);
 };
 
+// Threads per CTA of the resident kernel and its entry for (rng mode, units per thread K,
+// per-generator parameter table).
+constexpr int kPersistThreads = 1024;
+void* dm_persist_kernel_ptr(int mode, int K, bool params);
+
 // True when every edge bit agrees with the bit of the vertex across it and no edge leaves
 // the array: then rebuilding a colour from the other reproduces it, which the persistent
 // engine relies on outside its windows.

@@ -36,6 +36,7 @@ _SIG = {
                                    C.c_double, C.c_int, _P, _P]),
     "orc_tinymt_u32": (C.c_uint, [C.c_uint, C.c_uint, C.c_uint, C.c_uint, C.c_int]),
     "orc_philox4x32_10": (None, [_P, _P, _P]),
+    "orc_tmt_seed_states": (None, [C.c_uint, _L, _P]),
 }
 
 _lib = None
@@ -189,4 +190,10 @@ def philox4x32_10(ctr, key):
     k = np.ascontiguousarray(np.asarray(key, np.uint32))
     out = np.zeros(4, np.uint32)
     lib().orc_philox4x32_10(_p(c), _p(k), _p(out))
+    return out
+
+
+def tmt_seed_states(seed: int, count: int) -> np.ndarray:
+    out = np.zeros((count, 4), np.uint32)
+    lib().orc_tmt_seed_states(seed & 0xFFFFFFFF, count, _p(out))
     return out
