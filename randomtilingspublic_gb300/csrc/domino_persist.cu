@@ -32,23 +32,19 @@ namespace rt {
 
 namespace {
 
-constexpr int kThreads = 1024;
+constexpr int kThreads = kPersistThreads;
+constexpr int kWorkers = kThreads - 32;  // warp 0 handles the neighbour exchange
+constexpr uint32_t kNoUnit = 0xffffffffu;
 
-__device__ __forceinline__ uint8_t flip_site(uint32_t e, uint32_t u, uint32_t lo_up, uint32_t w_up, uint32_t lo_dn,
-                                             uint32_t w_dn) {
-  if (e == 3u) return (u - lo_up) < w_up ? 12 : 3;
-  if (e == 12u) return (u - lo_dn) < w_dn ? 3 : 12;
-  return (uint8_t)e;
+// Byte-parallel flip of NCH coupled chains of one site (one byte per chain in x): a byte
+// equal to 3 becomes 12 when up is all-ones, a byte equal to 12 becomes 3 when dn is, both
+// by XOR with 15.
+__device__ __forceinline__ uint32_t flip_bytes(uint32_t x, uint32_t up, uint32_t dn, uint32_t bytes_mask) {
+  const uint32_t eq3 = __vcmpeq4(x, 0x03030303u), eq12 = __vcmpeq4(x, 0x0c0c0c0cu);
+  return x ^ (((eq3 & up) | (eq12 & dn)) & 0x0f0f0f0fu & bytes_mask);
 }
 
-struct Smem {
-  uint8_t* p;
-  int R, W;  // rows (band + 2 halo), window bytes
-  // byte of chain ch, colour t, colour-array row i (band-relative index ri = i - r0 + 1), window column x
-  __device__ uint8_t* row(int ch, int t, int ri) const { return p + ((size_t)(ch * 2 + t) * R + ri) * W; }
-};
-
-// Waits until *flag >= target; returns false when the wait gave up or another CTA failed.
+// Waits until *flag >= target; false when the wait gave up or another CTA failed.
 __device__ bool wait_flag(unsigned* flag, unsigned target, int* error, long max_spin) {
   cuda::atomic_ref<unsigned, cuda::thread_scope_device> f(*flag);
   cuda::atomic_ref<int, cuda::thread_scope_device> err(*error);
@@ -60,202 +56,307 @@ __device__ bool wait_flag(unsigned* flag, unsigned target, int* error, long max_
       err.compare_exchange_strong(zero, 1, cuda::memory_order_relaxed);
       return false;
     }
-    __nanosleep(64);
+    if (it > 64) __nanosleep(32);
   }
   return true;
 }
 
-template <int kMode, int K, bool kParams>
+__device__ __forceinline__ void workers_sync() { asm volatile("bar.sync 1, %0;" ::"r"(kWorkers) : "memory"); }
+
+// Shared memory: two colour planes, each R rows (band rows plus one halo row above and
+// below) of Wb = W * NCH bytes; cell x of a row holds its NCH chains in consecutive bytes.
+template <int NCH>
+struct Planes {
+  uint8_t* p;
+  int R, Wb;
+  __device__ uint8_t* row(int t, int ri) const { return p + ((size_t)t * R + ri) * Wb; }
+};
+
+// Rebuilds the passive colour 1-t of band row ri (colour-array row i) from the active
+// colour t: bit 1 from the site above (its bit 2), bit 2 from below (its bit 1), bit 4 from
+// the left active neighbour (its 8), bit 8 from the right one (its 4); left/right are
+// columns m-1/m or m/m+1 by the parity of i+t.  Word w holds 4/NCH cells x NCH chains.
+template <int NCH>
+__device__ __forceinline__ void rebuild_word(const Planes<NCH>& pl, int t, int ri, int i, int w, int words, int wlo,
+                                             int cols) {
+  const uint32_t* A0 = reinterpret_cast<const uint32_t*>(pl.row(t, ri - 1));
+  const uint32_t* A1 = reinterpret_cast<const uint32_t*>(pl.row(t, ri));
+  const uint32_t* A2 = reinterpret_cast<const uint32_t*>(pl.row(t, ri + 1));
+  uint32_t* Pw = reinterpret_cast<uint32_t*>(pl.row(1 - t, ri));
+  const uint32_t cur = A1[w];
+  uint32_t left, right;
+  if ((i + t) & 1) {
+    const uint32_t next = w + 1 < words ? A1[w + 1] : 0u;
+    left = cur;
+    right = __funnelshift_rc(cur, next, 8 * NCH);
+  } else {
+    const uint32_t prev = w > 0 ? A1[w - 1] : 0u;
+    left = __funnelshift_lc(prev, cur, 8 * NCH);
+    right = cur;
+  }
+  const uint32_t v = ((A0[w] >> 1) & 0x01010101u) | ((A2[w] & 0x01010101u) << 1) | ((left & 0x08080808u) >> 1) |
+                     ((right & 0x04040404u) << 1);
+  // Kept as they are: the window's first and last cell (they never change and lack a
+  // neighbour here) and columns outside [1, cols], which the reference never rebuilds.
+  constexpr int kCells = 4 / NCH;
+  constexpr uint32_t kCellMask = NCH == 4 ? 0xffffffffu : ((1u << (8 * NCH)) - 1u);
+  uint32_t keep = 0;
+  const int c0 = wlo + kCells * w;
+#pragma unroll
+  for (int k = 0; k < kCells; ++k) {
+    const int c = c0 + k;
+    const bool edge = (w == 0 && k == 0) || (w == words - 1 && k == kCells - 1);
+    if (edge || c < 1 || c > cols) keep |= kCellMask << (8 * NCH * k);
+  }
+  Pw[w] = (v & ~keep) | (Pw[w] & keep);
+}
+
+template <int kMode, int K, bool kParams, int NCH>
 __global__ void __launch_bounds__(kThreads, 1) k_persist(PersistArgs a) {
   extern __shared__ __align__(16) uint8_t smem_raw[];
+  __shared__ uint4 s_rule[4];
   __shared__ int s_abort;
   const int b = blockIdx.x;
   const DmBand band = a.bands[b];
-  const int nch = a.nch;
-  const int R = band.r1 - band.r0 + 2, W = band.whi - band.wlo, words = W / 4;
-  Smem sm{smem_raw, R, W};
-  const int tid = threadIdx.x;
+  const int R = band.r1 - band.r0 + 2, W = band.whi - band.wlo, Wb = W * NCH;
+  const int words = Wb / 4, vecs = Wb / 16;
+  const Planes<NCH> pl{smem_raw, R, Wb};
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
 
-  // Load rows r0-1 .. r1 of both colours of every chain (window only).
-  for (int idx = tid; idx < nch * 2 * R * words; idx += kThreads) {
-    const int w = idx % words, rest = idx / words, ri = rest % R, ct = rest / R;
-    const int ch = ct >> 1, t = ct & 1;
-    const uint8_t* g = a.base + (size_t)ch * a.chain_stride + (size_t)t * a.colour_stride +
-                       (size_t)(band.r0 - 1 + ri) * a.P + band.wlo;
-    reinterpret_cast<uint32_t*>(sm.row(ch, t, ri))[w] = reinterpret_cast<const uint32_t*>(g)[w];
+  // Load rows r0-1 .. r1 of both colours, interleaving the chains.
+  for (int rr = warp; rr < 2 * R; rr += kThreads / 32) {
+    const int t = rr / R, ri = rr - t * R;
+    uint8_t* dst = pl.row(t, ri);
+    for (int x = lane; x < W; x += 32) {
+#pragma unroll
+      for (int ch = 0; ch < NCH; ++ch)
+        dst[x * NCH + ch] = a.base[(size_t)ch * a.chain_stride + (size_t)t * a.colour_stride +
+                                   (size_t)(band.r0 - 1 + ri) * a.P + band.wlo + x];
+    }
   }
+  if (tid < 4) s_rule[tid] = make_uint4(a.rule.lo_up[tid], a.rule.w_up[tid], a.rule.lo_dn[tid], a.rule.w_dn[tid]);
   if (tid == 0) s_abort = 0;
 
-  // This thread's units: list index tid + s * kThreads, rows enumerated in order.
-  uint32_t pos[K];
+  // Worker thread wt holds units wt + s * kWorkers: the band's first row, its last row,
+  // then the rows between (a.row_prefix in that order).  Per unit: the byte offset of its
+  // (first) site in a colour plane, its row parity (bit 31) and, in fast mode, the sites of
+  // its quad inside [1, cols] (bits 24..27); the generator state (TinyMT) and, where a draw
+  // needs it, the position (i << 16) | u.
+  constexpr bool kNeedWhere = (kMode != RT_RNG_TINYMT) || kParams;
+  uint32_t unit[K];
+  uint32_t where[kNeedWhere ? K : 1];
   uint4 st[K];
-#pragma unroll
-  for (int s = 0; s < K; ++s) {
-    const int c = tid + s * kThreads;
-    pos[s] = 0xffffffffu;
-    st[s] = make_uint4(0, 0, 0, 0);
-    if (c < band.units) {
-      // binary search the band's rows for the one holding unit c
-      int lo = band.r0, hi = band.r1 - 1;
+  int boundary_slots = 0;
+  const bool worker = warp > 0;
+  const int wt = tid - 32;
+  auto decode = [&](int c, int& i, int& u) {
+    if (c < band.nb_first) {
+      i = band.r0;
+    } else if (c < band.nb_boundary) {
+      i = band.r1 - 1;
+    } else {
+      int lo = band.r0 + 1, hi = band.r1 - 2;
       while (lo < hi) {
         const int mid = (lo + hi + 1) >> 1;
         if (a.row_prefix[mid] <= c) lo = mid;
         else hi = mid - 1;
       }
-      const int i = lo, u = a.row_lo[i] + (c - a.row_prefix[i]);
-      pos[s] = ((uint32_t)i << 16) | (uint32_t)u;
+      i = lo;
+    }
+    u = a.row_lo[i] + (c - a.row_prefix[i]);
+  };
+#pragma unroll
+  for (int s = 0; s < K; ++s) {
+    unit[s] = kNoUnit;
+    if (kNeedWhere) where[s] = 0;
+    st[s] = make_uint4(0, 0, 0, 0);
+    const int c = wt + s * kWorkers;
+    if (worker && c < band.units) {
+      int i, u;
+      decode(c, i, u);
+      const int ri = i - band.r0 + 1;
+      const int m0 = kMode == RT_RNG_TINYMT ? u : 4 * u;
+      uint32_t valid = 0;
+      if (kMode != RT_RNG_TINYMT) {
+#pragma unroll
+        for (int k4 = 0; k4 < 4; ++k4)
+          if (m0 + k4 >= 1 && m0 + k4 <= a.cols) valid |= 1u << k4;
+      }
+      unit[s] = (uint32_t)(ri * Wb + (m0 - band.wlo) * NCH) | (valid << 24) | ((uint32_t)(i & 1) << 31);
+      if (kNeedWhere) where[s] = ((uint32_t)i << 16) | (uint32_t)u;
       if (kMode == RT_RNG_TINYMT) st[s] = a.tmt[(int64_t)(i - 1) * a.cols + (u - 1)];
     }
   }
+  boundary_slots = (band.nb_boundary + kWorkers - 1) / kWorkers;
   __syncthreads();
 
   const int up = b - 1, dn = b + 1;
-  const DmBand bu = up >= 0 ? a.bands[up] : band, bd = dn < a.nbands ? a.bands[dn] : band;
-  for (int64_t h = 0; h < a.steps; ++h) {
-    const int64_t hh = a.h0 + h;
-    const int t = (kMode == RT_RNG_TINYMT) ? (a.colours[h] ? 1 : 0) : ((hh & 1) ? 0 : 1);
-    // 1. flip
-#pragma unroll
-    for (int s = 0; s < K; ++s) {
-      if (pos[s] == 0xffffffffu) continue;
-      const int i = (int)(pos[s] >> 16), u = (int)(pos[s] & 0xffffu);
-      const int c = (i & 1) | (t << 1);
-      const uint32_t lo_up = a.rule.lo_up[c], w_up = a.rule.w_up[c], lo_dn = a.rule.lo_dn[c], w_dn = a.rule.w_dn[c];
-      const int ri = i - band.r0 + 1;
-      if (kMode == RT_RNG_TINYMT) {
-        uint32_t m1 = kTmtMat1, m2 = kTmtMat2, tm = kTmtTmat;
-        if (kParams) {
-          const uint4 p = __ldg(&a.tmt_params[(int64_t)(i - 1) * a.cols + (u - 1)]);
-          m1 = p.x; m2 = p.y; tm = p.z;
-        }
-        const uint32_t r = tmt_next_u23(st[s], m1, m2, tm);
-        const int x = u - band.wlo;
-        for (int ch = 0; ch < nch; ++ch) {
-          uint8_t* q = sm.row(ch, t, ri) + x;
-          const uint32_t e = *q;
-          const uint8_t n = flip_site(e, r, lo_up, w_up, lo_dn, w_dn);
-          if (n != e) *q = n;
-        }
+
+  auto flip_unit = [&](int s, int t, int h) {
+    const uint32_t pk = unit[s];
+    if (pk == kNoUnit) return;
+    const uint4 rl = s_rule[(pk >> 31) | (t << 1)];
+    uint8_t* q = pl.row(t, 0) + (pk & 0xffffffu);
+    if (kMode == RT_RNG_TINYMT) {
+      uint32_t m1 = kTmtMat1, m2 = kTmtMat2, tm = kTmtTmat;
+      if (kParams) {
+        const int i = (int)(where[kNeedWhere ? s : 0] >> 16), u = (int)(where[kNeedWhere ? s : 0] & 0xffffu);
+        const uint4 p = __ldg(&a.tmt_params[(int64_t)(i - 1) * a.cols + (u - 1)]);
+        m1 = p.x; m2 = p.y; tm = p.z;
+      }
+      const uint32_t r = tmt_next_u23(st[s], m1, m2, tm);
+      const uint32_t upm = (r - rl.x) < rl.y ? 0xffffffffu : 0u, dnm = (r - rl.z) < rl.w ? 0xffffffffu : 0u;
+      if (NCH == 1) {
+        const uint32_t x = *q, y = flip_bytes(x, upm, dnm, 0xffu);
+        if (y != x) *q = (uint8_t)y;
+      } else if (NCH == 2) {
+        uint16_t* q2 = reinterpret_cast<uint16_t*>(q);
+        const uint32_t x = *q2, y = flip_bytes(x, upm, dnm, 0xffffu);
+        if (y != x) *q2 = (uint16_t)y;
       } else {
-        const uint4 r4 = fast_quad(a.fast_seed, a.fast_stream, hh, (uint32_t)i, (uint32_t)u);
-        const uint32_t rr[4] = {r4.x, r4.y, r4.z, r4.w};
-        for (int ch = 0; ch < nch; ++ch) {
-          uint8_t* rowp = sm.row(ch, t, ri);
+        uint32_t* q4 = reinterpret_cast<uint32_t*>(q);
+        const uint32_t x = *q4, y = flip_bytes(x, upm, dnm, 0xffffffffu);
+        if (y != x) *q4 = y;
+      }
+    } else {
+      const uint4 r4 = fast_quad(a.fast_seed, a.fast_stream, a.h0 + h, where[kNeedWhere ? s : 0] >> 16,
+                                 where[kNeedWhere ? s : 0] & 0xffffu);
+      const uint32_t rr[4] = {r4.x, r4.y, r4.z, r4.w};
+      const uint32_t valid = (pk >> 24) & 0xfu;
 #pragma unroll
-          for (int k4 = 0; k4 < 4; ++k4) {
-            const int m = 4 * u + k4;
-            if (m < 1 || m > a.cols) continue;
-            uint8_t* q = rowp + (m - band.wlo);
-            const uint32_t e = *q;
-            const uint8_t n = flip_site(e, rr[k4], lo_up, w_up, lo_dn, w_dn);
-            if (n != e) *q = n;
-          }
+      for (int k4 = 0; k4 < 4; ++k4) {
+        if (!((valid >> k4) & 1u)) continue;
+        const uint32_t upm = (rr[k4] - rl.x) < rl.y ? 0xffffffffu : 0u, dnm = (rr[k4] - rl.z) < rl.w ? 0xffffffffu : 0u;
+        uint8_t* qk = q + k4 * NCH;
+        if (NCH == 1) {
+          const uint32_t x = *qk, y = flip_bytes(x, upm, dnm, 0xffu);
+          if (y != x) *qk = (uint8_t)y;
+        } else if (NCH == 2) {
+          uint16_t* q2 = reinterpret_cast<uint16_t*>(qk);
+          const uint32_t x = *q2, y = flip_bytes(x, upm, dnm, 0xffffu);
+          if (y != x) *q2 = (uint16_t)y;
+        } else {
+          uint32_t* q4 = reinterpret_cast<uint32_t*>(qk);
+          const uint32_t x = *q4, y = flip_bytes(x, upm, dnm, 0xffffffffu);
+          if (y != x) *q4 = y;
         }
       }
     }
-    __syncthreads();
-    // 2. publish the band's first and last rows of colour t
-    const int slot = (int)(h & 1);
-    for (int idx = tid; idx < 2 * nch * words; idx += kThreads) {
-      const int w = idx % words, rest = idx / words, ch = rest % nch, which = rest / nch;
-      const int ri = which == 0 ? 1 : R - 2;
-      uint8_t* g = a.xbuf + ((((size_t)slot * a.nbands + b) * 2 + which) * nch + ch) * a.P + band.wlo;
-      __stcg(reinterpret_cast<uint32_t*>(g) + w, reinterpret_cast<const uint32_t*>(sm.row(ch, t, ri))[w]);
+  };
+
+  const int rows = R - 2;
+  const int nsteps = (int)a.steps;  // at most 65536 per launch
+  const int par0 = (int)(a.h0 & 1);
+  for (int h = 0; h < nsteps; ++h) {
+    const int t = (kMode == RT_RNG_TINYMT) ? (a.colours[h] ? 1 : 0) : (((par0 ^ h) & 1) ? 0 : 1);
+    const int slot = h & 1;
+    // 1. flip the slots holding the band's first and last rows
+    if (worker) {
+#pragma unroll
+      for (int s = 0; s < K; ++s)
+        if (s < boundary_slots) flip_unit(s, t, h);
     }
-    __threadfence();
     __syncthreads();
-    if (tid == 0) {
-      cuda::atomic_ref<unsigned, cuda::thread_scope_device> f(a.flags[b]);
-      f.store((unsigned)(h + 1), cuda::memory_order_release);
+    if (!worker) {
+      // 2. warp 0: publish the two boundary rows, release the half-sweep count, wait for the
+      //    neighbours, copy their rows into the halo rows.
+      const uint4* top = reinterpret_cast<const uint4*>(pl.row(t, 1));
+      const uint4* bot = reinterpret_cast<const uint4*>(pl.row(t, R - 2));
+      uint4* gtop = reinterpret_cast<uint4*>(a.xbuf + (((size_t)slot * a.nbands + b) * 2 + 0) * a.P * NCH +
+                                             (size_t)band.wlo * NCH);
+      uint4* gbot = reinterpret_cast<uint4*>(a.xbuf + (((size_t)slot * a.nbands + b) * 2 + 1) * a.P * NCH +
+                                             (size_t)band.wlo * NCH);
+      for (int v = lane; v < vecs; v += 32) {
+        __stcg(gtop + v, top[v]);
+        __stcg(gbot + v, bot[v]);
+      }
+      __threadfence();
+      __syncwarp();
       bool ok = true;
-      if (up >= 0) ok = wait_flag(&a.flags[up], (unsigned)(h + 1), a.error, a.max_spin);
-      if (ok && dn < a.nbands) ok = wait_flag(&a.flags[dn], (unsigned)(h + 1), a.error, a.max_spin);
-      s_abort = ok ? 0 : 1;
+      if (lane == 0) {
+        cuda::atomic_ref<unsigned, cuda::thread_scope_device> f(a.flags[b]);
+        f.store((unsigned)(h + 1), cuda::memory_order_release);
+        if (up >= 0) ok = wait_flag(&a.flags[up], (unsigned)(h + 1), a.error, a.max_spin);
+        if (ok && dn < a.nbands) ok = wait_flag(&a.flags[dn], (unsigned)(h + 1), a.error, a.max_spin);
+        s_abort = ok ? 0 : 1;
+      }
+      ok = __shfl_sync(0xffffffffu, ok ? 1 : 0, 0) != 0;
+      if (ok) {
+        if (up >= 0) {
+          const int lo = max(band.wlo, a.bands[up].wlo), hi = min(band.whi, a.bands[up].whi);
+          const uint4* g = reinterpret_cast<const uint4*>(a.xbuf + (((size_t)slot * a.nbands + up) * 2 + 1) * a.P * NCH +
+                                                          (size_t)lo * NCH);
+          uint4* d = reinterpret_cast<uint4*>(pl.row(t, 0) + (lo - band.wlo) * NCH);
+          for (int v = lane; v < (hi - lo) * NCH / 16; v += 32) d[v] = __ldcg(g + v);
+        }
+        if (dn < a.nbands) {
+          const int lo = max(band.wlo, a.bands[dn].wlo), hi = min(band.whi, a.bands[dn].whi);
+          const uint4* g = reinterpret_cast<const uint4*>(a.xbuf + (((size_t)slot * a.nbands + dn) * 2 + 0) * a.P * NCH +
+                                                          (size_t)lo * NCH);
+          uint4* d = reinterpret_cast<uint4*>(pl.row(t, R - 1) + (lo - band.wlo) * NCH);
+          for (int v = lane; v < (hi - lo) * NCH / 16; v += 32) d[v] = __ldcg(g + v);
+        }
+      }
+    } else {
+      // 3. workers: the remaining flips, then the rebuild of the rows that need no halo.
+#pragma unroll
+      for (int s = 0; s < K; ++s)
+        if (s >= boundary_slots) flip_unit(s, t, h);
+      workers_sync();
+      for (int r = warp; r <= rows - 2; r += kWorkers / 32) {  // band rows 1 .. rows-2 (0-based), warps 1..31
+        const int ri = r + 1, i = band.r0 + r;
+        for (int w = lane; w < words; w += 32) rebuild_word<NCH>(pl, t, ri, i, w, words, band.wlo, a.cols);
+      }
     }
     __syncthreads();
     if (s_abort) break;
-    // 3. halo rows from the neighbours (the part inside both windows)
-    {
-      const int ulo = max(band.wlo, bu.wlo), uhi = min(band.whi, bu.whi);
-      const int dlo = max(band.wlo, bd.wlo), dhi = min(band.whi, bd.whi);
-      const int uw = up >= 0 ? max(0, (uhi - ulo) / 4) : 0, dw = dn < a.nbands ? max(0, (dhi - dlo) / 4) : 0;
-      for (int idx = tid; idx < nch * (uw + dw); idx += kThreads) {
-        const int ch = idx % nch, rest = idx / nch;
-        const bool top = rest < uw;
-        const int w = top ? rest : rest - uw;
-        const int nb = top ? up : dn, which = top ? 1 : 0, col = (top ? ulo : dlo) + 4 * w;
-        const uint8_t* g = a.xbuf + ((((size_t)slot * a.nbands + nb) * 2 + which) * nch + ch) * a.P + col;
-        const uint32_t v = __ldcg(reinterpret_cast<const uint32_t*>(g));
-        reinterpret_cast<uint32_t*>(sm.row(ch, t, top ? 0 : R - 1) + (col - band.wlo))[0] = v;
-      }
-    }
-    __syncthreads();
-    // 4. rebuild the passive colour 1-t of rows r0 .. r1-1: bit 1 from the site above (its
-    //    bit 2), bit 2 from below (its bit 1), bit 4 from the left active neighbour (its 8),
-    //    bit 8 from the right one (its 4); left/right are columns m-1/m or m/m+1 by (i+t).
-    const int rows = R - 2;
-    for (int idx = tid; idx < nch * rows * words; idx += kThreads) {
-      const int w = idx % words, rest = idx / words, r = rest % rows, ch = rest / rows;
-      const int ri = r + 1, i = band.r0 + r;
-      const uint32_t* A0 = reinterpret_cast<const uint32_t*>(sm.row(ch, t, ri - 1));
-      const uint32_t* A1 = reinterpret_cast<const uint32_t*>(sm.row(ch, t, ri));
-      const uint32_t* A2 = reinterpret_cast<const uint32_t*>(sm.row(ch, t, ri + 1));
-      uint32_t* Pw = reinterpret_cast<uint32_t*>(sm.row(ch, 1 - t, ri));
-      const uint32_t cur = A1[w];
-      const uint32_t prev = w > 0 ? A1[w - 1] : 0u, next = w + 1 < words ? A1[w + 1] : 0u;
-      uint32_t left, right;
-      if ((i + t) & 1) {  // left = m, right = m + 1
-        left = cur;
-        right = __funnelshift_r(cur, next, 8);
-      } else {            // left = m - 1, right = m
-        left = __funnelshift_l(prev, cur, 8);
-        right = cur;
-      }
-      uint32_t v = ((A0[w] >> 1) & 0x01010101u) | ((A2[w] & 0x01010101u) << 1) | ((left & 0x08080808u) >> 1) |
-                   ((right & 0x04040404u) << 1);
-      // Kept as they are: the window's edge sites (they never change and lack a neighbour
-      // here) and columns outside [1, cols], which the reference never rebuilds.
-      uint32_t keep = 0;
-      if (w == 0) keep |= 0x000000ffu;
-      if (w == words - 1) keep |= 0xff000000u;
-      const int c0 = band.wlo + 4 * w;
-      if (c0 < 1) keep |= 0x000000ffu;
-      if (c0 + 3 > a.cols) {
-#pragma unroll
-        for (int k4 = 0; k4 < 4; ++k4)
-          if (c0 + k4 > a.cols) keep |= 0xffu << (8 * k4);
-      }
-      const uint32_t old = Pw[w];
-      Pw[w] = (v & ~keep) | (old & keep);
+    // 4. rebuild the band's first and last rows (they read the halo rows)
+    for (int r = warp; r < (rows > 1 ? 2 : 1); r += kThreads / 32) {
+      const int rr = r == 0 ? 0 : rows - 1;
+      for (int w = lane; w < words; w += 32) rebuild_word<NCH>(pl, t, rr + 1, band.r0 + rr, w, words, band.wlo, a.cols);
     }
     __syncthreads();
   }
 
   // Write back the band rows of both colours and the generator states.
-  for (int idx = tid; idx < nch * 2 * (R - 2) * words; idx += kThreads) {
-    const int w = idx % words, rest = idx / words, r = rest % (R - 2), ct = rest / (R - 2);
-    const int ch = ct >> 1, t = ct & 1;
-    uint8_t* g = a.base + (size_t)ch * a.chain_stride + (size_t)t * a.colour_stride + (size_t)(band.r0 + r) * a.P +
-                 band.wlo;
-    reinterpret_cast<uint32_t*>(g)[w] = reinterpret_cast<const uint32_t*>(sm.row(ch, t, r + 1))[w];
+  for (int rr = warp; rr < 2 * rows; rr += kThreads / 32) {
+    const int t = rr / rows, r = rr - t * rows;
+    const uint8_t* src = pl.row(t, r + 1);
+    for (int x = lane; x < W; x += 32) {
+#pragma unroll
+      for (int ch = 0; ch < NCH; ++ch)
+        a.base[(size_t)ch * a.chain_stride + (size_t)t * a.colour_stride + (size_t)(band.r0 + r) * a.P + band.wlo + x] =
+            src[x * NCH + ch];
+    }
   }
   if (kMode == RT_RNG_TINYMT) {
 #pragma unroll
     for (int s = 0; s < K; ++s) {
-      if (pos[s] == 0xffffffffu) continue;
-      const int i = (int)(pos[s] >> 16), u = (int)(pos[s] & 0xffffu);
+      if (unit[s] == kNoUnit) continue;
+      int i, u;
+      decode(wt + s * kWorkers, i, u);
       a.tmt[(int64_t)(i - 1) * a.cols + (u - 1)] = st[s];
     }
   }
 }
 
-template <int kMode, bool kParams>
-void* kernel_for(int K) {
+template <int kMode, bool kParams, int NCH>
+void* kernel_for_k(int K) {
   switch (K) {
-    case 1: return (void*)k_persist<kMode, 1, kParams>;
-    case 2: return (void*)k_persist<kMode, 2, kParams>;
-    case 4: return (void*)k_persist<kMode, 4, kParams>;
-    case 8: return (void*)k_persist<kMode, 8, kParams>;
+    case 1: return (void*)k_persist<kMode, 1, kParams, NCH>;
+    case 2: return (void*)k_persist<kMode, 2, kParams, NCH>;
+    case 4: return (void*)k_persist<kMode, 4, kParams, NCH>;
+    case 8: return (void*)k_persist<kMode, 8, kParams, NCH>;
+  }
+  return nullptr;
+}
+
+template <int kMode, bool kParams>
+void* kernel_for(int K, int nch) {
+  switch (nch) {
+    case 1: return kernel_for_k<kMode, kParams, 1>(K);
+    case 2: return kernel_for_k<kMode, kParams, 2>(K);
+    case 4: return kernel_for_k<kMode, kParams, 4>(K);
   }
   return nullptr;
 }
@@ -349,12 +450,22 @@ rt_status PersistPlan::build(const std::vector<uint8_t>& cand, int N, int P, int
     for (; r <= rows; ++r) bands.back().units += row_cnt[r];
     bands.back().r1 = rows + 1;
   }
-  // Row prefix (unit index of the first unit of each row within its band) and windows.
+  // Row prefix: unit index of the first unit of each row within its band, numbering the
+  // band's first row, then its last row, then the rows between (the kernel flips and
+  // publishes the boundary rows first).  Windows: 16-cell aligned.
   max_units = 0;
   smem_bytes = 0;
   for (DmBand& bd : bands) {
     int u = 0, wl = P, wh = 0;
-    for (int i = bd.r0; i < bd.r1; ++i) {
+    row_prefix[bd.r0] = 0;
+    u = row_cnt[bd.r0];
+    bd.nb_first = u;
+    if (bd.r1 - 1 > bd.r0) {
+      row_prefix[bd.r1 - 1] = u;
+      u += row_cnt[bd.r1 - 1];
+    }
+    bd.nb_boundary = u;
+    for (int i = bd.r0 + 1; i < bd.r1 - 1; ++i) {
       row_prefix[i] = u;
       u += row_cnt[i];
     }
@@ -365,17 +476,17 @@ rt_status PersistPlan::build(const std::vector<uint8_t>& cand, int N, int P, int
     }
     if (wh <= wl) {  // band without candidates: any aligned window works
       wl = 0;
-      wh = 4;
+      wh = 16;
     }
-    bd.wlo = std::max(0, wl) & ~3;
-    bd.whi = std::min(P, (wh + 3) & ~3);
+    bd.wlo = std::max(0, wl) & ~15;
+    bd.whi = std::min(P, (wh + 15) & ~15);
     max_units = std::max(max_units, bd.units);
     const size_t sb = (size_t)2 * nch * (bd.r1 - bd.r0 + 2) * (bd.whi - bd.wlo);
     smem_bytes = std::max(smem_bytes, sb);
   }
   K = 0;
   for (int k : {1, 2, 4, 8})
-    if ((int64_t)k * kThreads >= max_units) {
+    if ((int64_t)k * (kThreads - 32) >= max_units) {
       K = k;
       break;
     }
@@ -423,9 +534,12 @@ rt_status PersistEngine::prepare(DmSampler& s) {
   if (rt_status st = plan.build(s.candidates, s.N, s.P, s.opts.rng_mode, s.active, sms, smem_optin)) return st;
   if (!plan.ok) return RT_OK;
   const bool params = s.tmt_params != nullptr;
-  kernel = s.opts.rng_mode == RT_RNG_TINYMT
-               ? (params ? kernel_for<RT_RNG_TINYMT, true>(plan.K) : kernel_for<RT_RNG_TINYMT, false>(plan.K))
-               : kernel_for<RT_RNG_FAST, false>(plan.K);
+  if (s.active == 3) {
+    plan.ok = false;
+    plan.why = "three swept chains (the resident kernel takes 1, 2 or 4)";
+    return RT_OK;
+  }
+  kernel = dm_persist_kernel_ptr(s.opts.rng_mode, plan.K, params, s.active);
   RT_CUDA_P(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)plan.smem_bytes));
   int per_sm = 0;
   RT_CUDA_P(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kThreads, plan.smem_bytes));
@@ -516,9 +630,10 @@ rt_status PersistEngine::check_error(DmSampler& s) {
 
 namespace rt {
 
-void* dm_persist_kernel_ptr(int mode, int K, bool params) {
-  if (mode == RT_RNG_TINYMT) return params ? kernel_for<RT_RNG_TINYMT, true>(K) : kernel_for<RT_RNG_TINYMT, false>(K);
-  return kernel_for<RT_RNG_FAST, false>(K);
+void* dm_persist_kernel_ptr(int mode, int K, bool params, int nch) {
+  if (mode == RT_RNG_TINYMT)
+    return params ? kernel_for<RT_RNG_TINYMT, true>(K, nch) : kernel_for<RT_RNG_TINYMT, false>(K, nch);
+  return kernel_for<RT_RNG_FAST, false>(K, nch);
 }
 
 }  // namespace rt

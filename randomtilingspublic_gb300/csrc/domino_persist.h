@@ -14,9 +14,10 @@ namespace rt {
 struct DmSampler;
 
 // One CTA's share: colour-array rows [r0, r1), shared-memory column window [wlo, whi)
-// (bytes, multiples of 4), and its number of units (flip-candidate sites or quads).
+// (cells, multiples of 16), its number of units (flip-candidate sites or quads), and how
+// many of them lie in its first row and in its first plus last rows.
 struct DmBand {
-  int r0, r1, wlo, whi, units, pad0, pad1, pad2;
+  int r0, r1, wlo, whi, units, nb_first, nb_boundary, pad;
 };
 
 struct PersistArgs {
@@ -29,7 +30,7 @@ struct PersistArgs {
   const int* row_lo;      // first unit of each row
   const int* row_prefix;  // unit index of that first unit within the row's band
   DmRule rule;
-  uint8_t* xbuf;          // [2 slots][band][top, bottom][chain][P]
+  uint8_t* xbuf;          // [2 slots][band][top, bottom][P x chains, chain-interleaved]
   unsigned* flags;        // per band: half-sweeps published; flags[nbands] is the error word
   int* error;
   long max_spin;
@@ -73,7 +74,8 @@ struct PersistEngine {
 // Threads per CTA of the resident kernel and its entry for (rng mode, units per thread K,
 // per-generator parameter table).
 constexpr int kPersistThreads = 1024;
-void* dm_persist_kernel_ptr(int mode, int K, bool params);
+// nch: swept chains, 1, 2 or 4.
+void* dm_persist_kernel_ptr(int mode, int K, bool params, int nch);
 
 // True when every edge bit agrees with the bit of the vertex across it and no edge leaves
 // the array: then rebuilding a colour from the other reproduces it, which the persistent
