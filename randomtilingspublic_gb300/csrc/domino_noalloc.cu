@@ -119,7 +119,7 @@ extern "C" RT_API rt_status rt_dm_sweep_noalloc(uint8_t* dev_chains, void* dev_g
   if (rt_status st = plan.build(cand, N, P, o.rng_mode, n_chains, std::min(sms, kMaxBands), (size_t)optin - 1024))
     return st;
   if (!plan.ok) return fail(RT_ERR_INVALID_ARGUMENT, "sweep_noalloc: " + plan.why);
-  void* kernel = dm_persist_kernel_ptr(o.rng_mode, plan.K, false, n_chains);
+  void* kernel = dm_persist_kernel_ptr(o.rng_mode, plan.K, false, n_chains, false);
   NOALLOC_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)plan.smem_bytes));
   int per_sm = 0;
   NOALLOC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kPersistThreads, plan.smem_bytes));

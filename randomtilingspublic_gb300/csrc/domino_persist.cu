@@ -111,252 +111,306 @@ __device__ __forceinline__ void rebuild_word(const Planes<NCH>& pl, int t, int r
   Pw[w] = (v & ~keep) | (Pw[w] & keep);
 }
 
-template <int kMode, int K, bool kParams, int NCH>
-__global__ void __launch_bounds__(kThreads, 1) k_persist(PersistArgs a) {
-  extern __shared__ __align__(16) uint8_t smem_raw[];
-  __shared__ uint4 s_rule[4];
-  __shared__ int s_abort;
-  const int b = blockIdx.x;
-  const DmBand band = a.bands[b];
-  const int R = band.r1 - band.r0 + 2, W = band.whi - band.wlo, Wb = W * NCH;
-  const int words = Wb / 4, vecs = Wb / 16;
-  const Planes<NCH> pl{smem_raw, R, Wb};
-  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+// XORs mask into the byte(s) of chain-interleaved cell offset off of a plane (atomically:
+// two flips in one half-sweep can touch the same word).
+__device__ __forceinline__ void xor_cell(uint8_t* plane, uint32_t off, uint32_t mask) {
+  atomicXor(reinterpret_cast<unsigned*>(plane + (off & ~3u)), mask << (8 * (off & 3u)));
+}
 
-  // Load rows r0-1 .. r1 of both colours, interleaving the chains.
-  for (int rr = warp; rr < 2 * R; rr += kThreads / 32) {
-    const int t = rr / R, ri = rr - t * R;
-    uint8_t* dst = pl.row(t, ri);
-    for (int x = lane; x < W; x += 32) {
-#pragma unroll
-      for (int ch = 0; ch < NCH; ++ch)
-        dst[x * NCH + ch] = a.base[(size_t)ch * a.chain_stride + (size_t)t * a.colour_stride +
-                                   (size_t)(band.r0 - 1 + ri) * a.P + band.wlo + x];
+// Per-CTA constants kept in shared memory, so that neither role pins them in registers.
+struct BandCtx {
+  PersistArgs a;
+  DmBand band;
+  int R, W, Wb, words, vecs, rows, boundary_slots, abort;
+  uint4 rule[4];
+};
+
+template <int NCH>
+__device__ __forceinline__ Planes<NCH> planes_of(uint8_t* smem, const BandCtx& c, int K, bool need_where) {
+  return Planes<NCH>{smem + (size_t)K * kThreads * 4 * (need_where ? 2 : 1), c.R, c.Wb};
+}
+
+// Unit c of the band -> colour-array row i and unit column u (site column in TinyMT mode,
+// column quad in fast mode): the first row, the last row, then the rows between.
+__device__ __forceinline__ void decode_unit(const BandCtx& c, int k, int& i, int& u) {
+  const DmBand& b = c.band;
+  if (k < b.nb_first) {
+    i = b.r0;
+  } else if (k < b.nb_boundary) {
+    i = b.r1 - 1;
+  } else {
+    int lo = b.r0 + 1, hi = b.r1 - 2;
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (c.a.row_prefix[mid] <= k) lo = mid;
+      else hi = mid - 1;
     }
+    i = lo;
   }
-  if (tid < 4) s_rule[tid] = make_uint4(a.rule.lo_up[tid], a.rule.w_up[tid], a.rule.lo_dn[tid], a.rule.w_dn[tid]);
-  if (tid == 0) s_abort = 0;
+  u = c.a.row_lo[i] + (k - c.a.row_prefix[i]);
+}
 
-  // Worker thread wt holds units wt + s * kWorkers: the band's first row, its last row,
-  // then the rows between (a.row_prefix in that order).  Per unit: the byte offset of its
-  // (first) site in a colour plane, its row parity (bit 31) and, in fast mode, the sites of
-  // its quad inside [1, cols] (bits 24..27); the generator state (TinyMT) and, where a draw
-  // needs it, the position (i << 16) | u.
+// Worker warps (1..31): flips, sparse passive updates or the interior rebuild, and the
+// rebuild of the band's boundary rows.
+template <int kMode, int K, bool kParams, int NCH, bool kSparse>
+__device__ __noinline__ void worker_role(uint8_t* smem, BandCtx& c) {
   constexpr bool kNeedWhere = (kMode != RT_RNG_TINYMT) || kParams;
-  uint32_t unit[K];
-  uint32_t where[kNeedWhere ? K : 1];
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31, wt = tid - 32;
+  uint32_t* s_unit = reinterpret_cast<uint32_t*>(smem);
+  uint32_t* s_where = s_unit + K * kThreads;
+  const Planes<NCH> pl = planes_of<NCH>(smem, c, K, kNeedWhere);
   uint4 st[K];
-  int boundary_slots = 0;
-  const bool worker = warp > 0;
-  const int wt = tid - 32;
-  auto decode = [&](int c, int& i, int& u) {
-    if (c < band.nb_first) {
-      i = band.r0;
-    } else if (c < band.nb_boundary) {
-      i = band.r1 - 1;
-    } else {
-      int lo = band.r0 + 1, hi = band.r1 - 2;
-      while (lo < hi) {
-        const int mid = (lo + hi + 1) >> 1;
-        if (a.row_prefix[mid] <= c) lo = mid;
-        else hi = mid - 1;
-      }
-      i = lo;
-    }
-    u = a.row_lo[i] + (c - a.row_prefix[i]);
-  };
 #pragma unroll
   for (int s = 0; s < K; ++s) {
-    unit[s] = kNoUnit;
-    if (kNeedWhere) where[s] = 0;
+    s_unit[s * kThreads + tid] = kNoUnit;
     st[s] = make_uint4(0, 0, 0, 0);
-    const int c = wt + s * kWorkers;
-    if (worker && c < band.units) {
+    const int k = wt + s * kWorkers;
+    if (k < c.band.units) {
       int i, u;
-      decode(c, i, u);
-      const int ri = i - band.r0 + 1;
+      decode_unit(c, k, i, u);
+      const int ri = i - c.band.r0 + 1;
       const int m0 = kMode == RT_RNG_TINYMT ? u : 4 * u;
       uint32_t valid = 0;
       if (kMode != RT_RNG_TINYMT) {
 #pragma unroll
         for (int k4 = 0; k4 < 4; ++k4)
-          if (m0 + k4 >= 1 && m0 + k4 <= a.cols) valid |= 1u << k4;
+          if (m0 + k4 >= 1 && m0 + k4 <= c.a.cols) valid |= 1u << k4;
       }
-      unit[s] = (uint32_t)(ri * Wb + (m0 - band.wlo) * NCH) | (valid << 24) | ((uint32_t)(i & 1) << 31);
-      if (kNeedWhere) where[s] = ((uint32_t)i << 16) | (uint32_t)u;
-      if (kMode == RT_RNG_TINYMT) st[s] = a.tmt[(int64_t)(i - 1) * a.cols + (u - 1)];
+      s_unit[s * kThreads + tid] =
+          (uint32_t)(ri * c.Wb + (m0 - c.band.wlo) * NCH) | (valid << 24) | ((uint32_t)(i & 1) << 31);
+      if (kNeedWhere) s_where[s * kThreads + tid] = ((uint32_t)i << 16) | (uint32_t)u;
+      if (kMode == RT_RNG_TINYMT) st[s] = c.a.tmt[(int64_t)(i - 1) * c.a.cols + (u - 1)];
     }
   }
-  boundary_slots = (band.nb_boundary + kWorkers - 1) / kWorkers;
-  __syncthreads();
+  __syncthreads();  // init
 
-  const int up = b - 1, dn = b + 1;
-
+  // Toggles, in the passive colour 1-t, the bit of the edge shared with the flipped site at
+  // unit offset pk: bit 2 of the site above, bit 1 below, bit 8 of the passive site to its
+  // left and bit 4 of the one to its right (columns m-1/m or m/m+1 by the parity of i+t);
+  // ones has 0x01 in the byte of each chain that flipped.
+  auto passive_xor = [&](uint32_t pk, int t, uint32_t ones) {
+    uint8_t* pp = pl.row(1 - t, 0);
+    const uint32_t off = pk & 0xffffffu, wb = (uint32_t)c.Wb;
+    const int odd = (int)((pk >> 31) ^ (uint32_t)t) & 1;
+    xor_cell(pp, off - wb, ones << 1);
+    xor_cell(pp, off + wb, ones);
+    xor_cell(pp, odd ? off - NCH : off, ones << 3);
+    xor_cell(pp, odd ? off : off + NCH, ones << 2);
+  };
+  auto flip_cell = [&](uint8_t* q, uint32_t pk, int t, uint32_t r, const uint4& rl) {
+    const uint32_t upm = (r - rl.x) < rl.y ? 0xffffffffu : 0u, dnm = (r - rl.z) < rl.w ? 0xffffffffu : 0u;
+    uint32_t x, y;
+    if (NCH == 1) {
+      x = *q;
+      y = flip_bytes(x, upm, dnm, 0xffu);
+      if (y != x) *q = (uint8_t)y;
+    } else if (NCH == 2) {
+      uint16_t* q2 = reinterpret_cast<uint16_t*>(q);
+      x = *q2;
+      y = flip_bytes(x, upm, dnm, 0xffffu);
+      if (y != x) *q2 = (uint16_t)y;
+    } else {
+      uint32_t* q4 = reinterpret_cast<uint32_t*>(q);
+      x = *q4;
+      y = flip_bytes(x, upm, dnm, 0xffffffffu);
+      if (y != x) *q4 = y;
+    }
+    if (kSparse && y != x) passive_xor(pk, t, (x ^ y) & 0x01010101u);
+  };
   auto flip_unit = [&](int s, int t, int h) {
-    const uint32_t pk = unit[s];
+    const uint32_t pk = s_unit[s * kThreads + tid];
     if (pk == kNoUnit) return;
-    const uint4 rl = s_rule[(pk >> 31) | (t << 1)];
+    const uint4 rl = c.rule[(pk >> 31) | (t << 1)];
     uint8_t* q = pl.row(t, 0) + (pk & 0xffffffu);
     if (kMode == RT_RNG_TINYMT) {
       uint32_t m1 = kTmtMat1, m2 = kTmtMat2, tm = kTmtTmat;
       if (kParams) {
-        const int i = (int)(where[kNeedWhere ? s : 0] >> 16), u = (int)(where[kNeedWhere ? s : 0] & 0xffffu);
-        const uint4 p = __ldg(&a.tmt_params[(int64_t)(i - 1) * a.cols + (u - 1)]);
+        const uint32_t wh = s_where[s * kThreads + tid];
+        const uint4 p = __ldg(&c.a.tmt_params[(int64_t)((wh >> 16) - 1) * c.a.cols + ((wh & 0xffffu) - 1)]);
         m1 = p.x; m2 = p.y; tm = p.z;
       }
-      const uint32_t r = tmt_next_u23(st[s], m1, m2, tm);
-      const uint32_t upm = (r - rl.x) < rl.y ? 0xffffffffu : 0u, dnm = (r - rl.z) < rl.w ? 0xffffffffu : 0u;
-      if (NCH == 1) {
-        const uint32_t x = *q, y = flip_bytes(x, upm, dnm, 0xffu);
-        if (y != x) *q = (uint8_t)y;
-      } else if (NCH == 2) {
-        uint16_t* q2 = reinterpret_cast<uint16_t*>(q);
-        const uint32_t x = *q2, y = flip_bytes(x, upm, dnm, 0xffffu);
-        if (y != x) *q2 = (uint16_t)y;
-      } else {
-        uint32_t* q4 = reinterpret_cast<uint32_t*>(q);
-        const uint32_t x = *q4, y = flip_bytes(x, upm, dnm, 0xffffffffu);
-        if (y != x) *q4 = y;
-      }
+      flip_cell(q, pk, t, tmt_next_u23(st[s], m1, m2, tm), rl);
     } else {
-      const uint4 r4 = fast_quad(a.fast_seed, a.fast_stream, a.h0 + h, where[kNeedWhere ? s : 0] >> 16,
-                                 where[kNeedWhere ? s : 0] & 0xffffu);
+      const uint32_t wh = s_where[s * kThreads + tid];
+      const uint4 r4 = fast_quad(c.a.fast_seed, c.a.fast_stream, c.a.h0 + h, wh >> 16, wh & 0xffffu);
       const uint32_t rr[4] = {r4.x, r4.y, r4.z, r4.w};
       const uint32_t valid = (pk >> 24) & 0xfu;
 #pragma unroll
-      for (int k4 = 0; k4 < 4; ++k4) {
-        if (!((valid >> k4) & 1u)) continue;
-        const uint32_t upm = (rr[k4] - rl.x) < rl.y ? 0xffffffffu : 0u, dnm = (rr[k4] - rl.z) < rl.w ? 0xffffffffu : 0u;
-        uint8_t* qk = q + k4 * NCH;
-        if (NCH == 1) {
-          const uint32_t x = *qk, y = flip_bytes(x, upm, dnm, 0xffu);
-          if (y != x) *qk = (uint8_t)y;
-        } else if (NCH == 2) {
-          uint16_t* q2 = reinterpret_cast<uint16_t*>(qk);
-          const uint32_t x = *q2, y = flip_bytes(x, upm, dnm, 0xffffu);
-          if (y != x) *q2 = (uint16_t)y;
-        } else {
-          uint32_t* q4 = reinterpret_cast<uint32_t*>(qk);
-          const uint32_t x = *q4, y = flip_bytes(x, upm, dnm, 0xffffffffu);
-          if (y != x) *q4 = y;
-        }
-      }
+      for (int k4 = 0; k4 < 4; ++k4)
+        if ((valid >> k4) & 1u) flip_cell(q + k4 * NCH, pk + k4 * NCH, t, rr[k4], rl);
     }
   };
 
-  const int rows = R - 2;
-  const int nsteps = (int)a.steps;  // at most 65536 per launch
-  const int par0 = (int)(a.h0 & 1);
+  const int nsteps = (int)c.a.steps, par0 = (int)(c.a.h0 & 1);
   for (int h = 0; h < nsteps; ++h) {
-    const int t = (kMode == RT_RNG_TINYMT) ? (a.colours[h] ? 1 : 0) : (((par0 ^ h) & 1) ? 0 : 1);
-    const int slot = h & 1;
-    // 1. flip the slots holding the band's first and last rows
-    if (worker) {
+    const int t = (kMode == RT_RNG_TINYMT) ? (c.a.colours[h] ? 1 : 0) : (((par0 ^ h) & 1) ? 0 : 1);
+    const int bslots = c.boundary_slots;
 #pragma unroll
-      for (int s = 0; s < K; ++s)
-        if (s < boundary_slots) flip_unit(s, t, h);
-    }
-    __syncthreads();
-    if (!worker) {
-      // 2. warp 0: publish the two boundary rows, release the half-sweep count, wait for the
-      //    neighbours, copy their rows into the halo rows.
-      const uint4* top = reinterpret_cast<const uint4*>(pl.row(t, 1));
-      const uint4* bot = reinterpret_cast<const uint4*>(pl.row(t, R - 2));
-      uint4* gtop = reinterpret_cast<uint4*>(a.xbuf + (((size_t)slot * a.nbands + b) * 2 + 0) * a.P * NCH +
-                                             (size_t)band.wlo * NCH);
-      uint4* gbot = reinterpret_cast<uint4*>(a.xbuf + (((size_t)slot * a.nbands + b) * 2 + 1) * a.P * NCH +
-                                             (size_t)band.wlo * NCH);
-      for (int v = lane; v < vecs; v += 32) {
-        __stcg(gtop + v, top[v]);
-        __stcg(gbot + v, bot[v]);
-      }
-      __threadfence();
-      __syncwarp();
-      bool ok = true;
-      if (lane == 0) {
-        cuda::atomic_ref<unsigned, cuda::thread_scope_device> f(a.flags[b]);
-        f.store((unsigned)(h + 1), cuda::memory_order_release);
-        if (up >= 0) ok = wait_flag(&a.flags[up], (unsigned)(h + 1), a.error, a.max_spin);
-        if (ok && dn < a.nbands) ok = wait_flag(&a.flags[dn], (unsigned)(h + 1), a.error, a.max_spin);
-        s_abort = ok ? 0 : 1;
-      }
-      ok = __shfl_sync(0xffffffffu, ok ? 1 : 0, 0) != 0;
-      if (ok) {
-        if (up >= 0) {
-          const int lo = max(band.wlo, a.bands[up].wlo), hi = min(band.whi, a.bands[up].whi);
-          const uint4* g = reinterpret_cast<const uint4*>(a.xbuf + (((size_t)slot * a.nbands + up) * 2 + 1) * a.P * NCH +
-                                                          (size_t)lo * NCH);
-          uint4* d = reinterpret_cast<uint4*>(pl.row(t, 0) + (lo - band.wlo) * NCH);
-          for (int v = lane; v < (hi - lo) * NCH / 16; v += 32) d[v] = __ldcg(g + v);
-        }
-        if (dn < a.nbands) {
-          const int lo = max(band.wlo, a.bands[dn].wlo), hi = min(band.whi, a.bands[dn].whi);
-          const uint4* g = reinterpret_cast<const uint4*>(a.xbuf + (((size_t)slot * a.nbands + dn) * 2 + 0) * a.P * NCH +
-                                                          (size_t)lo * NCH);
-          uint4* d = reinterpret_cast<uint4*>(pl.row(t, R - 1) + (lo - band.wlo) * NCH);
-          for (int v = lane; v < (hi - lo) * NCH / 16; v += 32) d[v] = __ldcg(g + v);
-        }
-      }
-    } else {
-      // 3. workers: the remaining flips, then the rebuild of the rows that need no halo.
+    for (int s = 0; s < K; ++s)
+      if (s < bslots) flip_unit(s, t, h);
+    __syncthreads();  // #1: boundary rows final, the communication warp publishes them
 #pragma unroll
-      for (int s = 0; s < K; ++s)
-        if (s >= boundary_slots) flip_unit(s, t, h);
+    for (int s = 0; s < K; ++s)
+      if (s >= bslots) flip_unit(s, t, h);
+    if (!kSparse) {
       workers_sync();
-      for (int r = warp; r <= rows - 2; r += kWorkers / 32) {  // band rows 1 .. rows-2 (0-based), warps 1..31
-        const int ri = r + 1, i = band.r0 + r;
-        for (int w = lane; w < words; w += 32) rebuild_word<NCH>(pl, t, ri, i, w, words, band.wlo, a.cols);
+      const int rows = c.rows, words = c.words;
+      for (int r = warp; r <= rows - 2; r += kWorkers / 32) {
+        for (int w = lane; w < words; w += 32)
+          rebuild_word<NCH>(pl, t, r + 1, c.band.r0 + r, w, words, c.band.wlo, c.a.cols);
       }
     }
-    __syncthreads();
-    if (s_abort) break;
-    // 4. rebuild the band's first and last rows (they read the halo rows)
-    for (int r = warp; r < (rows > 1 ? 2 : 1); r += kThreads / 32) {
-      const int rr = r == 0 ? 0 : rows - 1;
-      for (int w = lane; w < words; w += 32) rebuild_word<NCH>(pl, t, rr + 1, band.r0 + rr, w, words, band.wlo, a.cols);
+    __syncthreads();  // #3: flips done, halo rows in place
+    if (c.abort) break;
+    {
+      const int rows = c.rows, words = c.words;
+      const int r = warp - 1;  // warps 1 and 2 rebuild the band's first and last rows
+      if (r < (rows > 1 ? 2 : 1)) {
+        const int rr = r == 0 ? 0 : rows - 1;
+        for (int w = lane; w < words; w += 32)
+          rebuild_word<NCH>(pl, t, rr + 1, c.band.r0 + rr, w, words, c.band.wlo, c.a.cols);
+      }
     }
-    __syncthreads();
-  }
-
-  // Write back the band rows of both colours and the generator states.
-  for (int rr = warp; rr < 2 * rows; rr += kThreads / 32) {
-    const int t = rr / rows, r = rr - t * rows;
-    const uint8_t* src = pl.row(t, r + 1);
-    for (int x = lane; x < W; x += 32) {
-#pragma unroll
-      for (int ch = 0; ch < NCH; ++ch)
-        a.base[(size_t)ch * a.chain_stride + (size_t)t * a.colour_stride + (size_t)(band.r0 + r) * a.P + band.wlo + x] =
-            src[x * NCH + ch];
-    }
+    __syncthreads();  // #4
   }
   if (kMode == RT_RNG_TINYMT) {
 #pragma unroll
     for (int s = 0; s < K; ++s) {
-      if (unit[s] == kNoUnit) continue;
+      if (s_unit[s * kThreads + tid] == kNoUnit) continue;
       int i, u;
-      decode(wt + s * kWorkers, i, u);
-      a.tmt[(int64_t)(i - 1) * a.cols + (u - 1)] = st[s];
+      decode_unit(c, wt + s * kWorkers, i, u);
+      c.a.tmt[(int64_t)(i - 1) * c.a.cols + (u - 1)] = st[s];
     }
   }
 }
 
-template <int kMode, bool kParams, int NCH>
+// Warp 0: publishes the band's boundary rows of the rotated colour, releases the half-sweep
+// count, waits (bounded) for both neighbour bands, and copies their rows into the halo.
+template <int kMode, int K, bool kParams, int NCH>
+__device__ __noinline__ void comm_role(uint8_t* smem, BandCtx& c) {
+  constexpr bool kNeedWhere = (kMode != RT_RNG_TINYMT) || kParams;
+  const int lane = threadIdx.x & 31, b = blockIdx.x, up = b - 1, dn = b + 1;
+  const Planes<NCH> pl = planes_of<NCH>(smem, c, K, kNeedWhere);
+  __syncthreads();  // init
+  const int nsteps = (int)c.a.steps, par0 = (int)(c.a.h0 & 1);
+  for (int h = 0; h < nsteps; ++h) {
+    const int t = (kMode == RT_RNG_TINYMT) ? (c.a.colours[h] ? 1 : 0) : (((par0 ^ h) & 1) ? 0 : 1);
+    const size_t slot = (size_t)(h & 1);
+    __syncthreads();  // #1
+    const int vecs = c.vecs, R = c.R, nb = c.a.nbands;
+    const size_t rowb = (size_t)c.a.P * NCH;
+    uint8_t* xb = c.a.xbuf;
+    {
+      const uint4* top = reinterpret_cast<const uint4*>(pl.row(t, 1));
+      const uint4* bot = reinterpret_cast<const uint4*>(pl.row(t, R - 2));
+      uint4* gtop = reinterpret_cast<uint4*>(xb + ((slot * nb + b) * 2 + 0) * rowb + (size_t)c.band.wlo * NCH);
+      uint4* gbot = reinterpret_cast<uint4*>(xb + ((slot * nb + b) * 2 + 1) * rowb + (size_t)c.band.wlo * NCH);
+      for (int v = lane; v < vecs; v += 32) {
+        __stcg(gtop + v, top[v]);
+        __stcg(gbot + v, bot[v]);
+      }
+    }
+    __threadfence();
+    __syncwarp();
+    int ok = 1;
+    if (lane == 0) {
+      cuda::atomic_ref<unsigned, cuda::thread_scope_device> f(c.a.flags[b]);
+      f.store((unsigned)(h + 1), cuda::memory_order_release);
+      if (up >= 0) ok = wait_flag(&c.a.flags[up], (unsigned)(h + 1), c.a.error, c.a.max_spin);
+      if (ok && dn < nb) ok = wait_flag(&c.a.flags[dn], (unsigned)(h + 1), c.a.error, c.a.max_spin);
+      c.abort = ok ? 0 : 1;
+    }
+    ok = __shfl_sync(0xffffffffu, ok, 0);
+    if (ok) {
+      if (up >= 0) {
+        const int lo = max(c.band.wlo, c.a.bands[up].wlo), hi = min(c.band.whi, c.a.bands[up].whi);
+        const uint4* g = reinterpret_cast<const uint4*>(xb + ((slot * nb + up) * 2 + 1) * rowb + (size_t)lo * NCH);
+        uint4* d = reinterpret_cast<uint4*>(pl.row(t, 0) + (lo - c.band.wlo) * NCH);
+        for (int v = lane; v < (hi - lo) * NCH / 16; v += 32) d[v] = __ldcg(g + v);
+      }
+      if (dn < nb) {
+        const int lo = max(c.band.wlo, c.a.bands[dn].wlo), hi = min(c.band.whi, c.a.bands[dn].whi);
+        const uint4* g = reinterpret_cast<const uint4*>(xb + ((slot * nb + dn) * 2 + 0) * rowb + (size_t)lo * NCH);
+        uint4* d = reinterpret_cast<uint4*>(pl.row(t, R - 1) + (lo - c.band.wlo) * NCH);
+        for (int v = lane; v < (hi - lo) * NCH / 16; v += 32) d[v] = __ldcg(g + v);
+      }
+    }
+    __syncthreads();  // #3
+    if (c.abort) break;
+    __syncthreads();  // #4
+  }
+}
+
+// kSparse: the passive colour is kept current by XOR updates from each flip (a flip toggles
+// all four edge bits of its site, so each of its four passive neighbours toggles the one bit
+// of the shared edge), and only the band's first and last rows are rebuilt in full, after
+// the neighbours' rows arrive.  Exact for consistent tilings.  Without kSparse every window
+// word is rebuilt each half-sweep, which reproduces the reference for any input.
+template <int kMode, int K, bool kParams, int NCH, bool kSparse>
+__global__ void __launch_bounds__(kThreads, 1) k_persist(PersistArgs a) {
+  extern __shared__ __align__(16) uint8_t smem_raw[];
+  __shared__ BandCtx c;
+  constexpr bool kNeedWhere = (kMode != RT_RNG_TINYMT) || kParams;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  if (tid == 0) {
+    c.a = a;
+    c.band = a.bands[blockIdx.x];
+    c.R = c.band.r1 - c.band.r0 + 2;
+    c.W = c.band.whi - c.band.wlo;
+    c.Wb = c.W * NCH;
+    c.words = c.Wb / 4;
+    c.vecs = c.Wb / 16;
+    c.rows = c.R - 2;
+    c.boundary_slots = (c.band.nb_boundary + kWorkers - 1) / kWorkers;
+    c.abort = 0;
+  }
+  if (tid < 4) c.rule[tid] = make_uint4(a.rule.lo_up[tid], a.rule.w_up[tid], a.rule.lo_dn[tid], a.rule.w_dn[tid]);
+  __syncthreads();
+  const Planes<NCH> pl = planes_of<NCH>(smem_raw, c, K, kNeedWhere);
+  const int R = c.R, W = c.W, r0 = c.band.r0, wlo = c.band.wlo;
+  // Load rows r0-1 .. r1 of both colours, interleaving the chains.
+  for (int rr = warp; rr < 2 * R; rr += kThreads / 32) {
+    const int t = rr / R, ri = rr - t * R;
+    uint8_t* dst = pl.row(t, ri);
+    const uint8_t* src = a.base + (size_t)t * a.colour_stride + (size_t)(r0 - 1 + ri) * a.P + wlo;
+    for (int x = lane; x < W; x += 32) {
+#pragma unroll
+      for (int ch = 0; ch < NCH; ++ch) dst[x * NCH + ch] = src[(size_t)ch * a.chain_stride + x];
+    }
+  }
+  if (warp == 0) comm_role<kMode, K, kParams, NCH>(smem_raw, c);
+  else worker_role<kMode, K, kParams, NCH, kSparse>(smem_raw, c);
+  __syncthreads();
+  // Write back the band rows of both colours.
+  const int rows = R - 2;
+  for (int rr = warp; rr < 2 * rows; rr += kThreads / 32) {
+    const int t = rr / rows, r = rr - t * rows;
+    const uint8_t* src = pl.row(t, r + 1);
+    uint8_t* dst = a.base + (size_t)t * a.colour_stride + (size_t)(r0 + r) * a.P + wlo;
+    for (int x = lane; x < W; x += 32) {
+#pragma unroll
+      for (int ch = 0; ch < NCH; ++ch) dst[(size_t)ch * a.chain_stride + x] = src[x * NCH + ch];
+    }
+  }
+}
+
+template <int kMode, bool kParams, int NCH, bool kSparse>
 void* kernel_for_k(int K) {
   switch (K) {
-    case 1: return (void*)k_persist<kMode, 1, kParams, NCH>;
-    case 2: return (void*)k_persist<kMode, 2, kParams, NCH>;
-    case 4: return (void*)k_persist<kMode, 4, kParams, NCH>;
-    case 8: return (void*)k_persist<kMode, 8, kParams, NCH>;
+    case 1: return (void*)k_persist<kMode, 1, kParams, NCH, kSparse>;
+    case 2: return (void*)k_persist<kMode, 2, kParams, NCH, kSparse>;
+    case 4: return (void*)k_persist<kMode, 4, kParams, NCH, kSparse>;
+    case 8: return (void*)k_persist<kMode, 8, kParams, NCH, kSparse>;
   }
   return nullptr;
 }
 
-template <int kMode, bool kParams>
+template <int kMode, bool kParams, bool kSparse>
 void* kernel_for(int K, int nch) {
   switch (nch) {
-    case 1: return kernel_for_k<kMode, kParams, 1>(K);
-    case 2: return kernel_for_k<kMode, kParams, 2>(K);
-    case 4: return kernel_for_k<kMode, kParams, 4>(K);
+    case 1: return kernel_for_k<kMode, kParams, 1, kSparse>(K);
+    case 2: return kernel_for_k<kMode, kParams, 2, kSparse>(K);
+    case 4: return kSparse ? kernel_for_k<kMode, kParams, 4, kSparse>(K) : nullptr;
   }
   return nullptr;
 }
@@ -494,6 +548,8 @@ rt_status PersistPlan::build(const std::vector<uint8_t>& cand, int N, int P, int
     why = "too many flip candidates per band for register-resident generators";
     return RT_OK;
   }
+  const bool need_where = mode != RT_RNG_TINYMT;  // a parameter table adds the same again (see prepare)
+  smem_bytes += (size_t)K * kThreads * 4 * (need_where ? 2 : 1);
   if (smem_bytes > smem_limit) {
     why = "band window exceeds shared memory";
     return RT_OK;
@@ -539,7 +595,13 @@ rt_status PersistEngine::prepare(DmSampler& s) {
     plan.why = "three swept chains (the resident kernel takes 1, 2 or 4)";
     return RT_OK;
   }
-  kernel = dm_persist_kernel_ptr(s.opts.rng_mode, plan.K, params, s.active);
+  if (params && s.opts.rng_mode == RT_RNG_TINYMT) plan.smem_bytes += (size_t)plan.K * kThreads * 4;  // position table
+  if (plan.smem_bytes > smem_optin) {
+    plan.ok = false;
+    plan.why = "band window exceeds shared memory";
+    return RT_OK;
+  }
+  kernel = dm_persist_kernel_ptr(s.opts.rng_mode, plan.K, params, s.active, true);
   RT_CUDA_P(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)plan.smem_bytes));
   int per_sm = 0;
   RT_CUDA_P(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kThreads, plan.smem_bytes));
@@ -630,10 +692,12 @@ rt_status PersistEngine::check_error(DmSampler& s) {
 
 namespace rt {
 
-void* dm_persist_kernel_ptr(int mode, int K, bool params, int nch) {
+void* dm_persist_kernel_ptr(int mode, int K, bool params, int nch, bool sparse) {
+  if (!sparse) return mode == RT_RNG_TINYMT ? kernel_for<RT_RNG_TINYMT, false, false>(K, nch)
+                                            : kernel_for<RT_RNG_FAST, false, false>(K, nch);
   if (mode == RT_RNG_TINYMT)
-    return params ? kernel_for<RT_RNG_TINYMT, true>(K, nch) : kernel_for<RT_RNG_TINYMT, false>(K, nch);
-  return kernel_for<RT_RNG_FAST, false>(K, nch);
+    return params ? kernel_for<RT_RNG_TINYMT, true, true>(K, nch) : kernel_for<RT_RNG_TINYMT, false, true>(K, nch);
+  return kernel_for<RT_RNG_FAST, false, true>(K, nch);
 }
 
 }  // namespace rt

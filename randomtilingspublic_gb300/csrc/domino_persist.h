@@ -74,8 +74,10 @@ struct PersistEngine {
 // Threads per CTA of the resident kernel and its entry for (rng mode, units per thread K,
 // per-generator parameter table).
 constexpr int kPersistThreads = 1024;
-// nch: swept chains, 1, 2 or 4.
-void* dm_persist_kernel_ptr(int mode, int K, bool params, int nch);
+// nch: swept chains, 1, 2 or 4.  sparse: passive colour kept by per-flip XOR updates
+// (consistent tilings only) instead of a full rebuild each half-sweep; params and nch = 4
+// exist only with sparse.
+void* dm_persist_kernel_ptr(int mode, int K, bool params, int nch, bool sparse);
 
 // True when every edge bit agrees with the bit of the vertex across it and no edge leaves
 // the array: then rebuilding a colour from the other reproduces it, which the persistent
