@@ -183,7 +183,7 @@ RT_API rt_status rt_dm_sampler_engine_info(rt_dm_sampler* s, int64_t* out4);
    half-sweeps of the resident sweep kernel on chains the caller already holds on the
    device, and allocates nothing - no cudaMalloc, cudaFree or allocating library call.
    The kernel's scratch (neighbour exchange rows, flags, band plan, colours) is a fixed
-   static device array of about 1.2 MiB that every GPU loading the library keeps until the
+   static device array of about 2.2 MiB that every GPU loading the library keeps until the
    process exits.
    Layout: dev_chains holds n_chains chains, each two colour arrays (white then black, black
    being the vertices with i + j even) of N rows x P bytes, P = N/2 rounded up to a multiple

@@ -9,9 +9,9 @@
 // fixed size instead of memory allocated per call.  Limits: tiling side N <= 1024, at most
 // 2 chains, at most 65536 half-sweeps per call, at most 256 CTAs.
 //
-// Every GPU that loads the library holds the array (kScratchBytes, about 1.2 MiB) until the
+// Every GPU that loads the library holds the array (kScratchBytes, about 2.2 MiB) until the
 // process exits.  All calls share it and it keeps the last call's contents: each call clears
-// the flags and error word it relies on, and calls that overlap on the GPU (for example on
+// the exchange rows, flags and error word it relies on, and calls that overlap on the GPU (for example on
 // two streams at once) race on it, so callers must order them.
 #include <cuda_runtime.h>
 
@@ -33,7 +33,7 @@ constexpr int kMaxBands = 256;
 constexpr int64_t kMaxSteps = 65536;
 
 // Scratch layout (byte offsets, each 256-aligned).
-constexpr size_t kXbufBytes = (size_t)2 * kMaxBands * 2 * kMaxChains * kMaxPitch;  // 1 MiB
+constexpr size_t kXbufBytes = (size_t)2 * kMaxBands * 2 * kMaxChains * kMaxPitch * 2;  // 2 MiB
 constexpr size_t kOffFlags = kXbufBytes;
 constexpr size_t kFlagsBytes = 2048;  // kMaxBands + 1 words, padded
 constexpr size_t kOffBands = kOffFlags + kFlagsBytes;
@@ -136,6 +136,7 @@ extern "C" RT_API rt_status rt_dm_sweep_noalloc(uint8_t* dev_chains, void* dev_g
   if (o.rng_mode == RT_RNG_TINYMT)
     NOALLOC_CUDA(cudaMemcpyAsync(scratch + kOffColours, colours, (size_t)steps, cudaMemcpyHostToDevice, stream));
   NOALLOC_CUDA(cudaMemsetAsync(scratch + kOffFlags, 0, kFlagsBytes, stream));
+  NOALLOC_CUDA(cudaMemsetAsync(scratch, 0, dm_xbuf_bytes(nbands, n_chains, P), stream));  // no stale tags
 
   PersistArgs a{};
   a.base = dev_chains;

@@ -33,7 +33,8 @@ namespace rt {
 namespace {
 
 constexpr int kThreads = kPersistThreads;
-constexpr int kWorkers = kThreads - 32;  // warp 0 handles the neighbour exchange
+constexpr int kCommWarps = 2;  // warp 0 trades rows with the band above, warp 1 with the band below
+constexpr int kWorkers = kThreads - 32 * kCommWarps;
 constexpr uint32_t kNoUnit = 0xffffffffu;
 
 // Byte-parallel flip of NCH coupled chains of one site (one byte per chain in x): a byte
@@ -42,23 +43,6 @@ constexpr uint32_t kNoUnit = 0xffffffffu;
 __device__ __forceinline__ uint32_t flip_bytes(uint32_t x, uint32_t up, uint32_t dn, uint32_t bytes_mask) {
   const uint32_t eq3 = __vcmpeq4(x, 0x03030303u), eq12 = __vcmpeq4(x, 0x0c0c0c0cu);
   return x ^ (((eq3 & up) | (eq12 & dn)) & 0x0f0f0f0fu & bytes_mask);
-}
-
-// Waits until *flag >= target; false when the wait gave up or another CTA failed.
-__device__ bool wait_flag(unsigned* flag, unsigned target, int* error, long max_spin) {
-  cuda::atomic_ref<unsigned, cuda::thread_scope_device> f(*flag);
-  cuda::atomic_ref<int, cuda::thread_scope_device> err(*error);
-  long it = 0;
-  while (f.load(cuda::memory_order_acquire) < target) {
-    if ((++it & 255) == 0 && err.load(cuda::memory_order_relaxed) != 0) return false;
-    if (it > max_spin) {
-      int zero = 0;
-      err.compare_exchange_strong(zero, 1, cuda::memory_order_relaxed);
-      return false;
-    }
-    if (it > 64) __nanosleep(32);
-  }
-  return true;
 }
 
 __device__ __forceinline__ void workers_sync() { asm volatile("bar.sync 1, %0;" ::"r"(kWorkers) : "memory"); }
@@ -155,7 +139,8 @@ __device__ __forceinline__ void decode_unit(const BandCtx& c, int k, int& i, int
 template <int kMode, int K, bool kParams, int NCH, bool kSparse>
 __device__ __noinline__ void worker_role(uint8_t* smem, BandCtx& c) {
   constexpr bool kNeedWhere = (kMode != RT_RNG_TINYMT) || kParams;
-  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31, wt = tid - 32;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31, wt = tid - 32 * kCommWarps;
+  const int wwarp = warp - kCommWarps;  // worker warp index
   uint32_t* s_unit = reinterpret_cast<uint32_t*>(smem);
   uint32_t* s_where = s_unit + K * kThreads;
   const Planes<NCH> pl = planes_of<NCH>(smem, c, K, kNeedWhere);
@@ -255,7 +240,7 @@ __device__ __noinline__ void worker_role(uint8_t* smem, BandCtx& c) {
     if (!kSparse) {
       workers_sync();
       const int rows = c.rows, words = c.words;
-      for (int r = warp; r <= rows - 2; r += kWorkers / 32) {
+      for (int r = wwarp + 1; r <= rows - 2; r += kWorkers / 32) {
         for (int w = lane; w < words; w += 32)
           rebuild_word<NCH>(pl, t, r + 1, c.band.r0 + r, w, words, c.band.wlo, c.a.cols);
       }
@@ -264,7 +249,7 @@ __device__ __noinline__ void worker_role(uint8_t* smem, BandCtx& c) {
     if (c.abort) break;
     {
       const int rows = c.rows, words = c.words;
-      const int r = warp - 1;  // warps 1 and 2 rebuild the band's first and last rows
+      const int r = wwarp;  // the first two worker warps rebuild the band's first and last rows
       if (r < (rows > 1 ? 2 : 1)) {
         const int rr = r == 0 ? 0 : rows - 1;
         for (int w = lane; w < words; w += 32)
@@ -284,57 +269,93 @@ __device__ __noinline__ void worker_role(uint8_t* smem, BandCtx& c) {
   }
 }
 
-// Warp 0: publishes the band's boundary rows of the rotated colour, releases the half-sweep
-// count, waits (bounded) for both neighbour bands, and copies their rows into the halo.
+// Exchange words: the 4 data bytes and a tag (the half-sweep count h + 1) in one 64-bit
+// store, which is single-copy atomic, so a reader that sees the tag sees the data with it.
+__device__ __forceinline__ void st_tagged(uint64_t* p, uint64_t v) {
+  asm volatile("st.relaxed.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
+__device__ __forceinline__ uint64_t ld_tagged(const uint64_t* p) {
+  uint64_t v;
+  asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+  return v;
+}
+
+// Reads n tagged words into dst, polling until each carries tag want.  Loads are issued in
+// batches of kBatch per lane so that one memory round trip covers a batch.  Returns false
+// when the wait gave up (bounded) or another CTA reported failure.
+__device__ bool read_tagged(const uint64_t* src, uint32_t* dst, int n, uint32_t want, int* error, long max_spin) {
+  constexpr int kBatch = 9;
+  const int lane = threadIdx.x & 31;
+  cuda::atomic_ref<int, cuda::thread_scope_device> err(*error);
+  for (int base = lane; base < n; base += 32 * kBatch) {
+    uint64_t v[kBatch];
+#pragma unroll
+    for (int j = 0; j < kBatch; ++j) {
+      const int w = base + 32 * j;
+      v[j] = w < n ? ld_tagged(src + w) : ((uint64_t)want << 32);
+    }
+#pragma unroll
+    for (int j = 0; j < kBatch; ++j) {
+      const int w = base + 32 * j;
+      long it = 0;
+      while ((uint32_t)(v[j] >> 32) != want) {
+        if ((++it & 255) == 0 && err.load(cuda::memory_order_relaxed) != 0) return false;
+        if (it > max_spin) {
+          int zero = 0;
+          err.compare_exchange_strong(zero, 1, cuda::memory_order_relaxed);
+          return false;
+        }
+        if (it > 32) __nanosleep(32);
+        v[j] = ld_tagged(src + w);
+      }
+      if (w < n) dst[w] = (uint32_t)v[j];
+    }
+  }
+  return true;
+}
+
+// Warps 0 and 1: each publishes one boundary row of the rotated colour (warp 0 the first
+// row, for the band above; warp 1 the last row, for the band below) as tagged words, then
+// reads the matching row of that neighbour into its halo row.  Exchange slot h & 1 of band
+// b holds [2 rows][P x chains / 4 words] (see PersistArgs::xbuf).
 template <int kMode, int K, bool kParams, int NCH>
 __device__ __noinline__ void comm_role(uint8_t* smem, BandCtx& c) {
   constexpr bool kNeedWhere = (kMode != RT_RNG_TINYMT) || kParams;
-  const int lane = threadIdx.x & 31, b = blockIdx.x, up = b - 1, dn = b + 1;
+  const int lane = threadIdx.x & 31, which = threadIdx.x >> 5;  // 0: upper side, 1: lower side
+  const int b = blockIdx.x, nb_band = which == 0 ? b - 1 : b + 1;
   const Planes<NCH> pl = planes_of<NCH>(smem, c, K, kNeedWhere);
   __syncthreads();  // init
   const int nsteps = (int)c.a.steps, par0 = (int)(c.a.h0 & 1);
+  const int nbands = c.a.nbands;
+  const size_t row_words = (size_t)c.a.P * NCH / 4;
+  const bool has_nb = nb_band >= 0 && nb_band < nbands;
+  int lo = 0, hi = 0;
+  if (has_nb) {
+    lo = max(c.band.wlo, c.a.bands[nb_band].wlo);
+    hi = min(c.band.whi, c.a.bands[nb_band].whi);
+  }
+  const int n_in = hi > lo ? (hi - lo) * NCH / 4 : 0;
   for (int h = 0; h < nsteps; ++h) {
     const int t = (kMode == RT_RNG_TINYMT) ? (c.a.colours[h] ? 1 : 0) : (((par0 ^ h) & 1) ? 0 : 1);
     const size_t slot = (size_t)(h & 1);
+    const uint64_t tag = (uint64_t)(uint32_t)(h + 1) << 32;
     __syncthreads();  // #1
-    const int vecs = c.vecs, R = c.R, nb = c.a.nbands;
-    const size_t rowb = (size_t)c.a.P * NCH;
-    uint8_t* xb = c.a.xbuf;
     {
-      const uint4* top = reinterpret_cast<const uint4*>(pl.row(t, 1));
-      const uint4* bot = reinterpret_cast<const uint4*>(pl.row(t, R - 2));
-      uint4* gtop = reinterpret_cast<uint4*>(xb + ((slot * nb + b) * 2 + 0) * rowb + (size_t)c.band.wlo * NCH);
-      uint4* gbot = reinterpret_cast<uint4*>(xb + ((slot * nb + b) * 2 + 1) * rowb + (size_t)c.band.wlo * NCH);
-      for (int v = lane; v < vecs; v += 32) {
-        __stcg(gtop + v, top[v]);
-        __stcg(gbot + v, bot[v]);
-      }
+      const uint32_t* row = reinterpret_cast<const uint32_t*>(pl.row(t, which == 0 ? 1 : c.R - 2));
+      uint64_t* g = reinterpret_cast<uint64_t*>(c.a.xbuf) + ((slot * nbands + b) * 2 + which) * row_words +
+                    (size_t)c.band.wlo * NCH / 4;
+      const int n = c.words;
+      for (int w = lane; w < n; w += 32) st_tagged(g + w, tag | row[w]);
     }
-    __threadfence();
-    __syncwarp();
     int ok = 1;
-    if (lane == 0) {
-      cuda::atomic_ref<unsigned, cuda::thread_scope_device> f(c.a.flags[b]);
-      f.store((unsigned)(h + 1), cuda::memory_order_release);
-      if (up >= 0) ok = wait_flag(&c.a.flags[up], (unsigned)(h + 1), c.a.error, c.a.max_spin);
-      if (ok && dn < nb) ok = wait_flag(&c.a.flags[dn], (unsigned)(h + 1), c.a.error, c.a.max_spin);
-      c.abort = ok ? 0 : 1;
+    if (has_nb) {
+      const uint64_t* g = reinterpret_cast<const uint64_t*>(c.a.xbuf) +
+                          ((slot * nbands + nb_band) * 2 + (1 - which)) * row_words + (size_t)lo * NCH / 4;
+      uint32_t* d = reinterpret_cast<uint32_t*>(pl.row(t, which == 0 ? 0 : c.R - 1) + (lo - c.band.wlo) * NCH);
+      ok = read_tagged(g, d, n_in, (uint32_t)(h + 1), c.a.error, c.a.max_spin) ? 1 : 0;
     }
-    ok = __shfl_sync(0xffffffffu, ok, 0);
-    if (ok) {
-      if (up >= 0) {
-        const int lo = max(c.band.wlo, c.a.bands[up].wlo), hi = min(c.band.whi, c.a.bands[up].whi);
-        const uint4* g = reinterpret_cast<const uint4*>(xb + ((slot * nb + up) * 2 + 1) * rowb + (size_t)lo * NCH);
-        uint4* d = reinterpret_cast<uint4*>(pl.row(t, 0) + (lo - c.band.wlo) * NCH);
-        for (int v = lane; v < (hi - lo) * NCH / 16; v += 32) d[v] = __ldcg(g + v);
-      }
-      if (dn < nb) {
-        const int lo = max(c.band.wlo, c.a.bands[dn].wlo), hi = min(c.band.whi, c.a.bands[dn].whi);
-        const uint4* g = reinterpret_cast<const uint4*>(xb + ((slot * nb + dn) * 2 + 0) * rowb + (size_t)lo * NCH);
-        uint4* d = reinterpret_cast<uint4*>(pl.row(t, R - 1) + (lo - c.band.wlo) * NCH);
-        for (int v = lane; v < (hi - lo) * NCH / 16; v += 32) d[v] = __ldcg(g + v);
-      }
-    }
+    ok = __all_sync(0xffffffffu, ok);
+    if (!ok && lane == 0) c.abort = 1;
     __syncthreads();  // #3
     if (c.abort) break;
     __syncthreads();  // #4
@@ -378,7 +399,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_persist(PersistArgs a) {
       for (int ch = 0; ch < NCH; ++ch) dst[x * NCH + ch] = src[(size_t)ch * a.chain_stride + x];
     }
   }
-  if (warp == 0) comm_role<kMode, K, kParams, NCH>(smem_raw, c);
+  if (warp < kCommWarps) comm_role<kMode, K, kParams, NCH>(smem_raw, c);
   else worker_role<kMode, K, kParams, NCH, kSparse>(smem_raw, c);
   __syncthreads();
   // Write back the band rows of both colours.
@@ -540,7 +561,7 @@ rt_status PersistPlan::build(const std::vector<uint8_t>& cand, int N, int P, int
   }
   K = 0;
   for (int k : {1, 2, 4, 8})
-    if ((int64_t)k * (kThreads - 32) >= max_units) {
+    if ((int64_t)k * kWorkers >= max_units) {
       K = k;
       break;
     }
@@ -622,7 +643,7 @@ rt_status PersistEngine::prepare(DmSampler& s) {
   std::copy(plan.row_prefix.begin(), plan.row_prefix.end(), rows_host.begin() + (s.N + 1));
   RT_CUDA_P(cudaMemcpy(d_bands, plan.bands.data(), plan.bands.size() * sizeof(DmBand), cudaMemcpyHostToDevice));
   RT_CUDA_P(cudaMemcpy(d_rows, rows_host.data(), rows_host.size() * sizeof(int), cudaMemcpyHostToDevice));
-  xbuf_bytes = (size_t)2 * plan.bands.size() * 2 * s.active * s.P;
+  xbuf_bytes = dm_xbuf_bytes((int)plan.bands.size(), s.active, s.P);
   RT_CUDA_P(cudaMalloc(&d_xbuf, xbuf_bytes));
   RT_CUDA_P(cudaMalloc(&d_flags, (plan.bands.size() + 1) * sizeof(unsigned)));
   nch = s.active;
@@ -668,6 +689,7 @@ rt_status PersistEngine::launch(DmSampler& s, const uint8_t* colours_host, int64
       a.colours = d_colours;
     }
     RT_CUDA_P(cudaMemsetAsync(d_flags, 0, (plan.bands.size() + 1) * sizeof(unsigned), s.stream));
+    RT_CUDA_P(cudaMemsetAsync(d_xbuf, 0, xbuf_bytes, s.stream));  // no stale tags
     void* args[] = {&a};
     RT_CUDA_P(cudaLaunchCooperativeKernel(kernel, dim3((unsigned)plan.bands.size()), dim3(kThreads), args,
                                           plan.smem_bytes, s.stream));
@@ -691,6 +713,8 @@ rt_status PersistEngine::check_error(DmSampler& s) {
 }  // namespace rt
 
 namespace rt {
+
+size_t dm_xbuf_bytes(int nbands, int nch, int P) { return (size_t)2 * nbands * 2 * nch * P * 2; }
 
 void* dm_persist_kernel_ptr(int mode, int K, bool params, int nch, bool sparse) {
   if (!sparse) return mode == RT_RNG_TINYMT ? kernel_for<RT_RNG_TINYMT, false, false>(K, nch)

@@ -30,8 +30,8 @@ struct PersistArgs {
   const int* row_lo;      // first unit of each row
   const int* row_prefix;  // unit index of that first unit within the row's band
   DmRule rule;
-  uint8_t* xbuf;          // [2 slots][band][top, bottom][P x chains, chain-interleaved]
-  unsigned* flags;        // per band: half-sweeps published; flags[nbands] is the error word
+  uint8_t* xbuf;          // [2 slots][band][first, last row][P x chains / 4 tagged 64-bit words]
+  unsigned* flags;        // flags[nbands] is the error word (per-band words unused)
   int* error;
   long max_spin;
   int64_t steps, h0;
@@ -74,6 +74,9 @@ struct PersistEngine {
 // Threads per CTA of the resident kernel and its entry for (rng mode, units per thread K,
 // per-generator parameter table).
 constexpr int kPersistThreads = 1024;
+// Bytes of the exchange buffer: two slots x bands x two rows x P x nch bytes, each 4 data
+// bytes carried in one 8-byte tagged word.
+size_t dm_xbuf_bytes(int nbands, int nch, int P);
 // nch: swept chains, 1, 2 or 4.  sparse: passive colour kept by per-flip XOR updates
 // (consistent tilings only) instead of a full rebuild each half-sweep; params and nch = 4
 // exist only with sparse.
