@@ -511,8 +511,9 @@ rt_status PersistPlan::build(const std::vector<uint8_t>& cand, int N, int P, int
     bd.r0 = r;
     const int64_t target = (total * (g + 1)) / G;
     int units = 0;
-    while (r <= rows && (acc < target || r == bd.r0 || g == G - 1)) {
-      if (acc >= target && r > bd.r0 && g < G - 1) break;
+    // Take rows while that brings the running total nearer the target (the split lands on
+    // the row boundary closest to it); every band gets at least one row, the last the rest.
+    while (r <= rows && (2 * acc + row_cnt[r] <= 2 * target || r == bd.r0 || g == G - 1)) {
       acc += row_cnt[r];
       units += row_cnt[r];
       ++r;
