@@ -248,12 +248,12 @@ __device__ __noinline__ void worker_role(uint8_t* smem, BandCtx& c) {
     __syncthreads();  // #3: flips done, halo rows in place
     if (c.abort) break;
     {
-      const int rows = c.rows, words = c.words;
-      const int r = wwarp;  // the first two worker warps rebuild the band's first and last rows
-      if (r < (rows > 1 ? 2 : 1)) {
-        const int rr = r == 0 ? 0 : rows - 1;
-        for (int w = lane; w < words; w += 32)
-          rebuild_word<NCH>(pl, t, rr + 1, c.band.r0 + rr, w, words, c.band.wlo, c.a.cols);
+      // All worker threads share the rebuild of the band's first and last rows.
+      const int rows = c.rows, words = c.words, nrow = rows > 1 ? 2 : 1;
+      for (int k = wt; k < nrow * words; k += kWorkers) {
+        const int which = k >= words ? 1 : 0, w = k - which * words;
+        const int rr = which == 0 ? 0 : rows - 1;
+        rebuild_word<NCH>(pl, t, rr + 1, c.band.r0 + rr, w, words, c.band.wlo, c.a.cols);
       }
     }
     __syncthreads();  // #4
@@ -305,7 +305,6 @@ __device__ bool read_tagged(const uint64_t* src, uint32_t* dst, int n, uint32_t 
           err.compare_exchange_strong(zero, 1, cuda::memory_order_relaxed);
           return false;
         }
-        if (it > 32) __nanosleep(32);
         v[j] = ld_tagged(src + w);
       }
       if (w < n) dst[w] = (uint32_t)v[j];
