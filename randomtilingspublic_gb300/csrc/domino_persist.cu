@@ -37,12 +37,14 @@ constexpr int kCommWarps = 2;  // warp 0 trades rows with the band above, warp 1
 constexpr int kWorkers = kThreads - 32 * kCommWarps;
 constexpr uint32_t kNoUnit = 0xffffffffu;
 
-// Byte-parallel flip of NCH coupled chains of one site (one byte per chain in x): a byte
-// equal to 3 becomes 12 when up is all-ones, a byte equal to 12 becomes 3 when dn is, both
-// by XOR with 15.
+// Byte-parallel flip of NCH coupled chains of one site (one byte per chain in x, bytes
+// <= 15): a byte equal to 3 becomes 12 when up is all-ones, a byte equal to 12 becomes 3
+// when dn is, both by XOR with 15.  Byte b equals v exactly when bit 4 of (b ^ v) + 15 is
+// clear (the sum stays below 32, so no carry crosses a byte).
 __device__ __forceinline__ uint32_t flip_bytes(uint32_t x, uint32_t up, uint32_t dn, uint32_t bytes_mask) {
-  const uint32_t eq3 = __vcmpeq4(x, 0x03030303u), eq12 = __vcmpeq4(x, 0x0c0c0c0cu);
-  return x ^ (((eq3 & up) | (eq12 & dn)) & 0x0f0f0f0fu & bytes_mask);
+  const uint32_t ne3 = (x ^ 0x03030303u) + 0x0f0f0f0fu, ne12 = (x ^ 0x0c0c0c0cu) + 0x0f0f0f0fu;
+  const uint32_t hit = ((~ne3 & up) | (~ne12 & dn)) & 0x10101010u & bytes_mask;
+  return x ^ ((hit >> 4) * 15u);
 }
 
 __device__ __forceinline__ void workers_sync() { asm volatile("bar.sync 1, %0;" ::"r"(kWorkers) : "memory"); }
@@ -173,8 +175,11 @@ __device__ __noinline__ void worker_role(uint8_t* smem, BandCtx& c) {
   // unit offset pk: bit 2 of the site above, bit 1 below, bit 8 of the passive site to its
   // left and bit 4 of the one to its right (columns m-1/m or m/m+1 by the parity of i+t);
   // ones has 0x01 in the byte of each chain that flipped.
+  uint8_t* plane_act = pl.row(0, 0);  // set per half-sweep
+  uint8_t* plane_pas = pl.row(1, 0);
+  const uint4* rule_t = c.rule;
   auto passive_xor = [&](uint32_t pk, int t, uint32_t ones) {
-    uint8_t* pp = pl.row(1 - t, 0);
+    uint8_t* pp = plane_pas;
     const uint32_t off = pk & 0xffffffu, wb = (uint32_t)c.Wb;
     const int odd = (int)((pk >> 31) ^ (uint32_t)t) & 1;
     xor_cell(pp, off - wb, ones << 1);
@@ -205,8 +210,8 @@ __device__ __noinline__ void worker_role(uint8_t* smem, BandCtx& c) {
   auto flip_unit = [&](int s, int t, int h) {
     const uint32_t pk = s_unit[s * kThreads + tid];
     if (pk == kNoUnit) return;
-    const uint4 rl = c.rule[(pk >> 31) | (t << 1)];
-    uint8_t* q = pl.row(t, 0) + (pk & 0xffffffu);
+    const uint4 rl = rule_t[pk >> 31];
+    uint8_t* q = plane_act + (pk & 0xffffffu);
     if (kMode == RT_RNG_TINYMT) {
       uint32_t m1 = kTmtMat1, m2 = kTmtMat2, tm = kTmtTmat;
       if (kParams) {
@@ -230,6 +235,9 @@ __device__ __noinline__ void worker_role(uint8_t* smem, BandCtx& c) {
   for (int h = 0; h < nsteps; ++h) {
     const int t = (kMode == RT_RNG_TINYMT) ? (c.a.colours[h] ? 1 : 0) : (((par0 ^ h) & 1) ? 0 : 1);
     const int bslots = c.boundary_slots;
+    plane_act = pl.row(t, 0);
+    plane_pas = pl.row(1 - t, 0);
+    rule_t = c.rule + 2 * t;
 #pragma unroll
     for (int s = 0; s < K; ++s)
       if (s < bslots) flip_unit(s, t, h);
