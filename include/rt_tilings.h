@@ -137,6 +137,39 @@ RT_API rt_status rt_domino_cftp(const int32_t* tmax, const int32_t* tmin, int32_
                                 int64_t first_steps, int32_t schedule, int32_t max_attempts,
                                 const rt_walk_opts* opts, int32_t* out, rt_cftp_stats* stats);
 
+/* ---- lozenge tilings (src/Lozenge/LozengeTiler.h:63-92) ---------------------------------
+   Vertices of the triangular lattice, N x N, each an edge mask over its six neighbours
+   (0,+1):8 (-1,+1):2 (-1,0):1 (0,-1):4 (+1,-1):16 (+1,0):32, set where a lozenge crosses
+   the edge; N must be a multiple of 3.  A domain is an M x 2M array of triangles, N = M+1. */
+
+/* LozengeTiler::AlmostHexDomain(n, m) (LozengeTiler.cpp:422-467): hexagon of side n with an
+   m x m corner removed (m = 0: the regular a = b = c = n hexagon), padded.  *rows = M. */
+RT_API rt_status rt_lozenge_almost_hex_domain(int32_t n, int32_t m, int32_t* out, int64_t cap, int32_t* rows);
+/* LozengeTiler::DomainToVertices / MaxTiling / MinTiling / HeightfuncToTiling /
+   TilingToHeightfunc / TilingToDomain (LozengeTiler.cpp:173-556). */
+RT_API rt_status rt_lozenge_domain_to_vertices(const int32_t* domain, int32_t m_rows, int32_t* out);
+RT_API rt_status rt_lozenge_max_tiling(const int32_t* domain, int32_t m_rows, int32_t* out);
+RT_API rt_status rt_lozenge_min_tiling(const int32_t* domain, int32_t m_rows, int32_t* out);
+RT_API rt_status rt_lozenge_heightfunc_to_tiling(const int32_t* hf, const int32_t* domain, int32_t n_side,
+                                                 int32_t* out);
+RT_API rt_status rt_lozenge_tiling_to_heightfunc(const int32_t* tiling, const int32_t* domain, int32_t n_side,
+                                                 int32_t* out);
+RT_API rt_status rt_lozenge_tiling_to_domain(const int32_t* tiling, int32_t n_side, int32_t* out);
+/* LozengeTiler::Walk(tiling&, int steps, long seed) (LozengeTiler.cpp:27-159): per step a
+   colour from default_random_engine(seed) + uniform_int_distribution(0, 2) (TinyMT mode,
+   generators seeded with seed itself) or h mod 3 (fast mode), then the rotation 25 <-> 38
+   (0.4 / 0.4, lozengekernel.cl:74-105) and the rebuild of the two other colours
+   (lozengekernel.cl:107-125).  opts->rule and the weights are ignored. */
+RT_API rt_status rt_lozenge_walk(int32_t* tiling, int32_t n_side, int64_t steps, int64_t seed,
+                                 const rt_walk_opts* opts);
+/* Coupling from the past from the max and min tilings with the reference's primitives: each
+   epoch is one Walk(t, steps_k, seed_k) of both chains on the shared stream, seeds from
+   mt19937(driver_seed), look-back prepending 2*steps.back() (schedule 0) or 2*steps.front()
+   (schedule 1); fast mode runs steps [-3T, 0), T = first_steps * 2^j. */
+RT_API rt_status rt_lozenge_cftp(const int32_t* tmax, const int32_t* tmin, int32_t n_side, int64_t driver_seed,
+                                 int64_t first_steps, int32_t schedule, int32_t max_attempts,
+                                 const rt_walk_opts* opts, int32_t* out, rt_cftp_stats* stats);
+
 /* ---- device-resident chains --------------------------------------------------------------
    A sampler keeps n_chains coupled chains of one N x N domain on the GPU; all chains see
    the same random stream (CFTP couples the max and min chains this way).  The building

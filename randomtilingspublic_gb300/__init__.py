@@ -104,6 +104,15 @@ _SIGNATURES = {
     "rt_dm_sampler_engine_info": (C.c_int32, [_P, _P]),
     "rt_domino_rule_table": (C.c_int32, [C.c_int32, C.c_int32, C.c_double, C.c_double, _P]),
     "rt_dm_sweep_noalloc": (C.c_int32, [_P, _P, C.c_int32, C.c_int32, _P, C.c_int64, C.c_uint64, C.c_int64, _P]),
+    "rt_lozenge_almost_hex_domain": (C.c_int32, [C.c_int32, C.c_int32, _P, C.c_int64, _P]),
+    "rt_lozenge_domain_to_vertices": (C.c_int32, [_P, C.c_int32, _P]),
+    "rt_lozenge_max_tiling": (C.c_int32, [_P, C.c_int32, _P]),
+    "rt_lozenge_min_tiling": (C.c_int32, [_P, C.c_int32, _P]),
+    "rt_lozenge_heightfunc_to_tiling": (C.c_int32, [_P, _P, C.c_int32, _P]),
+    "rt_lozenge_tiling_to_heightfunc": (C.c_int32, [_P, _P, C.c_int32, _P]),
+    "rt_lozenge_tiling_to_domain": (C.c_int32, [_P, C.c_int32, _P]),
+    "rt_lozenge_walk": (C.c_int32, [_P, C.c_int32, C.c_int64, C.c_int64, _P]),
+    "rt_lozenge_cftp": (C.c_int32, [_P, _P, C.c_int32, C.c_int64, C.c_int64, C.c_int32, C.c_int32, _P, _P, _P]),
 }
 
 _lib_handle = None
@@ -324,6 +333,105 @@ class DominoTiler:
         return out
 
 
+def _tri_side(d) -> int:
+    m = math.isqrt(len(d) // 2)
+    if 2 * m * m != len(d):
+        raise ValueError("expected an M x 2M triangle array")
+    return m
+
+
+class LozengeTiler:
+    """Lozenge tilings (src/Lozenge/LozengeTiler.h:46-92).  ``rng`` is 'tinymt' (bit-exact
+    with the reference's OpenCL path) or 'fast'."""
+
+    def __init__(self, rng: str = "tinymt", fast_stream: int = 0):
+        self.rng = rng
+        self.fast_stream = int(fast_stream)
+
+    def opts(self) -> _WalkOpts:
+        o = _WalkOpts()
+        lib().rt_walk_opts_default(C.byref(o))
+        o.rng_mode = RNG_MODES[self.rng]
+        o.fast_stream = self.fast_stream
+        return o
+
+    def Walk(self, t, steps: int, seed: int) -> None:
+        tt = _i32(t)
+        o = self.opts()
+        _check(lib().rt_lozenge_walk(_ptr(tt), side_of(tt), int(steps), int(seed), C.byref(o)))
+        _write_back(t, tt)
+
+    def cftp(self, tmax, tmin, driver_seed: int, first_steps: int = 128, schedule: int = 0, max_attempts: int = 20):
+        a, b = _i32(tmax), _i32(tmin)
+        out = np.zeros_like(a)
+        stats = CftpStats()
+        o = self.opts()
+        _check(lib().rt_lozenge_cftp(_ptr(a), _ptr(b), side_of(a), int(driver_seed), int(first_steps), int(schedule),
+                                     int(max_attempts), C.byref(o), _ptr(out), C.byref(stats)))
+        return out, stats.as_dict()
+
+    @staticmethod
+    def AlmostHexDomain(n: int, m: int) -> np.ndarray:
+        rows = C.c_int32()
+        r = 2 * n + 8
+        buf = np.zeros(2 * r * r, np.int32)
+        _check(lib().rt_lozenge_almost_hex_domain(n, m, _ptr(buf), buf.size, C.byref(rows)))
+        return buf[: 2 * rows.value * rows.value].copy()
+
+    @staticmethod
+    def Hexagon(n: int) -> np.ndarray:
+        """The a = b = c = n hexagon (declared at LozengeTiler.h:77; AlmostHexDomain(n, 0))."""
+        return LozengeTiler.AlmostHexDomain(n, 0)
+
+    @staticmethod
+    def DomainToVertices(d) -> np.ndarray:
+        dd = _i32(d)
+        m = _tri_side(dd)
+        out = np.zeros((m + 1) ** 2, np.int32)
+        _check(lib().rt_lozenge_domain_to_vertices(_ptr(dd), m, _ptr(out)))
+        return out
+
+    @staticmethod
+    def MaxTiling(d) -> np.ndarray:
+        dd = _i32(d)
+        m = _tri_side(dd)
+        out = np.zeros((m + 1) ** 2, np.int32)
+        _check(lib().rt_lozenge_max_tiling(_ptr(dd), m, _ptr(out)))
+        return out
+
+    @staticmethod
+    def MinTiling(d) -> np.ndarray:
+        dd = _i32(d)
+        m = _tri_side(dd)
+        out = np.zeros((m + 1) ** 2, np.int32)
+        _check(lib().rt_lozenge_min_tiling(_ptr(dd), m, _ptr(out)))
+        return out
+
+    @staticmethod
+    def TilingToHeightfunc(t, d) -> np.ndarray:
+        tt, dd = _i32(t), _i32(d)
+        n = side_of(tt)
+        out = np.zeros(n * n, np.int32)
+        _check(lib().rt_lozenge_tiling_to_heightfunc(_ptr(tt), _ptr(dd), n, _ptr(out)))
+        return out
+
+    @staticmethod
+    def HeightfuncToTiling(hf, d) -> np.ndarray:
+        hh, dd = _i32(hf), _i32(d)
+        n = side_of(hh)
+        out = np.zeros(n * n, np.int32)
+        _check(lib().rt_lozenge_heightfunc_to_tiling(_ptr(hh), _ptr(dd), n, _ptr(out)))
+        return out
+
+    @staticmethod
+    def TilingToDomain(t) -> np.ndarray:
+        tt = _i32(t)
+        n = side_of(tt)
+        out = np.zeros(2 * (n - 1) ** 2, np.int32)
+        _check(lib().rt_lozenge_tiling_to_domain(_ptr(tt), n, _ptr(out)))
+        return out
+
+
 class DominoSampler:
     """Device-resident coupled chains (rt_dm_sampler_*): the chains stay in HBM between
     calls; all chains share one random stream."""
@@ -411,5 +519,5 @@ def mt19937_draws(seed: int, count: int) -> np.ndarray:
     return rs.randint(0, 2**32, size=count, dtype=np.uint32)
 
 
-__all__ = ["DominoTiler", "DominoSampler", "RTError", "lib", "read_tinymt_params", "mt19937_colours",
+__all__ = ["DominoTiler", "DominoSampler", "LozengeTiler", "RTError", "lib", "read_tinymt_params", "mt19937_colours",
            "mt19937_draws", "CftpStats"]

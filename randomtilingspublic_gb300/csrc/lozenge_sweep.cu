@@ -1,0 +1,406 @@
+// The lozenge three-colour sweep on the GPU (reference: src/Lozenge/LozengeTiler.cpp:27-159
+// and src/Lozenge/lozengekernel.cl).
+//
+// Device layout of one chain: three colour arrays (colour c holds the vertices with
+// (j - i) mod 3 == c, column j / 3 of row i), each N rows x P bytes, P = N/3 rounded up to
+// 16.  One step rotates colour r: every vertex of that colour in state 25 becomes 38 with
+// probability 0.4 and every 38 becomes 25 with probability 0.4 (one draw decides both, so
+// coupled chains stay ordered), then rebuilds three bits of each of the two other colours.
+// TinyMT generator k = i * (N/3) + j for every vertex slot of the N x N/3 grid, as the
+// reference's NDRange numbers them.
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstring>
+#include <memory>
+#include <random>
+#include <string>
+#include <vector>
+
+#include "rng.cuh"
+#include "rt_internal.h"
+
+namespace rt {
+namespace {
+
+#define LZ_CUDA(expr)                                                                   \
+  do {                                                                                  \
+    cudaError_t _e = (expr);                                                            \
+    if (_e != cudaSuccess)                                                              \
+      return fail(RT_ERR_CUDA, std::string(#expr) + ": " + cudaGetErrorString(_e));     \
+  } while (0)
+
+struct LzView {
+  uint8_t* base;
+  int N, M, P, active;
+  size_t colour_stride, chain_stride;
+  uint4* tmt;
+  __host__ __device__ uint8_t* colour(int ch, int c) const {
+    return base + (size_t)ch * chain_stride + (size_t)c * colour_stride;
+  }
+};
+
+struct LzRule {
+  uint32_t lo_up, w_up, lo_dn, w_dn;
+};
+
+__device__ __forceinline__ uint8_t lz_flip(uint32_t e, uint32_t u, const LzRule& r) {
+  if (e == 25u) return (u - r.lo_up) < r.w_up ? 38 : 25;
+  if (e == 38u) return (u - r.lo_dn) < r.w_dn ? 25 : 38;
+  return (uint8_t)e;
+}
+
+__global__ void k_lz_seed(uint4* st, int64_t count, uint32_t seed) {
+  const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k < count) st[k] = tmt_seed(seed + (uint32_t)k, kTmtMat1, kTmtMat2, kTmtTmat);
+}
+
+__global__ void k_lz_rotate_tmt(LzView v, int r, LzRule rule) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x, i = blockIdx.y;
+  if (j >= v.M) return;
+  const int64_t k = (int64_t)i * v.M + j;
+  uint4 s = v.tmt[k];
+  const uint32_t u = tmt_next_u23(s, kTmtMat1, kTmtMat2, kTmtTmat);
+  v.tmt[k] = s;
+  for (int ch = 0; ch < v.active; ++ch) {
+    uint8_t* p = v.colour(ch, r) + (size_t)i * v.P + j;
+    const uint32_t e = *p;
+    const uint8_t n = lz_flip(e, u, rule);
+    if (n != e) *p = n;
+  }
+}
+
+__global__ void k_lz_rotate_fast(LzView v, int r, LzRule rule, uint64_t seed, uint32_t stream, int64_t h) {
+  const int q = blockIdx.x * blockDim.x + threadIdx.x, i = blockIdx.y;
+  if (4 * q >= v.M) return;
+  const uint4 d = fast_quad(seed, stream, h, (uint32_t)i, (uint32_t)q);
+  const uint32_t u4[4] = {d.x, d.y, d.z, d.w};
+  for (int ch = 0; ch < v.active; ++ch) {
+    uint8_t* row = v.colour(ch, r) + (size_t)i * v.P;
+#pragma unroll
+    for (int k4 = 0; k4 < 4; ++k4) {
+      const int j = 4 * q + k4;
+      if (j >= v.M) break;
+      const uint32_t e = row[j];
+      const uint8_t n = lz_flip(e, u4[k4], rule);
+      if (n != e) row[j] = n;
+    }
+  }
+}
+
+// lozengekernel.cl:107-125: colour (r+1) mod 3 gets bits 2, 4, 32 and colour (r+2) mod 3
+// bits 1, 8, 16 from the rotated colour's neighbours; the column offsets depend on i mod 3.
+__global__ void k_lz_update(LzView v, int r) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x + 1, i = blockIdx.y + 1;
+  if (j > v.M - 2 || i > v.N - 2) return;
+  const int im = i % 3;
+  const int p2 = im == (2 * r + 1) % 3, p4 = im == (2 * r + 2) % 3, p8 = im == (2 * r) % 3, p16 = p2;
+  for (int ch = 0; ch < v.active; ++ch) {
+    const uint8_t* A = v.colour(ch, r);
+    uint8_t* T2 = v.colour(ch, (r + 1) % 3) + (size_t)i * v.P + j;
+    uint8_t* T3 = v.colour(ch, (r + 2) % 3) + (size_t)i * v.P + j;
+    const uint8_t* up = A + (size_t)(i - 1) * v.P;
+    const uint8_t* mid = A + (size_t)i * v.P;
+    const uint8_t* dn = A + (size_t)(i + 1) * v.P;
+    *T2 = (uint8_t)((*T2 & ~(2 | 4 | 32)) | ((up[j + p2] & 16) >> 3) | ((mid[j - p4] & 8) >> 1) | ((dn[j] & 1) << 5));
+    *T3 = (uint8_t)((*T3 & ~(1 | 8 | 16)) | ((up[j] & 32) >> 5) | ((mid[j + p8] & 4) << 1) | ((dn[j - p16] & 2) << 3));
+  }
+}
+
+__global__ void k_lz_split(LzView v, int ch, const int32_t* t) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x, i = blockIdx.y;
+  if (j >= v.N) return;
+  const int c = ((j - i) % 3 + 3) % 3;
+  v.colour(ch, c)[(size_t)i * v.P + j / 3] = (uint8_t)t[(size_t)i * v.N + j];
+}
+
+__global__ void k_lz_merge(LzView v, int ch, int32_t* t) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x, i = blockIdx.y;
+  if (j >= v.N) return;
+  const int c = ((j - i) % 3 + 3) % 3;
+  t[(size_t)i * v.N + j] = v.colour(ch, c)[(size_t)i * v.P + j / 3];
+}
+
+__global__ void k_lz_diff(const uint32_t* x, const uint32_t* y, size_t words, unsigned long long* out) {
+  unsigned long long local = 0;
+  for (size_t w = (size_t)blockIdx.x * blockDim.x + threadIdx.x; w < words; w += (size_t)gridDim.x * blockDim.x)
+    local += __popc(__vcmpne4(x[w], y[w])) / 8;
+  for (int o = 16; o > 0; o >>= 1) local += __shfl_down_sync(0xffffffffu, local, o);
+  if ((threadIdx.x & 31) == 0 && local) atomicAdd(out, local);
+}
+
+// Acceptance intervals of the rotation (lozengekernel.cl:92-96): up when rd < 0.4, down when
+// 0.4 <= rd < 0.8.  TinyMT draws u23 = rd * 2^23 exactly; fast draws resolve the same 0.4 /
+// 0.4 on 32 bits.
+LzRule lz_rule(int rng_mode) {
+  LzRule r;
+  if (rng_mode == RT_RNG_TINYMT) {
+    auto below = [](double x) {  // number of u23 with u23 * 2^-23 < x
+      uint32_t lo = 0, hi = 1u << 23;
+      while (lo < hi) {
+        uint32_t mid = lo + (hi - lo) / 2;
+        float rd = (float)mid * (1.0f / 8388608.0f);
+        if ((double)rd < x) lo = mid + 1;
+        else hi = mid;
+      }
+      return lo;
+    };
+    const uint32_t c4 = below(.4), c8 = below(.8);
+    r = {0u, c4, c4, c8 - c4};
+  } else {
+    const uint32_t c4 = (uint32_t)std::ceil(0.4 * 4294967296.0), c8 = (uint32_t)std::ceil(0.8 * 4294967296.0);
+    r = {0u, c4, c4, c8 - c4};
+  }
+  return r;
+}
+
+struct LzSampler {
+  int N = 0, M = 0, P = 0, n_chains = 0, active = 0;
+  size_t colour_stride = 0, chain_stride = 0;
+  rt_walk_opts opts{};
+  LzRule rule{};
+  uint8_t* base = nullptr;
+  uint4* tmt = nullptr;
+  int32_t* scratch = nullptr;
+  unsigned long long* counter = nullptr;
+  cudaStream_t stream = nullptr;
+  bool own_stream = false;
+  int64_t interior[3] = {0, 0, 0};
+  int64_t steps_by_colour[3] = {0, 0, 0};
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+
+  ~LzSampler() {
+    if (base) cudaFree(base);
+    if (tmt) cudaFree(tmt);
+    if (scratch) cudaFree(scratch);
+    if (counter) cudaFree(counter);
+    if (ev0) cudaEventDestroy(ev0);
+    if (ev1) cudaEventDestroy(ev1);
+    if (own_stream && stream) cudaStreamDestroy(stream);
+  }
+  LzView view() const {
+    return LzView{base, N, M, P, active, colour_stride, chain_stride, tmt};
+  }
+  static rt_status create(int n_side, int chains, const rt_walk_opts& o, std::unique_ptr<LzSampler>* out) {
+    if (n_side < 9 || n_side % 3 || n_side > 32766)
+      return fail(RT_ERR_INVALID_ARGUMENT, "lozenge tiling side must be a multiple of 3 in [9, 32766]");
+    if (o.rng_mode != RT_RNG_TINYMT && o.rng_mode != RT_RNG_FAST) return fail(RT_ERR_INVALID_ARGUMENT, "unknown rng mode");
+    if (o.rng_mode == RT_RNG_FAST && o.fast_stream >= 65536u) return fail(RT_ERR_INVALID_ARGUMENT, "fast_stream must be < 65536");
+    if (o.tinymt_params) return fail(RT_ERR_INVALID_ARGUMENT, "lozenge sweep: per-generator parameter tables are not supported");
+    int devs = 0;
+    if (cudaGetDeviceCount(&devs) != cudaSuccess || devs == 0) {
+      cudaGetLastError();
+      return fail(RT_ERR_CUDA, "no CUDA device: the sweep has no CPU fallback");
+    }
+    auto s = std::make_unique<LzSampler>();
+    s->N = n_side;
+    s->M = n_side / 3;
+    s->P = (s->M + 15) / 16 * 16;
+    s->n_chains = s->active = chains;
+    s->opts = o;
+    s->rule = lz_rule(o.rng_mode);
+    s->colour_stride = (size_t)s->N * s->P;
+    s->chain_stride = 3 * s->colour_stride;
+    if (o.cuda_stream) {
+      s->stream = (cudaStream_t)o.cuda_stream;
+    } else {
+      LZ_CUDA(cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking));
+      s->own_stream = true;
+    }
+    LZ_CUDA(cudaEventCreate(&s->ev0));
+    LZ_CUDA(cudaEventCreate(&s->ev1));
+    LZ_CUDA(cudaMalloc(&s->base, s->chain_stride * chains));
+    LZ_CUDA(cudaMemsetAsync(s->base, 0, s->chain_stride * chains, s->stream));
+    LZ_CUDA(cudaMalloc(&s->scratch, (size_t)s->N * s->N * sizeof(int32_t)));
+    LZ_CUDA(cudaMalloc(&s->counter, sizeof(unsigned long long)));
+    if (o.rng_mode == RT_RNG_TINYMT) LZ_CUDA(cudaMalloc(&s->tmt, (size_t)s->N * s->M * sizeof(uint4)));
+    *out = std::move(s);
+    return RT_OK;
+  }
+  rt_status check() {
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return fail(RT_ERR_CUDA, std::string("kernel launch: ") + cudaGetErrorString(e));
+    return RT_OK;
+  }
+  rt_status load(int ch, const int32_t* t) {
+    for (size_t p = 0; p < (size_t)N * N; ++p)
+      if ((uint32_t)t[p] > 63u) return fail(RT_ERR_INVALID_ARGUMENT, "lozenge tiling values must be edge masks in [0, 63]");
+    if (ch == 0) {
+      // Interior vertices per colour (all six triangles covered): the flip attempts of one step.
+      std::vector<int32_t> dom((size_t)2 * (N - 1) * (N - 1)), cls((size_t)N * N);
+      if (rt_lozenge_tiling_to_domain(t, N, dom.data()) == RT_OK &&
+          rt_lozenge_domain_to_vertices(dom.data(), N - 1, cls.data()) == RT_OK) {
+        for (int c = 0; c < 3; ++c) interior[c] = 0;
+        for (int i = 0; i < N; ++i)
+          for (int j = 0; j < N; ++j)
+            if (cls[(size_t)i * N + j] == 1) interior[((j - i) % 3 + 3) % 3]++;
+      }
+      clear_error();
+    }
+    LZ_CUDA(cudaMemcpyAsync(scratch, t, (size_t)N * N * sizeof(int32_t), cudaMemcpyHostToDevice, stream));
+    k_lz_split<<<dim3((N + 255) / 256, N), 256, 0, stream>>>(view(), ch, scratch);
+    return check();
+  }
+  rt_status store(int ch, int32_t* t) {
+    k_lz_merge<<<dim3((N + 255) / 256, N), 256, 0, stream>>>(view(), ch, scratch);
+    if (rt_status s = check()) return s;
+    LZ_CUDA(cudaMemcpyAsync(t, scratch, (size_t)N * N * sizeof(int32_t), cudaMemcpyDeviceToHost, stream));
+    LZ_CUDA(cudaStreamSynchronize(stream));
+    return RT_OK;
+  }
+  rt_status copy_chain(int dst, int src) {
+    LZ_CUDA(cudaMemcpyAsync(base + dst * chain_stride, base + src * chain_stride, chain_stride, cudaMemcpyDeviceToDevice,
+                            stream));
+    return RT_OK;
+  }
+  rt_status seed(uint32_t s) {
+    const int64_t count = (int64_t)N * M;
+    k_lz_seed<<<(unsigned)((count + 255) / 256), 256, 0, stream>>>(tmt, count, s);
+    return check();
+  }
+  rt_status run(const uint8_t* colours, int64_t steps) {
+    const LzView v = view();
+    const dim3 gr((M + 127) / 128, N), gu((M + 127) / 128, N - 2);
+    for (int64_t s = 0; s < steps; ++s) {
+      const int r = colours[s];
+      k_lz_rotate_tmt<<<gr, 128, 0, stream>>>(v, r, rule);
+      k_lz_update<<<gu, 128, 0, stream>>>(v, r);
+      steps_by_colour[r]++;
+    }
+    return check();
+  }
+  rt_status run_fast(uint64_t seed_value, int64_t h0, int64_t steps) {
+    const LzView v = view();
+    const int quads = (M + 3) / 4;
+    const dim3 gr((quads + 127) / 128, N), gu((M + 127) / 128, N - 2);
+    for (int64_t s = 0; s < steps; ++s) {
+      const int64_t h = h0 + s;
+      const int r = (int)(((h % 3) + 3) % 3);
+      k_lz_rotate_fast<<<gr, 128, 0, stream>>>(v, r, rule, seed_value, opts.fast_stream, h);
+      k_lz_update<<<gu, 128, 0, stream>>>(v, r);
+      steps_by_colour[r]++;
+    }
+    return check();
+  }
+  rt_status diff(int a, int b, int64_t* nd) {
+    LZ_CUDA(cudaMemsetAsync(counter, 0, sizeof(unsigned long long), stream));
+    const size_t words = chain_stride / 4;
+    k_lz_diff<<<(unsigned)std::min<size_t>((words + 255) / 256, 1024), 256, 0, stream>>>(
+        reinterpret_cast<const uint32_t*>(base + a * chain_stride), reinterpret_cast<const uint32_t*>(base + b * chain_stride),
+        words, counter);
+    if (rt_status s = check()) return s;
+    unsigned long long h = 0;
+    LZ_CUDA(cudaMemcpyAsync(&h, counter, sizeof h, cudaMemcpyDeviceToHost, stream));
+    LZ_CUDA(cudaStreamSynchronize(stream));
+    *nd = (int64_t)h;
+    return RT_OK;
+  }
+};
+
+// LozengeTiler.cpp:84-90: colours from std::default_random_engine seeded with the walk seed
+// through uniform_int_distribution(0, 2).
+std::vector<uint8_t> lz_colours(int64_t seed, int64_t steps) {
+  std::default_random_engine gen;
+  std::uniform_int_distribution<int> dist(0, 2);
+  gen.seed(seed);
+  std::vector<uint8_t> c((size_t)steps);
+  for (int64_t s = 0; s < steps; ++s) c[(size_t)s] = (uint8_t)dist(gen);
+  return c;
+}
+
+rt_walk_opts opts_or_default(const rt_walk_opts* o) {
+  rt_walk_opts d;
+  rt_walk_opts_default(&d);
+  return o ? *o : d;
+}
+
+}  // namespace
+}  // namespace rt
+
+using namespace rt;
+
+extern "C" {
+
+RT_API rt_status rt_lozenge_walk(int32_t* tiling, int32_t n_side, int64_t steps, int64_t seed, const rt_walk_opts* opts) {
+  clear_error();
+  if (!tiling || steps < 0) return fail(RT_ERR_INVALID_ARGUMENT, "lozenge walk: NULL tiling or negative steps");
+  rt_walk_opts o = opts_or_default(opts);
+  std::unique_ptr<LzSampler> s;
+  if (rt_status st = LzSampler::create(n_side, 1, o, &s)) return st;
+  if (rt_status st = s->load(0, tiling)) return st;
+  if (o.rng_mode == RT_RNG_TINYMT) {
+    // LozengeTiler.cpp:71 (OpenCL branch): generators seeded with the walk seed itself.
+    if (rt_status st = s->seed((uint32_t)seed)) return st;
+    std::vector<uint8_t> col = lz_colours(seed, steps);
+    if (rt_status st = s->run(col.data(), steps)) return st;
+  } else {
+    if (rt_status st = s->run_fast((uint64_t)seed, 0, steps)) return st;
+  }
+  return s->store(0, tiling);
+}
+
+RT_API rt_status rt_lozenge_cftp(const int32_t* tmax, const int32_t* tmin, int32_t n_side, int64_t driver_seed,
+                                 int64_t first_steps, int32_t schedule, int32_t max_attempts, const rt_walk_opts* opts,
+                                 int32_t* out, rt_cftp_stats* stats) {
+  clear_error();
+  if (!tmax || !tmin || !out) return fail(RT_ERR_INVALID_ARGUMENT, "lozenge cftp: NULL tiling");
+  if (first_steps < 1 || max_attempts < 1 || max_attempts > 40 || (schedule != 0 && schedule != 1))
+    return fail(RT_ERR_INVALID_ARGUMENT, "lozenge cftp: first_steps >= 1, 1 <= max_attempts <= 40, schedule 0 or 1");
+  rt_walk_opts o = opts_or_default(opts);
+  std::unique_ptr<LzSampler> s;
+  if (rt_status st = LzSampler::create(n_side, 4, o, &s)) return st;
+  if (rt_status st = s->load(0, tmin)) return st;
+  if (rt_status st = s->load(2, tmin)) return st;
+  if (rt_status st = s->load(3, tmax)) return st;
+  s->active = 2;
+  std::mt19937 drv((uint32_t)driver_seed);
+  std::vector<int64_t> steps{first_steps};
+  std::vector<uint32_t> seeds{(uint32_t)drv()};
+  rt_cftp_stats st_out{};
+  float ms_total = 0.f;
+  for (int attempt = 1; attempt <= max_attempts; ++attempt) {
+    if (rt_status st = s->copy_chain(0, 2)) return st;
+    if (rt_status st = s->copy_chain(1, 3)) return st;
+    int64_t before[3] = {s->steps_by_colour[0], s->steps_by_colour[1], s->steps_by_colour[2]};
+    cudaEventRecord(s->ev0, s->stream);
+    int64_t look_back = 0;
+    if (o.rng_mode == RT_RNG_TINYMT) {
+      // Each epoch is one reference Walk(t, steps_k, seed_k) on both chains.
+      for (size_t k = 0; k < steps.size(); ++k) {
+        if (rt_status st = s->seed(seeds[k])) return st;
+        std::vector<uint8_t> col = lz_colours(seeds[k], steps[k]);
+        if (rt_status st = s->run(col.data(), steps[k])) return st;
+        look_back += steps[k];
+      }
+    } else {
+      const int64_t T = first_steps << (attempt - 1);
+      if (rt_status st = s->run_fast((uint64_t)driver_seed, -3 * T, 3 * T)) return st;
+      look_back = 3 * T;
+    }
+    cudaEventRecord(s->ev1, s->stream);
+    int64_t nd = -1;
+    if (rt_status st = s->diff(0, 1, &nd)) return st;
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, s->ev0, s->ev1);
+    ms_total += ms;
+    st_out.attempts = attempt;
+    st_out.total_steps += look_back;
+    st_out.final_steps = look_back;
+    for (int c = 0; c < 3; ++c) st_out.flip_attempts += 2 * (s->steps_by_colour[c] - before[c]) * s->interior[c];
+    st_out.seconds = ms_total * 1e-3;
+    if (nd == 0) {
+      if (stats) *stats = st_out;
+      return s->store(1, out);
+    }
+    if (o.rng_mode == RT_RNG_TINYMT) {
+      const int64_t next = schedule == 0 ? steps.back() * 2 : steps.front() * 2;
+      steps.insert(steps.begin(), next);
+      seeds.insert(seeds.begin(), (uint32_t)drv());
+    }
+  }
+  if (stats) *stats = st_out;
+  if (rt_status st = s->store(1, out)) return st;
+  return fail(RT_ERR_NOT_COALESCED, "lozenge cftp: chains did not coalesce within max_attempts");
+}
+
+}  // extern "C"

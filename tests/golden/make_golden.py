@@ -144,6 +144,72 @@ def main() -> None:
     out = {"generator": "tests/golden/make_golden.py", "cases": cases, "pins": pins, "host_cases": host_cases}
     (HERE / "domino_ref_cases.json").write_text(json.dumps(out, separators=(",", ":")))
     print(f"wrote {len(cases)} sweep cases, {len(host_cases)} host cases")
+    lozenge(args.ref)
+
+
+def lozenge(ref: str) -> None:
+    """Lozenge vectors from the reference-compiled src/Lozenge code (oracle/_ref/libref_lozenge.so)."""
+    lz = C.CDLL(str(ROOT / "oracle/_ref/libref_lozenge.so"))
+    P = lambda a: None if a is None else a.ctypes.data_as(C.c_void_p)
+    lz.ref_lz_walk.argtypes = [C.c_void_p, C.c_int, C.c_long, C.c_long, C.c_void_p, C.c_long]
+
+    def domain(n, m):
+        buf = np.zeros(2 * (2 * n + 9) ** 2, np.int32)
+        rows = lz.refh_lz_almost_hex_domain(n, m, P(buf), buf.size)
+        return buf[: 2 * rows * rows].copy(), rows
+
+    def extremal(d, rows, which):
+        out = np.zeros((rows + 1) ** 2, np.int32)
+        getattr(lz, f"refh_lz_{which}_tiling")(P(d), rows, P(out))
+        return out
+
+    def walk(t, n, steps, seed):
+        t = t.copy()
+        lz.ref_lz_walk(P(t), n, steps, seed, None, 0)
+        return t
+
+    cases, host = [], []
+    for n, m in [(2, 0), (3, 1), (5, 0), (10, 2)]:
+        d, rows = domain(n, m)
+        tmax, tmin = extremal(d, rows, "max"), extremal(d, rows, "min")
+        hf = np.zeros((rows + 1) ** 2, np.int32)
+        lz.refh_lz_tiling_to_heightfunc(P(tmax), P(d), rows + 1, P(hf))
+        v = np.zeros((rows + 1) ** 2, np.int32)
+        lz.refh_lz_domain_to_vertices(P(d), rows, P(v))
+        host.append({"n": n, "m": m, "domain": d.tolist(), "max": tmax.tolist(), "min": tmin.tolist(),
+                     "hf_max": hf.tolist(), "vertices": v.tolist()})
+        for which, start, steps, seed in [("max", tmax, 97, 34893), ("min", tmin, 250, -17)]:
+            cases.append({"name": f"lz_walk_hex{n}_{m}_{which}", "kind": "walk", "N": rows + 1, "start": start.tolist(),
+                          "steps": steps, "seed": seed, "expected": walk(start, rows + 1, steps, seed).tolist()})
+    # The MinimalLozenge example shape (Examples/MinimalLozengeEx.cpp:15-16): AlmostHexDomain(10, 2),
+    # MaxTiling start, 1000 steps; a fixed seed replaces its random_device.
+    d, rows = domain(10, 2)
+    start = extremal(d, rows, "max")
+    cases.append({"name": "lz_walk_minimal_lozenge", "kind": "walk", "N": rows + 1, "start": start.tolist(),
+                  "steps": 1000, "seed": 2018, "expected": walk(start, rows + 1, 1000, 2018).tolist()})
+    # CFTP from the reference's Walk: epochs of Walk(t, steps_k, seed_k) on both chains,
+    # seeds from mt19937(driver seed), prepending 2 * steps.back().
+    d, rows = domain(3, 0)
+    tmax, tmin = extremal(d, rows, "max"), extremal(d, rows, "min")
+    drv = np.random.RandomState(777)
+    draw = lambda: int(drv.randint(0, 2**32, dtype=np.uint32))
+    steps, seeds, attempts = [16], [draw()], 0
+    while True:
+        attempts += 1
+        top, bot = tmax.copy(), tmin.copy()
+        for st, sd in zip(steps, seeds):
+            top, bot = walk(top, rows + 1, st, sd), walk(bot, rows + 1, st, sd)
+        if np.array_equal(top, bot):
+            break
+        steps.insert(0, steps[-1] * 2)
+        seeds.insert(0, draw())
+        assert attempts < 40
+    cases.append({"name": "lz_cftp_hex3", "kind": "cftp", "N": rows + 1, "tmax": tmax.tolist(), "tmin": tmin.tolist(),
+                  "driver_seed": 777, "first_steps": 16, "schedule": 0, "attempts": attempts,
+                  "expected": top.tolist()})
+    (HERE / "lozenge_ref_cases.json").write_text(json.dumps({"generator": "tests/golden/make_golden.py", "cases": cases,
+                                                             "host_cases": host}, separators=(",", ":")))
+    print(f"wrote {len(cases)} lozenge sweep cases, {len(host)} lozenge host cases")
 
 
 if __name__ == "__main__":

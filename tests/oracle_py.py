@@ -197,3 +197,71 @@ def tmt_seed_states(seed: int, count: int) -> np.ndarray:
     out = np.zeros((count, 4), np.uint32)
     lib().orc_tmt_seed_states(seed & 0xFFFFFFFF, count, _p(out))
     return out
+
+
+# ---- lozenge ---------------------------------------------------------------------------
+_LZ_SIG = {
+    "orc_lz_almost_hex_domain": (C.c_int, [C.c_int, C.c_int, _P, _L]),
+    "orc_lz_domain_to_vertices": (None, [_P, C.c_int, _P]),
+    "orc_lz_max_tiling": (C.c_int, [_P, C.c_int, _P]),
+    "orc_lz_min_tiling": (C.c_int, [_P, C.c_int, _P]),
+    "orc_lz_heightfunc_to_tiling": (None, [_P, _P, C.c_int, _P]),
+    "orc_lz_tiling_to_heightfunc": (None, [_P, _P, C.c_int, _P]),
+    "orc_lz_tiling_to_domain": (None, [_P, C.c_int, _P]),
+    "orc_lz_walk_tinymt": (C.c_int, [_P, C.c_int, _L, _L, _P, _L]),
+    "orc_lz_walk_fast": (C.c_int, [_P, C.c_int, _L, _L, C.c_ulong, C.c_uint]),
+    "orc_lz_cftp": (C.c_int, [_P, _P, C.c_int, _L, _L, C.c_int, C.c_int, C.c_int, C.c_uint, _P, _P]),
+}
+
+
+def lz_lib() -> C.CDLL:
+    h = lib()
+    for name, (res, args) in _LZ_SIG.items():
+        f = getattr(h, name)
+        f.restype = res
+        f.argtypes = args
+    return h
+
+
+def lz_almost_hex(n: int, m: int) -> np.ndarray:
+    buf = np.zeros(2 * (2 * n + 9) ** 2, np.int32)
+    rows = lz_lib().orc_lz_almost_hex_domain(n, m, _p(buf), buf.size)
+    return buf[: 2 * rows * rows].copy()
+
+
+def _tri(d) -> int:
+    import math
+    return math.isqrt(len(d) // 2)
+
+
+def lz_extremal(d, which: str):
+    d = _i32(d)
+    m = _tri(d)
+    out = np.zeros((m + 1) ** 2, np.int32)
+    rc = getattr(lz_lib(), f"orc_lz_{which}_tiling")(_p(d), m, _p(out))
+    return rc, out
+
+
+def lz_tiling_to_heightfunc(t, d) -> np.ndarray:
+    t, d = _i32(t), _i32(d)
+    n = _side(t)
+    out = np.zeros(n * n, np.int32)
+    lz_lib().orc_lz_tiling_to_heightfunc(_p(t), _p(d), n, _p(out))
+    return out
+
+
+def lz_walk_tinymt(t: np.ndarray, n: int, steps: int, seed: int) -> None:
+    assert lz_lib().orc_lz_walk_tinymt(_p(t), n, steps, seed, None, 0) == 0
+
+
+def lz_walk_fast(t: np.ndarray, n: int, h0: int, steps: int, seed: int, stream: int = 0) -> None:
+    assert lz_lib().orc_lz_walk_fast(_p(t), n, h0, steps, seed, stream) == 0
+
+
+def lz_cftp(tmax, tmin, n, driver_seed, first, schedule, max_attempts, fast=False, stream=0):
+    tmax, tmin = _i32(tmax), _i32(tmin)
+    out = np.zeros_like(tmax)
+    total = C.c_long()
+    att = lz_lib().orc_lz_cftp(_p(tmax), _p(tmin), n, driver_seed, first, schedule, max_attempts, 1 if fast else 0,
+                               stream, _p(out), C.addressof(total))
+    return out, att, total.value
