@@ -170,6 +170,43 @@ RT_API rt_status rt_lozenge_cftp(const int32_t* tmax, const int32_t* tmin, int32
                                  int64_t first_steps, int32_t schedule, int32_t max_attempts,
                                  const rt_walk_opts* opts, int32_t* out, rt_cftp_stats* stats);
 
+/* ---- batched coupling from the past --------------------------------------------------------
+   No counterpart in the reference (which runs one instance at a time).  Many independent
+   fast-mode CFTP instances of uneven sizes, dominoes and lozenges mixed, in one persistent
+   launch: each CTA takes instances from a device work queue and runs an instance's whole
+   CFTP in shared memory.  Instance k returns exactly what rt_domino_cftp / rt_lozenge_cftp
+   return with rng_mode RT_RNG_FAST, fast_stream = stream and driver_seed = seed. */
+#define RT_MODEL_DOMINO 0
+#define RT_MODEL_LOZENGE 1
+
+typedef struct rt_cftp_instance {
+  int32_t model;        /* RT_MODEL_DOMINO or RT_MODEL_LOZENGE */
+  int32_t n_side;       /* tiling side N */
+  int32_t rule;         /* dominoes: RT_DOMINO_CFTP or RT_DOMINO_CFTP_TWOPERIODIC */
+  int32_t max_attempts; /* <= 40 */
+  double weight_a, weight_b;
+  uint64_t seed;        /* driver seed of the instance's draws */
+  uint32_t stream;      /* < 65536 */
+  int32_t pad;
+  int64_t first_steps;  /* sweeps of the first attempt; attempt j uses first_steps * 2^j */
+  const int32_t* tmax;  /* host N x N extremal tilings */
+  const int32_t* tmin;
+  int32_t* out;         /* host N x N sample (the top chain of the last attempt) */
+  int32_t attempts;     /* out: attempts run; negative when the instance did not coalesce */
+  int32_t pad2;
+  int64_t final_steps;  /* out: half-sweeps (steps) of the last attempt */
+} rt_cftp_instance;
+
+typedef struct rt_batch_stats {
+  int32_t instances, coalesced, ctas, pad;
+  double seconds;       /* device time of the batch kernel */
+} rt_batch_stats;
+
+/* Runs every instance; RT_ERR_NOT_COALESCED if any instance ran out of attempts (its out
+   and attempts are still written).  Each instance's two chains must fit one CTA's shared
+   memory (about 2 x N^2 bytes: N up to about 330 for dominoes, 340 for lozenges). */
+RT_API rt_status rt_cftp_batch(rt_cftp_instance* inst, int32_t count, void* cuda_stream, rt_batch_stats* stats);
+
 /* ---- device-resident chains --------------------------------------------------------------
    A sampler keeps n_chains coupled chains of one N x N domain on the GPU; all chains see
    the same random stream (CFTP couples the max and min chains this way).  The building

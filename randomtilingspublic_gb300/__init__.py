@@ -69,6 +69,20 @@ class CftpStats(C.Structure):
         return {f: getattr(self, f) for f, _ in self._fields_}
 
 
+class CftpInstance(C.Structure):
+    _fields_ = [
+        ("model", C.c_int32), ("n_side", C.c_int32), ("rule", C.c_int32), ("max_attempts", C.c_int32),
+        ("weight_a", C.c_double), ("weight_b", C.c_double), ("seed", C.c_uint64), ("stream", C.c_uint32),
+        ("pad", C.c_int32), ("first_steps", C.c_int64), ("tmax", C.c_void_p), ("tmin", C.c_void_p),
+        ("out", C.c_void_p), ("attempts", C.c_int32), ("pad2", C.c_int32), ("final_steps", C.c_int64),
+    ]
+
+
+class BatchStats(C.Structure):
+    _fields_ = [("instances", C.c_int32), ("coalesced", C.c_int32), ("ctas", C.c_int32), ("pad", C.c_int32),
+                ("seconds", C.c_double)]
+
+
 _P = C.c_void_p
 _SIGNATURES = {
     "rt_walk_opts_default": (None, [_P]),
@@ -104,6 +118,7 @@ _SIGNATURES = {
     "rt_dm_sampler_engine_info": (C.c_int32, [_P, _P]),
     "rt_domino_rule_table": (C.c_int32, [C.c_int32, C.c_int32, C.c_double, C.c_double, _P]),
     "rt_dm_sweep_noalloc": (C.c_int32, [_P, _P, C.c_int32, C.c_int32, _P, C.c_int64, C.c_uint64, C.c_int64, _P]),
+    "rt_cftp_batch": (C.c_int32, [_P, C.c_int32, _P, _P]),
     "rt_lozenge_almost_hex_domain": (C.c_int32, [C.c_int32, C.c_int32, _P, C.c_int64, _P]),
     "rt_lozenge_domain_to_vertices": (C.c_int32, [_P, C.c_int32, _P]),
     "rt_lozenge_max_tiling": (C.c_int32, [_P, C.c_int32, _P]),
@@ -506,6 +521,36 @@ class DominoSampler:
         return {"engine": int(out[0]), "units": int(out[1]), "bands": int(out[2]), "units_per_thread": int(out[3])}
 
 
+def cftp_batch(jobs, cuda_stream: int | None = None):
+    """Batched fast-mode CFTP (rt_cftp_batch).  jobs: dicts with model ('domino' or
+    'lozenge'), tmax, tmin, seed, stream and optional rule, a, b, first_steps, max_attempts.
+    Returns (samples, per-job attempts, stats dict)."""
+    n = len(jobs)
+    arr = (CftpInstance * n)()
+    keep = []
+    outs = []
+    for k, j in enumerate(jobs):
+        tmax, tmin = _i32(j["tmax"]), _i32(j["tmin"])
+        out = np.zeros_like(tmax)
+        keep += [tmax, tmin]
+        outs.append(out)
+        x = arr[k]
+        x.model = 0 if j["model"] == "domino" else 1
+        x.n_side = side_of(tmax)
+        x.rule = DOMINO_RULES[j.get("rule", "cftp")]
+        x.max_attempts = int(j.get("max_attempts", 20))
+        x.weight_a, x.weight_b = float(j.get("a", 1.0)), float(j.get("b", 1.0))
+        x.seed, x.stream = int(j["seed"]), int(j["stream"])
+        x.first_steps = int(j.get("first_steps", 8))
+        x.tmax, x.tmin, x.out = _ptr(tmax), _ptr(tmin), _ptr(out)
+    stats = BatchStats()
+    st = lib().rt_cftp_batch(arr, n, cuda_stream, C.byref(stats))
+    if st not in (RT_OK, RT_ERR_NOT_COALESCED):
+        _check(st)
+    attempts = [arr[k].attempts for k in range(n)]
+    return outs, attempts, {f: getattr(stats, f) for f, _ in BatchStats._fields_ if f != "pad"}
+
+
 def mt19937_colours(seed: int, steps: int, skip: int = 0) -> np.ndarray:
     """Colour stream of the reference's host loop: mt19937(seed)() % 2 per step, after
     ``skip`` draws (DominoTiler.cpp:51,70)."""
@@ -519,5 +564,5 @@ def mt19937_draws(seed: int, count: int) -> np.ndarray:
     return rs.randint(0, 2**32, size=count, dtype=np.uint32)
 
 
-__all__ = ["DominoTiler", "DominoSampler", "LozengeTiler", "RTError", "lib", "read_tinymt_params", "mt19937_colours",
+__all__ = ["DominoTiler", "DominoSampler", "LozengeTiler", "cftp_batch", "RTError", "lib", "read_tinymt_params", "mt19937_colours",
            "mt19937_draws", "CftpStats"]
