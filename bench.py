@@ -166,6 +166,60 @@ def cpu_leg(rt, orc, tmax, tmin, interior, steps_per_sample: int, samples: int, 
     return rates
 
 
+BATCH_INSTANCES = 2048
+BATCH_ORDERS = (16, 48)   # Aztec diamond orders, uniform
+BATCH_SIDES = (8, 24)     # hexagon sides, uniform
+
+
+def batched_leg(rt, plain_samples: int = 8) -> dict:
+    """Batched fast-mode CFTP (rt_cftp_batch) on a mixed batch, against the same instances
+    run one at a time through the plain entry points (rt_domino_cftp / rt_lozenge_cftp).
+    Half the instances are Aztec diamonds, half hexagons; half of the diamonds are
+    2-periodic with a = 1, b ~ U[0.3, 1]; seed k, stream k."""
+    D, L = rt.DominoTiler, rt.LozengeTiler
+    rng = np.random.default_rng(20261203)
+    cache, jobs = {}, []
+    for k in range(BATCH_INSTANCES):
+        if k % 2 == 0:
+            order = int(rng.integers(BATCH_ORDERS[0], BATCH_ORDERS[1] + 1))
+            if ("d", order) not in cache:
+                d = D.AztecDiamond(order)
+                cache[("d", order)] = (D.MaxTiling(d), D.MinTiling(d))
+            tmax, tmin = cache[("d", order)]
+            weighted = (k // 2) % 2 == 1
+            jobs.append({"model": "domino", "tmax": tmax, "tmin": tmin, "seed": k, "stream": k,
+                         "rule": "cftp_twoperiodic" if weighted else "cftp", "a": 1.0,
+                         "b": float(rng.uniform(0.3, 1.0)) if weighted else 1.0, "first_steps": 64})
+        else:
+            side = int(rng.integers(BATCH_SIDES[0], BATCH_SIDES[1] + 1))
+            if ("l", side) not in cache:
+                d = L.Hexagon(side)
+                cache[("l", side)] = (L.MaxTiling(d), L.MinTiling(d))
+            tmax, tmin = cache[("l", side)]
+            jobs.append({"model": "lozenge", "tmax": tmax, "tmin": tmin, "seed": k, "stream": k, "first_steps": 64})
+    rt.cftp_batch(jobs[:64])  # warm-up
+    t0 = time.perf_counter()
+    outs, attempts, stats = rt.cftp_batch(jobs)
+    wall = time.perf_counter() - t0
+    lat = []
+    for job in jobs[:plain_samples]:
+        tiler = (rt.DominoTiler(rule=job["rule"], rng="fast", a=job["a"], b=job["b"], fast_stream=job["stream"])
+                 if job["model"] == "domino" else rt.LozengeTiler(rng="fast", fast_stream=job["stream"]))
+        t1 = time.perf_counter()
+        tiler.cftp(job["tmax"], job["tmin"], job["seed"], first_steps=job["first_steps"], schedule=1, max_attempts=20)
+        lat.append(time.perf_counter() - t1)
+    lat = np.array(lat)
+    plain_rate = 1.0 / lat.mean()
+    return {"workload": f"{BATCH_INSTANCES} CFTP instances: Aztec orders U{list(BATCH_ORDERS)} and hexagon sides "
+                        f"U{list(BATCH_SIDES)}, half 2-periodic (a=1, b~U[0.3,1]), seeds and streams 0..{BATCH_INSTANCES - 1}",
+            "samples_per_s": len(jobs) / wall, "coalesced": stats["coalesced"], "kernel_s": stats["seconds"],
+            "wall_s": wall, "ctas": stats["ctas"],
+            "plain_samples_per_s": plain_rate, "plain_sampled_instances": plain_samples,
+            "plain_latency_p50_s": float(np.percentile(lat, 50)), "plain_latency_p99_s": float(np.percentile(lat, 99)),
+            "batched_over_plain": (len(jobs) / wall) / plain_rate,
+            "api": "rt_cftp_batch vs rt_domino_cftp / rt_lozenge_cftp, fast RNG mode, identical samples"}
+
+
 def run_reference(args) -> None:
     rank, ws, local, dist = _dist()
     if rank != 0:
@@ -337,6 +391,9 @@ def run_ours(args) -> None:
                "sample": f"{sample} TinyMT half-sweeps of the coupled max/min chains (order {ORDER}) per attempt, "
                          f"2 attempts, {threads} host threads"}
     s.close()
+    batched = None
+    if rank == 0 and not args.no_batch:
+        batched = batched_leg(rt)
     if rank == 0:
         line = {
             "metric": METRIC, "value": value, "unit": "flip attempts/s", "n_gpus": ws, "steps": args.steps,
@@ -346,6 +403,7 @@ def run_ours(args) -> None:
                        "rng": args.mode, "engine": args.engine, "half_sweeps_per_step": HALF_SWEEPS,
                        "l2": "flushed between timed steps (256 MiB write)", "parallelism": f"replicas{ws}"},
             "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches, "clocks": clocks,
+            "batched_cftp": batched,
         }
         print(json.dumps(line))
     if dist is not None:
@@ -361,6 +419,7 @@ def main() -> None:
     ap.add_argument("--mode", choices=["tinymt", "fast"], default="tinymt")
     ap.add_argument("--engine", type=int, default=0)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-batch", action="store_true")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)
