@@ -42,6 +42,7 @@ typedef int32_t rt_status;
 #define RT_ERR_OUT_OF_MEMORY 5
 #define RT_ERR_NOT_COALESCED 6
 #define RT_ERR_BUFFER_TOO_SMALL 7
+#define RT_ERR_BUSY 8
 
 /* Random-number modes of the sweep. */
 #define RT_RNG_TINYMT 0 /* one TinyMT32 generator per site, the reference's OpenCL path
@@ -206,6 +207,35 @@ typedef struct rt_batch_stats {
    and attempts are still written).  Each instance's two chains must fit one CTA's shared
    memory (about 2 x N^2 bytes: N up to about 330 for dominoes, 340 for lozenges). */
 RT_API rt_status rt_cftp_batch(rt_cftp_instance* inst, int32_t count, void* cuda_stream, rt_batch_stats* stats);
+
+/* ---- serving: continuous batching ----------------------------------------------------------
+   No counterpart in the reference.  A request is one fast-mode CFTP instance
+   (rt_cftp_instance).  Submitted requests go to a ring of slots in pinned host memory that
+   the GPU reads directly; a persistent kernel's CTAs claim them in order as they free up
+   (requests that arrive while others run join without waiting for them), run each one's
+   CFTP in shared memory and flag it done.  The kernel leaves after idle_seconds without
+   work and is relaunched by the next submit / poll / wait.  Admission: a request needs a
+   free slot and its footprint (3 colour-split tilings) within memory_budget_bytes, else
+   RT_ERR_BUSY.  Results equal rt_cftp_batch's and the plain entry points'.  One host thread
+   per server. */
+typedef struct rt_server rt_server;
+typedef struct rt_server_opts {
+  int32_t slots;                 /* ring capacity: requests submitted and not yet collected */
+  int32_t max_side;              /* largest tiling side accepted, <= 330 */
+  int64_t memory_budget_bytes;   /* cap on the staged state of requests in flight */
+  double idle_seconds;           /* the kernel leaves after this long without work (0: 0.25 s) */
+  void* cuda_stream;             /* NULL: the server's own stream */
+} rt_server_opts;
+
+RT_API rt_status rt_server_create(const rt_server_opts* opts, rt_server** out);
+/* Copies the request (its tmax / tmin) and returns its ticket; req->out is not used here. */
+RT_API rt_status rt_server_submit(rt_server* s, const rt_cftp_instance* req, int64_t* ticket);
+RT_API rt_status rt_server_poll(rt_server* s, int64_t ticket, int32_t* done);
+/* Waits up to timeout_s, writes the sample to result->out (N x N) and result->attempts /
+   final_steps, and frees the ticket's slot. */
+RT_API rt_status rt_server_wait(rt_server* s, int64_t ticket, double timeout_s, rt_cftp_instance* result);
+/* Asks the kernel to leave, waits for it and frees everything. */
+RT_API rt_status rt_server_destroy(rt_server* s);
 
 /* ---- device-resident chains --------------------------------------------------------------
    A sampler keeps n_chains coupled chains of one N x N domain on the GPU; all chains see

@@ -31,6 +31,7 @@ RT_ERR_TIMEOUT = 4
 RT_ERR_OUT_OF_MEMORY = 5
 RT_ERR_NOT_COALESCED = 6
 RT_ERR_BUFFER_TOO_SMALL = 7
+RT_ERR_BUSY = 8
 
 RNG_MODES = {"tinymt": 0, "fast": 1}
 DOMINO_RULES = {"plain": 0, "cftp": 1, "twoperiodic": 2, "cftp_twoperiodic": 3}
@@ -83,6 +84,11 @@ class BatchStats(C.Structure):
                 ("seconds", C.c_double)]
 
 
+class ServerOpts(C.Structure):
+    _fields_ = [("slots", C.c_int32), ("max_side", C.c_int32), ("memory_budget_bytes", C.c_int64),
+                ("idle_seconds", C.c_double), ("cuda_stream", C.c_void_p)]
+
+
 _P = C.c_void_p
 _SIGNATURES = {
     "rt_walk_opts_default": (None, [_P]),
@@ -119,6 +125,11 @@ _SIGNATURES = {
     "rt_domino_rule_table": (C.c_int32, [C.c_int32, C.c_int32, C.c_double, C.c_double, _P]),
     "rt_dm_sweep_noalloc": (C.c_int32, [_P, _P, C.c_int32, C.c_int32, _P, C.c_int64, C.c_uint64, C.c_int64, _P]),
     "rt_cftp_batch": (C.c_int32, [_P, C.c_int32, _P, _P]),
+    "rt_server_create": (C.c_int32, [_P, _P]),
+    "rt_server_submit": (C.c_int32, [_P, _P, _P]),
+    "rt_server_poll": (C.c_int32, [_P, C.c_int64, _P]),
+    "rt_server_wait": (C.c_int32, [_P, C.c_int64, C.c_double, _P]),
+    "rt_server_destroy": (C.c_int32, [_P]),
     "rt_lozenge_almost_hex_domain": (C.c_int32, [C.c_int32, C.c_int32, _P, C.c_int64, _P]),
     "rt_lozenge_domain_to_vertices": (C.c_int32, [_P, C.c_int32, _P]),
     "rt_lozenge_max_tiling": (C.c_int32, [_P, C.c_int32, _P]),
@@ -551,6 +562,66 @@ def cftp_batch(jobs, cuda_stream: int | None = None):
     return outs, attempts, {f: getattr(stats, f) for f, _ in BatchStats._fields_ if f != "pad"}
 
 
+def _instance(job) -> tuple:
+    tmax, tmin = _i32(job["tmax"]), _i32(job["tmin"])
+    x = CftpInstance()
+    x.model = 0 if job["model"] == "domino" else 1
+    x.n_side = side_of(tmax)
+    x.rule = DOMINO_RULES[job.get("rule", "cftp")]
+    x.max_attempts = int(job.get("max_attempts", 20))
+    x.weight_a, x.weight_b = float(job.get("a", 1.0)), float(job.get("b", 1.0))
+    x.seed, x.stream = int(job["seed"]), int(job["stream"])
+    x.first_steps = int(job.get("first_steps", 8))
+    x.tmax, x.tmin = _ptr(tmax), _ptr(tmin)
+    return x, (tmax, tmin)
+
+
+class Server:
+    """Continuous-batching CFTP server (rt_server_*): submit requests as they arrive, collect
+    each result when done."""
+
+    def __init__(self, slots: int = 4096, max_side: int = 130, memory_budget_bytes: int = 120 << 30,
+                 idle_seconds: float = 0.25):
+        o = ServerOpts(slots, max_side, memory_budget_bytes, idle_seconds, None)
+        h = C.c_void_p()
+        _check(lib().rt_server_create(C.byref(o), C.byref(h)))
+        self.h = h
+        self._side = {}
+
+    def submit(self, job) -> int:
+        x, keep = _instance(job)
+        t = C.c_int64()
+        _check(lib().rt_server_submit(self.h, C.byref(x), C.byref(t)))
+        self._side[t.value] = side_of(keep[0])
+        return t.value
+
+    def poll(self, ticket: int) -> bool:
+        d = C.c_int32()
+        _check(lib().rt_server_poll(self.h, ticket, C.byref(d)))
+        return bool(d.value)
+
+    def wait(self, ticket: int, timeout: float = 60.0):
+        n = self._side.pop(ticket)
+        out = np.zeros(n * n, np.int32)
+        x = CftpInstance()
+        x.out = _ptr(out)
+        st = lib().rt_server_wait(self.h, ticket, timeout, C.byref(x))
+        if st not in (RT_OK, RT_ERR_NOT_COALESCED):
+            _check(st)
+        return out, x.attempts, x.final_steps
+
+    def close(self) -> None:
+        if self.h:
+            lib().rt_server_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 def mt19937_colours(seed: int, steps: int, skip: int = 0) -> np.ndarray:
     """Colour stream of the reference's host loop: mt19937(seed)() % 2 per step, after
     ``skip`` draws (DominoTiler.cpp:51,70)."""
@@ -564,5 +635,5 @@ def mt19937_draws(seed: int, count: int) -> np.ndarray:
     return rs.randint(0, 2**32, size=count, dtype=np.uint32)
 
 
-__all__ = ["DominoTiler", "DominoSampler", "LozengeTiler", "cftp_batch", "RTError", "lib", "read_tinymt_params", "mt19937_colours",
+__all__ = ["DominoTiler", "DominoSampler", "LozengeTiler", "cftp_batch", "Server", "RTError", "lib", "read_tinymt_params", "mt19937_colours",
            "mt19937_draws", "CftpStats"]

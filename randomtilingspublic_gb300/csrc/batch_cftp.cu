@@ -14,9 +14,11 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <cstring>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "domino_rules.h"
@@ -161,6 +163,45 @@ __device__ void lozenge_step(uint8_t* sm, const DevInstance& in, int r, int64_t 
   __syncthreads();
 }
 
+// Runs one instance's CFTP in shared memory: tmax / tmin / out are its colour arrays in
+// global or mapped host memory (loaded with volatile reads, since a serving slot is reused).
+// Returns the attempts run (negative when it did not coalesce) and the last look-back.
+__device__ void run_instance(uint8_t* sm, const DevInstance& in, const uint8_t* tmax, const uint8_t* tmin, uint8_t* out,
+                             uint32_t lz_c4, uint32_t lz_c8, uint32_t* red, int* attempts_out, int64_t* look_out) {
+  const int ncol = in.model == 0 ? 2 : 3;
+  const size_t chain = (size_t)ncol * in.N * in.P;
+  const uint32_t* gmax = reinterpret_cast<const uint32_t*>(tmax);
+  const uint32_t* gmin = reinterpret_cast<const uint32_t*>(tmin);
+  uint32_t* s32 = reinterpret_cast<uint32_t*>(sm);
+  const int words = (int)(chain / 4);
+  int attempts = 0;
+  int64_t look = 0;
+  bool done = false;
+  for (int att = 0; att < in.max_attempts && !done; ++att) {
+    // chain 0 starts at the min tiling, chain 1 at the max tiling
+    for (int w = threadIdx.x; w < words; w += kBatchThreads) {
+      s32[w] = __ldcv(gmin + w);
+      s32[words + w] = __ldcv(gmax + w);
+    }
+    __syncthreads();
+    const int64_t T = in.first_sweeps << att;
+    look = ncol * T;
+    for (int64_t h = -look; h < 0; ++h) {
+      if (in.model == 0) domino_half_sweep(sm, in, (h & 1) ? 0 : 1, h);
+      else lozenge_step(sm, in, (int)(((h % 3) + 3) % 3), h, lz_c4, lz_c8);
+    }
+    uint32_t differ = 0;
+    for (int w = threadIdx.x; w < words; w += kBatchThreads) differ += s32[w] != s32[words + w];
+    differ = block_sum(differ, red);
+    attempts = att + 1;
+    done = differ == 0;
+  }
+  uint32_t* gout = reinterpret_cast<uint32_t*>(out);
+  for (int w = threadIdx.x; w < words; w += kBatchThreads) __stcg(gout + w, s32[words + w]);
+  *attempts_out = done ? attempts : -attempts;
+  *look_out = look;
+}
+
 __global__ void __launch_bounds__(kBatchThreads) k_batch_cftp(BatchArgs a, uint32_t lz_c4, uint32_t lz_c8) {
   extern __shared__ __align__(16) uint8_t sm[];
   __shared__ int s_idx;
@@ -173,43 +214,167 @@ __global__ void __launch_bounds__(kBatchThreads) k_batch_cftp(BatchArgs a, uint3
     if (idx >= a.count) break;
     DevInstance& g = a.inst[idx];
     const DevInstance in = g;
-    const int ncol = in.model == 0 ? 2 : 3;
-    const size_t plane = (size_t)in.N * in.P, chain = ncol * plane;
-    const uint32_t* gmax = reinterpret_cast<const uint32_t*>(a.tilings + in.off_max);
-    const uint32_t* gmin = reinterpret_cast<const uint32_t*>(a.tilings + in.off_min);
-    uint32_t* s32 = reinterpret_cast<uint32_t*>(sm);
-    const int words = (int)(chain / 4);
-    int attempts = 0;
-    int64_t look = 0;
-    bool done = false;
-    for (int att = 0; att < in.max_attempts && !done; ++att) {
-      // chain 0 starts at the min tiling, chain 1 at the max tiling
-      for (int w = threadIdx.x; w < words; w += kBatchThreads) {
-        s32[w] = gmin[w];
-        s32[words + w] = gmax[w];
-      }
-      __syncthreads();
-      const int64_t T = in.first_sweeps << att;
-      look = ncol * T;
-      for (int64_t h = -look; h < 0; ++h) {
-        if (in.model == 0) domino_half_sweep(sm, in, (h & 1) ? 0 : 1, h);
-        else lozenge_step(sm, in, (int)(((h % 3) + 3) % 3), h, lz_c4, lz_c8);
-      }
-      uint32_t differ = 0;
-      for (int w = threadIdx.x; w < words; w += kBatchThreads) differ += s32[w] != s32[words + w];
-      differ = block_sum(differ, red);
-      attempts = att + 1;
-      done = differ == 0;
-    }
-    uint32_t* gout = reinterpret_cast<uint32_t*>(a.tilings + in.off_out);
-    for (int w = threadIdx.x; w < words; w += kBatchThreads) gout[w] = s32[words + w];
+    int att;
+    int64_t look;
+    run_instance(sm, in, a.tilings + in.off_max, a.tilings + in.off_min, a.tilings + in.off_out, lz_c4, lz_c8, red, &att,
+                 &look);
     if (threadIdx.x == 0) {
-      g.attempts = done ? attempts : -attempts;
+      g.attempts = att;
       g.final_half_sweeps = look;
     }
     __syncthreads();
   }
 }
+
+// ---- serving: continuous batching on a persistent kernel ------------------------------------
+// Shared with the host in pinned, device-mapped memory.
+struct ServeRing {
+  uint64_t tail;       // requests published by the host (release store after the slot is written)
+  uint32_t shutdown;   // host asks the kernel to leave
+  uint32_t pad;
+};
+
+struct ServeArgs {
+  ServeRing* ring;             // mapped host memory
+  DevInstance* desc;           // [slots], mapped host memory
+  uint8_t* data;               // [slots][slot_bytes], mapped host memory
+  uint64_t* done;              // [slots], mapped host memory: ticket + 1 once finished
+  unsigned long long* head;    // device memory: tickets claimed so far
+  int slots;
+  size_t slot_bytes;
+  long idle_polls;             // polls without work before a CTA leaves
+};
+
+__device__ __forceinline__ uint64_t ld_acquire_sys(const uint64_t* p) {
+  uint64_t v;
+  asm volatile("ld.acquire.sys.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ void st_release_sys(uint64_t* p, uint64_t v) {
+  asm volatile("st.release.sys.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
+
+// Each CTA claims the next published ticket (compare-and-swap on the device head, only
+// when head < tail, so an idle CTA never takes a ticket it will not serve), runs that
+// request's CFTP and releases its done word.  A CTA leaves after idle_polls polls without
+// work or when the host sets shutdown; the host relaunches the kernel when it finds
+// published work and no kernel running.
+__global__ void __launch_bounds__(kBatchThreads) k_serve(ServeArgs a, uint32_t lz_c4, uint32_t lz_c8) {
+  extern __shared__ __align__(16) uint8_t sm[];
+  __shared__ long long s_ticket;
+  __shared__ uint32_t red[kBatchThreads / 32];
+  for (;;) {
+    if (threadIdx.x == 0) {
+      long long claimed = -1;
+      long polls = 0;
+      while (true) {
+        if (*(volatile uint32_t*)&a.ring->shutdown) break;
+        const uint64_t tail = ld_acquire_sys(&a.ring->tail);
+        const unsigned long long h = *(volatile unsigned long long*)a.head;
+        if (h < tail) {
+          if (atomicCAS(a.head, h, h + 1) == h) {
+            claimed = (long long)h;
+            break;
+          }
+          continue;
+        }
+        if (++polls > a.idle_polls) break;
+        __nanosleep(256);
+      }
+      s_ticket = claimed;
+    }
+    __syncthreads();
+    const long long ticket = s_ticket;
+    __syncthreads();
+    if (ticket < 0) break;
+    const int slot = (int)(ticket % a.slots);
+    DevInstance in;
+    {
+      const volatile uint32_t* src = reinterpret_cast<const volatile uint32_t*>(a.desc + slot);
+      uint32_t* dst = reinterpret_cast<uint32_t*>(&in);
+      for (int w = 0; w < (int)(sizeof(DevInstance) / 4); ++w) dst[w] = src[w];
+    }
+    uint8_t* base = a.data + (size_t)slot * a.slot_bytes;
+    int att;
+    int64_t look;
+    run_instance(sm, in, base + in.off_max, base + in.off_min, base + in.off_out, lz_c4, lz_c8, red, &att, &look);
+    __threadfence_system();
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      volatile DevInstance* d = a.desc + slot;
+      d->attempts = att;
+      d->final_half_sweeps = look;
+      __threadfence_system();
+      st_release_sys(a.done + slot, (uint64_t)ticket + 1);
+    }
+    __syncthreads();
+  }
+}
+
+// Packs an instance request into a DevInstance and its colour-split extremal tilings.
+rt_status pack_instance(const rt_cftp_instance& x, DevInstance* d, size_t* chain_bytes) {
+  if (!x.tmax || !x.tmin) return fail(RT_ERR_INVALID_ARGUMENT, "cftp instance: NULL tiling");
+  if (x.first_steps < 1 || x.max_attempts < 1 || x.max_attempts > 40)
+    return fail(RT_ERR_INVALID_ARGUMENT, "cftp instance: first_steps >= 1 and 1 <= max_attempts <= 40");
+  if (x.stream >= 65536u) return fail(RT_ERR_INVALID_ARGUMENT, "cftp instance: stream must be < 65536");
+  std::memset(d, 0, sizeof *d);
+  d->model = x.model;
+  d->N = x.n_side;
+  if (x.model == RT_MODEL_DOMINO) {
+    if (x.n_side < 6 || x.n_side % 2) return fail(RT_ERR_INVALID_ARGUMENT, "cftp instance: domino side must be even >= 6");
+    if (x.rule != RT_DOMINO_CFTP && x.rule != RT_DOMINO_CFTP_TWOPERIODIC)
+      return fail(RT_ERR_INVALID_ARGUMENT, "cftp instance: domino instances need a monotone rule");
+    DmRule r;
+    const char* err = nullptr;
+    if (!dm_rule_build(x.rule, RT_RNG_FAST, x.weight_a, x.weight_b, &r, &err)) return fail(RT_ERR_INVALID_ARGUMENT, err);
+    std::memcpy(d->lo_up, r.lo_up, sizeof r.lo_up);
+    std::memcpy(d->w_up, r.w_up, sizeof r.w_up);
+    std::memcpy(d->lo_dn, r.lo_dn, sizeof r.lo_dn);
+    std::memcpy(d->w_dn, r.w_dn, sizeof r.w_dn);
+    d->cols = x.n_side / 2 - 1;
+    d->P = ((x.n_side / 2) + 15) / 16 * 16;
+  } else if (x.model == RT_MODEL_LOZENGE) {
+    if (x.n_side < 9 || x.n_side % 3)
+      return fail(RT_ERR_INVALID_ARGUMENT, "cftp instance: lozenge side must be a multiple of 3 >= 9");
+    d->cols = x.n_side / 3;
+    d->P = ((x.n_side / 3) + 15) / 16 * 16;
+  } else {
+    return fail(RT_ERR_INVALID_ARGUMENT, "cftp instance: model must be RT_MODEL_DOMINO or RT_MODEL_LOZENGE");
+  }
+  d->seed = x.seed;
+  d->stream = x.stream;
+  d->max_attempts = x.max_attempts;
+  d->first_sweeps = x.first_steps;
+  *chain_bytes = (size_t)(x.model == RT_MODEL_DOMINO ? 2 : 3) * d->N * d->P;
+  return RT_OK;
+}
+
+// Colour split of an N x N tiling into ncol arrays of N x P bytes at dst.
+rt_status split_into(const int32_t* t, const DevInstance& d, uint8_t* dst) {
+  const int N = d.N, ncol = d.model == RT_MODEL_DOMINO ? 2 : 3;
+  const size_t plane = (size_t)N * d.P;
+  std::memset(dst, 0, plane * ncol);
+  for (int i = 0; i < N; ++i)
+    for (int j = 0; j < N; ++j) {
+      const int32_t v = t[(size_t)i * N + j];
+      if ((uint32_t)v > 63u) return fail(RT_ERR_INVALID_ARGUMENT, "cftp instance: tiling values out of range");
+      const int c = ncol == 2 ? (((i + j) & 1) == 0 ? 1 : 0) : ((j - i) % 3 + 3) % 3;
+      dst[(size_t)c * plane + (size_t)i * d.P + (ncol == 2 ? j / 2 : j / 3)] = (uint8_t)v;
+    }
+  return RT_OK;
+}
+
+void merge_from(const uint8_t* src, const DevInstance& d, int32_t* t) {
+  const int N = d.N, ncol = d.model == RT_MODEL_DOMINO ? 2 : 3;
+  const size_t plane = (size_t)N * d.P;
+  for (int i = 0; i < N; ++i)
+    for (int j = 0; j < N; ++j) {
+      const int c = ncol == 2 ? (((i + j) & 1) == 0 ? 1 : 0) : ((j - i) % 3 + 3) % 3;
+      t[(size_t)i * N + j] = src[(size_t)c * plane + (size_t)i * d.P + (ncol == 2 ? j / 2 : j / 3)];
+    }
+}
+
+uint32_t lz_cut(double p) { return (uint32_t)std::ceil(p * 4294967296.0); }
 
 }  // namespace
 }  // namespace rt
@@ -375,6 +540,187 @@ RT_API rt_status rt_cftp_batch(rt_cftp_instance* inst, int32_t count, void* cuda
   if (e1) cudaEventDestroy(e1);
   cleanup();
   return status;
+}
+
+}  // extern "C"
+
+// ---- server (host side) ----------------------------------------------------------------------
+struct rt_server {
+  int slots = 0, max_side = 0;
+  size_t slot_bytes = 0, smem = 0;
+  int64_t budget = 0, in_flight_bytes = 0;
+  long idle_polls = 0;
+  ServeRing* ring = nullptr;           // pinned + mapped
+  DevInstance* desc = nullptr;
+  uint8_t* data = nullptr;
+  uint64_t* done = nullptr;
+  ServeRing* d_ring = nullptr;         // device views of the mapped memory
+  DevInstance* d_desc = nullptr;
+  uint8_t* d_data = nullptr;
+  uint64_t* d_done = nullptr;
+  unsigned long long* d_head = nullptr;
+  cudaStream_t stream = nullptr;
+  bool own_stream = false;
+  cudaEvent_t ev_exit = nullptr;
+  bool launched = false;
+  int grid = 0;
+  int64_t next_ticket = 0;
+  std::vector<int64_t> owner;          // ticket held by each slot, -1 when free
+  std::vector<int64_t> footprint;
+};
+
+static rt_status server_launch(rt_server* s) {
+  ServeArgs a{s->d_ring, s->d_desc, s->d_data, s->d_done, s->d_head, s->slots, s->slot_bytes, s->idle_polls};
+  k_serve<<<s->grid, kBatchThreads, s->smem, s->stream>>>(a, lz_cut(0.4), lz_cut(0.8));
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return fail(RT_ERR_CUDA, std::string("server launch: ") + cudaGetErrorString(e));
+  BT_CUDA(cudaEventRecord(s->ev_exit, s->stream));
+  s->launched = true;
+  return RT_OK;
+}
+
+// Relaunches the persistent kernel when none is running (it leaves after idle_polls polls).
+static rt_status server_ensure_running(rt_server* s) {
+  if (s->launched) {
+    cudaError_t q = cudaEventQuery(s->ev_exit);
+    if (q == cudaErrorNotReady) return RT_OK;
+    if (q != cudaSuccess) return fail(RT_ERR_CUDA, std::string("server kernel: ") + cudaGetErrorString(q));
+  }
+  return server_launch(s);
+}
+
+extern "C" {
+
+RT_API rt_status rt_server_create(const rt_server_opts* o, rt_server** out) {
+  clear_error();
+  if (!o || !out) return fail(RT_ERR_INVALID_ARGUMENT, "server_create: NULL argument");
+  *out = nullptr;
+  if (o->slots < 1 || o->slots > (1 << 20) || o->max_side < 9 || o->max_side > 330 || o->memory_budget_bytes < 1)
+    return fail(RT_ERR_INVALID_ARGUMENT, "server_create: 1 <= slots <= 2^20, 9 <= max_side <= 330, budget > 0");
+  int dev = 0, sms = 0, optin = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) {
+    cudaGetLastError();
+    return fail(RT_ERR_CUDA, "no CUDA device: the sweep has no CPU fallback");
+  }
+  BT_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  BT_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+  auto s = std::make_unique<rt_server>();
+  s->slots = o->slots;
+  s->max_side = o->max_side;
+  const size_t pd = (size_t)((o->max_side / 2) + 15) / 16 * 16, pl = (size_t)((o->max_side / 3) + 15) / 16 * 16;
+  const size_t chain = std::max((size_t)2 * o->max_side * pd, (size_t)3 * o->max_side * pl);
+  s->slot_bytes = (3 * chain + 255) / 256 * 256;
+  s->smem = 2 * chain;
+  if (s->smem > (size_t)optin - 1024) return fail(RT_ERR_INVALID_ARGUMENT, "server_create: max_side too large for one CTA");
+  s->budget = o->memory_budget_bytes;
+  s->idle_polls = (long)std::max(1.0, (o->idle_seconds > 0 ? o->idle_seconds : 0.25) * 2.0e6);
+  BT_CUDA(cudaHostAlloc(&s->ring, sizeof(ServeRing), cudaHostAllocMapped));
+  BT_CUDA(cudaHostAlloc(&s->desc, sizeof(DevInstance) * s->slots, cudaHostAllocMapped));
+  BT_CUDA(cudaHostAlloc(&s->data, s->slot_bytes * s->slots, cudaHostAllocMapped));
+  BT_CUDA(cudaHostAlloc(&s->done, sizeof(uint64_t) * s->slots, cudaHostAllocMapped));
+  std::memset(s->ring, 0, sizeof(ServeRing));
+  std::memset(s->done, 0, sizeof(uint64_t) * s->slots);
+  BT_CUDA(cudaHostGetDevicePointer((void**)&s->d_ring, s->ring, 0));
+  BT_CUDA(cudaHostGetDevicePointer((void**)&s->d_desc, s->desc, 0));
+  BT_CUDA(cudaHostGetDevicePointer((void**)&s->d_data, s->data, 0));
+  BT_CUDA(cudaHostGetDevicePointer((void**)&s->d_done, s->done, 0));
+  BT_CUDA(cudaMalloc(&s->d_head, sizeof(unsigned long long)));
+  BT_CUDA(cudaMemset(s->d_head, 0, sizeof(unsigned long long)));
+  if (o->cuda_stream) {
+    s->stream = (cudaStream_t)o->cuda_stream;
+  } else {
+    BT_CUDA(cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking));
+    s->own_stream = true;
+  }
+  BT_CUDA(cudaEventCreateWithFlags(&s->ev_exit, cudaEventDisableTiming));
+  BT_CUDA(cudaFuncSetAttribute(k_serve, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)s->smem));
+  int per_sm = 0;
+  BT_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_serve, kBatchThreads, s->smem));
+  s->grid = std::max(1, per_sm) * sms;
+  s->owner.assign(s->slots, -1);
+  s->footprint.assign(s->slots, 0);
+  *out = s.release();
+  return RT_OK;
+}
+
+RT_API rt_status rt_server_submit(rt_server* s, const rt_cftp_instance* req, int64_t* ticket) {
+  clear_error();
+  if (!s || !req || !ticket) return fail(RT_ERR_INVALID_ARGUMENT, "server_submit: NULL argument");
+  if (req->n_side > s->max_side) return fail(RT_ERR_INVALID_ARGUMENT, "server_submit: tiling side above the server's max_side");
+  DevInstance d;
+  size_t chain = 0;
+  if (rt_status st = pack_instance(*req, &d, &chain)) return st;
+  const int64_t foot = (int64_t)(3 * chain);  // extremal tilings + result staged for the request
+  const int64_t t = s->next_ticket;
+  const int slot = (int)(t % s->slots);
+  if (s->owner[slot] >= 0) return fail(RT_ERR_BUSY, "server_submit: no free slot (collect finished requests first)");
+  if (s->in_flight_bytes + foot > s->budget) return fail(RT_ERR_BUSY, "server_submit: memory budget reached");
+  uint8_t* base = s->data + (size_t)slot * s->slot_bytes;
+  d.off_max = 0;
+  d.off_min = (int64_t)chain;
+  d.off_out = (int64_t)(2 * chain);
+  if (rt_status st = split_into(req->tmax, d, base)) return st;
+  if (rt_status st = split_into(req->tmin, d, base + chain)) return st;
+  std::memcpy(s->desc + slot, &d, sizeof d);
+  s->owner[slot] = t;
+  s->footprint[slot] = foot;
+  s->in_flight_bytes += foot;
+  s->next_ticket = t + 1;
+  __atomic_store_n(&s->ring->tail, (uint64_t)(t + 1), __ATOMIC_RELEASE);
+  *ticket = t;
+  return server_ensure_running(s);
+}
+
+RT_API rt_status rt_server_poll(rt_server* s, int64_t ticket, int32_t* done) {
+  clear_error();
+  if (!s || !done || ticket < 0 || ticket >= s->next_ticket) return fail(RT_ERR_INVALID_ARGUMENT, "server_poll: bad ticket");
+  const int slot = (int)(ticket % s->slots);
+  if (s->owner[slot] != ticket) return fail(RT_ERR_INVALID_ARGUMENT, "server_poll: ticket already collected");
+  *done = __atomic_load_n(s->done + slot, __ATOMIC_ACQUIRE) == (uint64_t)ticket + 1;
+  if (!*done) return server_ensure_running(s);
+  return RT_OK;
+}
+
+RT_API rt_status rt_server_wait(rt_server* s, int64_t ticket, double timeout_s, rt_cftp_instance* result) {
+  clear_error();
+  if (!s || !result || !result->out || ticket < 0 || ticket >= s->next_ticket)
+    return fail(RT_ERR_INVALID_ARGUMENT, "server_wait: bad arguments");
+  const int slot = (int)(ticket % s->slots);
+  if (s->owner[slot] != ticket) return fail(RT_ERR_INVALID_ARGUMENT, "server_wait: ticket already collected");
+  const auto t0 = std::chrono::steady_clock::now();
+  for (int spins = 0;; ++spins) {
+    if (__atomic_load_n(s->done + slot, __ATOMIC_ACQUIRE) == (uint64_t)ticket + 1) break;
+    if (rt_status st = server_ensure_running(s)) return st;
+    if (std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count() > timeout_s)
+      return fail(RT_ERR_TIMEOUT, "server_wait: request not finished within the timeout");
+    if (spins > 64) std::this_thread::sleep_for(std::chrono::microseconds(20));
+  }
+  DevInstance d;
+  std::memcpy(&d, s->desc + slot, sizeof d);
+  merge_from(s->data + (size_t)slot * s->slot_bytes + d.off_out, d, result->out);
+  result->attempts = d.attempts;
+  result->final_steps = d.final_half_sweeps;
+  s->owner[slot] = -1;
+  s->in_flight_bytes -= s->footprint[slot];
+  s->footprint[slot] = 0;
+  if (d.attempts < 0) return fail(RT_ERR_NOT_COALESCED, "server_wait: the request did not coalesce");
+  return RT_OK;
+}
+
+RT_API rt_status rt_server_destroy(rt_server* s) {
+  clear_error();
+  if (!s) return RT_OK;
+  if (s->ring) __atomic_store_n(&s->ring->shutdown, 1u, __ATOMIC_RELEASE);
+  if (s->stream) cudaStreamSynchronize(s->stream);
+  if (s->ev_exit) cudaEventDestroy(s->ev_exit);
+  if (s->own_stream && s->stream) cudaStreamDestroy(s->stream);
+  if (s->d_head) cudaFree(s->d_head);
+  if (s->ring) cudaFreeHost(s->ring);
+  if (s->desc) cudaFreeHost(s->desc);
+  if (s->data) cudaFreeHost(s->data);
+  if (s->done) cudaFreeHost(s->done);
+  delete s;
+  return RT_OK;
 }
 
 }  // extern "C"

@@ -34,6 +34,7 @@ RT_API const char* rt_status_string(rt_status s) {
     case RT_ERR_OUT_OF_MEMORY: return "out of memory";
     case RT_ERR_NOT_COALESCED: return "chains did not coalesce";
     case RT_ERR_BUFFER_TOO_SMALL: return "output buffer too small";
+    case RT_ERR_BUSY: return "busy: no free slot or over the memory budget";
   }
   return "unknown status";
 }
