@@ -232,6 +232,67 @@ def batched_leg(rt, plain_samples: int = 8) -> dict:
             "api": "rt_cftp_batch vs rt_domino_cftp / rt_lozenge_cftp, fast RNG mode, identical samples"}
 
 
+SERVE_RATE, SERVE_SECONDS = 2000.0, 5.0
+
+
+def serving_leg(rt) -> dict:
+    """Continuous-batching server under a Poisson request stream (mean SERVE_RATE / s for
+    SERVE_SECONDS): models domino / lozenge alternately, sizes log-uniform in the batched
+    leg's ranges, weights as there.  Latency = completion time - arrival time."""
+    D, L = rt.DominoTiler, rt.LozengeTiler
+    rng = np.random.default_rng(20261203)
+    cache = {}
+
+    def request(k):
+        if k % 2 == 0:
+            order = int(np.exp(rng.uniform(np.log(BATCH_ORDERS[0]), np.log(BATCH_ORDERS[1] + 1))))
+            if ("d", order) not in cache:
+                d = D.AztecDiamond(order)
+                cache[("d", order)] = (D.MaxTiling(d), D.MinTiling(d))
+            tmax, tmin = cache[("d", order)]
+            w = (k // 2) % 2 == 1
+            return {"model": "domino", "tmax": tmax, "tmin": tmin, "seed": k, "stream": k & 0xFFFF,
+                    "rule": "cftp_twoperiodic" if w else "cftp", "a": 1.0,
+                    "b": float(rng.uniform(*BATCH_B)) if w else 1.0, "first_steps": BATCH_FIRST,
+                    "max_attempts": BATCH_ATTEMPTS}
+        side = int(np.exp(rng.uniform(np.log(BATCH_SIDES[0]), np.log(BATCH_SIDES[1] + 1))))
+        if ("l", side) not in cache:
+            d = L.Hexagon(side)
+            cache[("l", side)] = (L.MaxTiling(d), L.MinTiling(d))
+        tmax, tmin = cache[("l", side)]
+        return {"model": "lozenge", "tmax": tmax, "tmin": tmin, "seed": k, "stream": k & 0xFFFF,
+                "first_steps": BATCH_FIRST, "max_attempts": BATCH_ATTEMPTS}
+
+    arrivals = np.cumsum(rng.exponential(1.0 / SERVE_RATE, size=int(SERVE_RATE * SERVE_SECONDS * 1.2)))
+    arrivals = arrivals[arrivals < SERVE_SECONDS]
+    reqs = [request(k) for k in range(len(arrivals))]
+    srv = rt.Server(slots=1 << 16, max_side=max(2 * BATCH_ORDERS[1] + 6, 3 * ((2 * BATCH_SIDES[1] + 9) // 3 + 1)),
+                    memory_budget_bytes=120 << 30, idle_seconds=0.5)
+    srv.wait(srv.submit(reqs[0]))  # warm-up
+    pending, lat, served = {}, [], 0
+    t0 = time.perf_counter()
+    k = 0
+    while k < len(reqs) or pending:
+        now = time.perf_counter() - t0
+        while k < len(reqs) and arrivals[k] <= now:
+            pending[srv.submit(reqs[k])] = arrivals[k]
+            k += 1
+        for t in list(pending):
+            if srv.poll(t):
+                srv.wait(t)
+                lat.append(time.perf_counter() - t0 - pending.pop(t))
+                served += 1
+    wall = time.perf_counter() - t0
+    srv.close()
+    lat = np.array(lat)
+    return {"workload": f"Poisson arrivals, mean {SERVE_RATE:.0f}/s for {SERVE_SECONDS:.0f} s ({len(reqs)} requests): "
+                        f"Aztec orders log-U{list(BATCH_ORDERS)} (half 2-periodic, b~U{list(BATCH_B)}) and hexagon "
+                        f"sides log-U{list(BATCH_SIDES)}",
+            "samples_per_s": served / wall, "latency_p50_s": float(np.percentile(lat, 50)),
+            "latency_p99_s": float(np.percentile(lat, 99)), "requests": len(reqs),
+            "api": "rt_server_submit / rt_server_poll / rt_server_wait (continuous batching)"}
+
+
 def run_reference(args) -> None:
     rank, ws, local, dist = _dist()
     if rank != 0:
@@ -403,9 +464,10 @@ def run_ours(args) -> None:
                "sample": f"{sample} TinyMT half-sweeps of the coupled max/min chains (order {ORDER}) per attempt, "
                          f"2 attempts, {threads} host threads"}
     s.close()
-    batched = None
+    batched = serving = None
     if rank == 0 and not args.no_batch:
         batched = batched_leg(rt)
+        serving = serving_leg(rt)
     if rank == 0:
         line = {
             "metric": METRIC, "value": value, "unit": "flip attempts/s", "n_gpus": ws, "steps": args.steps,
@@ -415,7 +477,7 @@ def run_ours(args) -> None:
                        "rng": args.mode, "engine": args.engine, "half_sweeps_per_step": HALF_SWEEPS,
                        "l2": "flushed between timed steps (256 MiB write)", "parallelism": f"replicas{ws}"},
             "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches, "clocks": clocks,
-            "batched_cftp": batched,
+            "batched_cftp": batched, "served_cftp": serving,
         }
         print(json.dumps(line))
     if dist is not None:
