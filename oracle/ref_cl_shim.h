@@ -25,4 +25,7 @@ inline float as_float(uint x) {
   std::memcpy(&f, &x, sizeof f);
   return f;
 }
-inline int select(int x, int y, bool c) { return c ? y : x; }
+template <class T>
+inline T select(T x, T y, bool c) {
+  return c ? y : x;
+}
