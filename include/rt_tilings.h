@@ -171,6 +171,32 @@ RT_API rt_status rt_lozenge_cftp(const int32_t* tmax, const int32_t* tmin, int32
                                  int64_t first_steps, int32_t schedule, int32_t max_attempts,
                                  const rt_walk_opts* opts, int32_t* out, rt_cftp_stats* stats);
 
+/* ---- rectangle-triangle tilings (src/RectTriangle/RectTriangleTiler.h:32-86) -----------
+   Vertices of the triangular lattice, N x N with N a multiple of 3 and three rows/columns of
+   zero padding, each holding six hexadecimal digits: the covering codes of the six triangles
+   around it (RectTriangleTiler.h:14-22); a digit d of a tiling weighs wt_d (d = 1-3),
+   wr_((d-4) mod 3 + 1) (d = 4-9) or wm_((d-10) mod 3 + 1) (d = 10-15), as the weight table at
+   recttrianglekernel.cl:13. */
+
+/* RectTriangleTiler::maxHex (top != 0) / minHex (top == 0) (RectTriangleTiler.cpp:480-600):
+   the extremal tilings of the hexagon of side n >= 2 after the reference's shear and padding.
+   *side receives the side N; out needs N * N entries (cap). */
+RT_API rt_status rt_recttri_hex_tiling(int32_t n, int32_t top, int32_t* out, int64_t cap, int32_t* side);
+/* RectTriangleTiler::LozengeToRectTriangle(tiling&, domain&) (RectTriangleTiler.cpp:602-644):
+   a lozenge tiling (edge masks as rt_lozenge_*, N x N) of a domain of m_rows x 2 m_rows
+   triangles, read as an all-triangle rectangle-triangle tiling, N x N. */
+RT_API rt_status rt_recttri_from_lozenge(const int32_t* lozenge, int32_t n_side, const int32_t* domain,
+                                         int32_t m_rows, int32_t* out);
+/* RectTriangleTiler::Walk(tiling&, int steps, long seed) (RectTriangleTiler.cpp:33-171):
+   per step a colour ((i - j) mod 3) from default_random_engine(seed) +
+   uniform_int_distribution(0, 2) (TinyMT mode, generator k seeded with seed + k) or h mod 3
+   (fast mode), then flipTiles (recttrianglekernel.cl:25-118) on that colour and
+   updateTiles1/2 (:120-146) on the two others.  weights9 = {wt1, wt2, wt3, wm1, wm2, wm3,
+   wr1, wr2, wr3}, the compile-time constants of recttrianglekernel.cl:3-11 (NULL: all 1, the
+   reference's values); float arithmetic as the reference kernel.  opts->rule is ignored. */
+RT_API rt_status rt_recttri_walk(int32_t* tiling, int32_t n_side, int64_t steps, int64_t seed,
+                                 const double* weights9, const rt_walk_opts* opts);
+
 /* ---- batched coupling from the past --------------------------------------------------------
    No counterpart in the reference (which runs one instance at a time).  Many independent
    fast-mode CFTP instances of uneven sizes, dominoes and lozenges mixed, in one persistent

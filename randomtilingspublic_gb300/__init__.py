@@ -139,6 +139,9 @@ _SIGNATURES = {
     "rt_lozenge_tiling_to_domain": (C.c_int32, [_P, C.c_int32, _P]),
     "rt_lozenge_walk": (C.c_int32, [_P, C.c_int32, C.c_int64, C.c_int64, _P]),
     "rt_lozenge_cftp": (C.c_int32, [_P, _P, C.c_int32, C.c_int64, C.c_int64, C.c_int32, C.c_int32, _P, _P, _P]),
+    "rt_recttri_hex_tiling": (C.c_int32, [C.c_int32, C.c_int32, _P, C.c_int64, _P]),
+    "rt_recttri_from_lozenge": (C.c_int32, [_P, C.c_int32, _P, C.c_int32, _P]),
+    "rt_recttri_walk": (C.c_int32, [_P, C.c_int32, C.c_int64, C.c_int64, _P, _P]),
 }
 
 _lib_handle = None
@@ -458,6 +461,58 @@ class LozengeTiler:
         return out
 
 
+class RectTriangleTiler:
+    """Rectangle-triangle tilings (src/RectTriangle/RectTriangleTiler.h:32-86).  ``weights``
+    holds the nine tile weights {wt1, wt2, wt3, wm1, wm2, wm3, wr1, wr2, wr3}
+    (recttrianglekernel.cl:3-11; all 1 by default, the reference's values).  ``rng`` is
+    'tinymt' (bit-exact with the reference's OpenCL path) or 'fast'."""
+
+    def __init__(self, rng: str = "tinymt", fast_stream: int = 0, weights=None):
+        self.rng = rng
+        self.fast_stream = int(fast_stream)
+        self.weights = None if weights is None else np.ascontiguousarray(weights, np.float64)
+        if self.weights is not None and self.weights.shape != (9,):
+            raise ValueError("weights: nine values {wt1, wt2, wt3, wm1, wm2, wm3, wr1, wr2, wr3}")
+
+    def opts(self) -> _WalkOpts:
+        o = _WalkOpts()
+        lib().rt_walk_opts_default(C.byref(o))
+        o.rng_mode = RNG_MODES[self.rng]
+        o.fast_stream = self.fast_stream
+        return o
+
+    def Walk(self, t, steps: int, seed: int) -> None:
+        tt = _i32(t)
+        o = self.opts()
+        w = None if self.weights is None else self.weights.ctypes.data
+        _check(lib().rt_recttri_walk(_ptr(tt), side_of(tt), int(steps), int(seed), w, C.byref(o)))
+        _write_back(t, tt)
+
+    @staticmethod
+    def _hex(n: int, top: int) -> np.ndarray:
+        side = C.c_int32()
+        s = 2 * n + 9
+        buf = np.zeros(s * s, np.int32)
+        _check(lib().rt_recttri_hex_tiling(int(n), top, _ptr(buf), buf.size, C.byref(side)))
+        return buf[: side.value * side.value].copy()
+
+    @staticmethod
+    def maxHex(n: int) -> np.ndarray:
+        return RectTriangleTiler._hex(n, 1)
+
+    @staticmethod
+    def minHex(n: int) -> np.ndarray:
+        return RectTriangleTiler._hex(n, 0)
+
+    @staticmethod
+    def LozengeToRectTriangle(t, d) -> np.ndarray:
+        tt, dd = _i32(t), _i32(d)
+        n = side_of(tt)
+        out = np.zeros(n * n, np.int32)
+        _check(lib().rt_recttri_from_lozenge(_ptr(tt), n, _ptr(dd), _tri_side(dd), _ptr(out)))
+        return out
+
+
 class DominoSampler:
     """Device-resident coupled chains (rt_dm_sampler_*): the chains stay in HBM between
     calls; all chains share one random stream."""
@@ -635,5 +690,5 @@ def mt19937_draws(seed: int, count: int) -> np.ndarray:
     return rs.randint(0, 2**32, size=count, dtype=np.uint32)
 
 
-__all__ = ["DominoTiler", "DominoSampler", "LozengeTiler", "cftp_batch", "Server", "RTError", "lib", "read_tinymt_params", "mt19937_colours",
+__all__ = ["DominoTiler", "DominoSampler", "LozengeTiler", "RectTriangleTiler", "cftp_batch", "Server", "RTError", "lib", "read_tinymt_params", "mt19937_colours",
            "mt19937_draws", "CftpStats"]

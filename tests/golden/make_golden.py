@@ -1,4 +1,4 @@
-"""Generates tests/golden/domino_ref_cases.json from the reference's own code.
+"""Generates tests/golden/{domino,lozenge,recttri}_ref_cases.json from the reference's own code.
 
 Runs where the reference tree exists (it is not on the GPU machine): builds oracle/_ref
 (`make -C oracle ref`), which compiles the reference's domino .cl kernel files and its host
@@ -210,6 +210,71 @@ def lozenge(ref: str) -> None:
     (HERE / "lozenge_ref_cases.json").write_text(json.dumps({"generator": "tests/golden/make_golden.py", "cases": cases,
                                                              "host_cases": host}, separators=(",", ":")))
     print(f"wrote {len(cases)} lozenge sweep cases, {len(host)} lozenge host cases")
+    recttri(ref)
+
+
+def _read_matrix(path: Path) -> np.ndarray:
+    return np.array([int(x) for x in path.read_text().split()], np.int32)
+
+
+def recttri(ref: str) -> None:
+    """Rectangle-triangle vectors from the reference-compiled src/RectTriangle code
+    (oracle/_ref/libref_recttri.so); pins the committed fixtures
+    Examples/ExampleOuts/RectTriangle/{Max,Min,Slope}Tiling.txt (RectTriangleEx.cpp, N = 5)
+    against the reference's maxHex / minHex / slopeHex."""
+    rl = C.CDLL(str(ROOT / "oracle/_ref/libref_recttri.so"))
+    lz = C.CDLL(str(ROOT / "oracle/_ref/libref_lozenge.so"))
+    P = lambda a: None if a is None else a.ctypes.data_as(C.c_void_p)
+    rl.ref_rt_walk.argtypes = [C.c_void_p, C.c_int, C.c_long, C.c_long]
+    rl.refh_rt_hex.argtypes = [C.c_int, C.c_int, C.c_void_p, C.c_long]
+    rl.refh_rt_from_lozenge.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_int, C.c_void_p]
+
+    def hexagon(n, which):
+        buf = np.zeros((2 * n + 9) ** 2, np.int32)
+        side = rl.refh_rt_hex(n, which, P(buf), buf.size)
+        return buf[: side * side].copy(), side
+
+    def walk(t, n, steps, seed):
+        t = t.copy()
+        rl.ref_rt_walk(P(t), n, steps, seed)
+        return t
+
+    fixtures = Path(ref) / "Examples/ExampleOuts/RectTriangle"
+    for name, which in (("MaxTiling", 1), ("MinTiling", 0), ("SlopeTiling", 2)):
+        assert np.array_equal(_read_matrix(fixtures / f"{name}.txt"), hexagon(5, which)[0]), name
+    host, cases = [], []
+    for n in (2, 3, 5, 8, 13):
+        (tmax, side), (tmin, _) = hexagon(n, 1), hexagon(n, 0)
+        host.append({"n": n, "N": side, "max": tmax.tolist(), "min": tmin.tolist()})
+    for n, which, steps, seed in [(2, 0, 40, 1), (3, 1, 333, 99), (5, 0, 1000, 2018), (5, 1, 517, -5), (8, 0, 300, 77),
+                                  (13, 1, 200, 4242)]:
+        start, side = hexagon(n, which)
+        cases.append({"name": f"rt_walk_hex{n}_{'max' if which else 'min'}_{steps}", "N": side, "start": start.tolist(),
+                      "steps": steps, "seed": seed, "expected": walk(start, side, steps, seed).tolist()})
+    # the reference's own end state of RectTriangleEx (1000 steps from minHex(5), seed not
+    # recorded) as a start state
+    end = _read_matrix(fixtures / "EndTiling.txt")
+    side = int(np.sqrt(end.size))
+    cases.append({"name": "rt_walk_example_end_state", "N": side, "start": end.tolist(), "steps": 250, "seed": 31337,
+                  "expected": walk(end, side, 250, 31337).tolist()})
+    # LozengeToRectTriangle on lozenge extremal tilings of AlmostHexDomain(n, m)
+    conv = []
+    for n, m in ((3, 0), (4, 1), (6, 2)):
+        buf = np.zeros(2 * (2 * n + 9) ** 2, np.int32)
+        rows = lz.refh_lz_almost_hex_domain(n, m, P(buf), buf.size)
+        d = buf[: 2 * rows * rows].copy()
+        for which in ("max", "min"):
+            t = np.zeros((rows + 1) ** 2, np.int32)
+            getattr(lz, f"refh_lz_{which}_tiling")(P(d), rows, P(t))
+            out = np.zeros_like(t)
+            rl.refh_rt_from_lozenge(P(t), rows + 1, P(d), rows, P(out))
+            conv.append({"n": n, "m": m, "which": which, "domain": d.tolist(), "lozenge": t.tolist(),
+                         "expected": out.tolist()})
+    (HERE / "recttri_ref_cases.json").write_text(json.dumps(
+        {"generator": "tests/golden/make_golden.py", "fixtures_pinned": ["MaxTiling.txt", "MinTiling.txt",
+                                                                         "SlopeTiling.txt"],
+         "host_cases": host, "cases": cases, "from_lozenge": conv}, separators=(",", ":")))
+    print(f"wrote {len(cases)} rectangle-triangle sweep cases, {len(host)} host cases, {len(conv)} conversions")
 
 
 if __name__ == "__main__":

@@ -45,8 +45,7 @@ _lib = None
 def lib() -> C.CDLL:
     global _lib
     if _lib is None:
-        if not ORACLE_LIB.exists():
-            subprocess.run(["make", "-s", "-C", str(ORACLE_DIR)], check=True)
+        subprocess.run(["make", "-s", "-C", str(ORACLE_DIR)], check=True)
         h = C.CDLL(str(ORACLE_LIB))
         for name, (res, args) in _SIG.items():
             f = getattr(h, name)
@@ -265,3 +264,42 @@ def lz_cftp(tmax, tmin, n, driver_seed, first, schedule, max_attempts, fast=Fals
     att = lz_lib().orc_lz_cftp(_p(tmax), _p(tmin), n, driver_seed, first, schedule, max_attempts, 1 if fast else 0,
                                stream, _p(out), C.addressof(total))
     return out, att, total.value
+
+
+# ---- rectangle-triangle ----------------------------------------------------------------
+_RT_SIG = {
+    "orc_rt_hex": (C.c_int, [C.c_int, C.c_int, _P, _L]),
+    "orc_rt_walk_tinymt": (C.c_int, [_P, C.c_int, _L, _L, _P]),
+    "orc_rt_walk_fast": (C.c_int, [_P, C.c_int, _L, _L, C.c_ulong, C.c_uint, _P]),
+}
+RT_UNIT_WEIGHTS = np.ones(9, np.float64)
+
+
+def rt_lib() -> C.CDLL:
+    h = lib()
+    for name, (res, args) in _RT_SIG.items():
+        f = getattr(h, name)
+        f.restype = res
+        f.argtypes = args
+    return h
+
+
+def rt_hex(n: int, top: bool) -> np.ndarray:
+    buf = np.zeros((2 * n + 9) ** 2, np.int32)
+    side = rt_lib().orc_rt_hex(n, 1 if top else 0, _p(buf), buf.size)
+    assert side > 0
+    return buf[: side * side].copy()
+
+
+def _w9(weights) -> np.ndarray:
+    return np.ascontiguousarray(RT_UNIT_WEIGHTS if weights is None else np.asarray(weights, np.float64))
+
+
+def rt_walk_tinymt(t: np.ndarray, n: int, steps: int, seed: int, weights=None) -> None:
+    w = _w9(weights)
+    assert rt_lib().orc_rt_walk_tinymt(_p(t), n, steps, seed, _p(w)) == 0
+
+
+def rt_walk_fast(t: np.ndarray, n: int, h0: int, steps: int, seed: int, stream: int = 0, weights=None) -> None:
+    w = _w9(weights)
+    assert rt_lib().orc_rt_walk_fast(_p(t), n, h0, steps, seed, stream, _p(w)) == 0
