@@ -197,6 +197,39 @@ RT_API rt_status rt_recttri_from_lozenge(const int32_t* lozenge, int32_t n_side,
 RT_API rt_status rt_recttri_walk(int32_t* tiling, int32_t n_side, int64_t steps, int64_t seed,
                                  const double* weights9, const rt_walk_opts* opts);
 
+/* ---- six-vertex model ----------------------------------------------------------------------
+   No counterpart in the reference (which has no six-vertex model); the entry points follow the
+   shape of the per-model classes (domain / extremal states / Walk / CFTP / height function).
+   State: the height function on the (n+1) x (n+1) corners of an n x n vertex grid, int32,
+   h(below) - h(above) = +1 across a horizontal edge whose arrow points right and
+   h(right) - h(left) = +1 across a vertical edge whose arrow points up.  Vertex types from
+   the corner heights: a (NE == SW, NW != SE), b (NW == SE, NE != SW), c (both equal), weights
+   abc = {a, b, c} (NULL: all 1).  The boundary heights are never changed.
+   Sweep: four point classes (x mod 2, y mod 2), sub-sweep s updates class s mod 4 by heat
+   bath (h' +- 1 at points whose four edge neighbours equal h'), draws from Philox4x32-10
+   bit planes keyed by (seed, opts->fast_stream, s).  Only RT_RNG_FAST exists for this model
+   (opts NULL: fast mode, stream 0). */
+
+/* Heat-bath thresholds T[3 k1 + k2] = min(floor(P 2^32), 2^32 - 1), P = W+ / (W+ + W-). */
+RT_API rt_status rt_sv_thresholds(double a, double b, double c, uint32_t* out9);
+/* Domain-wall boundary, maximal (top != 0: min(x + y, 2n - x - y)) or minimal (|x - y|)
+   height function, (n+1)^2 entries. */
+RT_API rt_status rt_sv_dwbc_height(int32_t n, int32_t top, int32_t* out);
+/* Domain-wall height function <-> alternating sign matrix (n x n, entries (NE + SW - NW - SE)/2). */
+RT_API rt_status rt_sv_height_to_asm(const int32_t* h, int32_t n, int32_t* out);
+RT_API rt_status rt_sv_asm_to_height(const int32_t* a, int32_t n, int32_t* out);
+/* 4 * sweeps sub-sweeps (s = 0 .. 4 sweeps - 1) on h in place.  stats (optional): flip
+   attempts ((n-1)^2 per sweep) and the device time of the sweeps. */
+RT_API rt_status rt_sv_walk(int32_t* h, int32_t n, int64_t sweeps, int64_t seed, const double* abc,
+                            const rt_walk_opts* opts, rt_cftp_stats* stats);
+/* Coupling from the past from hmax >= hmin (same boundary): attempt j runs sub-sweeps
+   [-4 T, 0), T = first_sweeps * 2^j, both chains on the same draws.  Exact for
+   c >= max(a, b) (the heat-bath update is then monotone); RT_ERR_INVALID_ARGUMENT otherwise.
+   RT_ERR_NOT_COALESCED after max_attempts (out then holds the top chain). */
+RT_API rt_status rt_sv_cftp(const int32_t* hmax, const int32_t* hmin, int32_t n, int64_t seed, int64_t first_sweeps,
+                            int32_t max_attempts, const double* abc, const rt_walk_opts* opts, int32_t* out,
+                            rt_cftp_stats* stats);
+
 /* ---- batched coupling from the past --------------------------------------------------------
    No counterpart in the reference (which runs one instance at a time).  Many independent
    fast-mode CFTP instances of uneven sizes, dominoes and lozenges mixed, in one persistent

@@ -142,6 +142,12 @@ _SIGNATURES = {
     "rt_recttri_hex_tiling": (C.c_int32, [C.c_int32, C.c_int32, _P, C.c_int64, _P]),
     "rt_recttri_from_lozenge": (C.c_int32, [_P, C.c_int32, _P, C.c_int32, _P]),
     "rt_recttri_walk": (C.c_int32, [_P, C.c_int32, C.c_int64, C.c_int64, _P, _P]),
+    "rt_sv_thresholds": (C.c_int32, [C.c_double, C.c_double, C.c_double, _P]),
+    "rt_sv_dwbc_height": (C.c_int32, [C.c_int32, C.c_int32, _P]),
+    "rt_sv_height_to_asm": (C.c_int32, [_P, C.c_int32, _P]),
+    "rt_sv_asm_to_height": (C.c_int32, [_P, C.c_int32, _P]),
+    "rt_sv_walk": (C.c_int32, [_P, C.c_int32, C.c_int64, C.c_int64, _P, _P, _P]),
+    "rt_sv_cftp": (C.c_int32, [_P, _P, C.c_int32, C.c_int64, C.c_int64, C.c_int32, _P, _P, _P, _P]),
 }
 
 _lib_handle = None
@@ -513,6 +519,75 @@ class RectTriangleTiler:
         return out
 
 
+class SixVertexTiler:
+    """Six-vertex model on an n x n grid (no counterpart in the reference; shaped like its
+    per-model classes).  State: the (n+1) x (n+1) int32 height function; weights a, b, c;
+    fast (Philox) random mode only, ``fast_stream`` selects an independent stream."""
+
+    def __init__(self, a: float = 1.0, b: float = 1.0, c: float = 1.0, fast_stream: int = 0):
+        self.abc = np.array([a, b, c], np.float64)
+        self.fast_stream = int(fast_stream)
+
+    def opts(self) -> _WalkOpts:
+        o = _WalkOpts()
+        lib().rt_walk_opts_default(C.byref(o))
+        o.rng_mode = RNG_MODES["fast"]
+        o.fast_stream = self.fast_stream
+        return o
+
+    def Walk(self, h, sweeps: int, seed: int) -> dict:
+        hh = _i32(h)
+        o, st = self.opts(), CftpStats()
+        _check(lib().rt_sv_walk(_ptr(hh), side_of(hh) - 1, int(sweeps), int(seed), self.abc.ctypes.data, C.byref(o),
+                                C.byref(st)))
+        _write_back(h, hh)
+        return st.as_dict()
+
+    def cftp(self, hmax, hmin, seed: int, first_sweeps: int = 16, max_attempts: int = 20):
+        a, b = _i32(hmax), _i32(hmin)
+        out = np.zeros_like(a)
+        o, st = self.opts(), CftpStats()
+        _check(lib().rt_sv_cftp(_ptr(a), _ptr(b), side_of(a) - 1, int(seed), int(first_sweeps), int(max_attempts),
+                                self.abc.ctypes.data, C.byref(o), _ptr(out), C.byref(st)))
+        return out, st.as_dict()
+
+    @staticmethod
+    def Thresholds(a: float, b: float, c: float) -> np.ndarray:
+        out = np.zeros(9, np.uint32)
+        _check(lib().rt_sv_thresholds(float(a), float(b), float(c), _ptr(out)))
+        return out
+
+    @staticmethod
+    def MaxHeight(n: int) -> np.ndarray:
+        """Domain-wall boundary, maximal height function min(x + y, 2n - x - y)."""
+        out = np.zeros((n + 1) ** 2, np.int32)
+        _check(lib().rt_sv_dwbc_height(int(n), 1, _ptr(out)))
+        return out
+
+    @staticmethod
+    def MinHeight(n: int) -> np.ndarray:
+        """Domain-wall boundary, minimal height function |x - y|."""
+        out = np.zeros((n + 1) ** 2, np.int32)
+        _check(lib().rt_sv_dwbc_height(int(n), 0, _ptr(out)))
+        return out
+
+    @staticmethod
+    def HeightToASM(h) -> np.ndarray:
+        hh = _i32(h)
+        n = side_of(hh) - 1
+        out = np.zeros(n * n, np.int32)
+        _check(lib().rt_sv_height_to_asm(_ptr(hh), n, _ptr(out)))
+        return out
+
+    @staticmethod
+    def ASMToHeight(a) -> np.ndarray:
+        aa = _i32(a)
+        n = side_of(aa)
+        out = np.zeros((n + 1) ** 2, np.int32)
+        _check(lib().rt_sv_asm_to_height(_ptr(aa), n, _ptr(out)))
+        return out
+
+
 class DominoSampler:
     """Device-resident coupled chains (rt_dm_sampler_*): the chains stay in HBM between
     calls; all chains share one random stream."""
@@ -690,5 +765,5 @@ def mt19937_draws(seed: int, count: int) -> np.ndarray:
     return rs.randint(0, 2**32, size=count, dtype=np.uint32)
 
 
-__all__ = ["DominoTiler", "DominoSampler", "LozengeTiler", "RectTriangleTiler", "cftp_batch", "Server", "RTError", "lib", "read_tinymt_params", "mt19937_colours",
+__all__ = ["DominoTiler", "DominoSampler", "LozengeTiler", "RectTriangleTiler", "SixVertexTiler", "cftp_batch", "Server", "RTError", "lib", "read_tinymt_params", "mt19937_colours",
            "mt19937_draws", "CftpStats"]

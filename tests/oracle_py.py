@@ -303,3 +303,48 @@ def rt_walk_tinymt(t: np.ndarray, n: int, steps: int, seed: int, weights=None) -
 def rt_walk_fast(t: np.ndarray, n: int, h0: int, steps: int, seed: int, stream: int = 0, weights=None) -> None:
     w = _w9(weights)
     assert rt_lib().orc_rt_walk_fast(_p(t), n, h0, steps, seed, stream, _p(w)) == 0
+
+
+# ---- six-vertex --------------------------------------------------------------------------
+_SV_SIG = {
+    "orc_sv_thresholds": (None, [C.c_double, C.c_double, C.c_double, _P]),
+    "orc_sv_dwbc": (None, [C.c_int, C.c_int, _P]),
+    "orc_sv_draw": (C.c_uint, [C.c_ulong, C.c_uint, _L, C.c_uint, C.c_uint]),
+    "orc_sv_walk": (C.c_int, [_P, C.c_int, _L, _L, C.c_ulong, C.c_uint, C.c_double, C.c_double, C.c_double]),
+    "orc_sv_cftp": (C.c_int, [_P, _P, C.c_int, C.c_ulong, C.c_uint, _L, C.c_int, C.c_double, C.c_double, C.c_double,
+                              _P, _P]),
+}
+
+
+def sv_lib() -> C.CDLL:
+    h = lib()
+    for name, (res, args) in _SV_SIG.items():
+        f = getattr(h, name)
+        f.restype = res
+        f.argtypes = args
+    return h
+
+
+def sv_thresholds(a, b, c) -> np.ndarray:
+    out = np.zeros(9, np.uint32)
+    sv_lib().orc_sv_thresholds(a, b, c, _p(out))
+    return out
+
+
+def sv_dwbc(n: int, top: bool) -> np.ndarray:
+    out = np.zeros((n + 1) ** 2, np.int32)
+    sv_lib().orc_sv_dwbc(n, 1 if top else 0, _p(out))
+    return out
+
+
+def sv_walk(h: np.ndarray, n: int, s0: int, count: int, seed: int, stream: int = 0, a=1.0, b=1.0, c=1.0) -> None:
+    assert sv_lib().orc_sv_walk(_p(h), n, s0, count, seed, stream, a, b, c) == 0
+
+
+def sv_cftp(hmax, hmin, n, seed, stream, first_sweeps, max_attempts, a=1.0, b=1.0, c=1.0):
+    hmax, hmin = _i32(hmax), _i32(hmin)
+    out = np.zeros_like(hmax)
+    used = C.c_long()
+    att = sv_lib().orc_sv_cftp(_p(hmax), _p(hmin), n, seed, stream, first_sweeps, max_attempts, a, b, c, _p(out),
+                               C.addressof(used))
+    return out, att, used.value
