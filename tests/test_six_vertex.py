@@ -136,7 +136,7 @@ def test_walk_matches_oracle(rt, orc, abc):
             orc.sv_walk(b, n, 0, 4 * sweeps, seed, stream, *abc)
             assert np.array_equal(a, b), (n, top, abc)
             assert stats["flip_attempts"] == (n - 1) ** 2 * sweeps
-            if n >= 7:
+            if n >= 7 and max(abc) / min(abc) < 3:  # strongly a-weighted chains may stay at the maximum
                 assert not np.array_equal(a, start)
 
 
