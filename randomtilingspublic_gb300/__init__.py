@@ -522,17 +522,20 @@ class RectTriangleTiler:
 class SixVertexTiler:
     """Six-vertex model on an n x n grid (no counterpart in the reference; shaped like its
     per-model classes).  State: the (n+1) x (n+1) int32 height function; weights a, b, c;
-    fast (Philox) random mode only, ``fast_stream`` selects an independent stream."""
+    fast (Philox) random mode only, ``fast_stream`` selects an independent stream.  ``engine``:
+    0 automatic, 1 one kernel per sub-sweep, 2 the cluster-resident kernel."""
 
-    def __init__(self, a: float = 1.0, b: float = 1.0, c: float = 1.0, fast_stream: int = 0):
+    def __init__(self, a: float = 1.0, b: float = 1.0, c: float = 1.0, fast_stream: int = 0, engine: int = 0):
         self.abc = np.array([a, b, c], np.float64)
         self.fast_stream = int(fast_stream)
+        self.engine = int(engine)
 
     def opts(self) -> _WalkOpts:
         o = _WalkOpts()
         lib().rt_walk_opts_default(C.byref(o))
         o.rng_mode = RNG_MODES["fast"]
         o.fast_stream = self.fast_stream
+        o.engine = self.engine
         return o
 
     def Walk(self, h, sweeps: int, seed: int) -> dict:

@@ -17,6 +17,7 @@
 // bit b of data word w is point k = 32 w + b of the class row (x = 2k + px, y = 2r + py).
 // A thread owns one word: 32 points updated with bitwise logic, the random comparison done
 // bit-sliced from the most significant plane down and stopped once every lane is decided.
+#include <cooperative_groups.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -66,58 +67,200 @@ __device__ __forceinline__ uint32_t east_of(const uint32_t* row, int idx, int px
   return px ? __funnelshift_r(row[idx], row[idx + 1], 1) : row[idx];
 }
 
-// One sub-sweep of one class; blockIdx.y is the chain.
-__global__ void __launch_bounds__(128) k_sv_sub(SvLaunch L) {
-  const int g = blockIdx.x * blockDim.x + threadIdx.x;
-  if (g >= L.words * L.rows) return;
-  const int w = g % L.words, r = L.r_lo + g / L.words, idx = w + 1;
-  const int px = L.px, py = L.py, cls = px | (py << 1);
-  uint32_t* chain = L.base + (size_t)blockIdx.y * L.chain_words;
-  uint32_t* F = chain + (size_t)cls * L.class_words + (size_t)r * L.P;
-  const uint32_t* Hrow = chain + (size_t)(cls ^ 1) * L.class_words + (size_t)r * L.P;
-  const uint32_t* V = chain + (size_t)(cls ^ 2) * L.class_words;
-  const uint32_t* D = chain + (size_t)(cls ^ 3) * L.class_words;
-  const int rn = py ? r : r - 1, rs = py ? r + 1 : r;
+// The rows one word update reads and writes: the word's own row F (class px, py), the same
+// row of class (1-px, py) (west/east neighbours), rows above/below of class (px, 1-py)
+// (north/south) and of class (1-px, 1-py) (diagonals).
+struct SvRows {
+  uint32_t* F;
+  const uint32_t *H, *Vn, *Vs, *Dn, *Ds;
+};
 
-  // interior bits of this word: k in [k_lo, k_hi]
-  const int k0 = 32 * w;
-  const int lo = max(L.k_lo - k0, 0), hi = min(L.k_hi - k0, 31);
-  if (hi < lo) return;
-  const uint32_t imask = (hi - lo == 31 ? 0xffffffffu : ((1u << (hi - lo + 1)) - 1u)) << lo;
+// Updates data word w (index idx = w + 1) of class row r in NCH chains that share the draws.
+__device__ __forceinline__ uint4 sv_block(uint32_t w, uint32_t r, int q, uint32_t c2, uint32_t c3, uint64_t seed) {
+  return philox4x32_10(make_uint4(w | ((uint32_t)q << 24), r, c2, c3), (uint32_t)seed, (uint32_t)(seed >> 32));
+}
 
-  const uint32_t f = F[idx];
-  const uint32_t wv = west_of(Hrow, idx, px), ev = east_of(Hrow, idx, px);
-  const uint32_t nv = V[(size_t)rn * L.P + idx], sv = V[(size_t)rs * L.P + idx];
-  const uint32_t flip = ~(wv ^ ev) & ~(wv ^ nv) & ~(wv ^ sv) & imask;
-  if (!flip) return;
-  const uint32_t sup = (px ^ py) ? wv : ~wv;  // sigma of h' + 1 (neighbour parity 1 - (px ^ py))
-  const uint32_t* Dn = D + (size_t)rn * L.P;
-  const uint32_t* Ds = D + (size_t)rs * L.P;
-  const uint32_t e1a = ~(west_of(Dn, idx, px) ^ sup), e1b = ~(east_of(Ds, idx, px) ^ sup);
-  const uint32_t e2a = ~(east_of(Dn, idx, px) ^ sup), e2b = ~(west_of(Ds, idx, px) ^ sup);
-  const uint32_t a0 = ~(e1a | e1b), a1 = e1a ^ e1b, a2 = e1a & e1b;
-  const uint32_t b0 = ~(e2a | e2b), b1 = e2a ^ e2b, b2 = e2a & e2b;
-  const uint32_t mk[9] = {a0 & b0, a0 & b1, a0 & b2, a1 & b0, a1 & b1, a1 & b2, a2 & b0, a2 & b1, a2 & b2};
-
-  uint32_t lt = 0, und = flip;
-  const uint32_t c2 = (uint32_t)(uint64_t)L.s, c3 = ((uint32_t)((uint64_t)L.s >> 32) & 0xffffu) | (L.stream << 16);
+// Blocks q < NPRE of the draws arrive precomputed in pre[] (they do not depend on the state).
+template <int NCH, int NPRE = 0>
+__device__ __forceinline__ void sv_update_word(const SvRows (&rows)[NCH], int idx, int px, int py, uint32_t imask,
+                                               uint32_t w, uint32_t r, const uint32_t (&T)[9], uint64_t seed,
+                                               uint32_t c2, uint32_t c3, const uint4* pre = nullptr) {
+  uint32_t f[NCH], flip[NCH], sup[NCH], mk[NCH][9], lt[NCH], und[NCH];
+  uint32_t any = 0;
+#pragma unroll
+  for (int c = 0; c < NCH; ++c) {
+    const SvRows& R = rows[c];
+    f[c] = R.F[idx];
+    const uint32_t wv = west_of(R.H, idx, px), ev = east_of(R.H, idx, px);
+    const uint32_t nv = R.Vn[idx], sv = R.Vs[idx];
+    flip[c] = ~(wv ^ ev) & ~(wv ^ nv) & ~(wv ^ sv) & imask;
+    sup[c] = (px ^ py) ? wv : ~wv;  // sigma of h' + 1 (neighbour parity 1 - (px ^ py))
+    const uint32_t e1a = ~(west_of(R.Dn, idx, px) ^ sup[c]), e1b = ~(east_of(R.Ds, idx, px) ^ sup[c]);
+    const uint32_t e2a = ~(east_of(R.Dn, idx, px) ^ sup[c]), e2b = ~(west_of(R.Ds, idx, px) ^ sup[c]);
+    const uint32_t a0 = ~(e1a | e1b), a1 = e1a ^ e1b, a2 = e1a & e1b;
+    const uint32_t b0 = ~(e2a | e2b), b1 = e2a ^ e2b, b2 = e2a & e2b;
+    mk[c][0] = a0 & b0, mk[c][1] = a0 & b1, mk[c][2] = a0 & b2;
+    mk[c][3] = a1 & b0, mk[c][4] = a1 & b1, mk[c][5] = a1 & b2;
+    mk[c][6] = a2 & b0, mk[c][7] = a2 & b1, mk[c][8] = a2 & b2;
+    lt[c] = 0;
+    und[c] = flip[c];
+    any |= flip[c];
+  }
+  if (!any) return;
 #pragma unroll
   for (int q = 0; q < 8; ++q) {
-    if (!und) break;
-    const uint4 R = philox4x32_10(make_uint4((uint32_t)w | ((uint32_t)q << 24), (uint32_t)r, c2, c3), (uint32_t)L.seed,
-                                  (uint32_t)(L.seed >> 32));
-    const uint32_t planes[4] = {R.x, R.y, R.z, R.w};
+    uint32_t open = 0;
+#pragma unroll
+    for (int c = 0; c < NCH; ++c) open |= und[c];
+    if (!open) break;
+    const uint4 Rq = q < NPRE ? pre[q] : sv_block(w, r, q, c2, c3, seed);
+    const uint32_t planes[4] = {Rq.x, Rq.y, Rq.z, Rq.w};
 #pragma unroll
     for (int t = 0; t < 4; ++t) {
       const int j = 31 - (4 * q + t);
-      uint32_t Tj = 0;
 #pragma unroll
-      for (int m = 0; m < 9; ++m) Tj |= ((L.T[m] >> j) & 1u) ? mk[m] : 0u;
-      lt |= und & ~planes[t] & Tj;
-      und &= ~(planes[t] ^ Tj);
+      for (int c = 0; c < NCH; ++c) {
+        uint32_t Tj = 0;
+#pragma unroll
+        for (int m = 0; m < 9; ++m) Tj |= ((T[m] >> j) & 1u) ? mk[c][m] : 0u;
+        lt[c] |= und[c] & ~planes[t] & Tj;
+        und[c] &= ~(planes[t] ^ Tj);
+      }
     }
   }
-  F[idx] = (f & ~flip) | (flip & ~(lt ^ sup));
+#pragma unroll
+  for (int c = 0; c < NCH; ++c)
+    if (flip[c]) rows[c].F[idx] = (f[c] & ~flip[c]) | (flip[c] & ~(lt[c] ^ sup[c]));
+}
+
+__device__ __forceinline__ uint32_t interior_mask(int w, int k_lo, int k_hi) {
+  const int k0 = 32 * w;
+  const int lo = max(k_lo - k0, 0), hi = min(k_hi - k0, 31);
+  if (hi < lo) return 0u;
+  return (hi - lo == 31 ? 0xffffffffu : ((1u << (hi - lo + 1)) - 1u)) << lo;
+}
+
+// One sub-sweep of one class over global memory; blockIdx.y is the chain.
+__global__ void __launch_bounds__(128) k_sv_sub(SvLaunch L) {
+  const int g = blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= L.words * L.rows) return;
+  const int w = g % L.words, r = L.r_lo + g / L.words;
+  const int px = L.px, py = L.py, cls = px | (py << 1);
+  const uint32_t imask = interior_mask(w, L.k_lo, L.k_hi);
+  if (!imask) return;
+  uint32_t* chain = L.base + (size_t)blockIdx.y * L.chain_words;
+  const uint32_t* V = chain + (size_t)(cls ^ 2) * L.class_words;
+  const uint32_t* D = chain + (size_t)(cls ^ 3) * L.class_words;
+  const int rn = py ? r : r - 1, rs = py ? r + 1 : r;
+  const SvRows rows[1] = {{chain + (size_t)cls * L.class_words + (size_t)r * L.P,
+                           chain + (size_t)(cls ^ 1) * L.class_words + (size_t)r * L.P, V + (size_t)rn * L.P,
+                           V + (size_t)rs * L.P, D + (size_t)rn * L.P, D + (size_t)rs * L.P}};
+  const uint32_t c2 = (uint32_t)(uint64_t)L.s, c3 = ((uint32_t)((uint64_t)L.s >> 32) & 0xffffu) | (L.stream << 16);
+  sv_update_word<1>(rows, w + 1, px, py, imask, (uint32_t)w, (uint32_t)r, L.T, L.seed, c2, c3);
+}
+
+// Resident engine: one thread-block cluster holds NCH chains in shared memory, CTA `rank`
+// owning class rows [rank * rpc, rank * rpc + rpc) of all four classes; the one halo row
+// above and below is read from the neighbouring CTA's shared memory (distributed shared
+// memory).  A cluster barrier separates sub-sweeps; no other waits.
+struct SvClusterArgs {
+  uint32_t* base;
+  size_t chain_words, class_words;
+  int P, n, R, rpc;
+  uint32_t T[9];
+  uint64_t seed;
+  uint32_t stream;
+  int64_t s0, count;
+};
+
+template <int NCH>
+constexpr int sv_cluster_max_threads() {
+  return 512;
+}
+
+__device__ __forceinline__ void cluster_arrive_release() { asm volatile("barrier.cluster.arrive.release.aligned;" ::: "memory"); }
+__device__ __forceinline__ void cluster_wait_acquire() { asm volatile("barrier.cluster.wait.acquire.aligned;" ::: "memory"); }
+
+// The class rows, words and interior columns of sub-sweep s restricted to rows [r0, r1).
+struct SvSub {
+  int px, py, cls, r_lo, r_hi, k_lo, k_hi, words;
+  uint32_t c2, c3;
+};
+
+__device__ __forceinline__ SvSub sv_sub_of(int64_t s, int n, int r0, int r1, uint32_t stream) {
+  SvSub u;
+  u.px = (int)(s & 1);
+  u.py = (int)((s >> 1) & 1);
+  u.cls = u.px | (u.py << 1);
+  u.r_lo = max(u.py ? 0 : 1, r0);
+  u.r_hi = min((n - 1 - u.py) / 2, r1 - 1);
+  u.k_lo = u.px ? 0 : 1;
+  u.k_hi = (n - 1 - u.px) / 2;
+  u.words = u.k_hi / 32 + 1;
+  u.c2 = (uint32_t)(uint64_t)s;
+  u.c3 = ((uint32_t)((uint64_t)s >> 32) & 0xffffu) | (stream << 16);
+  return u;
+}
+
+template <int NCH>
+__global__ void __launch_bounds__(sv_cluster_max_threads<NCH>()) k_sv_cluster(SvClusterArgs A) {
+  namespace cg = cooperative_groups;
+  cg::cluster_group cluster = cg::this_cluster();
+  extern __shared__ uint32_t sm[];  // [NCH][4][rpc][P]
+  const int rank = (int)cluster.block_rank(), C = (int)cluster.num_blocks();
+  const int r0 = rank * A.rpc, r1 = min(r0 + A.rpc, A.R), P = A.P;
+  const int own = max(r1 - r0, 0);
+  const int tid = threadIdx.x, nt = blockDim.x;
+  for (int i = tid; i < NCH * 4 * own * P; i += nt) {
+    const int p = i % P, lr = (i / P) % own, cc = i / (P * own);  // cc = chain * 4 + class
+    sm[((size_t)cc * A.rpc + lr) * P + p] =
+        A.base[(size_t)(cc >> 2) * A.chain_words + (size_t)(cc & 3) * A.class_words + (size_t)(r0 + lr) * P + p];
+  }
+  // shared memory of the CTAs above and below (rows r0 - 1 and r1 live there)
+  uint32_t* const up = rank > 0 ? cluster.map_shared_rank(sm, rank - 1) : sm;
+  uint32_t* const dn = rank + 1 < C ? cluster.map_shared_rank(sm, rank + 1) : sm;
+  const size_t plane = (size_t)A.rpc * P;  // words of one class of one chain
+  auto row = [&](int c, int cls, int r) -> uint32_t* {
+    uint32_t* b = r < r0 ? up + (size_t)(A.rpc - 1) * P : r >= r1 ? dn : sm + (size_t)(r - r0) * P;
+    return b + (size_t)(c * 4 + cls) * plane;
+  };
+  const int n = A.n;
+  constexpr int kPre = 2;
+  uint4 pre[kPre];
+  SvSub u = sv_sub_of(A.s0, n, r0, r1, A.stream);
+  if (tid < (u.r_hi - u.r_lo + 1) * u.words)
+    for (int q = 0; q < kPre; ++q) pre[q] = sv_block(tid % u.words, u.r_lo + tid / u.words, q, u.c2, u.c3, A.seed);
+  cluster.sync();
+  for (int64_t s = A.s0; s < A.s0 + A.count; ++s) {
+    const int items = (u.r_hi - u.r_lo + 1) * u.words;
+    for (int it = tid; it < items; it += nt) {
+      const int w = it % u.words, r = u.r_lo + it / u.words;
+      const uint32_t imask = interior_mask(w, u.k_lo, u.k_hi);
+      if (!imask) continue;
+      const int rn = u.py ? r : r - 1, rs = u.py ? r + 1 : r;
+      SvRows rows[NCH];
+#pragma unroll
+      for (int c = 0; c < NCH; ++c)
+        rows[c] = {row(c, u.cls, r), row(c, u.cls ^ 1, r), row(c, u.cls ^ 2, rn), row(c, u.cls ^ 2, rs),
+                   row(c, u.cls ^ 3, rn), row(c, u.cls ^ 3, rs)};
+      if (it == tid)
+        sv_update_word<NCH, kPre>(rows, w + 1, u.px, u.py, imask, (uint32_t)w, (uint32_t)r, A.T, A.seed, u.c2, u.c3, pre);
+      else
+        sv_update_word<NCH>(rows, w + 1, u.px, u.py, imask, (uint32_t)w, (uint32_t)r, A.T, A.seed, u.c2, u.c3);
+    }
+    // the next sub-sweep's first draws do not depend on the state: compute them while the
+    // other CTAs of the cluster reach the barrier
+    cluster_arrive_release();
+    u = sv_sub_of(s + 1, n, r0, r1, A.stream);
+    if (s + 1 < A.s0 + A.count && tid < (u.r_hi - u.r_lo + 1) * u.words)
+      for (int q = 0; q < kPre; ++q) pre[q] = sv_block(tid % u.words, u.r_lo + tid / u.words, q, u.c2, u.c3, A.seed);
+    cluster_wait_acquire();
+  }
+  for (int i = tid; i < NCH * 4 * own * P; i += nt) {
+    const int p = i % P, lr = (i / P) % own, cc = i / (P * own);
+    A.base[(size_t)(cc >> 2) * A.chain_words + (size_t)(cc & 3) * A.class_words + (size_t)(r0 + lr) * P + p] =
+        sm[((size_t)cc * A.rpc + lr) * P + p];
+  }
 }
 
 // OR of (top ^ bottom) over all words of the two chains.
@@ -231,9 +374,107 @@ rt_status sv_check_device() {
   return RT_OK;
 }
 
-// Sub-sweeps [s0, s0 + count) on `chains` chains stored back to back at dev.
+struct SvClusterPlan {
+  bool ok = false;
+  int C = 0, rpc = 0, threads = 0;
+  size_t smem = 0;
+};
+
+template <int NCH>
+SvClusterPlan sv_cluster_plan_for(const SvGeom& G) {
+  SvClusterPlan best;
+  const int words = (G.n / 2) / 32 + 1;
+  for (int cmax : {16, 8}) {
+    SvClusterPlan p;
+    p.rpc = (G.R + cmax - 1) / cmax;
+    p.C = (G.R + p.rpc - 1) / p.rpc;
+    p.smem = (size_t)NCH * 4 * p.rpc * G.P * sizeof(uint32_t);
+    if (p.smem > 200 * 1024) continue;
+    p.threads = std::min(sv_cluster_max_threads<NCH>(), std::max(64, (p.rpc * words + 31) / 32 * 32));
+    auto kern = k_sv_cluster<NCH>;
+    if (cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) != cudaSuccess ||
+        cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)p.smem) != cudaSuccess) {
+      cudaGetLastError();
+      continue;
+    }
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(p.C);
+    cfg.blockDim = dim3(p.threads);
+    cfg.dynamicSmemBytes = p.smem;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = p.C;
+    at[0].val.clusterDim.y = 1;
+    at[0].val.clusterDim.z = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    int clusters = 0;
+    if (cudaOccupancyMaxActiveClusters(&clusters, kern, &cfg) != cudaSuccess || clusters < 1) {
+      cudaGetLastError();
+      continue;
+    }
+    p.ok = true;
+    return p;
+  }
+  return best;
+}
+
+SvClusterPlan sv_cluster_plan(const SvGeom& G, int chains) {
+  return chains == 1 ? sv_cluster_plan_for<1>(G) : sv_cluster_plan_for<2>(G);
+}
+
+// Per-CTA work above which the whole-GPU per-sub-sweep kernels are faster than one cluster.
+constexpr int kSvClusterMaxItems = 1024;
+
+bool sv_use_cluster(const SvGeom& G, const SvClusterPlan& p, int engine) {
+  if (engine == 1 || !p.ok) return false;
+  if (engine == 2) return true;
+  return (int64_t)p.rpc * ((G.n / 2) / 32 + 1) <= kSvClusterMaxItems;
+}
+
+// Sub-sweeps [s0, s0 + count) on `chains` (1 or 2) chains stored back to back at dev;
+// returns the kernel launches, or -1 when engine 2 was asked for and no cluster fits.
 int64_t sv_run(uint32_t* dev, int chains, const SvGeom& G, const std::vector<uint32_t>& T, uint64_t seed,
-               uint32_t stream, int64_t s0, int64_t count, cudaStream_t st) {
+               uint32_t stream, int64_t s0, int64_t count, cudaStream_t st, int engine) {
+  const SvClusterPlan plan = engine == 1 ? SvClusterPlan{} : sv_cluster_plan(G, chains);
+  if (engine == 2 && !plan.ok) return -1;
+  int64_t launches = 0;
+  if (sv_use_cluster(G, plan, engine)) {
+    SvClusterArgs A{};
+    A.base = dev;
+    A.chain_words = G.chain_words;
+    A.class_words = G.class_words;
+    A.P = G.P;
+    A.n = G.n;
+    A.R = G.R;
+    A.rpc = plan.rpc;
+    std::memcpy(A.T, T.data(), sizeof A.T);
+    A.seed = seed;
+    A.stream = stream;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(plan.C);
+    cfg.blockDim = dim3(plan.threads);
+    cfg.dynamicSmemBytes = plan.smem;
+    cfg.stream = st;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = plan.C;
+    at[0].val.clusterDim.y = 1;
+    at[0].val.clusterDim.z = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    constexpr int64_t kChunk = 8192;  // sub-sweeps per launch
+    for (int64_t done = 0; done < count; done += kChunk) {
+      A.s0 = s0 + done;
+      A.count = std::min(kChunk, count - done);
+      if (chains == 1)
+        cudaLaunchKernelEx(&cfg, k_sv_cluster<1>, A);
+      else
+        cudaLaunchKernelEx(&cfg, k_sv_cluster<2>, A);
+      ++launches;
+    }
+    return launches;
+  }
   SvLaunch L{};
   L.base = dev;
   L.chain_words = G.chain_words;
@@ -243,7 +484,6 @@ int64_t sv_run(uint32_t* dev, int chains, const SvGeom& G, const std::vector<uin
   std::memcpy(L.T, T.data(), sizeof L.T);
   L.seed = seed;
   L.stream = stream;
-  int64_t launches = 0;
   for (int64_t s = s0; s < s0 + count; ++s) {
     fill_launch(L, G, s);
     const int threads = L.words * L.rows;
@@ -345,7 +585,12 @@ RT_API rt_status rt_sv_walk(int32_t* h, int32_t n, int64_t sweeps, int64_t seed,
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);
   cudaEventRecord(e0, st);
-  const int64_t launches = sv_run(dev.chains, 1, G, T, (uint64_t)seed, o.fast_stream, 0, 4 * sweeps, st);
+  const int64_t launches = sv_run(dev.chains, 1, G, T, (uint64_t)seed, o.fast_stream, 0, 4 * sweeps, st, o.engine);
+  if (launches < 0) {
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    return fail(RT_ERR_INVALID_ARGUMENT, "six-vertex walk: no thread-block cluster holds this size (engine 2)");
+  }
   cudaEventRecord(e1, st);
   cudaMemcpyAsync(bits.data(), dev.chains, bits.size() * sizeof(uint32_t), cudaMemcpyDeviceToHost, st);
   const cudaError_t err = cudaStreamSynchronize(st);
@@ -364,7 +609,6 @@ RT_API rt_status rt_sv_walk(int32_t* h, int32_t n, int64_t sweeps, int64_t seed,
     stats->flip_attempts = sv_interior_points(n) * sweeps;
     stats->seconds = ms * 1e-3;
   }
-  (void)launches;
   return RT_OK;
 }
 
@@ -419,7 +663,11 @@ RT_API rt_status rt_sv_cftp(const int32_t* hmax, const int32_t* hmin, int32_t n,
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
     cudaEventRecord(e0, st);
-    sv_run(dev.chains, 2, G, T, (uint64_t)seed, o.fast_stream, -4 * Tsw, 4 * Tsw, st);
+    if (sv_run(dev.chains, 2, G, T, (uint64_t)seed, o.fast_stream, -4 * Tsw, 4 * Tsw, st, o.engine) < 0) {
+      cudaEventDestroy(e0);
+      cudaEventDestroy(e1);
+      return fail(RT_ERR_INVALID_ARGUMENT, "six-vertex cftp: no thread-block cluster holds this size (engine 2)");
+    }
     cudaEventRecord(e1, st);
     k_sv_diff<<<64, 256, 0, st>>>(dev.chains, dev.chains + G.chain_words, G.chain_words, dev.flag);
     uint32_t differ = 1;

@@ -123,15 +123,16 @@ def test_oracle_cftp_samples_follow_the_gibbs_law(rt, orc, abc):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("engine", [1, 2])
 @pytest.mark.parametrize("abc", [(1.0, 1.0, 1.0), (1.0, 1.0, 1.5), (0.6, 1.7, 0.9), (2.5, 0.4, 1.1)])
-def test_walk_matches_oracle(rt, orc, abc):
+def test_walk_matches_oracle(rt, orc, abc, engine):
     S = rt.SixVertexTiler
     for n, sweeps, seed, stream in ((2, 3, 1, 0), (3, 10, 5, 1), (7, 40, -3, 2), (33, 25, 99, 7), (64, 20, 2026, 65535),
-                                    (101, 12, 7, 3)):
+                                    (101, 12, 7, 3), (190, 6, 11, 12)):
         for top in (False, True):
             start = S.MaxHeight(n) if top else S.MinHeight(n)
             a = start.copy()
-            stats = S(*abc, fast_stream=stream).Walk(a, sweeps, seed)
+            stats = S(*abc, fast_stream=stream, engine=engine).Walk(a, sweeps, seed)
             b = start.copy()
             orc.sv_walk(b, n, 0, 4 * sweeps, seed, stream, *abc)
             assert np.array_equal(a, b), (n, top, abc)
@@ -165,12 +166,13 @@ def test_walk_from_a_non_dwbc_boundary_keeps_its_boundary(rt, orc):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("engine", [1, 2])
 @pytest.mark.parametrize("abc", [(1.0, 1.0, 1.5), (0.9, 0.5, 1.0)])
-def test_cftp_matches_oracle(rt, orc, abc):
+def test_cftp_matches_oracle(rt, orc, abc, engine):
     S = rt.SixVertexTiler
     for n, seed in ((6, 1), (10, 2), (17, 3)):
         hmax, hmin = S.MaxHeight(n), S.MinHeight(n)
-        out, stats = S(*abc, fast_stream=9).cftp(hmax, hmin, seed, first_sweeps=4, max_attempts=16)
+        out, stats = S(*abc, fast_stream=9, engine=engine).cftp(hmax, hmin, seed, first_sweeps=4, max_attempts=16)
         ref, att, used = orc.sv_cftp(hmax, hmin, n, seed, 9, 4, 16, *abc)
         assert att == stats["attempts"] and 4 * used == stats["final_steps"]
         assert np.array_equal(out, ref)
@@ -215,6 +217,21 @@ def test_refined_enumeration_formula_matches_enumeration(rt):
         for st in states:
             first[int(np.argmax(S.HeightToASM(st.ravel())[:n]))] += 1
         assert [int(v) for v in refined_asm(n)] == first.tolist()
+
+
+@pytest.mark.gpu
+def test_engines_agree_at_the_benchmark_size(rt):
+    # n = 512, a = b = 1, c = 1.5: the cluster-resident and per-sub-sweep engines give the
+    # same heights after 300 sweeps, and the result is a valid domain-wall height function
+    S = rt.SixVertexTiler
+    n = 512
+    a, b = S.MaxHeight(n), S.MaxHeight(n)
+    sa = S(1.0, 1.0, 1.5, engine=2).Walk(a, 300, 5)
+    S(1.0, 1.0, 1.5, engine=1).Walk(b, 300, 5)
+    assert np.array_equal(a, b) and not np.array_equal(a, S.MaxHeight(n))
+    asm = S.HeightToASM(a).reshape(n, n)
+    assert np.array_equal(asm.sum(0), np.ones(n)) and np.array_equal(asm.sum(1), np.ones(n))
+    assert sa["flip_attempts"] == 511 * 511 * 300
 
 
 @pytest.mark.gpu
