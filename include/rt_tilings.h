@@ -230,6 +230,40 @@ RT_API rt_status rt_sv_cftp(const int32_t* hmax, const int32_t* hmin, int32_t n,
                             int32_t max_attempts, const double* abc, const rt_walk_opts* opts, int32_t* out,
                             rt_cftp_stats* stats);
 
+/* ---- bibone tilings: dimers of the triangular lattice (src/TriangleDimer/TriangleDimerTiler.h:
+   84-216) -------------------------------------------------------------------------------------
+   Tiling format of the reference: side N = 2M, vertex (a, b); t[2a][2b+1], t[2a+1][2b] and
+   t[2a+1][2b+1] hold the edge states of the lozenges around the horizontal, up-left and
+   up-right edges (TriangleDimerTiler.h:17-28); the first and last three rows and columns are
+   zero.  Dimer form: one byte per vertex, bit 1 the edge (a,b)-(a,b+1), bit 2 (a,b)-(a-1,b),
+   bit 4 (a,b)-(a-1,b+1). */
+
+/* TriangleDimerTiler::IceCreamCone(n, m) (TriangleDimerTiler.cpp:697-793): the downward
+   triangle of side n with a side-m triangle cut from its top-left corner.  *side = 2 (n + 4). */
+RT_API rt_status rt_td_icecream_cone(int32_t n, int32_t m, int32_t* out, int64_t cap, int32_t* side);
+/* No counterpart in the reference: the rows x cols rhombus of vertices (cols even) covered by
+   horizontal dimers in a brick pattern, padded by three vertices; *side = 2 (max(rows, cols) + 6). */
+RT_API rt_status rt_td_rhombus_brick(int32_t rows, int32_t cols, int32_t* out, int64_t cap, int32_t* side);
+/* Tiling format <-> dimer bytes ((N/2)^2 of them). */
+RT_API rt_status rt_td_dimers(const int32_t* tiling, int32_t n_side, uint8_t* out);
+RT_API rt_status rt_td_from_dimers(const uint8_t* dimers, int32_t n_side, int32_t* out);
+/* TriangleDimerTiler::TilingToVertices / TilingToDomain / DimerIndicator
+   (TriangleDimerTiler.cpp:923-982, 35-99): the covered-vertex grid ((N/2+1)^2), the domain of
+   triangles ((N/2) x N) and the M x M indicator of dimers of orientation c (0 horizontal,
+   1 up-left, 2 up-right). */
+RT_API rt_status rt_td_vertices(const int32_t* tiling, int32_t n_side, int32_t* out);
+RT_API rt_status rt_td_domain(const int32_t* tiling, int32_t n_side, int32_t* out);
+RT_API rt_status rt_td_dimer_indicator(const int32_t* tiling, int32_t n_side, int32_t c, int32_t* out);
+/* TriangleDimerTiler::Walk(tiling&, int steps, long seed) (TriangleDimerTiler.cpp:101-695):
+   per step a move type, orientation and colour (plus slice and parity for butterflies) from
+   default_random_engine(seed) (TinyMT mode; every generator draws each step, generator
+   row * M + column seeded seed + k) or from Philox keyed by (seed, opts->fast_stream, step)
+   (fast mode); sites of that class toggle their lozenge / triangle / butterfly cycle with
+   probability 1/2 when one half of it is covered.  stats (optional): flip attempts (sites of
+   the chosen class on covered vertices) and the device time. */
+RT_API rt_status rt_td_walk(int32_t* tiling, int32_t n_side, int64_t steps, int64_t seed, const rt_walk_opts* opts,
+                            rt_cftp_stats* stats);
+
 /* ---- batched coupling from the past --------------------------------------------------------
    No counterpart in the reference (which runs one instance at a time).  Many independent
    fast-mode CFTP instances of uneven sizes, dominoes and lozenges mixed, in one persistent

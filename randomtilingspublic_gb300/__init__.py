@@ -142,6 +142,14 @@ _SIGNATURES = {
     "rt_recttri_hex_tiling": (C.c_int32, [C.c_int32, C.c_int32, _P, C.c_int64, _P]),
     "rt_recttri_from_lozenge": (C.c_int32, [_P, C.c_int32, _P, C.c_int32, _P]),
     "rt_recttri_walk": (C.c_int32, [_P, C.c_int32, C.c_int64, C.c_int64, _P, _P]),
+    "rt_td_icecream_cone": (C.c_int32, [C.c_int32, C.c_int32, _P, C.c_int64, _P]),
+    "rt_td_rhombus_brick": (C.c_int32, [C.c_int32, C.c_int32, _P, C.c_int64, _P]),
+    "rt_td_dimers": (C.c_int32, [_P, C.c_int32, _P]),
+    "rt_td_from_dimers": (C.c_int32, [_P, C.c_int32, _P]),
+    "rt_td_walk": (C.c_int32, [_P, C.c_int32, C.c_int64, C.c_int64, _P, _P]),
+    "rt_td_vertices": (C.c_int32, [_P, C.c_int32, _P]),
+    "rt_td_domain": (C.c_int32, [_P, C.c_int32, _P]),
+    "rt_td_dimer_indicator": (C.c_int32, [_P, C.c_int32, C.c_int32, _P]),
     "rt_sv_thresholds": (C.c_int32, [C.c_double, C.c_double, C.c_double, _P]),
     "rt_sv_dwbc_height": (C.c_int32, [C.c_int32, C.c_int32, _P]),
     "rt_sv_height_to_asm": (C.c_int32, [_P, C.c_int32, _P]),
@@ -519,6 +527,86 @@ class RectTriangleTiler:
         return out
 
 
+class TriangleDimerTiler:
+    """Bibone tilings, i.e. dimer coverings of the triangular lattice
+    (src/TriangleDimer/TriangleDimerTiler.h:84-216).  ``rng`` is 'tinymt' (bit-exact with the
+    reference's OpenCL path) or 'fast'."""
+
+    def __init__(self, rng: str = "tinymt", fast_stream: int = 0):
+        self.rng = rng
+        self.fast_stream = int(fast_stream)
+
+    def opts(self) -> _WalkOpts:
+        o = _WalkOpts()
+        lib().rt_walk_opts_default(C.byref(o))
+        o.rng_mode = RNG_MODES[self.rng]
+        o.fast_stream = self.fast_stream
+        return o
+
+    def Walk(self, t, steps: int, seed: int) -> dict:
+        tt = _i32(t)
+        o, st = self.opts(), CftpStats()
+        _check(lib().rt_td_walk(_ptr(tt), side_of(tt), int(steps), int(seed), C.byref(o), C.byref(st)))
+        _write_back(t, tt)
+        return st.as_dict()
+
+    @staticmethod
+    def IceCreamCone(n: int, m: int) -> np.ndarray:
+        side = C.c_int32()
+        s = 2 * (n + 4)
+        buf = np.zeros(s * s, np.int32)
+        _check(lib().rt_td_icecream_cone(int(n), int(m), _ptr(buf), buf.size, C.byref(side)))
+        return buf[: side.value * side.value].copy()
+
+    @staticmethod
+    def RhombusBrick(rows: int, cols: int) -> np.ndarray:
+        side = C.c_int32()
+        s = 2 * (max(rows, cols) + 6)
+        buf = np.zeros(s * s, np.int32)
+        _check(lib().rt_td_rhombus_brick(int(rows), int(cols), _ptr(buf), buf.size, C.byref(side)))
+        return buf[: side.value * side.value].copy()
+
+    @staticmethod
+    def Dimers(t) -> np.ndarray:
+        """Dimer bytes ((N/2) x (N/2)): bit 1 (a,b)-(a,b+1), 2 (a,b)-(a-1,b), 4 (a,b)-(a-1,b+1)."""
+        tt = _i32(t)
+        n = side_of(tt)
+        out = np.zeros((n // 2) ** 2, np.uint8)
+        _check(lib().rt_td_dimers(_ptr(tt), n, _ptr(out)))
+        return out
+
+    @staticmethod
+    def TilingToVertices(t) -> np.ndarray:
+        tt = _i32(t)
+        n = side_of(tt)
+        out = np.zeros((n // 2 + 1) ** 2, np.int32)
+        _check(lib().rt_td_vertices(_ptr(tt), n, _ptr(out)))
+        return out
+
+    @staticmethod
+    def TilingToDomain(t) -> np.ndarray:
+        tt = _i32(t)
+        n = side_of(tt)
+        out = np.zeros((n // 2) * n, np.int32)
+        _check(lib().rt_td_domain(_ptr(tt), n, _ptr(out)))
+        return out
+
+    @staticmethod
+    def DimerIndicator(t, c: int) -> np.ndarray:
+        tt = _i32(t)
+        n = side_of(tt)
+        out = np.zeros((n // 2) ** 2, np.int32)
+        _check(lib().rt_td_dimer_indicator(_ptr(tt), n, int(c), _ptr(out)))
+        return out
+
+    @staticmethod
+    def FromDimers(d, n_side: int) -> np.ndarray:
+        dd = np.ascontiguousarray(np.asarray(d, np.uint8).ravel())
+        out = np.zeros(n_side * n_side, np.int32)
+        _check(lib().rt_td_from_dimers(_ptr(dd), int(n_side), _ptr(out)))
+        return out
+
+
 class SixVertexTiler:
     """Six-vertex model on an n x n grid (no counterpart in the reference; shaped like its
     per-model classes).  State: the (n+1) x (n+1) int32 height function; weights a, b, c;
@@ -768,5 +856,5 @@ def mt19937_draws(seed: int, count: int) -> np.ndarray:
     return rs.randint(0, 2**32, size=count, dtype=np.uint32)
 
 
-__all__ = ["DominoTiler", "DominoSampler", "LozengeTiler", "RectTriangleTiler", "SixVertexTiler", "cftp_batch", "Server", "RTError", "lib", "read_tinymt_params", "mt19937_colours",
+__all__ = ["DominoTiler", "DominoSampler", "LozengeTiler", "RectTriangleTiler", "SixVertexTiler", "TriangleDimerTiler", "cftp_batch", "Server", "RTError", "lib", "read_tinymt_params", "mt19937_colours",
            "mt19937_draws", "CftpStats"]

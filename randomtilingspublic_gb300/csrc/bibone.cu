@@ -1,0 +1,417 @@
+// Bibone tilings: dimer coverings of regions of the triangular lattice (reference:
+// src/TriangleDimer/, class TriangleDimerTiler).
+//
+// The reference stores, per lattice edge, the states of the edges around it in eight arrays
+// (three lozenge, two triangle, three butterfly orientations) and re-derives all of them
+// after each move with up to 11 kernels.  Here the state is the dimer configuration itself,
+// one byte per vertex (bit 1: H(a,b) = (a,b)-(a,b+1), bit 2: L(a,b) = (a,b)-(a-1,b), bit 4:
+// R(a,b) = (a,b)-(a-1,b+1)), and every move of the reference is the toggle of an alternating
+// cycle of edges: lozenges (4-cycles, triangledimerkernel.cl:4-22), side-2 triangles
+// (6-cycles, :191-211) and butterflies (8-cycles, :331-353).  A step is one kernel: each
+// site of the chosen class whose cycle has one half covered flips with probability 1/2.
+// Same-class cycles are edge-disjoint (the reference's colourings), and two cycles that can
+// flip together share no vertex, so byte read-modify-writes never race.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <random>
+#include <string>
+#include <vector>
+
+#include "rng.cuh"
+#include "rt_internal.h"
+
+namespace rt {
+namespace {
+
+enum : uint8_t { kH = 1, kL = 2, kR = 4 };
+
+struct TdEdge {
+  int8_t da, db;
+  uint8_t bit;
+};
+struct TdCycle {
+  int n;
+  TdEdge a[4], b[4];  // the two alternating halves; a = state 5 / 45 / 85, b = 10 / 54 / 170
+};
+
+// Cycles by class: lozenge H, L, R (eH/eL/eR of the reference), triangle up / down (tU/tD),
+// butterfly H, L, R (bH/bL/bR), at site (a, b).
+__constant__ TdCycle c_cycles[8] = {
+    {2, {{-1, 0, kR}, {0, 0, kR}}, {{-1, 1, kL}, {0, 0, kL}}},
+    {2, {{-1, 0, kH}, {0, -1, kH}}, {{0, 0, kR}, {0, -1, kR}}},
+    {2, {{-1, 0, kH}, {0, 0, kH}}, {{0, 1, kL}, {0, 0, kL}}},
+    {3, {{-1, 0, kH}, {0, 1, kR}, {1, 0, kL}}, {{0, 0, kL}, {-1, 1, kH}, {1, 0, kR}}},
+    {3, {{0, -1, kH}, {0, 1, kL}, {-1, 0, kR}}, {{0, -1, kR}, {0, 0, kH}, {-1, 1, kL}}},
+    {4, {{-1, 0, kL}, {-2, 1, kH}, {0, 1, kL}, {0, -1, kH}}, {{-2, 0, kH}, {-1, 1, kR}, {0, 0, kH}, {0, -1, kR}}},
+    {4, {{-1, 0, kR}, {0, 1, kL}, {1, -1, kR}, {0, -1, kL}}, {{-1, 1, kL}, {0, 0, kH}, {1, -1, kL}, {-1, -1, kH}}},
+    {4, {{-1, 0, kR}, {-1, 1, kH}, {1, 0, kR}, {0, -1, kH}}, {{-1, 1, kL}, {0, 1, kR}, {1, 0, kL}, {0, -1, kR}}},
+};
+
+// One step's class: move type (0 lozenge, 1 triangle, 2 butterfly), orientation / colour r1,
+// colour r2, butterfly slice p1 and parity p2 (TriangleDimerTiler.cpp:269-276, 459-460).
+struct TdStep {
+  int type, r1, r2, p1, p2;
+};
+
+__host__ __device__ inline int td_cycle_of(const TdStep& s) {
+  return s.type == 0 ? s.r1 : s.type == 1 ? (s.r2 == 1 ? 4 : 3) : 5 + s.r1;
+}
+
+__host__ __device__ inline bool td_in_class(const TdStep& s, int a, int b) {
+  if (s.type == 0) return (((1 - (s.r1 & 1)) * a + ((1 + s.r1) / 2) * b) % 2) == s.r2;
+  if (s.type == 1) return (((b - a) % 3 + 3) % 3) == s.r1;
+  const int b1 = 1 - (s.r1 & 1), b2 = (1 + s.r1) / 2, b3 = s.r1 & 1;
+  return ((b1 * a + b2 * b) % 3) == s.p1 && ((b1 * b + b3 * a) & 1) == s.p2;
+}
+
+__device__ __forceinline__ void td_try_flip(uint8_t* D, int M, int c, int a, int b) {
+  const TdCycle& C = c_cycles[c];
+  bool ha = true, hb = true;
+  for (int k = 0; k < C.n; ++k) {
+    const int xa = a + C.a[k].da, ya = b + C.a[k].db, xb = a + C.b[k].da, yb = b + C.b[k].db;
+    // cycles reaching past the array never move (the padding keeps every domain cycle inside)
+    if (xa < 0 || ya < 0 || xa >= M || ya >= M || xb < 0 || yb < 0 || xb >= M || yb >= M) return;
+    ha = ha && (D[(size_t)xa * M + ya] & C.a[k].bit);
+    hb = hb && (D[(size_t)xb * M + yb] & C.b[k].bit);
+  }
+  if (!ha && !hb) return;
+  for (int k = 0; k < C.n; ++k) {
+    D[(size_t)(a + C.a[k].da) * M + b + C.a[k].db] ^= C.a[k].bit;
+    D[(size_t)(a + C.b[k].da) * M + b + C.b[k].db] ^= C.b[k].bit;
+  }
+}
+
+__global__ void k_td_seed(uint4* st, int64_t count, uint32_t seed) {
+  const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k < count) st[k] = tmt_seed(seed + (uint32_t)k, kTmtMat1, kTmtMat2, kTmtTmat);
+}
+
+// TinyMT mode: every generator draws (as every work item of the reference's rotate kernel
+// does); sites of the class flip when rd < 0.5, i.e. the 23-bit draw is below 2^22.
+__global__ void k_td_step_tmt(uint8_t* D, uint4* tmt, int M, TdStep s) {
+  const int b = blockIdx.x * blockDim.x + threadIdx.x, a = blockIdx.y;
+  if (b >= M) return;
+  const size_t k = (size_t)a * M + b;
+  uint4 g = tmt[k];
+  const uint32_t u = tmt_next_u23(g, kTmtMat1, kTmtMat2, kTmtTmat);
+  tmt[k] = g;
+  if (u < (1u << 22) && td_in_class(s, a, b)) td_try_flip(D, M, td_cycle_of(s), a, b);
+}
+
+// Fast mode: a thread owns columns 4q .. 4q+3 of row a and one Philox block of draws.
+__global__ void k_td_step_fast(uint8_t* D, int M, TdStep s, uint64_t seed, uint32_t stream, int64_t h) {
+  const int q = blockIdx.x * blockDim.x + threadIdx.x, a = blockIdx.y;
+  if (4 * q >= M) return;
+  bool any = false;
+#pragma unroll
+  for (int k = 0; k < 4; ++k) any |= (4 * q + k < M) && td_in_class(s, a, 4 * q + k);
+  if (!any) return;
+  const uint4 d = fast_quad(seed, stream, h, (uint32_t)a, (uint32_t)q);
+  const uint32_t u[4] = {d.x, d.y, d.z, d.w};
+  const int c = td_cycle_of(s);
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    const int b = 4 * q + k;
+    if (b < M && u[k] < 0x80000000u && td_in_class(s, a, b)) td_try_flip(D, M, c, a, b);
+  }
+}
+
+// Philox4x32-10 on the host (the fast-mode step schedule).
+void philox_host(uint32_t c[4], uint32_t k0, uint32_t k1) {
+  for (int r = 0; r < 10; ++r) {
+    const uint64_t p0 = (uint64_t)0xD2511F53u * c[0], p1 = (uint64_t)0xCD9E8D57u * c[2];
+    const uint32_t n0 = (uint32_t)(p1 >> 32) ^ c[1] ^ k0, n1 = (uint32_t)p1, n2 = (uint32_t)(p0 >> 32) ^ c[3] ^ k1,
+                   n3 = (uint32_t)p0;
+    c[0] = n0, c[1] = n1, c[2] = n2, c[3] = n3;
+    k0 += 0x9E3779B9u;
+    k1 += 0xBB67AE85u;
+  }
+}
+
+// Fast-mode schedule: step h's class from Philox(ctr = {~0, ~0, lo32(h), hi16(h) | s << 16}).
+TdStep td_fast_step(uint64_t seed, uint32_t stream, int64_t h) {
+  uint32_t c[4] = {0xffffffffu, 0xffffffffu, (uint32_t)(uint64_t)h,
+                   ((uint32_t)((uint64_t)h >> 32) & 0xffffu) | (stream << 16)};
+  philox_host(c, (uint32_t)seed, (uint32_t)(seed >> 32));
+  return TdStep{(int)(c[0] % 3u), (int)(c[1] % 3u), (int)(c[2] & 1u), (int)((c[3] >> 1) % 3u), (int)(c[3] & 1u)};
+}
+
+void td_from_tiling(const int32_t* t, int N, uint8_t* D) {
+  const int M = N / 2;
+  for (int a = 0; a < M; ++a)
+    for (int b = 0; b < M; ++b) {
+      const int eR = t[(size_t)(2 * a + 1) * N + 2 * b + 1], eH = t[(size_t)(2 * a) * N + 2 * b + 1];
+      D[(size_t)a * M + b] = (uint8_t)(((eR & 4) ? kH : 0) | ((eR & 8) ? kL : 0) | ((eH & 4) ? kR : 0));
+    }
+}
+
+// Lozenge states from the dimers (the reference's tiling format); the (even, even) entries,
+// which hold no state, are left as they are.
+void td_to_tiling(const uint8_t* D, int N, int32_t* t) {
+  const int M = N / 2;
+  auto bit = [&](int a, int b, int k) -> int {
+    return (a >= 0 && b >= 0 && a < M && b < M && (D[(size_t)a * M + b] & k)) ? 1 : 0;
+  };
+  for (int a = 0; a < M; ++a)
+    for (int b = 0; b < M; ++b) {
+      t[(size_t)(2 * a) * N + 2 * b + 1] = bit(a - 1, b, kR) + 2 * bit(a - 1, b + 1, kL) + 4 * bit(a, b, kR) + 8 * bit(a, b, kL);
+      t[(size_t)(2 * a + 1) * N + 2 * b] = bit(a - 1, b, kH) + 2 * bit(a, b, kR) + 4 * bit(a, b - 1, kH) + 8 * bit(a, b - 1, kR);
+      t[(size_t)(2 * a + 1) * N + 2 * b + 1] = bit(a - 1, b, kH) + 2 * bit(a, b + 1, kL) + 4 * bit(a, b, kH) + 8 * bit(a, b, kL);
+    }
+}
+
+// Number of dimers at each vertex: 0 off the domain, 1 on it for a dimer covering.
+std::vector<int> td_cover(const uint8_t* D, int M) {
+  std::vector<int> c((size_t)M * M, 0);
+  auto add = [&](int a, int b) {
+    if (a >= 0 && b >= 0 && a < M && b < M) ++c[(size_t)a * M + b];
+  };
+  for (int a = 0; a < M; ++a)
+    for (int b = 0; b < M; ++b) {
+      const uint8_t v = D[(size_t)a * M + b];
+      if (v & kH) add(a, b), add(a, b + 1);
+      if (v & kL) add(a, b), add(a - 1, b);
+      if (v & kR) add(a, b), add(a - 1, b + 1);
+    }
+  return c;
+}
+
+}  // namespace
+}  // namespace rt
+
+using namespace rt;
+
+extern "C" {
+
+RT_API rt_status rt_td_icecream_cone(int32_t n, int32_t m, int32_t* out, int64_t cap, int32_t* side) {
+  clear_error();
+  if (n < 1 || m < 0 || !side) return fail(RT_ERR_INVALID_ARGUMENT, "bibone icecream_cone: n >= 1, m >= 0");
+  const int E = n + 4, T = 2 * E, k = ((n + 1) * (n + 2) / 2) % 2;
+  *side = T;
+  if (!out || cap < (int64_t)T * T) return fail(RT_ERR_BUFFER_TOO_SMALL, "bibone icecream_cone: output too small");
+  // As the reference, the layout is built even when m > n - 1 or the vertex count is odd (it
+  // prints a warning and covers the domain less its top-right vertex).
+  // The reference's dimer layout (TriangleDimerTiler.cpp:714-740): horizontal dimers in every
+  // other column, the slanted right side closed by L / R dimers, the cut corner staggered
+  std::vector<uint8_t> D((size_t)E * E, 0);
+  auto set = [&](int a, int b, uint8_t bit) {
+    if (a >= 0 && a < E) D[(size_t)a * E + b] |= bit;
+  };
+  for (int i = 2; i < E - 2; ++i)
+    for (int j = 2; j < E - i; ++j) {
+      if (i < m + 2) {
+        if ((i + j) % 2 == m % 2 && (m != 0 && j > m + 3 - i)) set(i - 1, j, kH);
+        if ((n - m) % 2 == 0 && (i % 2) == 0 && j == E - i - 1) set(i, j, kR);
+      } else {
+        const bool closes_l = i % 4 == (3 + n % 2 + 2 * k) % 4 && j == E - i - 1;
+        if (j % 2 == 0 && !closes_l) set(i - 1, j, kH);
+        if (closes_l) set(i, j, kL);
+        if (i % 4 == (2 + n % 2 + 2 * k) % 4 && j == E - i - 1) set(i, j, kR);
+      }
+    }
+  std::vector<int32_t> t((size_t)T * T, 0);
+  td_to_tiling(D.data(), T, t.data());
+  for (int i = 0; i < T; ++i)
+    for (int j = 0; j < T; ++j)
+      out[(size_t)i * T + j] = (i >= 3 && j >= 3 && i < T - 1 && j < T - 1) ? t[(size_t)i * T + j] : 0;
+  return RT_OK;
+}
+
+RT_API rt_status rt_td_rhombus_brick(int32_t rows, int32_t cols, int32_t* out, int64_t cap, int32_t* side) {
+  clear_error();
+  if (rows < 1 || cols < 2 || cols % 2 || !side)
+    return fail(RT_ERR_INVALID_ARGUMENT, "bibone rhombus: rows >= 1 and an even number of columns >= 2");
+  const int M = std::max(rows, cols) + 6, T = 2 * M;
+  *side = T;
+  if (!out || cap < (int64_t)T * T) return fail(RT_ERR_BUFFER_TOO_SMALL, "bibone rhombus: output too small");
+  std::vector<uint8_t> D((size_t)M * M, 0);
+  for (int a = 0; a < rows; ++a)
+    for (int b = 0; b < cols; b += 2) D[(size_t)(a + 3) * M + b + 3] = kH;
+  std::fill(out, out + (size_t)T * T, 0);
+  td_to_tiling(D.data(), T, out);
+  return RT_OK;
+}
+
+RT_API rt_status rt_td_dimers(const int32_t* t, int32_t n_side, uint8_t* out) {
+  clear_error();
+  if (!t || !out || n_side < 2 || n_side % 2) return fail(RT_ERR_INVALID_ARGUMENT, "bibone dimers: even side >= 2");
+  td_from_tiling(t, n_side, out);
+  return RT_OK;
+}
+
+RT_API rt_status rt_td_from_dimers(const uint8_t* dimers, int32_t n_side, int32_t* out) {
+  clear_error();
+  if (!dimers || !out || n_side < 2 || n_side % 2) return fail(RT_ERR_INVALID_ARGUMENT, "bibone from_dimers: even side >= 2");
+  td_to_tiling(dimers, n_side, out);
+  return RT_OK;
+}
+
+// TriangleDimerTiler::TilingToVertices (TriangleDimerTiler.cpp:923-949): an (N/2+1)^2 grid,
+// entry (i, j) (2 <= i, j < N/2 - 1) is 1 when vertex (i-1, j) is covered by a dimer.
+RT_API rt_status rt_td_vertices(const int32_t* tiling, int32_t n_side, int32_t* out) {
+  clear_error();
+  if (!tiling || !out || n_side < 4 || n_side % 2) return fail(RT_ERR_INVALID_ARGUMENT, "bibone vertices: even side >= 4");
+  const int M = n_side / 2, V = M + 1;
+  std::vector<uint8_t> D((size_t)M * M);
+  td_from_tiling(tiling, n_side, D.data());
+  const std::vector<int> c = td_cover(D.data(), M);
+  std::fill(out, out + (size_t)V * V, 0);
+  for (int i = 2; i < V - 2; ++i)
+    for (int j = 2; j < V - 2; ++j) out[(size_t)i * V + j] = c[(size_t)(i - 1) * M + j] > 0;
+  return RT_OK;
+}
+
+// TriangleDimerTiler::TilingToDomain (:951-982): (V-1) x 2(V-1) triangles over the vertex grid
+// above, even columns the triangle (i, j/2), (i, j/2+1), (i+1, j/2), odd columns
+// (i, j/2+1), (i+1, j/2), (i+1, j/2+1); 1 when all three vertices are covered.
+RT_API rt_status rt_td_domain(const int32_t* tiling, int32_t n_side, int32_t* out) {
+  clear_error();
+  if (!tiling || !out || n_side < 4 || n_side % 2) return fail(RT_ERR_INVALID_ARGUMENT, "bibone domain: even side >= 4");
+  const int V = n_side / 2 + 1;
+  std::vector<int32_t> v((size_t)V * V);
+  rt_td_vertices(tiling, n_side, v.data());
+  auto at = [&](int i, int j) { return v[(size_t)i * V + j]; };
+  for (int i = 0; i < V - 1; ++i)
+    for (int j = 0; j < 2 * (V - 1); ++j) {
+      const bool in = j % 2 == 0 ? (at(i, j / 2) && at(i, j / 2 + 1) && at(i + 1, j / 2))
+                                 : (at(i, j / 2 + 1) && at(i + 1, j / 2) && at(i + 1, j / 2 + 1));
+      out[(size_t)i * 2 * (V - 1) + j] = in ? 1 : 0;
+    }
+  return RT_OK;
+}
+
+// TriangleDimerTiler::DimerIndicator(t, c) (:35-99): M x M, for c = 0 the horizontal dimers
+// (entry (a, b) is the edge (a-1, b)-(a-1, b+1)), c = 1 the up-left ones (a, b)-(a-1, b),
+// c = 2 the up-right ones (a, b)-(a-1, b+1).
+RT_API rt_status rt_td_dimer_indicator(const int32_t* tiling, int32_t n_side, int32_t c, int32_t* out) {
+  clear_error();
+  if (!tiling || !out || n_side < 4 || n_side % 2 || c < 0 || c > 2)
+    return fail(RT_ERR_INVALID_ARGUMENT, "bibone dimer_indicator: even side >= 4, c in {0, 1, 2}");
+  const int M = n_side / 2;
+  std::vector<uint8_t> D((size_t)M * M);
+  td_from_tiling(tiling, n_side, D.data());
+  for (int a = 0; a < M; ++a)
+    for (int b = 0; b < M; ++b) {
+      const int v = c == 0 ? (a > 0 ? (D[(size_t)(a - 1) * M + b] & kH) : 0)
+                           : (D[(size_t)a * M + b] & (c == 1 ? kL : kR));
+      out[(size_t)a * M + b] = v ? 1 : 0;
+    }
+  return RT_OK;
+}
+
+RT_API rt_status rt_td_walk(int32_t* tiling, int32_t n_side, int64_t steps, int64_t seed, const rt_walk_opts* opts,
+                            rt_cftp_stats* stats) {
+  clear_error();
+  rt_walk_opts o;
+  rt_walk_opts_default(&o);
+  if (opts) o = *opts;
+  if (!tiling || steps < 0) return fail(RT_ERR_INVALID_ARGUMENT, "bibone walk: NULL tiling or negative steps");
+  if (n_side < 8 || n_side % 2 || n_side > 2 * 32767)
+    return fail(RT_ERR_INVALID_ARGUMENT, "bibone tiling side must be even, in [8, 65534]");
+  if (o.rng_mode != RT_RNG_TINYMT && o.rng_mode != RT_RNG_FAST) return fail(RT_ERR_INVALID_ARGUMENT, "unknown rng mode");
+  if (o.rng_mode == RT_RNG_FAST && o.fast_stream >= 65536u) return fail(RT_ERR_INVALID_ARGUMENT, "fast_stream must be < 65536");
+  const int N = n_side, M = N / 2;
+  std::vector<uint8_t> D((size_t)M * M);
+  td_from_tiling(tiling, N, D.data());
+  {
+    // the state must be a dimer covering of its vertex set, and must round-trip
+    std::vector<int32_t> back((size_t)N * N, 0);
+    for (size_t p = 0; p < back.size(); ++p) back[p] = tiling[p];
+    td_to_tiling(D.data(), N, back.data());
+    for (size_t p = 0; p < back.size(); ++p)
+      if (back[p] != tiling[p]) return fail(RT_ERR_INVALID_ARGUMENT, "bibone walk: tiling states are not those of a dimer configuration");
+    for (int v : td_cover(D.data(), M))
+      if (v > 1) return fail(RT_ERR_INVALID_ARGUMENT, "bibone walk: two dimers share a vertex");
+  }
+  int devs = 0;
+  if (cudaGetDeviceCount(&devs) != cudaSuccess || devs == 0) {
+    cudaGetLastError();
+    return fail(RT_ERR_CUDA, "no CUDA device: the sweep has no CPU fallback");
+  }
+  // flip attempts: sites of each class whose cycle anchor is a covered vertex
+  std::vector<int> cover = td_cover(D.data(), M);
+  cudaStream_t st = (cudaStream_t)o.cuda_stream;
+  uint8_t* dD = nullptr;
+  uint4* tmt = nullptr;
+  auto cleanup = [&]() {
+    if (dD) cudaFree(dD);
+    if (tmt) cudaFree(tmt);
+  };
+  if (cudaMalloc(&dD, D.size()) != cudaSuccess ||
+      (o.rng_mode == RT_RNG_TINYMT && cudaMalloc(&tmt, (size_t)M * M * sizeof(uint4)) != cudaSuccess)) {
+    cudaGetLastError();
+    cleanup();
+    return fail(RT_ERR_OUT_OF_MEMORY, "bibone walk: device allocation failed");
+  }
+  cudaMemcpyAsync(dD, D.data(), D.size(), cudaMemcpyHostToDevice, st);
+  std::vector<TdStep> sched((size_t)steps);
+  if (o.rng_mode == RT_RNG_TINYMT) {
+    // TriangleDimerTiler.cpp:269-276, 459-460: type, r1, r2 (and p1, p2 for butterflies)
+    std::default_random_engine gen;
+    std::uniform_int_distribution<int> d1(0, 2), d2(0, 1);
+    gen.seed(seed);
+    for (auto& s : sched) {
+      s.type = d1(gen);
+      s.r1 = d1(gen);
+      s.r2 = d2(gen);
+      s.p1 = s.p2 = 0;
+      if (s.type == 2) s.p1 = d1(gen), s.p2 = d2(gen);
+    }
+  } else {
+    for (int64_t h = 0; h < steps; ++h) sched[(size_t)h] = td_fast_step((uint64_t)seed, o.fast_stream, h);
+  }
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  if (o.rng_mode == RT_RNG_TINYMT) {
+    const int64_t count = (int64_t)M * M;
+    k_td_seed<<<(unsigned)((count + 255) / 256), 256, 0, st>>>(tmt, count, (uint32_t)seed);
+  }
+  cudaEventRecord(e0, st);
+  const dim3 g_all((M + 127) / 128, M), g_quad(((M + 3) / 4 + 127) / 128, M);
+  for (int64_t h = 0; h < steps; ++h) {
+    if (o.rng_mode == RT_RNG_TINYMT)
+      k_td_step_tmt<<<g_all, 128, 0, st>>>(dD, tmt, M, sched[(size_t)h]);
+    else
+      k_td_step_fast<<<g_quad, 128, 0, st>>>(dD, M, sched[(size_t)h], (uint64_t)seed, o.fast_stream, h);
+  }
+  cudaEventRecord(e1, st);
+  cudaError_t le = cudaGetLastError();
+  cudaMemcpyAsync(D.data(), dD, D.size(), cudaMemcpyDeviceToHost, st);
+  const cudaError_t se = cudaStreamSynchronize(st);
+  float ms = 0.f;
+  if (se == cudaSuccess) cudaEventElapsedTime(&ms, e0, e1);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cleanup();
+  if (le != cudaSuccess || se != cudaSuccess)
+    return fail(RT_ERR_CUDA, std::string("bibone walk: ") + cudaGetErrorString(le != cudaSuccess ? le : se));
+  td_to_tiling(D.data(), N, tiling);
+  if (stats) {
+    std::memset(stats, 0, sizeof *stats);
+    // per class, the sites whose anchor vertex is covered
+    int64_t attempts = 0;
+    std::vector<int64_t> per_class(3 * 3 * 2 * 3 * 2, -1);
+    for (const TdStep& s : sched) {
+      const size_t key = (((size_t)s.type * 3 + s.r1) * 2 + s.r2) * 6 + (s.type == 2 ? s.p1 * 2 + s.p2 : 0);
+      if (per_class[key] < 0) {
+        int64_t c = 0;
+        for (int a = 0; a < M; ++a)
+          for (int b = 0; b < M; ++b) c += cover[(size_t)a * M + b] && td_in_class(s, a, b);
+        per_class[key] = c;
+      }
+      attempts += per_class[key];
+    }
+    stats->attempts = 1;
+    stats->total_steps = steps;
+    stats->final_steps = steps;
+    stats->flip_attempts = attempts;
+    stats->seconds = ms * 1e-3;
+  }
+  return RT_OK;
+}
+
+}  // extern "C"

@@ -1,4 +1,4 @@
-"""Generates tests/golden/{domino,lozenge,recttri}_ref_cases.json from the reference's own code.
+"""Generates tests/golden/{domino,lozenge,recttri,bibone}_ref_cases.json from the reference's own code.
 
 Runs where the reference tree exists (it is not on the GPU machine): builds oracle/_ref
 (`make -C oracle ref`), which compiles the reference's domino .cl kernel files and its host
@@ -275,6 +275,48 @@ def recttri(ref: str) -> None:
                                                                          "SlopeTiling.txt"],
          "host_cases": host, "cases": cases, "from_lozenge": conv}, separators=(",", ":")))
     print(f"wrote {len(cases)} rectangle-triangle sweep cases, {len(host)} host cases, {len(conv)} conversions")
+    bibone(ref)
+
+
+def bibone(ref: str) -> None:
+    """Bibone (triangular-lattice dimer) vectors from the reference-compiled src/TriangleDimer
+    code (oracle/_ref/libref_tdimer.so: its .cl kernels run by the Walk host loop, and its
+    IceCreamCone).  Pins the committed Examples/ExampleOuts/TriangleDimer/DimerStart.txt
+    (SaveMatrix of IceCreamCone(6, 0), TriangleDimerEx.cpp:31-34) against the reference's
+    IceCreamCone, and records its Domain.txt beside it: SaveMatrix writes floor(sqrt(size))^2
+    entries, so the file holds the first 196 of the 10 x 20 entries of TilingToDomain."""
+    td = C.CDLL(str(ROOT / "oracle/_ref/libref_tdimer.so"))
+    P = lambda a: None if a is None else a.ctypes.data_as(C.c_void_p)
+    td.refh_td_icecream.argtypes = [C.c_int, C.c_int, C.c_void_p, C.c_long]
+    td.ref_td_walk.argtypes = [C.c_void_p, C.c_int, C.c_long, C.c_long]
+
+    def cone(n, m):
+        buf = np.zeros(4 * (n + 8) ** 2, np.int32)
+        side = td.refh_td_icecream(n, m, P(buf), buf.size)
+        return buf[: side * side].copy(), side
+
+    def walk(t, n, steps, seed):
+        t = t.copy()
+        td.ref_td_walk(P(t), n, steps, seed)
+        return t
+
+    fixtures = Path(ref) / "Examples/ExampleOuts/TriangleDimer"
+    start = _read_matrix(fixtures / "DimerStart.txt")
+    assert np.array_equal(start, cone(6, 0)[0]), "DimerStart.txt"
+    example = {"n": 6, "m": 0, "tiling": start.tolist(), "domain": _read_matrix(fixtures / "Domain.txt").tolist()}
+    host, cases = [], []
+    for n, m in [(3, 0), (4, 1), (6, 0), (8, 2), (11, 3), (20, 4)]:
+        t, side = cone(n, m)
+        host.append({"n": n, "m": m, "N": side, "tiling": t.tolist()})
+    for n, m, steps, seed in [(4, 1, 1, 5), (4, 1, 50, 1), (7, 0, 400, 77), (8, 2, 1000, -3), (11, 3, 2000, 2018),
+                              (20, 4, 1500, 99)]:
+        t, side = cone(n, m)
+        cases.append({"name": f"td_walk_cone{n}_{m}_{steps}", "N": side, "start": t.tolist(), "steps": steps, "seed": seed,
+                      "expected": walk(t, side, steps, seed).tolist()})
+    (HERE / "bibone_ref_cases.json").write_text(json.dumps(
+        {"generator": "tests/golden/make_golden.py", "example": example, "host_cases": host, "cases": cases},
+        separators=(",", ":")))
+    print(f"wrote {len(cases)} bibone sweep cases, {len(host)} host cases")
 
 
 if __name__ == "__main__":

@@ -348,3 +348,36 @@ def sv_cftp(hmax, hmin, n, seed, stream, first_sweeps, max_attempts, a=1.0, b=1.
     att = sv_lib().orc_sv_cftp(_p(hmax), _p(hmin), n, seed, stream, first_sweeps, max_attempts, a, b, c, _p(out),
                                C.addressof(used))
     return out, att, used.value
+
+
+# ---- bibone (triangular-lattice dimers) -----------------------------------------------------
+_TD_SIG = {
+    "orc_td_icecream": (C.c_int, [C.c_int, C.c_int, _P, _L]),
+    "orc_td_walk_tinymt": (C.c_int, [_P, C.c_int, _L, _L]),
+    "orc_td_walk_fast": (C.c_int, [_P, C.c_int, _L, _L, C.c_ulong, C.c_uint]),
+    "orc_td_fast_step": (None, [C.c_ulong, C.c_uint, _L, _P]),
+}
+
+
+def td_lib() -> C.CDLL:
+    h = lib()
+    for name, (res, args) in _TD_SIG.items():
+        f = getattr(h, name)
+        f.restype = res
+        f.argtypes = args
+    return h
+
+
+def td_icecream(n: int, m: int) -> np.ndarray:
+    buf = np.zeros(4 * (n + 8) ** 2, np.int32)
+    side = td_lib().orc_td_icecream(n, m, _p(buf), buf.size)
+    assert side > 0
+    return buf[: side * side].copy()
+
+
+def td_walk_tinymt(t: np.ndarray, n_side: int, steps: int, seed: int) -> None:
+    assert td_lib().orc_td_walk_tinymt(_p(t), n_side, steps, seed) == 0
+
+
+def td_walk_fast(t: np.ndarray, n_side: int, h0: int, steps: int, seed: int, stream: int = 0) -> None:
+    assert td_lib().orc_td_walk_fast(_p(t), n_side, h0, steps, seed, stream) == 0
