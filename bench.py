@@ -293,6 +293,44 @@ def serving_leg(rt) -> dict:
             "api": "rt_server_submit / rt_server_poll / rt_server_wait (continuous batching)"}
 
 
+def single_instance_leg(rt) -> dict:
+    """The other single-instance workloads: one coupled max/min CFTP attempt on the lozenge
+    hexagon of side 512, 10^5 sweeps of bibone tilings of the 512 x 512 rhombus from the brick
+    start, and 10^5 sweeps of the six-vertex model with domain-wall boundary at n = 512,
+    a = b = 1, c = 1.5.  Fast (Philox) mode; rates from the device time of the sweeps."""
+    out = {}
+    L = rt.LozengeTiler(rng="fast")
+    d = L.Hexagon(512)
+    tmax, tmin = L.MaxTiling(d), L.MinTiling(d)
+    look_back = 4096  # sweeps of the single attempt (3 steps each)
+    o = L.opts()
+    stats = rt.CftpStats()
+    res = np.zeros_like(tmax)
+    status = rt.lib().rt_lozenge_cftp(tmax.ctypes.data, tmin.ctypes.data, int(np.sqrt(tmax.size)), 11, look_back, 0, 1,
+                                      C.byref(o), res.ctypes.data, C.byref(stats))
+    if status not in (rt.RT_OK, rt.RT_ERR_NOT_COALESCED):
+        raise rt.RTError(status, rt.lib().rt_last_error().decode())
+    out["lozenge_hexagon512_cftp_attempt"] = {
+        "value": stats.flip_attempts / stats.seconds, "unit": "flip attempts/s", "look_back_sweeps": look_back,
+        "coalesced": status == rt.RT_OK, "device_seconds": stats.seconds,
+        "us_per_sweep": stats.seconds / look_back * 1e6, "interior_vertices": 3 * 512 * 512 - 3 * 512 + 1}
+    T = rt.TriangleDimerTiler(rng="fast")
+    t = T.RhombusBrick(512, 512)
+    sweeps = 100_000
+    st = T.Walk(t, 3 * sweeps, 7)
+    out["bibone_rhombus512_walk"] = {
+        "value": st["flip_attempts"] / st["seconds"], "unit": "flip attempts/s", "sweeps": sweeps,
+        "steps": 3 * sweeps, "sweep": "3 steps (each step one move class)", "device_seconds": st["seconds"],
+        "us_per_step": st["seconds"] / (3 * sweeps) * 1e6}
+    S = rt.SixVertexTiler(1.0, 1.0, 1.5)
+    h = S.MaxHeight(512)
+    st = S.Walk(h, sweeps, 7)
+    out["six_vertex_dwbc512_walk"] = {
+        "value": st["flip_attempts"] / st["seconds"], "unit": "flip attempts/s", "sweeps": sweeps,
+        "weights": [1.0, 1.0, 1.5], "device_seconds": st["seconds"], "us_per_sweep": st["seconds"] / sweeps * 1e6}
+    return out
+
+
 def run_reference(args) -> None:
     rank, ws, local, dist = _dist()
     if rank != 0:
@@ -464,10 +502,12 @@ def run_ours(args) -> None:
                "sample": f"{sample} TinyMT half-sweeps of the coupled max/min chains (order {ORDER}) per attempt, "
                          f"2 attempts, {threads} host threads"}
     s.close()
-    batched = serving = None
+    batched = serving = single = None
     if rank == 0 and not args.no_batch:
         batched = batched_leg(rt)
         serving = serving_leg(rt)
+    if rank == 0 and not args.no_single:
+        single = single_instance_leg(rt)
     if rank == 0:
         line = {
             "metric": METRIC, "value": value, "unit": "flip attempts/s", "n_gpus": ws, "steps": args.steps,
@@ -477,7 +517,7 @@ def run_ours(args) -> None:
                        "rng": args.mode, "engine": args.engine, "half_sweeps_per_step": HALF_SWEEPS,
                        "l2": "flushed between timed steps (256 MiB write)", "parallelism": f"replicas{ws}"},
             "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches, "clocks": clocks,
-            "batched_cftp": batched, "served_cftp": serving,
+            "batched_cftp": batched, "served_cftp": serving, "single_instance": single,
         }
         print(json.dumps(line))
     if dist is not None:
@@ -494,6 +534,7 @@ def main() -> None:
     ap.add_argument("--engine", type=int, default=0)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-batch", action="store_true")
+    ap.add_argument("--no-single", action="store_true")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)
