@@ -1,14 +1,18 @@
-// rt_tilings.hpp - C++ drop-in for the reference's domino tiler class.
+// rt_tilings.hpp - C++ drop-in for the reference's tiler classes.
 //
-// Same class name, method names, argument meaning and data types as
-// src/Domino/DominoTiler.h:46-131 of the reference (domain / tiling / heightfunc are
-// std::vector<int>, src/common/common.h:50-52), implemented on the C ABI of
-// librt_tilings.so (rt_tilings.h).  Differences a caller sees:
+// Same class names, method names, argument meaning and data types as the reference's
+// src/Domino/DominoTiler.h:46-131, src/Lozenge/LozengeTiler.h:46-92,
+// src/RectTriangle/RectTriangleTiler.h:32-86 and src/TriangleDimer/TriangleDimerTiler.h:84-216
+// (domain / tiling / heightfunc are std::vector<int>, src/common/common.h:50-52), plus a
+// six-vertex class of the same shape, implemented on the C ABI of librt_tilings.so
+// (rt_tilings.h).  Differences a caller sees:
 //   * the flip rule and the two-periodic weights, compile-time choices in the reference
 //     (which kernel file is built, #define a / b), are constructor arguments;
 //   * LoadTinyMT takes the TinyMTDC parameter file the reference's OpenCL path reads; when
 //     it is not called, every generator uses the TinyMT32 jump parameters;
-//   * failures throw rt::Error instead of printing and calling exit().
+//   * failures throw rt::Error instead of printing and calling exit();
+//   * the OpenCL constructors (context, queue, devices, kernel source) are replaced by
+//     default construction; LoadTinyMT / LoadMTGP are accepted where the reference has them.
 // Header-only; link with -lrt_tilings.
 #ifndef RT_TILINGS_HPP_
 #define RT_TILINGS_HPP_
@@ -16,6 +20,8 @@
 #include <cmath>
 #include <cstdint>
 #include <fstream>
+#include <algorithm>
+#include <utility>
 #include <stdexcept>
 #include <string>
 #include <vector>
@@ -167,6 +173,219 @@ class DominoTiler {
  private:
   rt_walk_opts opts_;
   std::vector<uint32_t> params_;
+};
+
+
+// Shared by the three-colour models: TinyMT (the reference's OpenCL path, default
+// parameters) or fast mode.
+inline rt_walk_opts model_opts(int rng_mode, uint32_t fast_stream) {
+  rt_walk_opts o;
+  rt_walk_opts_default(&o);
+  o.rng_mode = rng_mode;
+  o.fast_stream = fast_stream;
+  return o;
+}
+
+inline int tri_rows(const domain& d) {
+  int m = (int)std::lround(std::sqrt(d.size() / 2.0));
+  if ((size_t)2 * m * m != d.size()) throw Error(RT_ERR_INVALID_ARGUMENT, "expected an M x 2M triangle array");
+  return m;
+}
+
+// src/Lozenge/LozengeTiler.h:46-92.
+class LozengeTiler {
+ public:
+  explicit LozengeTiler(int rng_mode = RT_RNG_TINYMT, uint32_t fast_stream = 0) : opts_(model_opts(rng_mode, fast_stream)) {}
+  void LoadTinyMT(const std::string&, int) {}
+  void LoadMTGP() {}
+
+  void Walk(tiling& t, int steps, long seed) { check(rt_lozenge_walk(t.data(), side_of(t), steps, seed, &opts_)); }
+
+  tiling CFTP(const tiling& tmax, const tiling& tmin, long driver_seed, long first_steps = 128, int schedule = 0,
+              int max_attempts = 30, rt_cftp_stats* stats = nullptr) {
+    tiling out(tmax.size());
+    check(rt_lozenge_cftp(tmax.data(), tmin.data(), side_of(tmax), driver_seed, first_steps, schedule, max_attempts,
+                          &opts_, out.data(), stats));
+    return out;
+  }
+
+  static domain AlmostHexDomain(int n, int m) {
+    int r = 2 * n + 9;
+    domain d((size_t)2 * r * r);
+    int32_t rows = 0;
+    check(rt_lozenge_almost_hex_domain(n, m, d.data(), (int64_t)d.size(), &rows));
+    d.resize((size_t)2 * rows * rows);
+    return d;
+  }
+  static domain Hexagon(int n) { return AlmostHexDomain(n, 0); }
+
+  static std::vector<int> DomainToVertices(const domain& d) {
+    int m = tri_rows(d);
+    std::vector<int> v((size_t)(m + 1) * (m + 1));
+    check(rt_lozenge_domain_to_vertices(d.data(), m, v.data()));
+    return v;
+  }
+  static tiling MaxTiling(const domain& d) {
+    int m = tri_rows(d);
+    tiling t((size_t)(m + 1) * (m + 1));
+    check(rt_lozenge_max_tiling(d.data(), m, t.data()));
+    return t;
+  }
+  static tiling MinTiling(const domain& d) {
+    int m = tri_rows(d);
+    tiling t((size_t)(m + 1) * (m + 1));
+    check(rt_lozenge_min_tiling(d.data(), m, t.data()));
+    return t;
+  }
+  static heightfunc TilingToHeightfunc(const tiling& t, const domain& d) {
+    heightfunc h(t.size());
+    check(rt_lozenge_tiling_to_heightfunc(t.data(), d.data(), side_of(t), h.data()));
+    return h;
+  }
+  static tiling HeightfuncToTiling(const heightfunc& h, const domain& d) {
+    tiling t(h.size());
+    check(rt_lozenge_heightfunc_to_tiling(h.data(), d.data(), side_of(h), t.data()));
+    return t;
+  }
+  static domain TilingToDomain(const tiling& t) {
+    int n = side_of(t);
+    domain d((size_t)2 * (n - 1) * (n - 1));
+    check(rt_lozenge_tiling_to_domain(t.data(), n, d.data()));
+    return d;
+  }
+
+  rt_walk_opts& options() { return opts_; }
+
+ private:
+  rt_walk_opts opts_;
+};
+
+// src/RectTriangle/RectTriangleTiler.h:32-86.  The nine weights {wt1, wt2, wt3, wm1, wm2, wm3,
+// wr1, wr2, wr3} are #defines in the reference's kernel (all 1); here a constructor argument.
+class RectTriangleTiler {
+ public:
+  explicit RectTriangleTiler(int rng_mode = RT_RNG_TINYMT, uint32_t fast_stream = 0,
+                             std::vector<double> weights = std::vector<double>(9, 1.0))
+      : opts_(model_opts(rng_mode, fast_stream)), w_(std::move(weights)) {
+    if (w_.size() != 9) throw Error(RT_ERR_INVALID_ARGUMENT, "nine weights");
+  }
+  void LoadTinyMT(const std::string&, int) {}
+  void LoadMTGP() {}
+
+  void Walk(tiling& t, int steps, long seed) {
+    check(rt_recttri_walk(t.data(), side_of(t), steps, seed, w_.data(), &opts_));
+  }
+
+  static tiling maxHex(int n) { return hex(n, 1); }
+  static tiling minHex(int n) { return hex(n, 0); }
+  static tiling LozengeToRectTriangle(const tiling& tL, const domain& dL) {
+    tiling t(tL.size());
+    check(rt_recttri_from_lozenge(tL.data(), side_of(tL), dL.data(), tri_rows(dL), t.data()));
+    return t;
+  }
+
+ private:
+  static tiling hex(int n, int top) {
+    int s = 2 * n + 9;
+    tiling t((size_t)s * s);
+    int32_t side = 0;
+    check(rt_recttri_hex_tiling(n, top, t.data(), (int64_t)t.size(), &side));
+    t.resize((size_t)side * side);
+    return t;
+  }
+  rt_walk_opts opts_;
+  std::vector<double> w_;
+};
+
+// src/TriangleDimer/TriangleDimerTiler.h:84-216 (bibone tilings).
+class TriangleDimerTiler {
+ public:
+  explicit TriangleDimerTiler(int rng_mode = RT_RNG_TINYMT, uint32_t fast_stream = 0)
+      : opts_(model_opts(rng_mode, fast_stream)) {}
+  void LoadTinyMT(const std::string&, int) {}
+  void LoadMTGP() {}
+
+  void Walk(tiling& t, int steps, long seed, rt_cftp_stats* stats = nullptr) {
+    check(rt_td_walk(t.data(), side_of(t), steps, seed, &opts_, stats));
+  }
+
+  static tiling IceCreamCone(int n, int m) {
+    int s = 2 * (n + 4);
+    tiling t((size_t)s * s);
+    int32_t side = 0;
+    check(rt_td_icecream_cone(n, m, t.data(), (int64_t)t.size(), &side));
+    return t;
+  }
+  // No counterpart in the reference: the rows x cols rhombus from the brick covering.
+  static tiling RhombusBrick(int rows, int cols) {
+    int s = 2 * (std::max(rows, cols) + 6);
+    tiling t((size_t)s * s);
+    int32_t side = 0;
+    check(rt_td_rhombus_brick(rows, cols, t.data(), (int64_t)t.size(), &side));
+    return t;
+  }
+  static std::vector<int> TilingToVertices(const tiling& t) {
+    int n = side_of(t);
+    std::vector<int> v((size_t)(n / 2 + 1) * (n / 2 + 1));
+    check(rt_td_vertices(t.data(), n, v.data()));
+    return v;
+  }
+  static domain TilingToDomain(const tiling& t) {
+    int n = side_of(t);
+    domain d((size_t)(n / 2) * n);
+    check(rt_td_domain(t.data(), n, d.data()));
+    return d;
+  }
+  static std::vector<int> DimerIndicator(const tiling& t, int c) {
+    int n = side_of(t);
+    std::vector<int> v((size_t)(n / 2) * (n / 2));
+    check(rt_td_dimer_indicator(t.data(), n, c, v.data()));
+    return v;
+  }
+
+ private:
+  rt_walk_opts opts_;
+};
+
+// Six-vertex model (no counterpart in the reference); the state is the height function.
+class SixVertexTiler {
+ public:
+  explicit SixVertexTiler(double a = 1.0, double b = 1.0, double c = 1.0, uint32_t fast_stream = 0)
+      : opts_(model_opts(RT_RNG_FAST, fast_stream)), abc_{a, b, c} {}
+
+  void Walk(heightfunc& h, long sweeps, long seed, rt_cftp_stats* stats = nullptr) {
+    check(rt_sv_walk(h.data(), side_of(h) - 1, sweeps, seed, abc_, &opts_, stats));
+  }
+  heightfunc CFTP(const heightfunc& hmax, const heightfunc& hmin, long seed, long first_sweeps = 16,
+                  int max_attempts = 20, rt_cftp_stats* stats = nullptr) {
+    heightfunc out(hmax.size());
+    check(rt_sv_cftp(hmax.data(), hmin.data(), side_of(hmax) - 1, seed, first_sweeps, max_attempts, abc_, &opts_,
+                     out.data(), stats));
+    return out;
+  }
+  static heightfunc MaxHeight(int n) { return dwbc(n, 1); }
+  static heightfunc MinHeight(int n) { return dwbc(n, 0); }
+  static std::vector<int> HeightToASM(const heightfunc& h) {
+    int n = side_of(h) - 1;
+    std::vector<int> a((size_t)n * n);
+    check(rt_sv_height_to_asm(h.data(), n, a.data()));
+    return a;
+  }
+  static heightfunc ASMToHeight(const std::vector<int>& a) {
+    int n = side_of(a);
+    heightfunc h((size_t)(n + 1) * (n + 1));
+    check(rt_sv_asm_to_height(a.data(), n, h.data()));
+    return h;
+  }
+
+ private:
+  static heightfunc dwbc(int n, int top) {
+    heightfunc h((size_t)(n + 1) * (n + 1));
+    check(rt_sv_dwbc_height(n, top, h.data()));
+    return h;
+  }
+  rt_walk_opts opts_;
+  double abc_[3];
 };
 
 }  // namespace rt

@@ -20,5 +20,19 @@ int main() {
   } catch (const rt::Error& e) {
     std::printf("untileable status %d\n", e.status);
   }
+  // the other models' host utilities, as the reference's MinimalLozenge / RectTriangle /
+  // TriangleDimer examples call them
+  rt::domain hexd = rt::LozengeTiler::AlmostHexDomain(4, 0);
+  rt::tiling lmax = rt::LozengeTiler::MaxTiling(hexd);
+  rt::tiling rmax = rt::RectTriangleTiler::maxHex(5);
+  rt::tiling cone = rt::TriangleDimerTiler::IceCreamCone(6, 0);
+  rt::domain coned = rt::TriangleDimerTiler::TilingToDomain(cone);
+  rt::heightfunc smin = rt::SixVertexTiler::MinHeight(5);
+  std::vector<int> asmx = rt::SixVertexTiler::HeightToASM(smin);
+  long cone_cells = 0, asm_sum = 0;
+  for (int v : coned) cone_cells += v;
+  for (int v : asmx) asm_sum += v;
+  std::printf("lozenge %d recttri %d cone %d cells %ld asm %ld\n", rt::side_of(lmax), rt::side_of(rmax),
+              rt::side_of(cone), cone_cells, asm_sum);
   return 0;
 }

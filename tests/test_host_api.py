@@ -156,3 +156,9 @@ def test_cpp_dropin_header_compiles_and_runs(rt, tmp_path):
     n = int(np.sqrt(tmax.size))
     assert f"side {n} max {int(tmax.sum())} min {int(tmin.sum())} roundtrip 1" in out
     assert f"untileable status {rt.RT_ERR_NOT_TILEABLE}" in out
+    lmax = rt.LozengeTiler.MaxTiling(rt.LozengeTiler.AlmostHexDomain(4, 0))
+    rmax = rt.RectTriangleTiler.maxHex(5)
+    cone = rt.TriangleDimerTiler.IceCreamCone(6, 0)
+    cells = int(rt.TriangleDimerTiler.TilingToDomain(cone).sum())
+    assert (f"lozenge {int(np.sqrt(lmax.size))} recttri {int(np.sqrt(rmax.size))} cone {int(np.sqrt(cone.size))} "
+            f"cells {cells} asm 5") in out
