@@ -20,6 +20,7 @@
 #include <string>
 #include <vector>
 
+#include "pdl.cuh"
 #include "rng.cuh"
 #include "rt_internal.h"
 
@@ -92,6 +93,7 @@ __global__ void k_td_seed(uint4* st, int64_t count, uint32_t seed) {
 // TinyMT mode: every generator draws (as every work item of the reference's rotate kernel
 // does); sites of the class flip when rd < 0.5, i.e. the 23-bit draw is below 2^22.
 __global__ void k_td_step_tmt(uint8_t* D, uint4* tmt, int M, TdStep s) {
+  pdl_begin();
   const int b = blockIdx.x * blockDim.x + threadIdx.x, a = blockIdx.y;
   if (b >= M) return;
   const size_t k = (size_t)a * M + b;
@@ -103,6 +105,7 @@ __global__ void k_td_step_tmt(uint8_t* D, uint4* tmt, int M, TdStep s) {
 
 // Fast mode: a thread owns columns 4q .. 4q+3 of row a and one Philox block of draws.
 __global__ void k_td_step_fast(uint8_t* D, int M, TdStep s, uint64_t seed, uint32_t stream, int64_t h) {
+  pdl_begin();
   const int q = blockIdx.x * blockDim.x + threadIdx.x, a = blockIdx.y;
   if (4 * q >= M) return;
   bool any = false;
@@ -374,9 +377,9 @@ RT_API rt_status rt_td_walk(int32_t* tiling, int32_t n_side, int64_t steps, int6
   const dim3 g_all((M + 127) / 128, M), g_quad(((M + 3) / 4 + 127) / 128, M);
   for (int64_t h = 0; h < steps; ++h) {
     if (o.rng_mode == RT_RNG_TINYMT)
-      k_td_step_tmt<<<g_all, 128, 0, st>>>(dD, tmt, M, sched[(size_t)h]);
+      pdl_launch(k_td_step_tmt, g_all, dim3(128), st, dD, tmt, M, sched[(size_t)h]);
     else
-      k_td_step_fast<<<g_quad, 128, 0, st>>>(dD, M, sched[(size_t)h], (uint64_t)seed, o.fast_stream, h);
+      pdl_launch(k_td_step_fast, g_quad, dim3(128), st, dD, M, sched[(size_t)h], (uint64_t)seed, o.fast_stream, h);
   }
   cudaEventRecord(e1, st);
   cudaError_t le = cudaGetLastError();

@@ -18,6 +18,7 @@
 
 #include "domino_rules.h"
 #include "domino_sweep.h"
+#include "pdl.cuh"
 #include "rng.cuh"
 #include "rt_internal.h"
 
@@ -60,6 +61,7 @@ __global__ void k_tmt_seed(uint4* st, const uint4* params, int64_t count, uint32
 // in every chain.
 template <bool kParams>
 __global__ void k_rotate_tmt(DmView v, int t, DmRule rule) {
+  pdl_begin();
   const int m = blockIdx.x * blockDim.x + threadIdx.x + 1;
   const int i = blockIdx.y * blockDim.y + threadIdx.y + 1;
   if (m > v.cols || i > v.rows) return;
@@ -85,6 +87,7 @@ __global__ void k_rotate_tmt(DmView v, int t, DmRule rule) {
 
 // Fast mode: one Philox call per column quad of a row gives the draws of its four sites.
 __global__ void k_rotate_fast(DmView v, int t, DmRule rule, uint64_t seed, uint32_t stream, int64_t h) {
+  pdl_begin();
   const int q = blockIdx.x * blockDim.x + threadIdx.x;
   const int i = blockIdx.y * blockDim.y + threadIdx.y + 1;
   if (4 * q > v.cols || i > v.rows) return;
@@ -106,6 +109,7 @@ __global__ void k_rotate_fast(DmView v, int t, DmRule rule, uint64_t seed, uint3
 }
 
 __global__ void k_update(DmView v, int t) {
+  pdl_begin();
   const int m = blockIdx.x * blockDim.x + threadIdx.x + 1;
   const int i = blockIdx.y * blockDim.y + threadIdx.y + 1;
   if (m > v.cols || i > v.rows) return;
@@ -321,9 +325,9 @@ rt_status DmSampler::run(const uint8_t* colours, int64_t steps) {
   const dim3 blk(128, 2), grd((v.cols + 127) / 128, (v.rows + 1) / 2);
   for (int64_t s = 0; s < steps; ++s) {
     const int t = colours[s] ? 1 : 0;
-    if (tmt_params) k_rotate_tmt<true><<<grd, blk, 0, stream>>>(v, t, rule);
-    else k_rotate_tmt<false><<<grd, blk, 0, stream>>>(v, t, rule);
-    k_update<<<grd, blk, 0, stream>>>(v, t);
+    if (tmt_params) pdl_launch(k_rotate_tmt<true>, grd, blk, stream, v, t, rule);
+    else pdl_launch(k_rotate_tmt<false>, grd, blk, stream, v, t, rule);
+    pdl_launch(k_update, grd, blk, stream, v, t);
     launches += 2;
     half_sweeps[t]++;
   }
@@ -351,8 +355,8 @@ rt_status DmSampler::run_fast(uint64_t seed_value, int64_t h0, int64_t steps) {
   for (int64_t s = 0; s < steps; ++s) {
     const int64_t h = h0 + s;
     const int t = (h & 1) ? 0 : 1;
-    k_rotate_fast<<<grd_r, blk, 0, stream>>>(v, t, rule, seed_value, opts.fast_stream, h);
-    k_update<<<grd_u, blk_u, 0, stream>>>(v, t);
+    pdl_launch(k_rotate_fast, grd_r, blk, stream, v, t, rule, seed_value, opts.fast_stream, h);
+    pdl_launch(k_update, grd_u, blk_u, stream, v, t);
     launches += 2;
     half_sweeps[t]++;
   }

@@ -17,6 +17,7 @@
 #include <string>
 #include <vector>
 
+#include "pdl.cuh"
 #include "rng.cuh"
 #include "rt_internal.h"
 
@@ -56,6 +57,7 @@ __global__ void k_lz_seed(uint4* st, int64_t count, uint32_t seed) {
 }
 
 __global__ void k_lz_rotate_tmt(LzView v, int r, LzRule rule) {
+  pdl_begin();
   const int j = blockIdx.x * blockDim.x + threadIdx.x, i = blockIdx.y;
   if (j >= v.M) return;
   const int64_t k = (int64_t)i * v.M + j;
@@ -71,6 +73,7 @@ __global__ void k_lz_rotate_tmt(LzView v, int r, LzRule rule) {
 }
 
 __global__ void k_lz_rotate_fast(LzView v, int r, LzRule rule, uint64_t seed, uint32_t stream, int64_t h) {
+  pdl_begin();
   const int q = blockIdx.x * blockDim.x + threadIdx.x, i = blockIdx.y;
   if (4 * q >= v.M) return;
   const uint4 d = fast_quad(seed, stream, h, (uint32_t)i, (uint32_t)q);
@@ -91,6 +94,7 @@ __global__ void k_lz_rotate_fast(LzView v, int r, LzRule rule, uint64_t seed, ui
 // lozengekernel.cl:107-125: colour (r+1) mod 3 gets bits 2, 4, 32 and colour (r+2) mod 3
 // bits 1, 8, 16 from the rotated colour's neighbours; the column offsets depend on i mod 3.
 __global__ void k_lz_update(LzView v, int r) {
+  pdl_begin();
   const int j = blockIdx.x * blockDim.x + threadIdx.x + 1, i = blockIdx.y + 1;
   if (j > v.M - 2 || i > v.N - 2) return;
   const int im = i % 3;
@@ -263,8 +267,8 @@ struct LzSampler {
     const dim3 gr((M + 127) / 128, N), gu((M + 127) / 128, N - 2);
     for (int64_t s = 0; s < steps; ++s) {
       const int r = colours[s];
-      k_lz_rotate_tmt<<<gr, 128, 0, stream>>>(v, r, rule);
-      k_lz_update<<<gu, 128, 0, stream>>>(v, r);
+      pdl_launch(k_lz_rotate_tmt, gr, dim3(128), stream, v, r, rule);
+      pdl_launch(k_lz_update, gu, dim3(128), stream, v, r);
       steps_by_colour[r]++;
     }
     return check();
@@ -276,8 +280,8 @@ struct LzSampler {
     for (int64_t s = 0; s < steps; ++s) {
       const int64_t h = h0 + s;
       const int r = (int)(((h % 3) + 3) % 3);
-      k_lz_rotate_fast<<<gr, 128, 0, stream>>>(v, r, rule, seed_value, opts.fast_stream, h);
-      k_lz_update<<<gu, 128, 0, stream>>>(v, r);
+      pdl_launch(k_lz_rotate_fast, gr, dim3(128), stream, v, r, rule, seed_value, opts.fast_stream, h);
+      pdl_launch(k_lz_update, gu, dim3(128), stream, v, r);
       steps_by_colour[r]++;
     }
     return check();

@@ -21,6 +21,7 @@
 #include <string>
 #include <vector>
 
+#include "pdl.cuh"
 #include "rng.cuh"
 #include "rt_internal.h"
 
@@ -84,6 +85,7 @@ __global__ void k_rt_seed(uint4* st, int64_t count, uint32_t seed) {
 }
 
 __global__ void k_rt_flip_tmt(RtView v, int r, RtWeights W) {
+  pdl_begin();
   const int j = blockIdx.x * blockDim.x + threadIdx.x, i = blockIdx.y;
   if (j >= v.M) return;
   const int64_t k = (int64_t)i * v.M + j;
@@ -96,6 +98,7 @@ __global__ void k_rt_flip_tmt(RtView v, int r, RtWeights W) {
 }
 
 __global__ void k_rt_flip_fast(RtView v, int r, RtWeights W, uint64_t seed, uint32_t stream, int64_t h) {
+  pdl_begin();
   const int q = blockIdx.x * blockDim.x + threadIdx.x, i = blockIdx.y;
   if (4 * q >= v.M) return;
   const uint4 d = fast_quad(seed, stream, h, (uint32_t)i, (uint32_t)q);
@@ -113,6 +116,7 @@ __global__ void k_rt_flip_fast(RtView v, int r, RtWeights W, uint64_t seed, uint
 // updateTiles1 / updateTiles2 (recttrianglekernel.cl:120-146): the digits of colour
 // (r+1) mod 3 and (r+2) mod 3 rebuilt from the rotated colour's neighbours.
 __global__ void k_rt_update(RtView v, int r) {
+  pdl_begin();
   const int j = blockIdx.x * blockDim.x + threadIdx.x + 1, i = blockIdx.y + 1;
   if (j > v.M - 2 || i > v.N - 2) return;
   const int32_t* A = v.colour(r);
@@ -292,14 +296,14 @@ RT_API rt_status rt_recttri_walk(int32_t* tiling, int32_t n_side, int64_t steps,
       gen.seed(seed);
       for (int64_t s = 0; s < steps; ++s) {
         const int r = dist(gen);
-        k_rt_flip_tmt<<<gr, 128, 0, stream>>>(v, r, W);
-        k_rt_update<<<gu, 128, 0, stream>>>(v, r);
+        pdl_launch(k_rt_flip_tmt, gr, dim3(128), stream, v, r, W);
+        pdl_launch(k_rt_update, gu, dim3(128), stream, v, r);
       }
     } else {
       for (int64_t s = 0; s < steps; ++s) {
         const int r = (int)(s % 3);
-        k_rt_flip_fast<<<gq, 128, 0, stream>>>(v, r, W, (uint64_t)seed, o.fast_stream, s);
-        k_rt_update<<<gu, 128, 0, stream>>>(v, r);
+        pdl_launch(k_rt_flip_fast, gq, dim3(128), stream, v, r, W, (uint64_t)seed, o.fast_stream, s);
+        pdl_launch(k_rt_update, gu, dim3(128), stream, v, r);
       }
     }
     cudaError_t le = cudaGetLastError();

@@ -26,6 +26,7 @@
 #include <string>
 #include <vector>
 
+#include "pdl.cuh"
 #include "rng.cuh"
 #include "rt_internal.h"
 
@@ -142,6 +143,7 @@ __device__ __forceinline__ uint32_t interior_mask(int w, int k_lo, int k_hi) {
 
 // One sub-sweep of one class over global memory; blockIdx.y is the chain.
 __global__ void __launch_bounds__(128) k_sv_sub(SvLaunch L) {
+  pdl_begin();
   const int g = blockIdx.x * blockDim.x + threadIdx.x;
   if (g >= L.words * L.rows) return;
   const int w = g % L.words, r = L.r_lo + g / L.words;
@@ -424,7 +426,7 @@ SvClusterPlan sv_cluster_plan(const SvGeom& G, int chains) {
 }
 
 // Per-CTA work above which the whole-GPU per-sub-sweep kernels are faster than one cluster.
-constexpr int kSvClusterMaxItems = 1024;
+constexpr int kSvClusterMaxItems = 256;
 
 bool sv_use_cluster(const SvGeom& G, const SvClusterPlan& p, int engine) {
   if (engine == 1 || !p.ok) return false;
@@ -488,7 +490,7 @@ int64_t sv_run(uint32_t* dev, int chains, const SvGeom& G, const std::vector<uin
     fill_launch(L, G, s);
     const int threads = L.words * L.rows;
     if (threads <= 0) continue;
-    k_sv_sub<<<dim3((threads + 127) / 128, chains), 128, 0, st>>>(L);
+    pdl_launch(k_sv_sub, dim3((threads + 127) / 128, chains), dim3(128), st, L);
     ++launches;
   }
   return launches;
