@@ -364,6 +364,13 @@ RT_API void* rt_dm_sampler_stream(rt_dm_sampler* s);
 RT_API int64_t rt_dm_sampler_interior_vertices(rt_dm_sampler* s);
 /* Kernels launched by this sampler since creation. */
 RT_API int64_t rt_dm_sampler_launches(rt_dm_sampler* s);
+/* Device-side statistics: adds the edge-placement indicators of a chain to a caller-owned
+   device array of 2 N^2 uint32 counters on the sampler's stream, no copy to the host.
+   counts[i N + j] counts vertex (i, j)'s bit 2 (a horizontal domino on faces (i, j-1), (i, j));
+   counts[N^2 + i N + j] its bit 8 (a vertical domino on faces (i-1, j), (i, j)).  No
+   counterpart in the reference; rt_domino_edge_indicators is the same on a host tiling. */
+RT_API rt_status rt_dm_sampler_accumulate_edges(rt_dm_sampler* s, int32_t chain, uint32_t* counts_device);
+RT_API rt_status rt_domino_edge_indicators(const int32_t* tiling, int32_t n_side, uint32_t* counts);
 /* The engine the next run will use: out4 = {engine (1 per-half-sweep kernels, 2 resident
    persistent kernel), flip-candidate units held by the persistent kernel, CTAs (bands),
    units per thread}. */

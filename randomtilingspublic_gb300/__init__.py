@@ -117,6 +117,8 @@ _SIGNATURES = {
     "rt_dm_sampler_run": (C.c_int32, [_P, _P, C.c_int64]),
     "rt_dm_sampler_run_fast": (C.c_int32, [_P, C.c_uint64, C.c_int64, C.c_int64]),
     "rt_dm_sampler_diff": (C.c_int32, [_P, C.c_int32, C.c_int32, _P]),
+    "rt_dm_sampler_accumulate_edges": (C.c_int32, [_P, C.c_int32, _P]),
+    "rt_domino_edge_indicators": (C.c_int32, [_P, C.c_int32, _P]),
     "rt_dm_sampler_sync": (C.c_int32, [_P]),
     "rt_dm_sampler_stream": (C.c_void_p, [_P]),
     "rt_dm_sampler_interior_vertices": (C.c_int64, [_P]),
@@ -727,6 +729,11 @@ class DominoSampler:
     def run_fast(self, seed: int, h0: int, steps: int) -> None:
         _check(lib().rt_dm_sampler_run_fast(self.h, seed, h0, steps))
 
+    def accumulate_edges(self, chain: int, counts_device_ptr: int) -> None:
+        """Adds chain's edge-placement indicators to a device array of 2 N^2 uint32 counters
+        (e.g. a torch.int32 tensor's data_ptr()), on the sampler's stream."""
+        _check(lib().rt_dm_sampler_accumulate_edges(self.h, int(chain), C.c_void_p(counts_device_ptr)))
+
     def diff(self, a: int, b: int) -> int:
         n = C.c_int64()
         _check(lib().rt_dm_sampler_diff(self.h, a, b, C.byref(n)))
@@ -847,6 +854,18 @@ def mt19937_colours(seed: int, steps: int, skip: int = 0) -> np.ndarray:
     """Colour stream of the reference's host loop: mt19937(seed)() % 2 per step, after
     ``skip`` draws (DominoTiler.cpp:51,70)."""
     return (mt19937_draws(seed, skip + steps)[skip:] % 2).astype(np.uint8)
+
+
+def edge_indicators(t, counts=None) -> np.ndarray:
+    """Adds a domino tiling's edge-placement indicators to counts (2 x N x N uint32, created
+    when None): [0] horizontal dominoes by the vertex above their middle edge, [1] vertical
+    dominoes by the vertex left of their middle edge."""
+    tt = _i32(t)
+    n = side_of(tt)
+    if counts is None:
+        counts = np.zeros(2 * n * n, np.uint32)
+    _check(lib().rt_domino_edge_indicators(_ptr(tt), n, _ptr(counts)))
+    return counts
 
 
 def mt19937_draws(seed: int, count: int) -> np.ndarray:

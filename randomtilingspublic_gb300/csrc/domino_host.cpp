@@ -334,3 +334,20 @@ RT_API rt_status rt_domino_tiling_to_domain(const int32_t* t, int32_t n_side, in
 }
 
 }  // extern "C"
+
+extern "C" {
+
+// Adds the edge-placement indicators of a tiling to counts ([2][N][N], the layout of
+// rt_dm_sampler_accumulate_edges).
+RT_API rt_status rt_domino_edge_indicators(const int32_t* tiling, int32_t n_side, uint32_t* counts) {
+  rt::clear_error();
+  if (!tiling || !counts || n_side < 1) return rt::fail(RT_ERR_INVALID_ARGUMENT, "edge_indicators: bad arguments");
+  const size_t nn = (size_t)n_side * n_side;
+  for (size_t k = 0; k < nn; ++k) {
+    if (tiling[k] & 2) counts[k] += 1u;
+    if (tiling[k] & 8) counts[nn + k] += 1u;
+  }
+  return RT_OK;
+}
+
+}  // extern "C"

@@ -137,6 +137,20 @@ __global__ void k_merge(DmView v, int ch, int32_t* tiling) {
   tiling[(size_t)i * v.N + j] = v.colour(ch, t)[(size_t)i * v.P + (j >> 1)];
 }
 
+// Edge-placement counters of chain ch, layout [2][N][N]: [0][i][j] counts bit 2 of vertex
+// (i, j) (the lattice edge to (i+1, j) lies inside a domino: a horizontal domino on faces
+// (i, j-1) and (i, j)), [1][i][j] counts bit 8 (the edge to (i, j+1) inside a vertical domino
+// on faces (i-1, j) and (i, j)).  One thread per vertex owns its two counters.
+__global__ void k_acc_edges(DmView v, int ch, uint32_t* counts) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x, i = blockIdx.y;
+  if (j >= v.N) return;
+  const int t = ((i + j) & 1) == 0 ? 1 : 0;
+  const uint8_t e = v.colour(ch, t)[(size_t)i * v.P + (j >> 1)];
+  const size_t k = (size_t)i * v.N + j;
+  if (e & 2) counts[k] += 1u;
+  if (e & 8) counts[(size_t)v.N * v.N + k] += 1u;
+}
+
 // Sites where chains a and b differ: per 4-byte word, XOR then count the non-zero bytes
 // (masks are < 16, so byte b is non-zero iff bit 4 of (b + 15) is set).
 __global__ void k_diff(DmView v, int a, int b, unsigned long long* out) {
@@ -382,6 +396,14 @@ rt_status DmSampler::diff(int a, int b, int64_t* ndiff) {
   return RT_OK;
 }
 
+rt_status DmSampler::accumulate_edges(int ch, uint32_t* counts) {
+  if (ch < 0 || ch >= n_chains || !counts) return fail(RT_ERR_INVALID_ARGUMENT, "accumulate_edges: bad arguments");
+  DmView v = view();
+  k_acc_edges<<<dim3((N + 255) / 256, N), 256, 0, stream>>>(v, ch, counts);
+  launches++;
+  return check_launch();
+}
+
 rt_status DmSampler::sync() {
   RT_CUDA(cudaStreamSynchronize(stream));
   if (persist) return persist->check_error(*this);
@@ -481,6 +503,10 @@ RT_API rt_status rt_dm_sampler_run_fast(rt_dm_sampler* s, uint64_t seed, int64_t
 RT_API rt_status rt_dm_sampler_diff(rt_dm_sampler* s, int32_t a, int32_t b, int64_t* ndiff) {
   RT_SAMPLER(s);
   return s->impl->diff(a, b, ndiff);
+}
+RT_API rt_status rt_dm_sampler_accumulate_edges(rt_dm_sampler* s, int32_t chain, uint32_t* counts_device) {
+  RT_SAMPLER(s);
+  return s->impl->accumulate_edges(chain, counts_device);
 }
 RT_API rt_status rt_dm_sampler_sync(rt_dm_sampler* s) {
   RT_SAMPLER(s);

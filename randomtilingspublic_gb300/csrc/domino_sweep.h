@@ -59,6 +59,7 @@ struct DmSampler {
   rt_status run(const uint8_t* colours, int64_t steps);
   rt_status run_fast(uint64_t seed, int64_t h0, int64_t steps);
   rt_status diff(int a, int b, int64_t* ndiff);
+  rt_status accumulate_edges(int ch, uint32_t* counts);
   rt_status sync();
   // Picks the engine for the next run: true when the persistent kernel will run it.
   rt_status use_persistent(bool* yes);
