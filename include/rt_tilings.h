@@ -143,6 +143,13 @@ RT_API rt_status rt_domino_cftp(const int32_t* tmax, const int32_t* tmin, int32_
    (0,+1):8 (-1,+1):2 (-1,0):1 (0,-1):4 (+1,-1):16 (+1,0):32, set where a lozenge crosses
    the edge; N must be a multiple of 3.  A domain is an M x 2M array of triangles, N = M+1. */
 
+/* Lozenge rules (rt_walk_opts.rule for the rt_lozenge_* sweeps): the reference's uniform
+   rotation (lozengekernel.cl, 0.4 / 0.4), or the q^volume rotation of qlozengekernel.cl with
+   q = rt_walk_opts.weight_a (the reference's #define q 0.99) and its down-move rescaling
+   corrected (identical decisions for q <= 1). */
+#define RT_LOZENGE_UNIFORM 0
+#define RT_LOZENGE_Q 1
+
 /* LozengeTiler::AlmostHexDomain(n, m) (LozengeTiler.cpp:422-467): hexagon of side n with an
    m x m corner removed (m = 0: the regular a = b = c = n hexagon), padded.  *rows = M. */
 RT_API rt_status rt_lozenge_almost_hex_domain(int32_t n, int32_t m, int32_t* out, int64_t cap, int32_t* rows);
@@ -160,7 +167,8 @@ RT_API rt_status rt_lozenge_tiling_to_domain(const int32_t* tiling, int32_t n_si
    colour from default_random_engine(seed) + uniform_int_distribution(0, 2) (TinyMT mode,
    generators seeded with seed itself) or h mod 3 (fast mode), then the rotation 25 <-> 38
    (0.4 / 0.4, lozengekernel.cl:74-105) and the rebuild of the two other colours
-   (lozengekernel.cl:107-125).  opts->rule and the weights are ignored. */
+   (lozengekernel.cl:107-125).  opts->rule selects RT_LOZENGE_UNIFORM or RT_LOZENGE_Q (q in
+   opts->weight_a). */
 RT_API rt_status rt_lozenge_walk(int32_t* tiling, int32_t n_side, int64_t steps, int64_t seed,
                                  const rt_walk_opts* opts);
 /* Coupling from the past from the max and min tilings with the reference's primitives: each
@@ -263,6 +271,15 @@ RT_API rt_status rt_td_dimer_indicator(const int32_t* tiling, int32_t n_side, in
    the chosen class on covered vertices) and the device time. */
 RT_API rt_status rt_td_walk(int32_t* tiling, int32_t n_side, int64_t steps, int64_t seed, const rt_walk_opts* opts,
                             rt_cftp_stats* stats);
+
+/* ---- the reference's text matrix format (src/common/common.cpp:84-178) --------------------
+   rt_save_matrix: rows x cols values, each followed by a space, one line per row
+   (SaveMatrix(v, M, N, file)); rt_save_matrix_square: SaveMatrix(v, file), floor(sqrt(size))
+   rows and columns.  rt_load_matrix: every run of decimal digits is one value (LoadMatrix;
+   like the reference it reads no sign); *count = values found, at most cap written. */
+RT_API rt_status rt_save_matrix(const int32_t* a, int64_t rows, int64_t cols, const char* path);
+RT_API rt_status rt_save_matrix_square(const int32_t* a, int64_t size, const char* path);
+RT_API rt_status rt_load_matrix(const char* path, int32_t* out, int64_t cap, int64_t* count);
 
 /* ---- batched coupling from the past --------------------------------------------------------
    No counterpart in the reference (which runs one instance at a time).  Many independent

@@ -167,10 +167,26 @@ void lmerge(const LChain& c, int* t) {
     for (int j = 0; j < c.N; ++j) t[(size_t)i * c.N + j] = c.X[colour_of(i, j)][(size_t)i * c.M + j / 3];
 }
 
-// lozengekernel.cl:92-96 with rd = u23 * 2^-23 (TinyMT) ; fast mode resolves the same
-// probabilities 0.4 / 0.4 on a 32-bit draw: up iff u < ceil(0.4 * 2^32), down iff
-// ceil(0.4 * 2^32) <= u < ceil(0.8 * 2^32).
+// The rotation rule: 0 = lozengekernel.cl:92-96 (up when rd < 0.4, down when 0.4 <= rd < 0.8);
+// 1 = qlozengekernel.cl:23-29 with q runtime and its down-move rescaling written as the
+// intended (rd - 0.5) / 0.5.  TinyMT: rd = u23 * 2^-23 in the reference's float expressions.
+// Fast mode: rule 0 up iff u < ceil(0.4 * 2^32), down iff ceil(0.4 * 2^32) <= u <
+// ceil(0.8 * 2^32); rule 1 up iff u < 2^31 and u <= q 2^31, down iff u >= 2^31 and
+// u - 2^31 <= 2^31 / q.
+int g_lz_rule = 0;
+double g_lz_q = 1.0;
+
 inline uint8_t lrotate_cl(uint8_t e, float rd) {
+  if (g_lz_rule == 1) {
+    if (rd < .5) {
+      rd = (float)(rd / .5);
+      if (e == 25 && g_lz_q >= rd) return 38;
+    } else {
+      rd = (float)((rd - .5) / .5);
+      if (e == 38 && 1 / g_lz_q >= rd) return 25;
+    }
+    return e;
+  }
   if ((double)rd < .4) {
     if (e == 25) return 38;
   } else if ((double)rd < .8) {
@@ -179,6 +195,10 @@ inline uint8_t lrotate_cl(uint8_t e, float rd) {
   return e;
 }
 inline uint8_t lrotate_fast(uint8_t e, uint32_t u) {
+  if (g_lz_rule == 1) {
+    if (u < 0x80000000u) return (e == 25 && (double)u <= g_lz_q * 2147483648.0) ? 38 : e;
+    return (e == 38 && (double)(u - 0x80000000u) <= 2147483648.0 / g_lz_q) ? 25 : e;
+  }
   const uint64_t c4 = (uint64_t)std::ceil(0.4 * 4294967296.0), c8 = (uint64_t)std::ceil(0.8 * 4294967296.0);
   if (u < c4) return e == 25 ? 38 : e;
   if (u < c8) return e == 38 ? 25 : e;
@@ -261,6 +281,12 @@ void lwalk_fast(std::vector<LChain*>& chains, long h0, long steps, unsigned long
 }  // namespace
 
 extern "C" {
+
+// Selects the rotation rule of the walks and CFTP below (0 uniform, 1 q^volume with q).
+void orc_lz_set_rule(int rule, double q) {
+  g_lz_rule = rule;
+  g_lz_q = q;
+}
 
 int orc_lz_almost_hex_domain(int n, int m, int* out, long cap) {
   // LozengeTiler.cpp:422-467: a 2n x 4n triangle array of the hexagon of side n with an m x 2m

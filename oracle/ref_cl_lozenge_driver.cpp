@@ -1,4 +1,5 @@
-// TEST INFRASTRUCTURE ONLY. Host driver for the reference's src/Lozenge/lozengekernel.cl,
+// TEST INFRASTRUCTURE ONLY. Host driver for the reference's src/Lozenge/lozengekernel.cl (and,
+// built a second time, qlozengekernel.cl),
 // compiled from the reference tree by oracle/Makefile.  The kernels come verbatim from the
 // reference file; this driver states the OpenCL host loop of LozengeTiler::Walk
 // (src/Lozenge/LozengeTiler.cpp:27-159, the #ifndef __NVCC__ branches) as NDRange loops.
@@ -8,17 +9,26 @@
 
 #include "ref_cl_shim.h"
 
+// REF_CELL: the element type the kernel file uses (char in lozengekernel.cl, int in
+// qlozengekernel.cl); REF_LZ_WALK: the exported name.
+#ifndef REF_CELL
+#define REF_CELL char
+#endif
+#ifndef REF_LZ_WALK
+#define REF_LZ_WALK ref_lz_walk
+#endif
+
 namespace refloz {
 #include REF_CL
 }
 
-extern "C" int ref_lz_walk(int* t, int N, long steps, long seed, const uint32_t* params, long nparams) {
+extern "C" int REF_LZ_WALK(int* t, int N, long steps, long seed, const uint32_t* params, long nparams) {
   const int M = N / 3;
-  std::vector<char> R((size_t)N * M, 0), B((size_t)N * M, 0), G((size_t)N * M, 0);
+  std::vector<REF_CELL> R((size_t)N * M, 0), B((size_t)N * M, 0), G((size_t)N * M, 0);
   for (int i = 0; i < N; ++i)
     for (int j = 0; j < N; ++j) {
       int c = ((j - i) % 3 + 3) % 3;
-      (c == 0 ? R : c == 1 ? B : G)[(size_t)i * M + j / 3] = (char)t[(size_t)i * N + j];
+      (c == 0 ? R : c == 1 ? B : G)[(size_t)i * M + j / 3] = (REF_CELL)t[(size_t)i * N + j];
     }
   std::vector<refloz::tinymt32wp_t> st((size_t)N * M);
   for (size_t k = 0; k < st.size(); ++k) {
@@ -36,7 +46,7 @@ extern "C" int ref_lz_walk(int* t, int N, long steps, long seed, const uint32_t*
   std::default_random_engine generator;
   std::uniform_int_distribution<int> distribution(0, 2);
   generator.seed(seed);
-  char* X[3] = {R.data(), B.data(), G.data()};
+  REF_CELL* X[3] = {R.data(), B.data(), G.data()};
   for (long s = 0; s < steps; ++s) {
     int r = distribution(generator);
     refcl::gsize[0] = N; refcl::gsize[1] = M; refcl::gsize[2] = 1; refcl::gid[2] = 0;

@@ -34,6 +34,7 @@ RT_ERR_BUFFER_TOO_SMALL = 7
 RT_ERR_BUSY = 8
 
 RNG_MODES = {"tinymt": 0, "fast": 1}
+RT_LOZENGE_UNIFORM, RT_LOZENGE_Q = 0, 1
 DOMINO_RULES = {"plain": 0, "cftp": 1, "twoperiodic": 2, "cftp_twoperiodic": 3}
 
 
@@ -144,6 +145,9 @@ _SIGNATURES = {
     "rt_recttri_hex_tiling": (C.c_int32, [C.c_int32, C.c_int32, _P, C.c_int64, _P]),
     "rt_recttri_from_lozenge": (C.c_int32, [_P, C.c_int32, _P, C.c_int32, _P]),
     "rt_recttri_walk": (C.c_int32, [_P, C.c_int32, C.c_int64, C.c_int64, _P, _P]),
+    "rt_save_matrix": (C.c_int32, [_P, C.c_int64, C.c_int64, C.c_char_p]),
+    "rt_save_matrix_square": (C.c_int32, [_P, C.c_int64, C.c_char_p]),
+    "rt_load_matrix": (C.c_int32, [C.c_char_p, _P, C.c_int64, _P]),
     "rt_td_icecream_cone": (C.c_int32, [C.c_int32, C.c_int32, _P, C.c_int64, _P]),
     "rt_td_rhombus_brick": (C.c_int32, [C.c_int32, C.c_int32, _P, C.c_int64, _P]),
     "rt_td_dimers": (C.c_int32, [_P, C.c_int32, _P]),
@@ -389,15 +393,23 @@ class LozengeTiler:
     """Lozenge tilings (src/Lozenge/LozengeTiler.h:46-92).  ``rng`` is 'tinymt' (bit-exact
     with the reference's OpenCL path) or 'fast'."""
 
-    def __init__(self, rng: str = "tinymt", fast_stream: int = 0):
+    def __init__(self, rng: str = "tinymt", fast_stream: int = 0, q: float | None = None):
+        """q: None for the reference's uniform rotation (lozengekernel.cl), else the q^volume
+        rotation of qlozengekernel.cl (down-move rescaling corrected)."""
         self.rng = rng
         self.fast_stream = int(fast_stream)
+        self.q = q
 
     def opts(self) -> _WalkOpts:
         o = _WalkOpts()
         lib().rt_walk_opts_default(C.byref(o))
         o.rng_mode = RNG_MODES[self.rng]
         o.fast_stream = self.fast_stream
+        if self.q is not None:
+            o.rule = RT_LOZENGE_Q
+            o.weight_a = float(self.q)
+        else:
+            o.rule = RT_LOZENGE_UNIFORM
         return o
 
     def Walk(self, t, steps: int, seed: int) -> None:
@@ -854,6 +866,25 @@ def mt19937_colours(seed: int, steps: int, skip: int = 0) -> np.ndarray:
     """Colour stream of the reference's host loop: mt19937(seed)() % 2 per step, after
     ``skip`` draws (DominoTiler.cpp:51,70)."""
     return (mt19937_draws(seed, skip + steps)[skip:] % 2).astype(np.uint8)
+
+
+def SaveMatrix(a, path, rows: int | None = None, cols: int | None = None) -> None:
+    """The reference's SaveMatrix (src/common/common.cpp:84-128): without rows/cols the
+    square overload (floor(sqrt(size))^2 values)."""
+    aa = _i32(a)
+    if rows is None:
+        _check(lib().rt_save_matrix_square(_ptr(aa), aa.size, str(path).encode()))
+    else:
+        _check(lib().rt_save_matrix(_ptr(aa), int(rows), int(cols), str(path).encode()))
+
+
+def LoadMatrix(path) -> np.ndarray:
+    """The reference's LoadMatrix (src/common/common.cpp:155-178): every run of digits."""
+    n = C.c_int64()
+    _check(lib().rt_load_matrix(str(path).encode(), None, 0, C.byref(n)))
+    out = np.zeros(n.value, np.int32)
+    _check(lib().rt_load_matrix(str(path).encode(), _ptr(out), out.size, C.byref(n)))
+    return out
 
 
 def edge_indicators(t, counts=None) -> np.ndarray:

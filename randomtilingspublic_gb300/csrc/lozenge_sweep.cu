@@ -10,6 +10,7 @@
 // reference's NDRange numbers them.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 #include <memory>
@@ -133,21 +134,50 @@ __global__ void k_lz_diff(const uint32_t* x, const uint32_t* y, size_t words, un
   if ((threadIdx.x & 31) == 0 && local) atomicAdd(out, local);
 }
 
-// Acceptance intervals of the rotation (lozengekernel.cl:92-96): up when rd < 0.4, down when
-// 0.4 <= rd < 0.8.  TinyMT draws u23 = rd * 2^23 exactly; fast draws resolve the same 0.4 /
-// 0.4 on 32 bits.
-LzRule lz_rule(int rng_mode) {
+// Acceptance intervals of the rotation.  Rule RT_LOZENGE_UNIFORM (lozengekernel.cl:92-96): up
+// when rd < 0.4, down when 0.4 <= rd < 0.8.  Rule RT_LOZENGE_Q (qlozengekernel.cl:23-29, q a
+// runtime argument): up (a cube added) when rd < 0.5 and q >= rd / 0.5, down when rd >= 0.5 and
+// 1 / q >= (rd - 0.5) / 0.5; the reference multiplies by 0.5 in the last expression, which
+// accepts every down move when rd >= 0.5 and breaks the q^volume law for q > 1 (identical
+// decisions for q <= 1).  TinyMT draws u23 = rd * 2^23 exactly; fast draws resolve the same
+// conditions on 32 bits (rd = u * 2^-32).
+template <class F>
+uint32_t count_below(uint32_t lo, uint32_t hi, F accept) {  // largest prefix [lo, x) with accept
+  while (lo < hi) {
+    const uint32_t mid = lo + (hi - lo) / 2;
+    if (accept(mid)) lo = mid + 1;
+    else hi = mid;
+  }
+  return lo;
+}
+
+LzRule lz_rule(int rng_mode, int rule, double q) {
   LzRule r;
+  if (rule == RT_LOZENGE_Q) {
+    if (rng_mode == RT_RNG_TINYMT) {
+      const uint32_t half = 1u << 22;
+      const uint32_t up = count_below(0, half, [&](uint32_t u) {
+        float rd = (float)u * (1.0f / 8388608.0f);
+        rd = (float)(rd / .5);
+        return q >= rd;
+      });
+      const uint32_t dn = count_below(half, 1u << 23, [&](uint32_t u) {
+        float rd = (float)u * (1.0f / 8388608.0f);
+        rd = (float)((rd - .5) / .5);
+        return 1 / q >= rd;
+      });
+      r = {0u, up, half, dn - half};
+    } else {
+      const double h = 2147483648.0;
+      const uint32_t up = (uint32_t)std::min(h, std::floor(q * h) + 1.0);
+      const uint32_t dn = (uint32_t)std::min(h, std::floor(h / q) + 1.0);
+      r = {0u, up, 0x80000000u, dn};
+    }
+    return r;
+  }
   if (rng_mode == RT_RNG_TINYMT) {
     auto below = [](double x) {  // number of u23 with u23 * 2^-23 < x
-      uint32_t lo = 0, hi = 1u << 23;
-      while (lo < hi) {
-        uint32_t mid = lo + (hi - lo) / 2;
-        float rd = (float)mid * (1.0f / 8388608.0f);
-        if ((double)rd < x) lo = mid + 1;
-        else hi = mid;
-      }
-      return lo;
+      return count_below(0, 1u << 23, [&](uint32_t u) { return (double)((float)u * (1.0f / 8388608.0f)) < x; });
     };
     const uint32_t c4 = below(.4), c8 = below(.8);
     r = {0u, c4, c4, c8 - c4};
@@ -191,6 +221,9 @@ struct LzSampler {
     if (o.rng_mode != RT_RNG_TINYMT && o.rng_mode != RT_RNG_FAST) return fail(RT_ERR_INVALID_ARGUMENT, "unknown rng mode");
     if (o.rng_mode == RT_RNG_FAST && o.fast_stream >= 65536u) return fail(RT_ERR_INVALID_ARGUMENT, "fast_stream must be < 65536");
     if (o.tinymt_params) return fail(RT_ERR_INVALID_ARGUMENT, "lozenge sweep: per-generator parameter tables are not supported");
+    if (o.rule != RT_LOZENGE_UNIFORM && o.rule != RT_LOZENGE_Q) return fail(RT_ERR_INVALID_ARGUMENT, "lozenge sweep: unknown rule");
+    if (o.rule == RT_LOZENGE_Q && (!(o.weight_a > 0.0) || !std::isfinite(o.weight_a)))
+      return fail(RT_ERR_INVALID_ARGUMENT, "lozenge sweep: q (weight_a) must be finite and > 0");
     int devs = 0;
     if (cudaGetDeviceCount(&devs) != cudaSuccess || devs == 0) {
       cudaGetLastError();
@@ -202,7 +235,7 @@ struct LzSampler {
     s->P = (s->M + 15) / 16 * 16;
     s->n_chains = s->active = chains;
     s->opts = o;
-    s->rule = lz_rule(o.rng_mode);
+    s->rule = lz_rule(o.rng_mode, o.rule, o.weight_a);
     s->colour_stride = (size_t)s->N * s->P;
     s->chain_stride = 3 * s->colour_stride;
     if (o.cuda_stream) {

@@ -207,8 +207,20 @@ def lozenge(ref: str) -> None:
     cases.append({"name": "lz_cftp_hex3", "kind": "cftp", "N": rows + 1, "tmax": tmax.tolist(), "tmin": tmin.tolist(),
                   "driver_seed": 777, "first_steps": 16, "schedule": 0, "attempts": attempts,
                   "expected": top.tolist()})
+    # the q-weighted kernel (qlozengekernel.cl, q = 0.99 as compiled; oracle/_ref/libref_qlozenge.so)
+    qlz = C.CDLL(str(ROOT / "oracle/_ref/libref_qlozenge.so"))
+    qlz.ref_qlz_walk.argtypes = [C.c_void_p, C.c_int, C.c_long, C.c_long, C.c_void_p, C.c_long]
+    qcases = []
+    for n, m, steps, seed in [(2, 0, 200, 1), (5, 1, 500, 77), (10, 2, 300, -5)]:
+        d, rows = domain(n, m)
+        start = extremal(d, rows, "max")
+        t = start.copy()
+        qlz.ref_qlz_walk(P(t), rows + 1, steps, seed, None, 0)
+        qcases.append({"name": f"qlz_walk_hex{n}_{m}", "kind": "walk", "N": rows + 1, "q": 0.99, "start": start.tolist(),
+                       "steps": steps, "seed": seed, "expected": t.tolist()})
     (HERE / "lozenge_ref_cases.json").write_text(json.dumps({"generator": "tests/golden/make_golden.py", "cases": cases,
-                                                             "host_cases": host}, separators=(",", ":")))
+                                                             "host_cases": host, "q_cases": qcases},
+                                                            separators=(",", ":")))
     print(f"wrote {len(cases)} lozenge sweep cases, {len(host)} lozenge host cases")
     recttri(ref)
 
@@ -242,6 +254,9 @@ def recttri(ref: str) -> None:
     fixtures = Path(ref) / "Examples/ExampleOuts/RectTriangle"
     for name, which in (("MaxTiling", 1), ("MinTiling", 0), ("SlopeTiling", 2)):
         assert np.array_equal(_read_matrix(fixtures / f"{name}.txt"), hexagon(5, which)[0]), name
+    # the exact bytes SaveMatrix wrote for maxHex(5), the format pin of rt_save_matrix
+    format_pin = {"file": "Examples/ExampleOuts/RectTriangle/MaxTiling.txt", "n": 5,
+                  "text": (fixtures / "MaxTiling.txt").read_text()}
     host, cases = [], []
     for n in (2, 3, 5, 8, 13):
         (tmax, side), (tmin, _) = hexagon(n, 1), hexagon(n, 0)
@@ -273,7 +288,7 @@ def recttri(ref: str) -> None:
     (HERE / "recttri_ref_cases.json").write_text(json.dumps(
         {"generator": "tests/golden/make_golden.py", "fixtures_pinned": ["MaxTiling.txt", "MinTiling.txt",
                                                                          "SlopeTiling.txt"],
-         "host_cases": host, "cases": cases, "from_lozenge": conv}, separators=(",", ":")))
+         "host_cases": host, "cases": cases, "from_lozenge": conv, "format_pin": format_pin}, separators=(",", ":")))
     print(f"wrote {len(cases)} rectangle-triangle sweep cases, {len(host)} host cases, {len(conv)} conversions")
     bibone(ref)
 

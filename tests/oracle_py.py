@@ -210,6 +210,7 @@ _LZ_SIG = {
     "orc_lz_walk_tinymt": (C.c_int, [_P, C.c_int, _L, _L, _P, _L]),
     "orc_lz_walk_fast": (C.c_int, [_P, C.c_int, _L, _L, C.c_ulong, C.c_uint]),
     "orc_lz_cftp": (C.c_int, [_P, _P, C.c_int, _L, _L, C.c_int, C.c_int, C.c_int, C.c_uint, _P, _P]),
+    "orc_lz_set_rule": (None, [C.c_int, C.c_double]),
 }
 
 
@@ -381,3 +382,17 @@ def td_walk_tinymt(t: np.ndarray, n_side: int, steps: int, seed: int) -> None:
 
 def td_walk_fast(t: np.ndarray, n_side: int, h0: int, steps: int, seed: int, stream: int = 0) -> None:
     assert td_lib().orc_td_walk_fast(_p(t), n_side, h0, steps, seed, stream) == 0
+
+
+class lz_rule:
+    """Context manager selecting the oracle's lozenge rotation rule (q = None: uniform)."""
+
+    def __init__(self, q=None):
+        self.q = q
+
+    def __enter__(self):
+        lz_lib().orc_lz_set_rule(0 if self.q is None else 1, 1.0 if self.q is None else float(self.q))
+        return self
+
+    def __exit__(self, *exc):
+        lz_lib().orc_lz_set_rule(0, 1.0)

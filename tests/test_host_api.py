@@ -162,3 +162,24 @@ def test_cpp_dropin_header_compiles_and_runs(rt, tmp_path):
     cells = int(rt.TriangleDimerTiler.TilingToDomain(cone).sum())
     assert (f"lozenge {int(np.sqrt(lmax.size))} recttri {int(np.sqrt(rmax.size))} cone {int(np.sqrt(cone.size))} "
             f"cells {cells} asm 5") in out
+
+
+def test_matrix_text_format_matches_the_reference_bytes(rt, tmp_path):
+    """rt_save_matrix writes what the reference's SaveMatrix wrote for maxHex(5) (the committed
+    Examples/ExampleOuts/RectTriangle/MaxTiling.txt, kept in tests/golden), and
+    rt_load_matrix reads it back."""
+    import json
+
+    pin = json.loads((ROOT / "tests/golden/recttri_ref_cases.json").read_text())["format_pin"]
+    t = rt.RectTriangleTiler.maxHex(pin["n"])
+    path = tmp_path / "max.txt"
+    rt.SaveMatrix(t, path)
+    assert path.read_text() == pin["text"]
+    assert np.array_equal(rt.LoadMatrix(path), t)
+    # rows x cols overload and the square overload's truncation to floor(sqrt(size))^2
+    rt.SaveMatrix(np.arange(6), tmp_path / "r.txt", rows=2, cols=3)
+    assert (tmp_path / "r.txt").read_text() == "0 1 2 \n3 4 5 \n"
+    rt.SaveMatrix(np.arange(10), tmp_path / "s.txt")
+    assert (tmp_path / "s.txt").read_text() == "0 1 2 \n3 4 5 \n6 7 8 \n"
+    (tmp_path / "neg.txt").write_text("-3 12\n7")
+    assert rt.LoadMatrix(tmp_path / "neg.txt").tolist() == [3, 12, 7]  # no sign, as the reference
