@@ -449,41 +449,9 @@ void* kernel_for(int K, int nch) {
 // Host: partition and launch
 // ---------------------------------------------------------------------------------------
 
-bool dm_tiling_consistent(const int32_t* t, int N) {
-  for (int i = 0; i < N; ++i)
-    for (int j = 0; j < N; ++j) {
-      const int32_t v = t[(size_t)i * N + j];
-      if (i + 1 < N && ((v >> 1) & 1) != (t[(size_t)(i + 1) * N + j] & 1)) return false;
-      if (j + 1 < N && ((v >> 3) & 1) != ((t[(size_t)i * N + j + 1] >> 2) & 1)) return false;
-      if ((i == 0 && (v & 1)) || (i == N - 1 && (v & 2)) || (j == 0 && (v & 4)) || (j == N - 1 && (v & 8)))
-        return false;
-    }
-  return true;
-}
-
-void dm_mark_candidates(const int32_t* t, int N, std::vector<uint8_t>& cand) {
-  // Interior vertices (four covered squares), then the cells (i, m) holding one.
-  const int M = N - 1, H = N / 2;
-  std::vector<uint8_t> sq((size_t)M * M);
-  for (int i = 0; i < M; ++i)
-    for (int j = 0; j < M; ++j)
-      sq[(size_t)i * M + j] = ((t[(size_t)i * N + j] & 10) != 0) || ((t[(size_t)(i + 1) * N + j + 1] & 5) != 0);
-  if (cand.size() != (size_t)N * H) cand.assign((size_t)N * H, 0);
-  for (int i = 1; i < M; ++i)
-    for (int j = 1; j < M; ++j)
-      if (sq[(size_t)(i - 1) * M + j - 1] && sq[(size_t)(i - 1) * M + j] && sq[(size_t)i * M + j - 1] &&
-          sq[(size_t)i * M + j])
-        cand[(size_t)i * H + j / 2] = 1;
-}
-
 rt_status PersistPlan::build(const std::vector<uint8_t>& cand, int N, int P, int mode, int nch, int nbands_max,
                              size_t smem_limit) {
-  ok = false;
-  why.clear();
   const int H = N / 2, cols = H - 2, rows = N - 2;
-  row_lo.assign(N, 0);
-  row_cnt.assign(N, 0);
-  row_prefix.assign(N + 1, 0);
   std::vector<int> lo(N, -1), hi(N, -1);  // candidate column range per row (cells)
   for (int i = 1; i <= rows; ++i)
     for (int m = 1; m <= cols; ++m)
@@ -491,6 +459,17 @@ rt_status PersistPlan::build(const std::vector<uint8_t>& cand, int N, int P, int
         if (lo[i] < 0) lo[i] = m;
         hi[i] = m;
       }
+  return build_from_rows(lo, hi, N, P, mode, nch, nbands_max, smem_limit);
+}
+
+rt_status PersistPlan::build_from_rows(const std::vector<int>& lo, const std::vector<int>& hi, int N, int P, int mode,
+                                       int nch, int nbands_max, size_t smem_limit) {
+  ok = false;
+  why.clear();
+  const int rows = N - 2;
+  row_lo.assign(N, 0);
+  row_cnt.assign(N, 0);
+  row_prefix.assign(N + 1, 0);
   // Units per row: cells [lo, hi] (TinyMT) or quads [lo/4, hi/4] (fast).
   int64_t total = 0;
   for (int i = 1; i <= rows; ++i) {
@@ -616,7 +595,8 @@ rt_status PersistEngine::prepare(DmSampler& s) {
     plan.why = "device lacks cooperative launch";
     return RT_OK;
   }
-  if (rt_status st = plan.build(s.candidates, s.N, s.P, s.opts.rng_mode, s.active, sms, smem_optin)) return st;
+  if (rt_status st = plan.build_from_rows(s.cand_lo, s.cand_hi, s.N, s.P, s.opts.rng_mode, s.active, sms, smem_optin))
+    return st;
   if (!plan.ok) return RT_OK;
   const bool params = s.tmt_params != nullptr;
   if (s.active == 3) {

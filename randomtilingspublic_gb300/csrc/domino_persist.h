@@ -49,6 +49,9 @@ struct PersistPlan {
   size_t smem_bytes = 0;
   rt_status build(const std::vector<uint8_t>& candidates, int N, int P, int mode, int nch, int nbands_max,
                   size_t smem_limit);
+  // The same from each colour-array row's lowest and highest candidate column (-1: none).
+  rt_status build_from_rows(const std::vector<int>& lo, const std::vector<int>& hi, int N, int P, int mode, int nch,
+                            int nbands_max, size_t smem_limit);
 };
 
 struct PersistEngine {
@@ -82,11 +85,5 @@ size_t dm_xbuf_bytes(int nbands, int nch, int P);
 // exist only with sparse.
 void* dm_persist_kernel_ptr(int mode, int K, bool params, int nch, bool sparse);
 
-// True when every edge bit agrees with the bit of the vertex across it and no edge leaves
-// the array: then rebuilding a colour from the other reproduces it, which the persistent
-// engine relies on outside its windows.
-bool dm_tiling_consistent(const int32_t* t, int N);
-// Marks cells (i, N/2 * i + m) holding an interior vertex of the tiling's domain.
-void dm_mark_candidates(const int32_t* t, int N, std::vector<uint8_t>& cand);
 
 }  // namespace rt

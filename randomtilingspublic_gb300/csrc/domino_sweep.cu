@@ -10,6 +10,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <climits>
 #include <cstring>
 #include <memory>
 #include <random>
@@ -120,6 +121,47 @@ __global__ void k_update(DmView v, int t) {
   }
 }
 
+// Scan of a host-layout tiling in device memory: flags bit 0 a value outside [0, 15], bit 1
+// an edge whose two endpoints disagree (or leaves the array); each colour-array row's
+// lowest/highest flip-candidate column (interior vertices: four covered squares around
+// them, columns 1 .. N/2 - 2); with `interior`, the interior vertices of each colour.
+__global__ void k_scan_tiling(const int32_t* t, int N, int* cand, unsigned long long* scan, int count_interior) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x, i = blockIdx.y, lane = threadIdx.x & 31;
+  unsigned f = 0;
+  int lo = INT_MAX, hi = -1;
+  bool inter = false;
+  if (j < N) {
+    const int32_t v = t[(size_t)i * N + j];
+    if ((uint32_t)v > 15u) f |= 1u;
+    if (i + 1 < N && ((v >> 1) & 1) != (t[(size_t)(i + 1) * N + j] & 1)) f |= 2u;
+    if (j + 1 < N && ((v >> 3) & 1) != ((t[(size_t)i * N + j + 1] >> 2) & 1)) f |= 2u;
+    if ((i == 0 && (v & 1)) || (i == N - 1 && (v & 2)) || (j == 0 && (v & 4)) || (j == N - 1 && (v & 8))) f |= 2u;
+    const int M = N - 1;
+    if (i >= 1 && i <= M - 1 && j >= 1 && j <= M - 1) {
+      auto sq = [&](int a, int b) {
+        return ((t[(size_t)a * N + b] & 10) != 0) || ((t[(size_t)(a + 1) * N + b + 1] & 5) != 0);
+      };
+      inter = sq(i - 1, j - 1) && sq(i - 1, j) && sq(i, j - 1) && sq(i, j);
+      const int m = j >> 1;
+      if (inter && m >= 1 && m <= N / 2 - 2) lo = hi = m;
+    }
+  }
+  f = __reduce_or_sync(0xffffffffu, f);
+  lo = __reduce_min_sync(0xffffffffu, lo);
+  hi = __reduce_max_sync(0xffffffffu, hi);
+  const unsigned black = __ballot_sync(0xffffffffu, inter && ((i + j) & 1) == 0);
+  const unsigned white = __ballot_sync(0xffffffffu, inter && ((i + j) & 1) == 1);
+  if (lane == 0) {
+    if (f) atomicOr(reinterpret_cast<unsigned*>(&scan[0]), f);
+    if (lo != INT_MAX) atomicMin(&cand[i], lo);
+    if (hi >= 0) atomicMax(&cand[N + i], hi);
+    if (count_interior) {
+      if (white) atomicAdd(&scan[1], (unsigned long long)__popc(white));
+      if (black) atomicAdd(&scan[2], (unsigned long long)__popc(black));
+    }
+  }
+}
+
 // Host-layout int32 tiling (N x N) <-> colour arrays of one chain.
 __global__ void k_split(DmView v, int ch, const int32_t* tiling) {
   const int j = blockIdx.x * blockDim.x + threadIdx.x;
@@ -183,6 +225,8 @@ DmSampler::~DmSampler() {
   if (base) cudaFree(base);
   if (scratch) cudaFree(scratch);
   if (counter) cudaFree(counter);
+  if (d_scan) cudaFree(d_scan);
+  if (d_cand) cudaFree(d_cand);
   if (ev0) cudaEventDestroy(ev0);
   if (ev1) cudaEventDestroy(ev1);
   if (own_stream && stream) cudaStreamDestroy(stream);
@@ -239,6 +283,13 @@ rt_status DmSampler::create(int n_side, int n_chains, const rt_walk_opts& o, std
   RT_CUDA(cudaMemsetAsync(s->base, 0, s->chain_stride * n_chains, s->stream));
   RT_CUDA(cudaMalloc(&s->scratch, (size_t)s->N * s->N * sizeof(int32_t)));
   RT_CUDA(cudaMalloc(&s->counter, sizeof(unsigned long long)));
+  RT_CUDA(cudaMalloc(&s->d_scan, 3 * sizeof(unsigned long long)));
+  RT_CUDA(cudaMalloc(&s->d_cand, 2 * (size_t)s->N * sizeof(int)));
+  {
+    std::vector<int> init(2 * (size_t)s->N, -1);
+    std::fill(init.begin(), init.begin() + s->N, INT_MAX);
+    RT_CUDA(cudaMemcpy(s->d_cand, init.data(), init.size() * sizeof(int), cudaMemcpyHostToDevice));
+  }
   const int64_t cells = (int64_t)(s->N - 2) * (s->N / 2 - 2);
   if (o.rng_mode == RT_RNG_TINYMT) {
     RT_CUDA(cudaMalloc(&s->tmt, cells * sizeof(uint4)));
@@ -268,29 +319,42 @@ rt_status DmSampler::check_launch() {
 
 rt_status DmSampler::load(int ch, const int32_t* tiling) {
   if (ch < 0 || ch >= n_chains || !tiling) return fail(RT_ERR_INVALID_ARGUMENT, "load: bad chain or NULL tiling");
-  for (size_t p = 0; p < (size_t)N * N; ++p)
-    if ((uint32_t)tiling[p] > 15u) return fail(RT_ERR_INVALID_ARGUMENT, "tiling values must be edge masks in [0, 15]");
-  consistent = consistent && dm_tiling_consistent(tiling, N);
-  dm_mark_candidates(tiling, N, candidates);
-  plan_dirty = true;
-  if (ch == 0) {
-    // Interior vertices per colour: the flip attempts of one half-sweep.
-    const int M = N - 1;
-    std::vector<uint8_t> sq((size_t)M * M);
-    for (int i = 0; i < M; ++i)
-      for (int j = 0; j < M; ++j)
-        sq[(size_t)i * M + j] = ((tiling[(size_t)i * N + j] & 10) != 0) || ((tiling[(size_t)(i + 1) * N + j + 1] & 5) != 0);
-    interior[0] = interior[1] = 0;
-    for (int i = 1; i < M; ++i)
-      for (int j = 1; j < M; ++j)
-        if (sq[(size_t)(i - 1) * M + j - 1] && sq[(size_t)(i - 1) * M + j] && sq[(size_t)i * M + j - 1] && sq[(size_t)i * M + j])
-          interior[((i + j) & 1) == 0 ? 1 : 0]++;
-  }
+  // The scan runs on the device copy: value range, consistency, flip candidates and (chain
+  // 0) the interior vertices per colour, which count the flip attempts of a half-sweep.
   RT_CUDA(cudaMemcpyAsync(scratch, tiling, (size_t)N * N * sizeof(int32_t), cudaMemcpyHostToDevice, stream));
+  RT_CUDA(cudaMemsetAsync(d_scan, 0, 3 * sizeof(unsigned long long), stream));
+  k_scan_tiling<<<dim3((N + 255) / 256, N), 256, 0, stream>>>(scratch, N, d_cand, d_scan, ch == 0);
+  launches++;
+  unsigned long long h[3] = {0, 0, 0};
+  RT_CUDA(cudaMemcpyAsync(h, d_scan, sizeof h, cudaMemcpyDeviceToHost, stream));
+  RT_CUDA(cudaStreamSynchronize(stream));
+  if (h[0] & 1u) return fail(RT_ERR_INVALID_ARGUMENT, "tiling values must be edge masks in [0, 15]");
+  consistent = consistent && !(h[0] & 2u);
+  if (ch == 0) {
+    interior[0] = (int64_t)h[1];
+    interior[1] = (int64_t)h[2];
+  }
+  plan_dirty = true;
   DmView v = view();
   k_split<<<dim3((N + 255) / 256, N), 256, 0, stream>>>(v, ch, scratch);
   launches++;
   return check_launch();
+}
+
+rt_status DmSampler::fetch_candidates() {
+  std::vector<int> both(2 * (size_t)N);
+  RT_CUDA(cudaMemcpyAsync(both.data(), d_cand, both.size() * sizeof(int), cudaMemcpyDeviceToHost, stream));
+  RT_CUDA(cudaStreamSynchronize(stream));
+  cand_lo.assign(N, -1);
+  cand_hi.assign(N, -1);
+  any_candidate = false;
+  for (int i = 0; i < N; ++i)
+    if (both[i] != INT_MAX) {
+      cand_lo[i] = both[i];
+      cand_hi[i] = both[N + i];
+      any_candidate = true;
+    }
+  return RT_OK;
 }
 
 rt_status DmSampler::store(int ch, int32_t* tiling) {
@@ -413,7 +477,10 @@ rt_status DmSampler::sync() {
 rt_status DmSampler::use_persistent(bool* yes) {
   *yes = false;
   if (opts.engine == 1) return RT_OK;
-  if (!consistent || candidates.empty()) {
+  if (plan_dirty) {
+    if (rt_status st = fetch_candidates()) return st;
+  }
+  if (!consistent || !any_candidate) {
     if (opts.engine == 2) return fail(RT_ERR_INVALID_ARGUMENT, "persistent engine needs consistent loaded tilings");
     return RT_OK;
   }

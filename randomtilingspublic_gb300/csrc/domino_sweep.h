@@ -40,9 +40,14 @@ struct DmSampler {
   int64_t interior[2] = {0, 0};     // interior vertices of colour 0 (white) and 1 (black)
   int64_t half_sweeps[2] = {0, 0};  // half-sweeps run per colour
   int64_t launches = 0;
-  // Persistent engine state: flip-candidate cells over all loaded chains, whether every
-  // loaded tiling is consistent, and the engine (re)planned when either changes.
-  std::vector<uint8_t> candidates;
+  // Persistent engine state: the flip-candidate column range of each colour-array row over
+  // all loaded chains (kept on the device by the load scan, fetched when the engine is
+  // planned), whether every loaded tiling is consistent, and the engine (re)planned when
+  // either changes.
+  int* d_cand = nullptr;                 // [2][N]: lowest (INT_MAX: none) and highest column
+  unsigned long long* d_scan = nullptr;  // flags, interior count of colour 0, of colour 1
+  std::vector<int> cand_lo, cand_hi;     // host copies (-1: no candidate)
+  bool any_candidate = false;
   bool consistent = true;
   bool plan_dirty = true;
   std::unique_ptr<PersistEngine> persist;
@@ -53,6 +58,7 @@ struct DmSampler {
   DmView view() const;
   rt_status check_launch();
   rt_status load(int ch, const int32_t* tiling);
+  rt_status fetch_candidates();
   rt_status store(int ch, int32_t* tiling);
   rt_status copy_chain(int dst, int src);
   rt_status seed(uint32_t s);
