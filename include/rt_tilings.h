@@ -94,6 +94,12 @@ RT_API rt_status rt_domino_domain_to_vertices(const int32_t* domain, int32_t m_s
    "NOT tileable" and returns a height function in that case). */
 RT_API rt_status rt_domino_max_tiling(const int32_t* domain, int32_t m_side, int32_t* out);
 RT_API rt_status rt_domino_min_tiling(const int32_t* domain, int32_t m_side, int32_t* out);
+/* Thurston's extremal tiling on the GPU (no counterpart in the reference): the same tiling
+   and the same errors as rt_domino_max_tiling (top != 0) / rt_domino_min_tiling, with the
+   bulk filled by parallel relaxation to the reference's shortest-path fixed point.  Domains
+   whose boundary is not one connected walk (holes) return RT_ERR_INVALID_ARGUMENT. */
+RT_API rt_status rt_domino_extremal_tiling_device(const int32_t* domain, int32_t m_side, int32_t top, int32_t* out,
+                                                  void* cuda_stream);
 /* DominoTiler::TilingToHeightfunc / HeightfuncToTiling / TilingToDomain
    (DominoTiler.cpp:555-593, 534-553, 595-609).  Heights outside the domain are INT32_MAX. */
 RT_API rt_status rt_domino_tiling_to_heightfunc(const int32_t* tiling, const int32_t* domain, int32_t n_side,

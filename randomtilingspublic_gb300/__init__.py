@@ -102,6 +102,7 @@ _SIGNATURES = {
     "rt_domino_domain_to_vertices": (C.c_int32, [_P, C.c_int32, _P]),
     "rt_domino_max_tiling": (C.c_int32, [_P, C.c_int32, _P]),
     "rt_domino_min_tiling": (C.c_int32, [_P, C.c_int32, _P]),
+    "rt_domino_extremal_tiling_device": (C.c_int32, [_P, C.c_int32, C.c_int32, _P, _P]),
     "rt_domino_tiling_to_heightfunc": (C.c_int32, [_P, _P, C.c_int32, _P]),
     "rt_domino_heightfunc_to_tiling": (C.c_int32, [_P, _P, C.c_int32, _P]),
     "rt_domino_tiling_to_domain": (C.c_int32, [_P, C.c_int32, _P]),
@@ -355,6 +356,15 @@ class DominoTiler:
         m = side_of(dd)
         out = np.zeros((m + 1) ** 2, dtype=np.int32)
         _check(lib().rt_domino_min_tiling(_ptr(dd), m, _ptr(out)))
+        return out
+
+    @staticmethod
+    def ExtremalTilingDevice(d, top: bool) -> np.ndarray:
+        """MaxTiling (top) / MinTiling computed on the GPU (rt_domino_extremal_tiling_device)."""
+        dd = _i32(d)
+        m = side_of(dd)
+        out = np.zeros((m + 1) ** 2, dtype=np.int32)
+        _check(lib().rt_domino_extremal_tiling_device(_ptr(dd), m, 1 if top else 0, _ptr(out), None))
         return out
 
     @staticmethod
