@@ -393,6 +393,18 @@ RT_API int64_t rt_dm_sampler_launches(rt_dm_sampler* s);
    counts[N^2 + i N + j] its bit 8 (a vertical domino on faces (i-1, j), (i, j)).  No
    counterpart in the reference; rt_domino_edge_indicators is the same on a host tiling. */
 RT_API rt_status rt_dm_sampler_accumulate_edges(rt_dm_sampler* s, int32_t chain, uint32_t* counts_device);
+/* Height functions on the device: TilingToHeightfunc (DominoTiler.cpp:555-593) of a chain,
+   for the domain given once (the (N-1)^2 face array the chains tile).  sums_device (int64,
+   N^2, may be NULL) receives += the heights of the vertices that have one; heights_device
+   (int32, N^2, may be NULL) the heights themselves (INT32_MAX where unset, as the
+   reference's infty).  For tilings (not arbitrary masks) the heights equal the host
+   function's. */
+RT_API rt_status rt_dm_sampler_set_domain(rt_dm_sampler* s, const int32_t* domain, int32_t m_side);
+RT_API rt_status rt_dm_sampler_accumulate_heights(rt_dm_sampler* s, int32_t chain, long long* sums_device,
+                                                  int32_t* heights_device);
+/* The same for one tiling in host memory. */
+RT_API rt_status rt_domino_heightfunc_device(const int32_t* tiling, const int32_t* domain, int32_t n_side,
+                                             int32_t* out, void* cuda_stream);
 RT_API rt_status rt_domino_edge_indicators(const int32_t* tiling, int32_t n_side, uint32_t* counts);
 /* The engine the next run will use: out4 = {engine (1 per-half-sweep kernels, 2 resident
    persistent kernel), flip-candidate units held by the persistent kernel, CTAs (bands),

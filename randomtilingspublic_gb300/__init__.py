@@ -120,6 +120,9 @@ _SIGNATURES = {
     "rt_dm_sampler_run_fast": (C.c_int32, [_P, C.c_uint64, C.c_int64, C.c_int64]),
     "rt_dm_sampler_diff": (C.c_int32, [_P, C.c_int32, C.c_int32, _P]),
     "rt_dm_sampler_accumulate_edges": (C.c_int32, [_P, C.c_int32, _P]),
+    "rt_dm_sampler_set_domain": (C.c_int32, [_P, _P, C.c_int32]),
+    "rt_dm_sampler_accumulate_heights": (C.c_int32, [_P, C.c_int32, _P, _P]),
+    "rt_domino_heightfunc_device": (C.c_int32, [_P, _P, C.c_int32, _P, _P]),
     "rt_domino_edge_indicators": (C.c_int32, [_P, C.c_int32, _P]),
     "rt_dm_sampler_sync": (C.c_int32, [_P]),
     "rt_dm_sampler_stream": (C.c_void_p, [_P]),
@@ -356,6 +359,15 @@ class DominoTiler:
         m = side_of(dd)
         out = np.zeros((m + 1) ** 2, dtype=np.int32)
         _check(lib().rt_domino_min_tiling(_ptr(dd), m, _ptr(out)))
+        return out
+
+    @staticmethod
+    def TilingToHeightfuncDevice(t, d) -> np.ndarray:
+        """TilingToHeightfunc computed on the GPU (rt_domino_heightfunc_device)."""
+        tt, dd = _i32(t), _i32(d)
+        n = side_of(tt)
+        out = np.zeros(n * n, dtype=np.int32)
+        _check(lib().rt_domino_heightfunc_device(_ptr(tt), _ptr(dd), n, _ptr(out), None))
         return out
 
     @staticmethod
@@ -750,6 +762,17 @@ class DominoSampler:
 
     def run_fast(self, seed: int, h0: int, steps: int) -> None:
         _check(lib().rt_dm_sampler_run_fast(self.h, seed, h0, steps))
+
+    def set_domain(self, d) -> None:
+        """The (N-1) x (N-1) face array the chains tile (for accumulate_heights)."""
+        self._domain = _i32(d)
+        _check(lib().rt_dm_sampler_set_domain(self.h, _ptr(self._domain), side_of(self._domain)))
+
+    def accumulate_heights(self, chain: int, sums_device_ptr: int = 0, heights_device_ptr: int = 0) -> None:
+        """Adds the chain's height function to int64 device sums (N^2) and/or writes it to an
+        int32 device array, on the sampler's stream."""
+        _check(lib().rt_dm_sampler_accumulate_heights(self.h, int(chain), C.c_void_p(sums_device_ptr or None),
+                                                      C.c_void_p(heights_device_ptr or None)))
 
     def accumulate_edges(self, chain: int, counts_device_ptr: int) -> None:
         """Adds chain's edge-placement indicators to a device array of 2 N^2 uint32 counters

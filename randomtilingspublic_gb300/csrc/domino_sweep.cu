@@ -227,6 +227,8 @@ DmSampler::~DmSampler() {
   if (counter) cudaFree(counter);
   if (d_scan) cudaFree(d_scan);
   if (d_cand) cudaFree(d_cand);
+  for (void* p : {(void*)d_dom, (void*)d_cls, (void*)d_h, (void*)d_hflags})
+    if (p) cudaFree(p);
   if (ev0) cudaEventDestroy(ev0);
   if (ev1) cudaEventDestroy(ev1);
   if (own_stream && stream) cudaStreamDestroy(stream);
@@ -468,6 +470,44 @@ rt_status DmSampler::accumulate_edges(int ch, uint32_t* counts) {
   return check_launch();
 }
 
+rt_status DmSampler::set_domain(const int32_t* domain, int m_side) {
+  if (!domain || m_side != N - 1) return fail(RT_ERR_INVALID_ARGUMENT, "set_domain: the domain must be (N-1) x (N-1)");
+  const int M = m_side;
+  for (int i = 0; i < M; ++i)
+    for (int j = 0; j < M; ++j)
+      if ((i < 1 || j < 1 || i >= M - 1 || j >= M - 1) && domain[(size_t)i * M + j])
+        return fail(RT_ERR_INVALID_ARGUMENT, "domain must have an empty outer ring of squares");
+  hf_start = dm_first_boundary_vertex(domain, M);
+  if (hf_start < 0) return fail(RT_ERR_INVALID_ARGUMENT, "set_domain: empty domain");
+  const size_t NN = (size_t)N * N;
+  if (!d_dom) {
+    RT_CUDA(cudaMalloc(&d_dom, (size_t)M * M * sizeof(int32_t)));
+    RT_CUDA(cudaMalloc(&d_cls, NN * sizeof(int32_t)));
+    RT_CUDA(cudaMalloc(&d_h, NN * sizeof(int32_t)));
+    RT_CUDA(cudaMalloc(&d_hflags, 16 * sizeof(unsigned)));
+  }
+  RT_CUDA(cudaMemcpyAsync(d_dom, domain, (size_t)M * M * sizeof(int32_t), cudaMemcpyHostToDevice, stream));
+  RT_CUDA(cudaMemsetAsync(d_hflags, 0, 16 * sizeof(unsigned), stream));
+  if (rt_status st = dm_classes_device(d_dom, M, d_cls, d_hflags + 8, stream)) return st;
+  RT_CUDA(cudaStreamSynchronize(stream));
+  return RT_OK;
+}
+
+rt_status DmSampler::accumulate_heights(int ch, long long* sums, int32_t* heights) {
+  if (ch < 0 || ch >= n_chains || (!sums && !heights)) return fail(RT_ERR_INVALID_ARGUMENT, "accumulate_heights: bad arguments");
+  if (!d_dom) return fail(RT_ERR_INVALID_ARGUMENT, "accumulate_heights: set the domain first (rt_dm_sampler_set_domain)");
+  DmView v = view();
+  k_merge<<<dim3((N + 255) / 256, N), 256, 0, stream>>>(v, ch, scratch);
+  launches++;
+  if (rt_status st = check_launch()) return st;
+  if (rt_status st = dm_heights_device(scratch, d_cls, d_dom, N, hf_start, d_h, d_hflags, stream)) return st;
+  if (sums) {
+    if (rt_status st = dm_heights_accumulate(d_h, N, sums, stream)) return st;
+  }
+  if (heights) RT_CUDA(cudaMemcpyAsync(heights, d_h, (size_t)N * N * sizeof(int32_t), cudaMemcpyDeviceToDevice, stream));
+  return RT_OK;
+}
+
 rt_status DmSampler::sync() {
   RT_CUDA(cudaStreamSynchronize(stream));
   if (persist) return persist->check_error(*this);
@@ -574,6 +614,15 @@ RT_API rt_status rt_dm_sampler_diff(rt_dm_sampler* s, int32_t a, int32_t b, int6
 RT_API rt_status rt_dm_sampler_accumulate_edges(rt_dm_sampler* s, int32_t chain, uint32_t* counts_device) {
   RT_SAMPLER(s);
   return s->impl->accumulate_edges(chain, counts_device);
+}
+RT_API rt_status rt_dm_sampler_set_domain(rt_dm_sampler* s, const int32_t* domain, int32_t m_side) {
+  RT_SAMPLER(s);
+  return s->impl->set_domain(domain, m_side);
+}
+RT_API rt_status rt_dm_sampler_accumulate_heights(rt_dm_sampler* s, int32_t chain, long long* sums_device,
+                                                  int32_t* heights_device) {
+  RT_SAMPLER(s);
+  return s->impl->accumulate_heights(chain, sums_device, heights_device);
 }
 RT_API rt_status rt_dm_sampler_sync(rt_dm_sampler* s) {
   RT_SAMPLER(s);

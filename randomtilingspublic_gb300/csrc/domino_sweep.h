@@ -24,6 +24,13 @@ struct DmView {
   }
 };
 
+// Device height functions (domino_thurston.cu).
+rt_status dm_heights_device(const int32_t* d_t, const int32_t* d_cls, const int32_t* d_dom, int N, int start,
+                            int32_t* d_h, unsigned* d_flags, cudaStream_t st);
+rt_status dm_heights_accumulate(const int32_t* d_h, int N, long long* sums, cudaStream_t st);
+rt_status dm_classes_device(const int32_t* d_dom, int M, int32_t* d_cls, unsigned* d_count, cudaStream_t st);
+int dm_first_boundary_vertex(const int32_t* domain, int M);
+
 struct DmSampler {
   int N = 0, P = 0, n_chains = 0, active = 0;
   size_t chain_stride = 0, colour_stride = 0;
@@ -59,6 +66,13 @@ struct DmSampler {
   rt_status check_launch();
   rt_status load(int ch, const int32_t* tiling);
   rt_status fetch_candidates();
+  // Device statistics: the domain the height function is taken on, then per-chain heights
+  // added to running sums.
+  rt_status set_domain(const int32_t* domain, int m_side);
+  rt_status accumulate_heights(int ch, long long* sums, int32_t* heights);
+  int32_t *d_dom = nullptr, *d_cls = nullptr, *d_h = nullptr;
+  unsigned* d_hflags = nullptr;
+  int hf_start = -1;
   rt_status store(int ch, int32_t* tiling);
   rt_status copy_chain(int dst, int src);
   rt_status seed(uint32_t s);

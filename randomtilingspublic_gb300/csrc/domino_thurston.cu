@@ -99,6 +99,74 @@ __global__ void __launch_bounds__(kTile * kTile) k_th_relax_tile(ThArgs a, unsig
   if (__syncthreads_or(any) && tx == 0 && ty == 0) *changed = 1u;
 }
 
+// Height function of a tiling (TilingToHeightfunc, DominoTiler.cpp:555-593): from the start
+// vertex (height 0), heights spread across every edge no domino covers (its bit clear at the
+// vertex it leaves) that touches the domain, by +-1 (th_step).  For a tiling the heights do
+// not depend on the path, so each unassigned vertex takes the value from its first assigned
+// neighbour; one tile at a time in shared memory until the tile stops changing.
+__device__ __forceinline__ bool th_touches(const int32_t* dom, int M, int ui, int uj, int nb) {
+  const int ai = ui + c_dirs[nb].fa_i, aj = uj + c_dirs[nb].fa_j, bi = ui + c_dirs[nb].fb_i, bj = uj + c_dirs[nb].fb_j;
+  const bool fa = ai >= 0 && aj >= 0 && ai < M && aj < M && dom[ai * M + aj];
+  const bool fb = bi >= 0 && bj >= 0 && bi < M && bj < M && dom[bi * M + bj];
+  return fa || fb;
+}
+
+__global__ void __launch_bounds__(kTile * kTile) k_hf_tile(const int32_t* t, const int32_t* cls, const int32_t* dom,
+                                                           int32_t* h, int N, unsigned* changed) {
+  pdl_begin();
+  __shared__ int32_t sh[kTile + 2][kTile + 2];
+  __shared__ int8_t st[kTile + 2][kTile + 2];
+  __shared__ int8_t sc[kTile + 2][kTile + 2];
+  const int M = N - 1, tx = threadIdx.x, ty = threadIdx.y;
+  const int j0 = blockIdx.x * kTile - 1, i0 = blockIdx.y * kTile - 1;
+  for (int k = ty * kTile + tx; k < (kTile + 2) * (kTile + 2); k += kTile * kTile) {
+    const int r = k / (kTile + 2), c = k % (kTile + 2), i = i0 + r, j = j0 + c;
+    const bool in = i >= 0 && j >= 0 && i < N && j < N;
+    sh[r][c] = in ? h[i * N + j] : kUnset;
+    st[r][c] = in ? (int8_t)t[i * N + j] : (int8_t)0;
+    sc[r][c] = in ? (int8_t)cls[i * N + j] : (int8_t)0;
+  }
+  __syncthreads();
+  const int r = ty + 1, c = tx + 1, i = i0 + r, j = j0 + c;
+  const bool open = i < N && j < N && sc[r][c] > 0;
+  constexpr int kOpp[4] = {1, 0, 3, 2};
+  bool any = false;
+  for (int round = 0; round < 2 * kTile * kTile; ++round) {
+    int32_t val = kUnset;
+    if (open && sh[r][c] == kUnset) {
+#pragma unroll
+      for (int nbv = 0; nbv < 4; ++nbv) {
+        const int ur = r + c_dirs[nbv].di, uc = c + c_dirs[nbv].dj;
+        if (sc[ur][uc] == 0 || sh[ur][uc] == kUnset) continue;
+        const int nb = kOpp[nbv];  // the step from u back to v
+        if (st[ur][uc] & c_dirs[nb].bit) continue;
+        const int ui = i + c_dirs[nbv].di, uj = j + c_dirs[nbv].dj;
+        if (!th_touches(dom, M, ui, uj, nb)) continue;
+        val = sh[ur][uc] + th_step(ui, uj, nb);
+        break;
+      }
+    }
+    const bool moved = val != kUnset;
+    __syncthreads();
+    if (moved) sh[r][c] = val;
+    any = any || moved;
+    if (!__syncthreads_or(moved)) break;
+  }
+  if (open && any) h[i * N + j] = sh[r][c];
+  if (__syncthreads_or(any) && tx == 0 && ty == 0) *changed = 1u;
+}
+
+__global__ void k_fill_unset(int32_t* h, int64_t nn, int start) {
+  const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (p < nn) h[p] = p == start ? 0 : kUnset;
+}
+
+// sums[p] += h[p] for assigned vertices.
+__global__ void k_hf_accumulate(const int32_t* h, int64_t nn, long long* sums) {
+  const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (p < nn && h[p] != kUnset) sums[p] += h[p];
+}
+
 // Vertex classes of DomainToVertices (DominoTiler.cpp:611-631): 0 outside, 1 interior (four
 // squares of the domain around it), 2 boundary; squares clamped into the array at its rim.
 __global__ void k_th_classes(const int32_t* d, int M, int32_t* cls, unsigned* boundary) {
@@ -157,6 +225,56 @@ __global__ void k_th_tiling(const int32_t* h, const int32_t* d, int N, int32_t* 
 }
 
 }  // namespace
+
+// Device height function of the host-layout tiling d_t (N x N) for the domain whose vertex
+// classes are d_cls, starting at vertex `start` (height 0).  d_h receives the heights
+// (INT32_MAX where unset); d_flags needs 8 words.
+rt_status dm_heights_device(const int32_t* d_t, const int32_t* d_cls, const int32_t* d_dom, int N, int start,
+                            int32_t* d_h, unsigned* d_flags, cudaStream_t st) {
+  const int64_t NN = (int64_t)N * N;
+  // every vertex unset, the start vertex at 0
+  k_fill_unset<<<(unsigned)((NN + 255) / 256), 256, 0, st>>>(d_h, NN, start);
+  constexpr int kBatch = 8;
+  const dim3 tgrid((N + kTile - 1) / kTile, (N + kTile - 1) / kTile), tblock(kTile, kTile);
+  for (int64_t passes = 0;; passes += kBatch) {
+    if (passes > NN + kBatch) return fail(RT_ERR_TIMEOUT, "height function: propagation did not converge");
+    cudaMemsetAsync(d_flags, 0, kBatch * sizeof(unsigned), st);
+    for (int k = 0; k < kBatch; ++k) pdl_launch(k_hf_tile, tgrid, tblock, st, d_t, d_cls, d_dom, d_h, N, d_flags + k);
+    unsigned last = 1;
+    cudaMemcpyAsync(&last, d_flags + kBatch - 1, sizeof last, cudaMemcpyDeviceToHost, st);
+    const cudaError_t e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) return fail(RT_ERR_CUDA, std::string("height function: ") + cudaGetErrorString(e));
+    if (!last) return RT_OK;
+  }
+}
+
+rt_status dm_heights_accumulate(const int32_t* d_h, int N, long long* sums, cudaStream_t st) {
+  const int64_t NN = (int64_t)N * N;
+  k_hf_accumulate<<<(unsigned)((NN + 255) / 256), 256, 0, st>>>(d_h, NN, sums);
+  const cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? RT_OK : fail(RT_ERR_CUDA, std::string("height sums: ") + cudaGetErrorString(e));
+}
+
+rt_status dm_classes_device(const int32_t* d_dom, int M, int32_t* d_cls, unsigned* d_count, cudaStream_t st) {
+  const int N = M + 1;
+  k_th_classes<<<dim3((N + 127) / 128, N), 128, 0, st>>>(d_dom, M, d_cls, d_count);
+  const cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? RT_OK : fail(RT_ERR_CUDA, std::string("vertex classes: ") + cudaGetErrorString(e));
+}
+
+// First boundary vertex in row-major order (the reference's start vertex), or -1.
+int dm_first_boundary_vertex(const int32_t* domain, int M) {
+  const int N = M + 1;
+  for (int p = 0; p < N * N; ++p) {
+    const int i = p / N, j = p % N;
+    const int lo_i = i == 0 ? 0 : i - 1, hi_i = i == M ? M - 1 : i, lo_j = j == 0 ? 0 : j - 1, hi_j = j == M ? M - 1 : j;
+    const bool any = domain[lo_i * M + lo_j] || domain[lo_i * M + hi_j] || domain[hi_i * M + lo_j] || domain[hi_i * M + hi_j];
+    const bool rim = i == 0 || j == 0 || i == M || j == M;
+    const bool all = domain[lo_i * M + lo_j] && domain[lo_i * M + hi_j] && domain[hi_i * M + lo_j] && domain[hi_i * M + hi_j];
+    if (any && (rim || !all)) return p;
+  }
+  return -1;
+}
 
 }  // namespace rt
 
@@ -292,6 +410,51 @@ RT_API rt_status rt_domino_extremal_tiling_device(const int32_t* domain, int32_t
     if (e != cudaSuccess) status = fail(RT_ERR_CUDA, std::string("extremal_tiling_device: ") + cudaGetErrorString(e));
     else if (bad) status = fail(RT_ERR_NOT_TILEABLE, "domain is not tileable (bulk height mismatch)");
     else std::copy(t.begin(), t.end(), out);  // written only on success, as the host version
+  }
+  cleanup();
+  return status;
+}
+
+RT_API rt_status rt_domino_heightfunc_device(const int32_t* tiling, const int32_t* domain, int32_t n_side,
+                                             int32_t* out, void* cuda_stream) {
+  clear_error();
+  if (!tiling || !domain || !out || n_side < 6) return fail(RT_ERR_INVALID_ARGUMENT, "heightfunc_device: bad arguments");
+  const int N = n_side, M = N - 1;
+  for (int i = 0; i < M; ++i)
+    for (int j = 0; j < M; ++j)
+      if ((i < 1 || j < 1 || i >= M - 1 || j >= M - 1) && domain[(size_t)i * M + j])
+        return fail(RT_ERR_INVALID_ARGUMENT, "domain must have an empty outer ring of squares");
+  const int start = dm_first_boundary_vertex(domain, M);
+  if (start < 0) return fail(RT_ERR_INVALID_ARGUMENT, "heightfunc_device: empty domain");
+  int devs = 0;
+  if (cudaGetDeviceCount(&devs) != cudaSuccess || devs == 0) {
+    cudaGetLastError();
+    return fail(RT_ERR_CUDA, "no CUDA device: the device height function has no CPU fallback");
+  }
+  cudaStream_t st = (cudaStream_t)cuda_stream;
+  const size_t NN = (size_t)N * N;
+  int32_t *d_t = nullptr, *d_cls = nullptr, *d_dom = nullptr, *d_h = nullptr;
+  unsigned* d_flags = nullptr;
+  auto cleanup = [&]() {
+    for (void* p : {(void*)d_t, (void*)d_cls, (void*)d_dom, (void*)d_h, (void*)d_flags})
+      if (p) cudaFree(p);
+  };
+  if (cudaMalloc(&d_t, NN * 4) != cudaSuccess || cudaMalloc(&d_cls, NN * 4) != cudaSuccess ||
+      cudaMalloc(&d_dom, (size_t)M * M * 4) != cudaSuccess || cudaMalloc(&d_h, NN * 4) != cudaSuccess ||
+      cudaMalloc(&d_flags, 16 * sizeof(unsigned)) != cudaSuccess) {
+    cudaGetLastError();
+    cleanup();
+    return fail(RT_ERR_OUT_OF_MEMORY, "heightfunc_device: device allocation failed");
+  }
+  cudaMemcpyAsync(d_t, tiling, NN * 4, cudaMemcpyHostToDevice, st);
+  cudaMemcpyAsync(d_dom, domain, (size_t)M * M * 4, cudaMemcpyHostToDevice, st);
+  cudaMemsetAsync(d_flags, 0, 16 * sizeof(unsigned), st);
+  rt_status status = dm_classes_device(d_dom, M, d_cls, d_flags + 8, st);
+  if (status == RT_OK) status = dm_heights_device(d_t, d_cls, d_dom, N, start, d_h, d_flags, st);
+  if (status == RT_OK) {
+    cudaMemcpyAsync(out, d_h, NN * 4, cudaMemcpyDeviceToHost, st);
+    const cudaError_t e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) status = fail(RT_ERR_CUDA, std::string("heightfunc_device: ") + cudaGetErrorString(e));
   }
   cleanup();
   return status;

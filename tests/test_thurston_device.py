@@ -51,3 +51,42 @@ def test_untileable_and_holed_domains_are_refused_before_the_device(rt):
     d[5:7, 5:7] = 0  # a 2 x 2 hole: the boundary is not one walk
     with pytest.raises(rt.RTError):
         D.ExtremalTilingDevice(d.ravel(), True)
+
+
+@pytest.mark.gpu
+def test_device_height_function_equals_the_host_function(rt):
+    D = rt.DominoTiler
+    for d in [D.AztecDiamond(5), D.AztecDiamond(64), D.Rectangle(10, 16)]:
+        tmax = D.MaxTiling(d)
+        n = int(np.sqrt(tmax.size))
+        t = tmax.copy()
+        D(rule="cftp", rng="fast", fast_stream=2).Walk(t, 400, 3)
+        for x in (tmax, D.MinTiling(d), t):
+            assert np.array_equal(D.TilingToHeightfuncDevice(x, d), D.TilingToHeightfunc(x, d))
+
+
+@pytest.mark.gpu
+def test_sampler_height_sums_equal_host_sums(rt):
+    torch = pytest.importorskip("torch")
+    D = rt.DominoTiler
+    d = D.AztecDiamond(48)
+    tmax = D.MaxTiling(d)
+    n = int(np.sqrt(tmax.size))
+    s = rt.DominoSampler(n, 1, rt.DominoTiler(rule="cftp", rng="fast", fast_stream=5))
+    s.load(0, tmax)
+    s.set_domain(d)
+    sums = torch.zeros(n * n, dtype=torch.int64, device="cuda")
+    heights = torch.zeros(n * n, dtype=torch.int32, device="cuda")
+    host = np.zeros(n * n, np.int64)
+    for k in range(12):
+        s.run_fast(31, 40 * k, 40)
+        s.accumulate_heights(0, sums.data_ptr(), heights.data_ptr())
+        t = s.store(0)
+        h = D.TilingToHeightfunc(t, d)
+        s.sync()
+        torch.cuda.synchronize()
+        assert np.array_equal(heights.cpu().numpy(), h)
+        host += np.where(h != np.iinfo(np.int32).max, h, 0)
+    torch.cuda.synchronize()
+    assert np.array_equal(sums.cpu().numpy(), host)
+    s.close()
