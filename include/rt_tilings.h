@@ -192,8 +192,9 @@ RT_API rt_status rt_lozenge_cftp(const int32_t* tmax, const int32_t* tmin, int32
    wr_((d-4) mod 3 + 1) (d = 4-9) or wm_((d-10) mod 3 + 1) (d = 10-15), as the weight table at
    recttrianglekernel.cl:13. */
 
-/* RectTriangleTiler::maxHex (top != 0) / minHex (top == 0) (RectTriangleTiler.cpp:480-600):
-   the extremal tilings of the hexagon of side n >= 2 after the reference's shear and padding.
+/* RectTriangleTiler::maxHex (top = 1) / minHex (top = 0) / slopeHex (top = 2)
+   (RectTriangleTiler.cpp:173-600): start tilings of the hexagon of side n >= 2 after the
+   reference's shear and padding.
    *side receives the side N; out needs N * N entries (cap). */
 RT_API rt_status rt_recttri_hex_tiling(int32_t n, int32_t top, int32_t* out, int64_t cap, int32_t* side);
 /* RectTriangleTiler::LozengeToRectTriangle(tiling&, domain&) (RectTriangleTiler.cpp:602-644):

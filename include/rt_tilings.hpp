@@ -278,6 +278,7 @@ class RectTriangleTiler {
 
   static tiling maxHex(int n) { return hex(n, 1); }
   static tiling minHex(int n) { return hex(n, 0); }
+  static tiling slopeHex(int n) { return hex(n, 2); }
   static tiling LozengeToRectTriangle(const tiling& tL, const domain& dL) {
     tiling t(tL.size());
     check(rt_recttri_from_lozenge(tL.data(), side_of(tL), dL.data(), tri_rows(dL), t.data()));

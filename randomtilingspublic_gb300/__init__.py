@@ -555,6 +555,10 @@ class RectTriangleTiler:
         return RectTriangleTiler._hex(n, 0)
 
     @staticmethod
+    def slopeHex(n: int) -> np.ndarray:
+        return RectTriangleTiler._hex(n, 2)
+
+    @staticmethod
     def LozengeToRectTriangle(t, d) -> np.ndarray:
         tt, dd = _i32(t), _i32(d)
         n = side_of(tt)

@@ -189,6 +189,100 @@ std::vector<int32_t> hex_extremal(int n, bool top) {
   return out;
 }
 
+// slopeHex (RectTriangleTiler.cpp:173-478): a start tiling of the hexagon of side n with the
+// hexagon split into six sloped sectors, each filled with a two-row (or two-column) periodic
+// pattern of rectangles, stitched along the three main lines and the diagonal.  Every vertex
+// (i, j) of the (2n+1)^2 array takes the code of the first region (in this order) that holds
+// it; `alt` picks between a region's two codes.
+std::vector<int32_t> hex_slope(int n) {
+  const int M = 2 * n + 1;
+  const bool ev = n % 2 == 0;
+  std::vector<int32_t> t((size_t)M * M, 0);
+  auto code = [&](int i, int j) -> int32_t {
+    auto pick = [](bool odd, int32_t a, int32_t b) { return odd ? a : b; };
+    const bool io = i % 2 == 1, jo = j % 2 == 1, pa = (i + j) % 2 != n % 2;
+    if (i == n && j == n) return ev ? 0x213312 : 0x122133;
+    if (i == n) {
+      if (j < n - 1) return pick(jo, 0x1be1fc, 0xe81c91);
+      if (j == n - 1) return ev ? 0x122133 : 0xe81c91;
+      if (j > n + 1) return pick(jo, 0xcf1eb1, 0x19c18e);
+      return ev ? 0x331221 : 0x29c38e;  // j == n + 1
+    }
+    if (j == n) {
+      if (i < n - 1) return pick(io, 0xd22afc, 0x7af229);
+      if (i == n - 1) return ev ? 0x122133 : 0x7af229;
+      if (i > n + 1) return pick(io, 0xcfa22d, 0x922fa7);
+      return ev ? 0x331221 : 0x913fa7;  // i == n + 1
+    }
+    if (i == j) {
+      if (i < n - 1) return pick(io, 0x33aebd, 0xbd7833);
+      if (i > n + 1) return pick(io, 0xdbea33, 0x3387db);
+      if (i == n + 1) return ev ? 0x122133 : 0x3387db;
+      return ev ? 0x331221 : 0xbd7812;  // i == n - 1
+    }
+    if (i < n && j < i) {
+      if (i == n - 1 && j < i - 1) return pick(jo, 0x855be8, 0x58881b);
+      if (i < n - 1 && j == i - 1) return pick(jo, 0x8eb558, 0x58388e);
+      if (i == n - 1 && j == i - 1) return ev ? 0x583812 : 0x8ebbe8;
+      return pick(jo, 0x855558, 0x588885);
+    }
+    if (i > n && j > i) {
+      if (i == n + 1 && j > i + 1) return pick(jo, 0x8eb558, 0xb18885);
+      if (i > n + 1 && j == i + 1) return pick(jo, 0x855be8, 0xe88385);
+      if (i == n + 1 && j == i + 1) return ev ? 0x218385 : 0x8ebbe8;
+      return pick(jo, 0x855558, 0x588885);
+    }
+    if (j < n && i < j) {
+      if (j == n - 1 && i < j - 1) return pick(io, 0x47d47a, 0x7477d2);
+      if (j < n - 1 && i == j - 1) return pick(io, 0xa74d74, 0x7473a7);
+      if (j == n - 1 && i == j - 1) return ev ? 0x747312 : 0xa7dd7a;
+      return pick(io, 0x474474, 0x747747);
+    }
+    if (j > n && i > j) {
+      if (j == n + 1 && i > j + 1) return pick(io, 0xa74d74, 0x2d7747);
+      if (j > n + 1 && i == j + 1) return pick(io, 0x47d47a, 0x7a3747);
+      if (j == n + 1 && i == j + 1) return ev ? 0x213747 : 0xa7dd7a;
+      return pick(io, 0x474474, 0x747747);
+    }
+    if (i < n && j > n && i > j - n) {
+      if (i == n - 1 && j > n + 1) return pick(pa, 0x6699cf, 0x996f19);
+      if (i < n - 1 && j == n + 1) return pick(pa, 0xfc9966, 0x296c99);
+      if (i == n - 1 && j == n + 1) return ev ? 0x296319 : 0xfc99cf;
+      return pick(pa, 0x669966, 0x996699);
+    }
+    if (i > n && j < n && i < j + n) {
+      if (i == n + 1 && j < n - 1) return pick(pa, 0xfc9966, 0x91f699);
+      if (i > n + 1 && j == n - 1) return pick(pa, 0x6699cf, 0x99c692);
+      if (i == n + 1 && j == n - 1) return ev ? 0x913692 : 0xfc99cf;
+      return pick(pa, 0x669966, 0x996699);
+    }
+    return 0;
+  };
+  for (int i = 1; i < M - 1; ++i)
+    for (int j = 1; j < M - 1; ++j) t[(size_t)i * M + j] = code(i, j);
+  auto at = [&](int i, int j) -> int32_t& { return t[(size_t)i * M + j]; };
+  // the rim: runs of half-covered vertices along the six sides, then their ends
+  for (int i = 2; i < n - 1; ++i) at(i, 0) = 0x008085, at(0, i) = 0x000747;
+  at(1, 0) = 0x00308e, at(0, 1) = 0x0003a7, at(n - 1, 0) = 0x00801b, at(0, n - 1) = 0x0007d2;
+  for (int i = n + 2; i < M - 2; ++i) at(i, M - 1) = 0x580800, at(M - 1, i) = 0x747000;
+  at(n + 1, M - 1) = 0xb10800, at(M - 1, n + 1) = 0x2d7000, at(M - 2, M - 1) = 0xe80300, at(M - 1, M - 2) = 0x7a3000;
+  for (int i = 2; i < n - 1; ++i) at(i, i + n) = 0x900690, at(i + n, i) = 0x096009;
+  at(1, n + 1) = 0x200c90, at(n + 1, 1) = 0x01f009, at(n - 1, M - 2) = 0x900f10, at(M - 2, n - 1) = 0x09c002;
+  // the six corners (n == 1: the single hexagon of triangles)
+  at(0, 0) = n == 1 ? 0x000012 : 0x000033;
+  at(M - 1, n) = n == 1 ? 0x013000 : 0x022000;
+  at(n, M - 1) = n == 1 ? 0x200300 : 0x100100;
+  at(0, n) = 0x000220, at(n, 0) = 0x001001, at(M - 1, M - 1) = 0x330000;
+  const int M2 = M + 6 + (3 - M % 3) % 3;
+  std::vector<int32_t> out((size_t)M2 * M2, 0);
+  for (int i = 0; i < M; ++i)
+    for (int j = 0; j < M; ++j) {
+      const int j2 = j + n + 3 - i;
+      if (j2 < M2) out[(size_t)(i + 3) * M2 + j2] = t[(size_t)i * M + j];
+    }
+  return out;
+}
+
 RtWeights make_weights(const double* w9) {
   // w9 = {wt1, wt2, wt3, wm1, wm2, wm3, wr1, wr2, wr3}; NULL: all 1 (the reference's values)
   float v[9];
@@ -208,8 +302,8 @@ extern "C" {
 
 RT_API rt_status rt_recttri_hex_tiling(int32_t n, int32_t top, int32_t* out, int64_t cap, int32_t* side) {
   clear_error();
-  if (n < 2 || !side) return fail(RT_ERR_INVALID_ARGUMENT, "recttri hex_tiling: side n >= 2");
-  std::vector<int32_t> t = hex_extremal(n, top != 0);
+  if (n < 2 || !side || top < 0 || top > 2) return fail(RT_ERR_INVALID_ARGUMENT, "recttri hex_tiling: side n >= 2, top 0, 1 or 2");
+  std::vector<int32_t> t = top == 2 ? hex_slope(n) : hex_extremal(n, top != 0);
   const int s = (int)std::lround(std::sqrt((double)t.size()));
   *side = s;
   if (!out || cap < (int64_t)t.size()) return fail(RT_ERR_BUFFER_TOO_SMALL, "recttri hex_tiling: output too small");

@@ -260,7 +260,7 @@ def recttri(ref: str) -> None:
     host, cases = [], []
     for n in (2, 3, 5, 8, 13):
         (tmax, side), (tmin, _) = hexagon(n, 1), hexagon(n, 0)
-        host.append({"n": n, "N": side, "max": tmax.tolist(), "min": tmin.tolist()})
+        host.append({"n": n, "N": side, "max": tmax.tolist(), "min": tmin.tolist(), "slope": hexagon(n, 2)[0].tolist()})
     for n, which, steps, seed in [(2, 0, 40, 1), (3, 1, 333, 99), (5, 0, 1000, 2018), (5, 1, 517, -5), (8, 0, 300, 77),
                                   (13, 1, 200, 4242)]:
         start, side = hexagon(n, which)

@@ -47,6 +47,8 @@ def test_host_utilities_match_reference_recttri_vectors(rt):
     for hc in GOLD["host_cases"]:
         assert np.array_equal(R.maxHex(hc["n"]), hc["max"])
         assert np.array_equal(R.minHex(hc["n"]), hc["min"])
+        assert np.array_equal(R.slopeHex(hc["n"]), hc["slope"])
+        assert inconsistent_triangles(R.slopeHex(hc["n"])) == 0 or hc["n"] == 2  # slopeHex(2) is not a tiling
         assert int(np.sqrt(len(hc["max"]))) == hc["N"] and hc["N"] % 3 == 0
     for cv in GOLD["from_lozenge"]:
         out = R.LozengeToRectTriangle(np.array(cv["lozenge"], np.int32), np.array(cv["domain"], np.int32))
