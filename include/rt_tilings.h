@@ -262,6 +262,13 @@ RT_API rt_status rt_td_rhombus_brick(int32_t rows, int32_t cols, int32_t* out, i
 /* Tiling format <-> dimer bytes ((N/2)^2 of them). */
 RT_API rt_status rt_td_dimers(const int32_t* tiling, int32_t n_side, uint8_t* out);
 RT_API rt_status rt_td_from_dimers(const uint8_t* dimers, int32_t n_side, int32_t* out);
+/* TriangleDimerTiler::TestButterfly(type) (TriangleDimerTiler.cpp:795-845, side 16; types
+   other than 0 H, 1 L, 2 R give the all-zero tiling), TilingToTriangleFlips (:846-873,
+   (N/2) x N) and TilingToButterflyFlips (:875-921, N x N): the move states the reference
+   derives from a tiling. */
+RT_API rt_status rt_td_test_butterfly(int32_t type, int32_t* out, int64_t cap, int32_t* side);
+RT_API rt_status rt_td_triangle_flips(const int32_t* tiling, int32_t n_side, int32_t* out);
+RT_API rt_status rt_td_butterfly_flips(const int32_t* tiling, int32_t n_side, int32_t* out);
 /* TriangleDimerTiler::TilingToVertices / TilingToDomain / DimerIndicator
    (TriangleDimerTiler.cpp:923-982, 35-99): the covered-vertex grid ((N/2+1)^2), the domain of
    triangles ((N/2) x N) and the M x M indicator of dimers of orientation c (0 horizontal,

@@ -325,6 +325,24 @@ class TriangleDimerTiler {
     check(rt_td_rhombus_brick(rows, cols, t.data(), (int64_t)t.size(), &side));
     return t;
   }
+  static tiling TestButterfly(int type) {
+    tiling t(16 * 16);
+    int32_t side = 0;
+    check(rt_td_test_butterfly(type, t.data(), (int64_t)t.size(), &side));
+    return t;
+  }
+  static std::vector<int> TilingToTriangleFlips(const tiling& t) {
+    int n = side_of(t);
+    std::vector<int> v((size_t)(n / 2) * n);
+    check(rt_td_triangle_flips(t.data(), n, v.data()));
+    return v;
+  }
+  static std::vector<int> TilingToButterflyFlips(const tiling& t) {
+    int n = side_of(t);
+    std::vector<int> v((size_t)n * n);
+    check(rt_td_butterfly_flips(t.data(), n, v.data()));
+    return v;
+  }
   static std::vector<int> TilingToVertices(const tiling& t) {
     int n = side_of(t);
     std::vector<int> v((size_t)(n / 2 + 1) * (n / 2 + 1));

@@ -49,3 +49,10 @@ extern "C" void refh_td_dimer_indicator(const int* t, int N, int c, int* out) {
   std::vector<int> v = TriangleDimerTiler::DimerIndicator(tt, c);
   std::memcpy(out, v.data(), v.size() * sizeof(int));
 }
+
+extern "C" int refh_td_test_butterfly(int type, int* out, long cap) {
+  tiling t = TriangleDimerTiler::TestButterfly(type);
+  if ((long)t.size() > cap) return -1;
+  std::memcpy(out, t.data(), t.size() * sizeof(int));
+  return (int)std::lround(std::sqrt((double)t.size()));
+}

@@ -158,6 +158,9 @@ _SIGNATURES = {
     "rt_td_from_dimers": (C.c_int32, [_P, C.c_int32, _P]),
     "rt_td_walk": (C.c_int32, [_P, C.c_int32, C.c_int64, C.c_int64, _P, _P]),
     "rt_td_vertices": (C.c_int32, [_P, C.c_int32, _P]),
+    "rt_td_test_butterfly": (C.c_int32, [C.c_int32, _P, C.c_int64, _P]),
+    "rt_td_triangle_flips": (C.c_int32, [_P, C.c_int32, _P]),
+    "rt_td_butterfly_flips": (C.c_int32, [_P, C.c_int32, _P]),
     "rt_td_domain": (C.c_int32, [_P, C.c_int32, _P]),
     "rt_td_dimer_indicator": (C.c_int32, [_P, C.c_int32, C.c_int32, _P]),
     "rt_sv_thresholds": (C.c_int32, [C.c_double, C.c_double, C.c_double, _P]),
@@ -613,6 +616,29 @@ class TriangleDimerTiler:
         n = side_of(tt)
         out = np.zeros((n // 2) ** 2, np.uint8)
         _check(lib().rt_td_dimers(_ptr(tt), n, _ptr(out)))
+        return out
+
+    @staticmethod
+    def TestButterfly(type_: int) -> np.ndarray:
+        side = C.c_int32()
+        buf = np.zeros(16 * 16, np.int32)
+        _check(lib().rt_td_test_butterfly(int(type_), _ptr(buf), buf.size, C.byref(side)))
+        return buf
+
+    @staticmethod
+    def TilingToTriangleFlips(t) -> np.ndarray:
+        tt = _i32(t)
+        n = side_of(tt)
+        out = np.zeros((n // 2) * n, np.int32)
+        _check(lib().rt_td_triangle_flips(_ptr(tt), n, _ptr(out)))
+        return out
+
+    @staticmethod
+    def TilingToButterflyFlips(t) -> np.ndarray:
+        tt = _i32(t)
+        n = side_of(tt)
+        out = np.zeros(n * n, np.int32)
+        _check(lib().rt_td_butterfly_flips(_ptr(tt), n, _ptr(out)))
         return out
 
     @staticmethod

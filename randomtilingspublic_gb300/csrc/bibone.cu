@@ -223,6 +223,98 @@ RT_API rt_status rt_td_icecream_cone(int32_t n, int32_t m, int32_t* out, int64_t
   return RT_OK;
 }
 
+// TriangleDimerTiler::TestButterfly(type) (TriangleDimerTiler.cpp:795-845): one butterfly of
+// orientation type (0 H, 1 L, 2 R) of four dimers in a side-16 tiling; other types give the
+// all-zero tiling (the reference prints a message).
+RT_API rt_status rt_td_test_butterfly(int32_t type, int32_t* out, int64_t cap, int32_t* side) {
+  clear_error();
+  const int E = 8, T = 2 * E;
+  if (!side) return fail(RT_ERR_INVALID_ARGUMENT, "test_butterfly: side is NULL");
+  *side = T;
+  if (!out || cap < (int64_t)T * T) return fail(RT_ERR_BUFFER_TOO_SMALL, "test_butterfly: output too small");
+  std::fill(out, out + (size_t)T * T, 0);
+  if (type < 0 || type > 2) return RT_OK;
+  std::vector<uint8_t> D((size_t)E * E, 0);
+  auto set = [&](int a, int b, uint8_t bit) { D[(size_t)a * E + b] |= bit; };
+  // the reference's h edges sit one vertex row below the edge they stand for
+  if (type == 0) set(1, 3, kH), set(3, 3, kH), set(2, 4, kR), set(3, 2, kR);
+  else if (type == 1) set(2, 3, kR), set(4, 2, kR), set(3, 2, kL), set(3, 4, kL);
+  else set(2, 4, kL), set(4, 3, kL), set(3, 2, kR), set(3, 4, kR);
+  std::vector<int32_t> t((size_t)T * T, 0);
+  td_to_tiling(D.data(), T, t.data());
+  for (int i = 3; i < T - 1; ++i)
+    for (int j = 3; j < T - 1; ++j) out[(size_t)i * T + j] = t[(size_t)i * T + j];
+  return RT_OK;
+}
+
+// TriangleDimerTiler::TilingToTriangleFlips (:846-873): (N/2) x N; row i, even column j the
+// state of the down triangle, odd column the up triangle, as three base-4 digits (the edge of
+// each neighbouring triangle that holds a dimer: 1, 2, 3, or 0), read from the lozenge states.
+RT_API rt_status rt_td_triangle_flips(const int32_t* t, int32_t n_side, int32_t* out) {
+  clear_error();
+  if (!t || !out || n_side < 4 || n_side % 2) return fail(RT_ERR_INVALID_ARGUMENT, "triangle_flips: even side >= 4");
+  const int N = n_side;
+  auto at = [&](int i, int j) { return t[(size_t)i * N + j]; };
+  std::fill(out, out + (size_t)(N / 2) * N, 0);
+  for (int i = 1; i < N / 2 - 1; ++i)
+    for (int j = 1; j < N - 1; ++j) {
+      const int eL = at(2 * i + 1, j), eR = at(2 * i + 1, j + 1), eU = at(2 * i, j + 1);  // j even: down triangle
+      int v;
+      if (j % 2 == 0) {
+        v = (((eL >> 2) & 1) + 2 * ((eL >> 3) & 1) + 3 * ((eR >> 3) & 1)) +
+            4 * (((eR >> 2) & 1) + 2 * ((eL >> 1) & 1) + 3 * ((eR >> 1) & 1)) +
+            16 * (2 * (eU & 1) + (eL & 1) + 3 * ((eU >> 1) & 1));
+      } else {
+        const int r = at(2 * i + 1, j), l = at(2 * i + 1, j + 1), h = at(2 * i + 2, j);  // odd: up triangle
+        v = ((r & 1) + 2 * ((r >> 3) & 1) + 3 * ((l >> 3) & 1)) + 4 * ((l & 1) + 2 * ((r >> 1) & 1) + 3 * ((l >> 1) & 1)) +
+            16 * (2 * ((h >> 3) & 1) + 3 * ((h >> 2) & 1) + ((r >> 2) & 1));
+      }
+      out[(size_t)i * N + j] = v;
+    }
+  return RT_OK;
+}
+
+// TriangleDimerTiler::TilingToButterflyFlips (:875-921): N x N, at each H / L / R position
+// the four neighbouring triangles' digits (weights 1, 4, 16, 64) and the centre edge (256).
+RT_API rt_status rt_td_butterfly_flips(const int32_t* t, int32_t n_side, int32_t* out) {
+  clear_error();
+  if (!t || !out || n_side < 4 || n_side % 2) return fail(RT_ERR_INVALID_ARGUMENT, "butterfly_flips: even side >= 4");
+  const int N = n_side;
+  auto at = [&](int i, int j) { return t[(size_t)i * N + j]; };
+  auto bit = [](int v, int k) { return (v >> k) & 1; };
+  std::fill(out, out + (size_t)N * N, 0);
+  for (int i = 2; i < N - 2; ++i)
+    for (int j = 2; j < N - 2; ++j) {
+      const int c0 = at(i, j);
+      int f1, f4, f16, f64, c;
+      if (i % 2 == 0) {
+        if (j % 2 == 0) continue;
+        const int up = at(i - 1, j), upr = at(i - 1, j + 1), dn = at(i + 1, j), dnl = at(i + 1, j - 1);
+        f1 = bit(up, 3) + 2 * bit(up, 0) + 3 * bit(c0, 0);
+        f4 = bit(upr, 0) + 2 * bit(upr, 1) + 3 * bit(c0, 1);
+        f16 = bit(dn, 1) + 2 * bit(dn, 2) + 3 * bit(c0, 2);
+        f64 = bit(dnl, 2) + 2 * bit(dnl, 3) + 3 * bit(c0, 3);
+        c = bit(upr, 2);
+      } else if (j % 2 == 0) {
+        const int ur = at(i - 1, j + 1), rr = at(i, j + 1), dl = at(i + 1, j - 1), ll = at(i, j - 1);
+        f1 = bit(ur, 0) + 2 * bit(ur, 1) + 3 * bit(c0, 0);
+        f4 = bit(rr, 1) + 2 * bit(rr, 2) + 3 * bit(c0, 1);
+        f16 = bit(dl, 2) + 2 * bit(dl, 3) + 3 * bit(c0, 2);
+        f64 = bit(ll, 3) + 2 * bit(ll, 0) + 3 * bit(c0, 3);
+        c = bit(rr, 3);
+      } else {
+        const int uu = at(i - 1, j), rr = at(i, j + 1), dd = at(i + 1, j), ll = at(i, j - 1);
+        f1 = bit(uu, 0) + 2 * bit(uu, 1) + 3 * bit(c0, 0);
+        f4 = bit(rr, 0) + 2 * bit(rr, 1) + 3 * bit(c0, 1);
+        f16 = bit(dd, 2) + 2 * bit(dd, 3) + 3 * bit(c0, 2);
+        f64 = bit(ll, 2) + 2 * bit(ll, 3) + 3 * bit(c0, 3);
+        c = bit(rr, 3);
+      }
+      out[(size_t)i * N + j] = f1 + 4 * f4 + 16 * f16 + 64 * f64 + 256 * c;
+    }
+  return RT_OK;
+}
+
 RT_API rt_status rt_td_rhombus_brick(int32_t rows, int32_t cols, int32_t* out, int64_t cap, int32_t* side) {
   clear_error();
   if (rows < 1 || cols < 2 || cols % 2 || !side)

@@ -319,17 +319,35 @@ def bibone(ref: str) -> None:
     start = _read_matrix(fixtures / "DimerStart.txt")
     assert np.array_equal(start, cone(6, 0)[0]), "DimerStart.txt"
     example = {"n": 6, "m": 0, "tiling": start.tolist(), "domain": _read_matrix(fixtures / "Domain.txt").tolist()}
+    td.refh_td_tri_flips.argtypes = [C.c_void_p, C.c_int, C.c_void_p]
+    td.refh_td_bfly_flips.argtypes = [C.c_void_p, C.c_int, C.c_void_p]
+    td.refh_td_test_butterfly.argtypes = [C.c_int, C.c_void_p, C.c_long]
+
+    def derived(t, side):
+        tri, bf = np.zeros((side // 2) * side, np.int32), np.zeros(side * side, np.int32)
+        td.refh_td_tri_flips(P(t), side, P(tri))
+        td.refh_td_bfly_flips(P(t), side, P(bf))
+        return tri.tolist(), bf.tolist()
+
     host, cases = [], []
     for n, m in [(3, 0), (4, 1), (6, 0), (8, 2), (11, 3), (20, 4)]:
         t, side = cone(n, m)
-        host.append({"n": n, "m": m, "N": side, "tiling": t.tolist()})
+        tri, bf = derived(t, side)
+        host.append({"n": n, "m": m, "N": side, "tiling": t.tolist(), "triangle_flips": tri, "butterfly_flips": bf})
+    butterflies = []
+    for typ in (0, 1, 2, 3):
+        buf = np.zeros(256, np.int32)
+        td.refh_td_test_butterfly(typ, P(buf), buf.size)
+        tri, bf = derived(buf, 16)
+        butterflies.append({"type": typ, "tiling": buf.tolist(), "triangle_flips": tri, "butterfly_flips": bf})
     for n, m, steps, seed in [(4, 1, 1, 5), (4, 1, 50, 1), (7, 0, 400, 77), (8, 2, 1000, -3), (11, 3, 2000, 2018),
                               (20, 4, 1500, 99)]:
         t, side = cone(n, m)
         cases.append({"name": f"td_walk_cone{n}_{m}_{steps}", "N": side, "start": t.tolist(), "steps": steps, "seed": seed,
                       "expected": walk(t, side, steps, seed).tolist()})
     (HERE / "bibone_ref_cases.json").write_text(json.dumps(
-        {"generator": "tests/golden/make_golden.py", "example": example, "host_cases": host, "cases": cases},
+        {"generator": "tests/golden/make_golden.py", "example": example, "host_cases": host, "cases": cases,
+         "test_butterflies": butterflies},
         separators=(",", ":")))
     print(f"wrote {len(cases)} bibone sweep cases, {len(host)} host cases")
 

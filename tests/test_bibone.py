@@ -115,6 +115,21 @@ def test_host_utilities_match_reference_vectors(rt):
         assert int(T.TilingToVertices(case["expected"]).sum()) == int(c1.sum())
 
 
+def test_derived_move_states_match_reference_vectors(rt):
+    T = rt.TriangleDimerTiler
+    for hc in GOLD["host_cases"]:
+        assert np.array_equal(T.TilingToTriangleFlips(hc["tiling"]), hc["triangle_flips"])
+        assert np.array_equal(T.TilingToButterflyFlips(hc["tiling"]), hc["butterfly_flips"])
+    for tb in GOLD["test_butterflies"]:
+        t = T.TestButterfly(tb["type"])
+        assert np.array_equal(t, tb["tiling"])
+        assert np.array_equal(T.TilingToButterflyFlips(t), tb["butterfly_flips"])
+        assert np.array_equal(T.TilingToTriangleFlips(t), tb["triangle_flips"])
+    # a test butterfly is flippable: its state at the centre is 85 or 170
+    for typ, (i, j) in ((0, (6, 7)), (1, (7, 6)), (2, (7, 7))):
+        assert T.TilingToButterflyFlips(T.TestButterfly(typ)).reshape(16, 16)[i, j] in (85, 170)
+
+
 def test_rhombus_brick_is_a_covering_of_the_rhombus(rt):
     T = rt.TriangleDimerTiler
     t = T.RhombusBrick(6, 8)
