@@ -6,12 +6,16 @@
 // (see dm_plan_partition).  Its flip candidates ("units": one site per unit in TinyMT mode,
 // a column quad in fast mode) are dealt round-robin to its threads, whose TinyMT generator
 // states stay in registers for the whole launch.  Each half-sweep:
-//   1. flip: every unit draws and tests its site of the rotated colour t in every chain;
-//   2. publish: the band's first and last rows of colour t go to a double-buffered exchange
-//      slot in global memory, then a release store of the half-sweep count to the band flag;
-//   3. wait: acquire-poll the two neighbour flags (bounded; on expiry an error code is set
-//      and every CTA leaves its loop), copy their rows into the halo rows;
-//   4. rebuild: the passive colour of the band, four sites per 32-bit word.
+//   1. flip: every unit draws and tests its site of the rotated colour t in every chain,
+//      the units of the band's first and last rows first;
+//   2. publish (two communication warps, while the workers flip the interior): the band's
+//      first and last rows of colour t go to a double-buffered exchange slot in global
+//      memory as 64-bit words that carry their half-sweep tag beside the data;
+//   3. wait: the same warps poll the neighbours' rows until every word carries the tag
+//      (bounded; on expiry an error code is set and every CTA leaves its loop) and copy
+//      them into the halo rows;
+//   4. rebuild: the passive colour of the band's first and last rows (the interior is kept
+//      current by XOR updates from each flip, or rebuilt in full for general inputs).
 // Only generators of flip candidates are advanced: the others never influence a flip, so
 // the tilings are identical to the per-half-sweep kernels (and to the reference).  The
 // rebuild is restricted to the window, which is exact when the loaded tilings are
@@ -232,8 +236,11 @@ __device__ __noinline__ void worker_role(uint8_t* smem, BandCtx& c) {
   };
 
   const int nsteps = (int)c.a.steps, par0 = (int)(c.a.h0 & 1);
+  // The colour of half-sweep h + 1 is loaded during half-sweep h, off the critical path.
+  int colour_next = (kMode == RT_RNG_TINYMT && nsteps > 0) ? c.a.colours[0] : 0;
   for (int h = 0; h < nsteps; ++h) {
-    const int t = (kMode == RT_RNG_TINYMT) ? (c.a.colours[h] ? 1 : 0) : (((par0 ^ h) & 1) ? 0 : 1);
+    const int t = (kMode == RT_RNG_TINYMT) ? (colour_next ? 1 : 0) : (((par0 ^ h) & 1) ? 0 : 1);
+    if (kMode == RT_RNG_TINYMT && h + 1 < nsteps) colour_next = c.a.colours[h + 1];
     const int bslots = c.boundary_slots;
     plane_act = pl.row(t, 0);
     plane_pas = pl.row(1 - t, 0);
@@ -289,33 +296,46 @@ __device__ __forceinline__ uint64_t ld_tagged(const uint64_t* p) {
 }
 
 // Reads n tagged words into dst, polling until each carries tag want.  Loads are issued in
-// batches of kBatch per lane so that one memory round trip covers a batch.  Returns false
-// when the wait gave up (bounded) or another CTA reported failure.
+// batches of kBatch per lane so that one memory round trip covers a batch, and every retry
+// re-issues all words of the batch still pending at once: a row that arrives late then
+// costs one more round trip, not one per word.  (Serial per-word polling turned a small
+// delay of one band into a delay of several microseconds for its neighbour, which locked
+// adjacent bands into alternating slow half-sweeps.)  Returns false when the wait gave up
+// (bounded) or another CTA reported failure.
 __device__ bool read_tagged(const uint64_t* src, uint32_t* dst, int n, uint32_t want, int* error, long max_spin) {
   constexpr int kBatch = 9;
   const int lane = threadIdx.x & 31;
   cuda::atomic_ref<int, cuda::thread_scope_device> err(*error);
   for (int base = lane; base < n; base += 32 * kBatch) {
     uint64_t v[kBatch];
+    uint32_t pending = 0;
 #pragma unroll
     for (int j = 0; j < kBatch; ++j) {
       const int w = base + 32 * j;
-      v[j] = w < n ? ld_tagged(src + w) : ((uint64_t)want << 32);
-    }
-#pragma unroll
-    for (int j = 0; j < kBatch; ++j) {
-      const int w = base + 32 * j;
-      long it = 0;
-      while ((uint32_t)(v[j] >> 32) != want) {
-        if ((++it & 255) == 0 && err.load(cuda::memory_order_relaxed) != 0) return false;
-        if (it > max_spin) {
-          int zero = 0;
-          err.compare_exchange_strong(zero, 1, cuda::memory_order_relaxed);
-          return false;
-        }
+      if (w < n) {
         v[j] = ld_tagged(src + w);
+        pending |= 1u << j;
       }
-      if (w < n) dst[w] = (uint32_t)v[j];
+    }
+    long it = 0;
+    for (;;) {
+#pragma unroll
+      for (int j = 0; j < kBatch; ++j) {
+        if (((pending >> j) & 1u) && (uint32_t)(v[j] >> 32) == want) {
+          dst[base + 32 * j] = (uint32_t)v[j];
+          pending &= ~(1u << j);
+        }
+      }
+      if (pending == 0) break;
+      if ((++it & 255) == 0 && err.load(cuda::memory_order_relaxed) != 0) return false;
+      if (it > max_spin) {
+        int zero = 0;
+        err.compare_exchange_strong(zero, 1, cuda::memory_order_relaxed);
+        return false;
+      }
+#pragma unroll
+      for (int j = 0; j < kBatch; ++j)
+        if ((pending >> j) & 1u) v[j] = ld_tagged(src + base + 32 * j);
     }
   }
   return true;
@@ -342,8 +362,10 @@ __device__ __noinline__ void comm_role(uint8_t* smem, BandCtx& c) {
     hi = min(c.band.whi, c.a.bands[nb_band].whi);
   }
   const int n_in = hi > lo ? (hi - lo) * NCH / 4 : 0;
+  int colour_next = (kMode == RT_RNG_TINYMT && nsteps > 0) ? c.a.colours[0] : 0;
   for (int h = 0; h < nsteps; ++h) {
-    const int t = (kMode == RT_RNG_TINYMT) ? (c.a.colours[h] ? 1 : 0) : (((par0 ^ h) & 1) ? 0 : 1);
+    const int t = (kMode == RT_RNG_TINYMT) ? (colour_next ? 1 : 0) : (((par0 ^ h) & 1) ? 0 : 1);
+    if (kMode == RT_RNG_TINYMT && h + 1 < nsteps) colour_next = c.a.colours[h + 1];
     const size_t slot = (size_t)(h & 1);
     const uint64_t tag = (uint64_t)(uint32_t)(h + 1) << 32;
     __syncthreads();  // #1
