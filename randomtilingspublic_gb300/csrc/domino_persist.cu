@@ -120,6 +120,40 @@ __device__ __forceinline__ Planes<NCH> planes_of(uint8_t* smem, const BandCtx& c
   return Planes<NCH>{smem + (size_t)K * kThreads * 4 * (need_where ? 2 : 1), c.R, c.Wb};
 }
 
+// Exchange words: the 4 data bytes and a tag (the half-sweep count h + 1) in one 64-bit
+// element, which is single-copy atomic, so a reader that sees the tag sees the data with it.
+// Accesses are 16-byte vectors of two such elements (each element stays atomic on its own):
+// every exchange row starts on a 32-byte boundary (P, wlo and whi are multiples of 16 cells).
+__device__ __forceinline__ void st_tagged2(uint64_t* p, uint64_t a, uint64_t b) {
+  asm volatile("st.relaxed.gpu.global.v2.u64 [%0], {%1, %2};" ::"l"(p), "l"(a), "l"(b) : "memory");
+}
+__device__ __forceinline__ void ld_tagged2(const uint64_t* p, uint64_t& a, uint64_t& b) {
+  asm volatile("ld.relaxed.gpu.global.v2.u64 {%0, %1}, [%2];" : "=l"(a), "=l"(b) : "l"(p) : "memory");
+}
+
+// Exchange slot h & 1 of band b holds [2 rows][P x chains / 4 words] (see PersistArgs::xbuf):
+// row 0 is the band's first row (read by the band above), row 1 its last (read below).
+template <int NCH>
+__device__ __forceinline__ uint64_t* exchange_row(const BandCtx& c, int h, int band, int which) {
+  const size_t row_words = (size_t)c.a.P * NCH / 4;
+  return reinterpret_cast<uint64_t*>(c.a.xbuf) + (((size_t)(h & 1) * c.a.nbands + band) * 2 + which) * row_words;
+}
+
+// Publishes the band's first and last rows of colour t for half-sweep h, one 16-byte
+// vector (four data words) per thread of the whole CTA, right after the boundary flips.
+template <int NCH>
+__device__ __forceinline__ void publish_rows(const BandCtx& c, const Planes<NCH>& pl, int t, int h) {
+  const int n4 = c.words >> 2;
+  const uint64_t tag = (uint64_t)(uint32_t)(h + 1) << 32;
+  for (int q = threadIdx.x; q < 2 * n4; q += blockDim.x) {
+    const int which = q >= n4 ? 1 : 0, qq = q - which * n4;
+    const uint4 d = reinterpret_cast<const uint4*>(pl.row(t, which == 0 ? 1 : c.R - 2))[qq];
+    uint64_t* g = exchange_row<NCH>(c, h, blockIdx.x, which) + (size_t)c.band.wlo * NCH / 4 + 4 * qq;
+    st_tagged2(g, tag | d.x, tag | d.y);
+    st_tagged2(g + 2, tag | d.z, tag | d.w);
+  }
+}
+
 // Unit c of the band -> colour-array row i and unit column u (site column in TinyMT mode,
 // column quad in fast mode): the first row, the last row, then the rows between.
 __device__ __forceinline__ void decode_unit(const BandCtx& c, int k, int& i, int& u) {
@@ -248,7 +282,8 @@ __device__ __noinline__ void worker_role(uint8_t* smem, BandCtx& c) {
 #pragma unroll
     for (int s = 0; s < K; ++s)
       if (s < bslots) flip_unit(s, t, h);
-    __syncthreads();  // #1: boundary rows final, the communication warp publishes them
+    __syncthreads();  // #1: boundary rows final
+    publish_rows<NCH>(c, pl, t, h);
 #pragma unroll
     for (int s = 0; s < K; ++s)
       if (s >= bslots) flip_unit(s, t, h);
@@ -284,36 +319,27 @@ __device__ __noinline__ void worker_role(uint8_t* smem, BandCtx& c) {
   }
 }
 
-// Exchange words: the 4 data bytes and a tag (the half-sweep count h + 1) in one 64-bit
-// store, which is single-copy atomic, so a reader that sees the tag sees the data with it.
-__device__ __forceinline__ void st_tagged(uint64_t* p, uint64_t v) {
-  asm volatile("st.relaxed.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
-}
-__device__ __forceinline__ uint64_t ld_tagged(const uint64_t* p) {
-  uint64_t v;
-  asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
-  return v;
-}
-
-// Reads n tagged words into dst, polling until each carries tag want.  Loads are issued in
-// batches of kBatch per lane so that one memory round trip covers a batch, and every retry
-// re-issues all words of the batch still pending at once: a row that arrives late then
-// costs one more round trip, not one per word.  (Serial per-word polling turned a small
-// delay of one band into a delay of several microseconds for its neighbour, which locked
-// adjacent bands into alternating slow half-sweeps.)  Returns false when the wait gave up
-// (bounded) or another CTA reported failure.
+// Reads n tagged words (n even, src 16-byte aligned) into dst, polling until each carries
+// tag want.  Each lane issues kBatch word pairs before it waits, so that one memory round
+// trip covers a batch (576 words per warp), and every retry re-issues all pairs of the
+// batch still pending at once: a row that arrives late then costs one more round trip, not
+// one per word.  (Serial per-word polling turned a small delay of one band into a delay of
+// several microseconds for its neighbour, which locked adjacent bands into alternating slow
+// half-sweeps.)  Returns false when the wait gave up (bounded) or another CTA reported
+// failure.
 __device__ bool read_tagged(const uint64_t* src, uint32_t* dst, int n, uint32_t want, int* error, long max_spin) {
   constexpr int kBatch = 9;
-  const int lane = threadIdx.x & 31;
+  const int lane = threadIdx.x & 31, n2 = n >> 1;
   cuda::atomic_ref<int, cuda::thread_scope_device> err(*error);
-  for (int base = lane; base < n; base += 32 * kBatch) {
-    uint64_t v[kBatch];
+  uint2* dst2 = reinterpret_cast<uint2*>(dst);
+  for (int base = lane; base < n2; base += 32 * kBatch) {
+    uint64_t v[2 * kBatch];
     uint32_t pending = 0;
 #pragma unroll
     for (int j = 0; j < kBatch; ++j) {
-      const int w = base + 32 * j;
-      if (w < n) {
-        v[j] = ld_tagged(src + w);
+      const int q = base + 32 * j;
+      if (q < n2) {
+        ld_tagged2(src + 2 * q, v[2 * j], v[2 * j + 1]);
         pending |= 1u << j;
       }
     }
@@ -321,8 +347,8 @@ __device__ bool read_tagged(const uint64_t* src, uint32_t* dst, int n, uint32_t 
     for (;;) {
 #pragma unroll
       for (int j = 0; j < kBatch; ++j) {
-        if (((pending >> j) & 1u) && (uint32_t)(v[j] >> 32) == want) {
-          dst[base + 32 * j] = (uint32_t)v[j];
+        if (((pending >> j) & 1u) && (uint32_t)(v[2 * j] >> 32) == want && (uint32_t)(v[2 * j + 1] >> 32) == want) {
+          dst2[base + 32 * j] = make_uint2((uint32_t)v[2 * j], (uint32_t)v[2 * j + 1]);
           pending &= ~(1u << j);
         }
       }
@@ -335,16 +361,16 @@ __device__ bool read_tagged(const uint64_t* src, uint32_t* dst, int n, uint32_t 
       }
 #pragma unroll
       for (int j = 0; j < kBatch; ++j)
-        if ((pending >> j) & 1u) v[j] = ld_tagged(src + base + 32 * j);
+        if ((pending >> j) & 1u) ld_tagged2(src + 2 * (base + 32 * j), v[2 * j], v[2 * j + 1]);
     }
   }
   return true;
 }
 
-// Warps 0 and 1: each publishes one boundary row of the rotated colour (warp 0 the first
-// row, for the band above; warp 1 the last row, for the band below) as tagged words, then
-// reads the matching row of that neighbour into its halo row.  Exchange slot h & 1 of band
-// b holds [2 rows][P x chains / 4 words] (see PersistArgs::xbuf).
+// Warps 0 and 1: after their share of the publication of the band's boundary rows, each
+// reads the facing boundary row of one neighbour (warp 0 the last row of the band above,
+// warp 1 the first row of the band below) into its halo row while the workers flip the
+// interior.
 template <int kMode, int K, bool kParams, int NCH>
 __device__ __noinline__ void comm_role(uint8_t* smem, BandCtx& c) {
   constexpr bool kNeedWhere = (kMode != RT_RNG_TINYMT) || kParams;
@@ -353,9 +379,7 @@ __device__ __noinline__ void comm_role(uint8_t* smem, BandCtx& c) {
   const Planes<NCH> pl = planes_of<NCH>(smem, c, K, kNeedWhere);
   __syncthreads();  // init
   const int nsteps = (int)c.a.steps, par0 = (int)(c.a.h0 & 1);
-  const int nbands = c.a.nbands;
-  const size_t row_words = (size_t)c.a.P * NCH / 4;
-  const bool has_nb = nb_band >= 0 && nb_band < nbands;
+  const bool has_nb = nb_band >= 0 && nb_band < c.a.nbands;
   int lo = 0, hi = 0;
   if (has_nb) {
     lo = max(c.band.wlo, c.a.bands[nb_band].wlo);
@@ -366,20 +390,11 @@ __device__ __noinline__ void comm_role(uint8_t* smem, BandCtx& c) {
   for (int h = 0; h < nsteps; ++h) {
     const int t = (kMode == RT_RNG_TINYMT) ? (colour_next ? 1 : 0) : (((par0 ^ h) & 1) ? 0 : 1);
     if (kMode == RT_RNG_TINYMT && h + 1 < nsteps) colour_next = c.a.colours[h + 1];
-    const size_t slot = (size_t)(h & 1);
-    const uint64_t tag = (uint64_t)(uint32_t)(h + 1) << 32;
     __syncthreads();  // #1
-    {
-      const uint32_t* row = reinterpret_cast<const uint32_t*>(pl.row(t, which == 0 ? 1 : c.R - 2));
-      uint64_t* g = reinterpret_cast<uint64_t*>(c.a.xbuf) + ((slot * nbands + b) * 2 + which) * row_words +
-                    (size_t)c.band.wlo * NCH / 4;
-      const int n = c.words;
-      for (int w = lane; w < n; w += 32) st_tagged(g + w, tag | row[w]);
-    }
+    publish_rows<NCH>(c, pl, t, h);
     int ok = 1;
     if (has_nb) {
-      const uint64_t* g = reinterpret_cast<const uint64_t*>(c.a.xbuf) +
-                          ((slot * nbands + nb_band) * 2 + (1 - which)) * row_words + (size_t)lo * NCH / 4;
+      const uint64_t* g = exchange_row<NCH>(c, h, nb_band, 1 - which) + (size_t)lo * NCH / 4;
       uint32_t* d = reinterpret_cast<uint32_t*>(pl.row(t, which == 0 ? 0 : c.R - 1) + (lo - c.band.wlo) * NCH);
       ok = read_tagged(g, d, n_in, (uint32_t)(h + 1), c.a.error, c.a.max_spin) ? 1 : 0;
     }
