@@ -543,11 +543,17 @@ def main() -> None:
 
 
 def _traffic_from_profile(mode: str, engine: int):
-    """DRAM bytes per launch of the sweep kernel from the committed ncu summary, if any."""
-    p = ROOT / "profiles" / "traffic.json"
-    if p.exists():
-        return json.loads(p.read_text()).get(f"{mode}_engine{engine}")
-    return None
+    """DRAM bytes per launch of the resident sweep kernel (dram__bytes_read.sum +
+    dram__bytes_write.sum of one ncu capture of this workload), read from the committed ncu
+    summary; None for the per-half-sweep engines, which that summary does not cover."""
+    import re
+
+    p = ROOT / "profiles" / "k_persist_aztec1024.md"
+    if engine != 2 or not p.exists():
+        return None
+    m = re.search(rf"traffic per launch \(dram__bytes_read\.sum \+ dram__bytes_write\.sum\):.*?\b{mode} (\d+) B",
+                  p.read_text())
+    return int(m.group(1)) if m else None
 
 
 if __name__ == "__main__":
