@@ -328,8 +328,10 @@ typedef struct rt_batch_stats {
 } rt_batch_stats;
 
 /* Runs every instance; RT_ERR_NOT_COALESCED if any instance ran out of attempts (its out
-   and attempts are still written).  Each instance's two chains must fit one CTA's shared
-   memory (about 2 x N^2 bytes: N up to about 330 for dominoes, 340 for lozenges). */
+   and attempts are still written).  Instances whose two chains fit one CTA's shared memory
+   (about 2 x N^2 bytes: N up to about 330 for dominoes, 340 for lozenges) run in the
+   persistent kernel; larger ones run after it, one at a time, through rt_domino_cftp /
+   rt_lozenge_cftp on the same stream (same samples); stats->seconds adds both. */
 RT_API rt_status rt_cftp_batch(rt_cftp_instance* inst, int32_t count, void* cuda_stream, rt_batch_stats* stats);
 
 /* ---- serving: continuous batching ----------------------------------------------------------

@@ -393,17 +393,22 @@ RT_API rt_status rt_cftp_batch(rt_cftp_instance* inst, int32_t count, void* cuda
   }
   BT_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
   BT_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
-  // Host side: validate, colour-split the extremal tilings, lay them out in one buffer.
-  std::vector<DevInstance> dv((size_t)count);
+  // Host side: validate every instance.  Instances whose two chains fit one CTA's shared
+  // memory go to the persistent kernel (colour-split, laid out in one buffer); the others run
+  // one by one through the single-instance entry points afterwards, which draw the same
+  // (seed, stream, half-sweep) keyed randomness and so return the same samples.
+  const size_t smem_limit = (size_t)optin - 1024;
+  std::vector<DevInstance> dv;
+  std::vector<int> small_idx, large_idx;
+  dv.reserve((size_t)count);
   size_t bytes = 0, smem_max = 0;
-  std::vector<std::pair<size_t, size_t>> spans;
   for (int k = 0; k < count; ++k) {
     const rt_cftp_instance& x = inst[k];
     if (!x.tmax || !x.tmin || !x.out) return fail(RT_ERR_INVALID_ARGUMENT, "cftp_batch: NULL tiling in instance");
     if (x.first_steps < 1 || x.max_attempts < 1 || x.max_attempts > 40)
       return fail(RT_ERR_INVALID_ARGUMENT, "cftp_batch: first_steps >= 1 and 1 <= max_attempts <= 40");
     if (x.stream >= 65536u) return fail(RT_ERR_INVALID_ARGUMENT, "cftp_batch: stream must be < 65536");
-    DevInstance& d = dv[k];
+    DevInstance d;
     std::memset(&d, 0, sizeof d);
     d.model = x.model;
     d.N = x.n_side;
@@ -433,18 +438,27 @@ RT_API rt_status rt_cftp_batch(rt_cftp_instance* inst, int32_t count, void* cuda
     d.first_sweeps = x.first_steps;
     const int ncol = x.model == RT_MODEL_DOMINO ? 2 : 3;
     const size_t chain = (size_t)ncol * d.N * d.P;
+    if (2 * chain > smem_limit) {
+      large_idx.push_back(k);
+      continue;
+    }
     smem_max = std::max(smem_max, 2 * chain);
     d.off_max = (int64_t)bytes;
     d.off_min = (int64_t)(bytes + chain);
     d.off_out = (int64_t)(bytes + 2 * chain);
     bytes += 3 * chain;
+    dv.push_back(d);
+    small_idx.push_back(k);
   }
-  if (smem_max > (size_t)optin - 1024)
-    return fail(RT_ERR_INVALID_ARGUMENT, "cftp_batch: an instance's two chains exceed one CTA's shared memory");
+  for (int k : large_idx)
+    for (const int32_t* t : {inst[k].tmax, inst[k].tmin})
+      for (size_t v = 0; v < (size_t)inst[k].n_side * inst[k].n_side; ++v)
+        if ((uint32_t)t[v] > 63u) return fail(RT_ERR_INVALID_ARGUMENT, "cftp_batch: tiling values out of range");
+  const int n_small = (int)small_idx.size();
   std::vector<uint8_t> host(bytes, 0);
-  for (int k = 0; k < count; ++k) {
-    const rt_cftp_instance& x = inst[k];
-    const DevInstance& d = dv[k];
+  for (int s = 0; s < n_small; ++s) {
+    const rt_cftp_instance& x = inst[small_idx[s]];
+    const DevInstance& d = dv[s];
     const int N = d.N, ncol = d.model == RT_MODEL_DOMINO ? 2 : 3;
     const size_t plane = (size_t)N * d.P;
     for (int which = 0; which < 2; ++which) {
@@ -477,7 +491,10 @@ RT_API rt_status rt_cftp_batch(rt_cftp_instance* inst, int32_t count, void* cuda
   };
   cudaEvent_t e0 = nullptr, e1 = nullptr;
   rt_status status = RT_OK;
+  int coalesced = 0, grid = 0;
+  double seconds = 0.0;
   do {
+    if (n_small == 0) break;
     if (cudaMalloc(&d_tilings, bytes) != cudaSuccess || cudaMalloc(&d_inst, dv.size() * sizeof(DevInstance)) != cudaSuccess ||
         cudaMalloc(&d_queue, sizeof(unsigned)) != cudaSuccess) {
       cudaGetLastError();
@@ -492,9 +509,9 @@ RT_API rt_status rt_cftp_batch(rt_cftp_instance* inst, int32_t count, void* cuda
     cudaFuncSetAttribute(k_batch_cftp, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_max);
     int per_sm = 0;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batch_cftp, kBatchThreads, smem_max);
-    const int grid = std::max(1, std::min(count, std::max(1, per_sm) * sms));
+    grid = std::max(1, std::min(n_small, std::max(1, per_sm) * sms));
     const uint32_t c4 = (uint32_t)std::ceil(0.4 * 4294967296.0), c8 = (uint32_t)std::ceil(0.8 * 4294967296.0);
-    BatchArgs ba{d_inst, count, d_tilings, d_queue};
+    BatchArgs ba{d_inst, n_small, d_tilings, d_queue};
     cudaEventRecord(e0, stream);
     k_batch_cftp<<<grid, kBatchThreads, smem_max, stream>>>(ba, c4, c8);
     cudaEventRecord(e1, stream);
@@ -512,10 +529,10 @@ RT_API rt_status rt_cftp_batch(rt_cftp_instance* inst, int32_t count, void* cuda
     }
     float ms = 0.f;
     cudaEventElapsedTime(&ms, e0, e1);
-    int coalesced = 0;
-    for (int k = 0; k < count; ++k) {
-      rt_cftp_instance& x = inst[k];
-      const DevInstance& d = dv[k];
+    seconds += ms * 1e-3;
+    for (int s = 0; s < n_small; ++s) {
+      rt_cftp_instance& x = inst[small_idx[s]];
+      const DevInstance& d = dv[s];
       const int N = d.N, ncol = d.model == RT_MODEL_DOMINO ? 2 : 3;
       const size_t plane = (size_t)N * d.P;
       const uint8_t* src = host.data() + d.off_out;
@@ -528,18 +545,46 @@ RT_API rt_status rt_cftp_batch(rt_cftp_instance* inst, int32_t count, void* cuda
       x.final_steps = d.final_half_sweeps;
       coalesced += d.attempts > 0;
     }
-    if (stats) {
-      stats->instances = count;
-      stats->coalesced = coalesced;
-      stats->seconds = ms * 1e-3;
-      stats->ctas = grid;
-    }
-    if (coalesced != count) status = fail(RT_ERR_NOT_COALESCED, "cftp_batch: some instances did not coalesce");
   } while (false);
   if (e0) cudaEventDestroy(e0);
   if (e1) cudaEventDestroy(e1);
   cleanup();
-  return status;
+  if (status != RT_OK) return status;
+  // Instances too large for one CTA: the single-instance path (the resident engine or the
+  // per-half-sweep kernels), one at a time on the same stream.
+  for (int k : large_idx) {
+    rt_cftp_instance& x = inst[k];
+    rt_walk_opts o;
+    rt_walk_opts_default(&o);
+    o.rng_mode = RT_RNG_FAST;
+    o.fast_stream = x.stream;
+    o.cuda_stream = cuda_stream;
+    rt_cftp_stats st;
+    std::memset(&st, 0, sizeof st);
+    rt_status r;
+    if (x.model == RT_MODEL_DOMINO) {
+      o.rule = x.rule;
+      o.weight_a = x.weight_a;
+      o.weight_b = x.weight_b;
+      r = rt_domino_cftp(x.tmax, x.tmin, x.n_side, (int64_t)x.seed, x.first_steps, 1, x.max_attempts, &o, x.out, &st);
+    } else {
+      o.rule = RT_LOZENGE_UNIFORM;
+      r = rt_lozenge_cftp(x.tmax, x.tmin, x.n_side, (int64_t)x.seed, x.first_steps, 1, x.max_attempts, &o, x.out, &st);
+    }
+    if (r != RT_OK && r != RT_ERR_NOT_COALESCED) return r;  // the entry point has set the message
+    x.attempts = r == RT_OK ? st.attempts : -st.attempts;
+    x.final_steps = st.final_steps;
+    coalesced += r == RT_OK;
+    seconds += st.seconds;
+  }
+  if (stats) {
+    stats->instances = count;
+    stats->coalesced = coalesced;
+    stats->seconds = seconds;
+    stats->ctas = grid;
+  }
+  if (coalesced != count) return fail(RT_ERR_NOT_COALESCED, "cftp_batch: some instances did not coalesce");
+  return RT_OK;
 }
 
 }  // extern "C"

@@ -73,3 +73,46 @@ def test_batch_rejects_bad_instances(rt):
         rt.cftp_batch([{"model": "domino", "tmax": tmax, "tmin": tmin, "seed": 1, "stream": 1, "rule": "plain"}])
     with pytest.raises(rt.RTError):
         rt.cftp_batch([{"model": "domino", "tmax": tmax, "tmin": tmin, "seed": 1, "stream": 70000}])
+
+
+def _plain(rt, job):
+    """The single-instance entry point called directly, so that a run that did not coalesce
+    still returns its sample and attempt count."""
+    import ctypes as C
+
+    if job["model"] == "domino":
+        tiler = rt.DominoTiler(rule=job["rule"], rng="fast", a=job["a"], b=job["b"], fast_stream=job["stream"])
+        fn = rt.lib().rt_domino_cftp
+    else:
+        tiler = rt.LozengeTiler(rng="fast", fast_stream=job["stream"])
+        fn = rt.lib().rt_lozenge_cftp
+    a, b = np.ascontiguousarray(job["tmax"], np.int32), np.ascontiguousarray(job["tmin"], np.int32)
+    out = np.zeros_like(a)
+    st = rt.CftpStats()
+    o = tiler.opts()
+    status = fn(rt._ptr(a), rt._ptr(b), rt.side_of(a), int(job["seed"]), int(job["first_steps"]), 1,
+                int(job.get("max_attempts", 20)), C.byref(o), rt._ptr(out), C.byref(st))
+    return status, out, st.attempts
+
+
+def test_oversized_instances_run_on_the_single_instance_path(rt):
+    """Instances whose two chains exceed one CTA's shared memory (an order-168 Aztec diamond,
+    a side-170 hexagon) run through the single-instance entry points inside the batch; every
+    instance of the mixed batch still equals its single-instance result, coalesced or not."""
+    D, L = rt.DominoTiler, rt.LozengeTiler
+    jobs = _jobs(rt, 6)
+    d = D.AztecDiamond(168)
+    jobs.append({"model": "domino", "tmax": D.MaxTiling(d), "tmin": D.MinTiling(d), "seed": 9, "stream": 7,
+                 "rule": "cftp", "a": 1.0, "b": 1.0, "first_steps": 1 << 18, "max_attempts": 2})
+    h = L.Hexagon(170)
+    jobs.append({"model": "lozenge", "tmax": L.MaxTiling(h), "tmin": L.MinTiling(h), "seed": 10, "stream": 8,
+                 "first_steps": 64, "max_attempts": 1})
+    outs, attempts, stats = rt.cftp_batch(jobs)
+    assert stats["instances"] == 8
+    assert attempts[-1] == -1  # 64 sweeps do not coalesce a side-170 hexagon
+    assert stats["coalesced"] == 8 - sum(a < 0 for a in attempts)
+    for job, out, att in zip(jobs, outs, attempts):
+        status, ref, ref_att = _plain(rt, job)
+        assert status in (rt.RT_OK, rt.RT_ERR_NOT_COALESCED)
+        assert abs(att) == ref_att and (att > 0) == (status == rt.RT_OK), job["model"]
+        assert np.array_equal(out, ref), (job["model"], rt.side_of(job["tmax"]))
