@@ -611,11 +611,7 @@ rt_status PersistPlan::build_from_rows(const std::vector<int>& lo, const std::ve
   } while (0)
 
 PersistEngine::~PersistEngine() {
-  if (d_bands) cudaFree(d_bands);
-  if (d_rows) cudaFree(d_rows);
-  if (d_xbuf) cudaFree(d_xbuf);
-  if (d_flags) cudaFree(d_flags);
-  if (d_colours) cudaFree(d_colours);
+  for (void* p : {(void*)d_bands, (void*)d_rows, (void*)d_xbuf, (void*)d_flags, (void*)d_colours}) dev_free(p, stream);
 }
 
 rt_status PersistEngine::prepare(DmSampler& s) {
@@ -657,20 +653,23 @@ rt_status PersistEngine::prepare(DmSampler& s) {
     return RT_OK;
   }
   // Device copies of the plan.
-  if (d_bands) cudaFree(d_bands), d_bands = nullptr;
-  if (d_rows) cudaFree(d_rows), d_rows = nullptr;
-  if (d_xbuf) cudaFree(d_xbuf), d_xbuf = nullptr;
-  if (d_flags) cudaFree(d_flags), d_flags = nullptr;
-  RT_CUDA_P(cudaMalloc(&d_bands, plan.bands.size() * sizeof(DmBand)));
-  RT_CUDA_P(cudaMalloc(&d_rows, 3 * (size_t)(s.N + 1) * sizeof(int)));
+  // Pool allocations ordered on the sampler's stream (device_pool.cpp).
+  stream = s.stream;
+  for (void** p : {(void**)&d_bands, (void**)&d_rows, (void**)&d_xbuf, (void**)&d_flags}) {
+    dev_free(*p, stream);
+    *p = nullptr;
+  }
+  if (rt_status st = dev_alloc(&d_bands, plan.bands.size() * sizeof(DmBand), stream)) return st;
+  if (rt_status st = dev_alloc(&d_rows, 3 * (size_t)(s.N + 1) * sizeof(int), stream)) return st;
   std::vector<int> rows_host(3 * (size_t)(s.N + 1), 0);
   std::copy(plan.row_lo.begin(), plan.row_lo.end(), rows_host.begin());
   std::copy(plan.row_prefix.begin(), plan.row_prefix.end(), rows_host.begin() + (s.N + 1));
-  RT_CUDA_P(cudaMemcpy(d_bands, plan.bands.data(), plan.bands.size() * sizeof(DmBand), cudaMemcpyHostToDevice));
-  RT_CUDA_P(cudaMemcpy(d_rows, rows_host.data(), rows_host.size() * sizeof(int), cudaMemcpyHostToDevice));
+  RT_CUDA_P(cudaMemcpyAsync(d_bands, plan.bands.data(), plan.bands.size() * sizeof(DmBand), cudaMemcpyHostToDevice,
+                            stream));
+  RT_CUDA_P(cudaMemcpyAsync(d_rows, rows_host.data(), rows_host.size() * sizeof(int), cudaMemcpyHostToDevice, stream));
   xbuf_bytes = dm_xbuf_bytes((int)plan.bands.size(), s.active, s.P);
-  RT_CUDA_P(cudaMalloc(&d_xbuf, xbuf_bytes));
-  RT_CUDA_P(cudaMalloc(&d_flags, (plan.bands.size() + 1) * sizeof(unsigned)));
+  if (rt_status st = dev_alloc(&d_xbuf, xbuf_bytes, stream)) return st;
+  if (rt_status st = dev_alloc(&d_flags, (plan.bands.size() + 1) * sizeof(unsigned), stream)) return st;
   nch = s.active;
   ready = true;
   return RT_OK;
@@ -705,9 +704,9 @@ rt_status PersistEngine::launch(DmSampler& s, const uint8_t* colours_host, int64
     a.fast_stream = s.opts.fast_stream;
     if (s.opts.rng_mode == RT_RNG_TINYMT) {
       if (colours_cap < n) {
-        if (d_colours) cudaFree(d_colours);
+        dev_free(d_colours, s.stream);
         d_colours = nullptr;
-        RT_CUDA_P(cudaMalloc(&d_colours, (size_t)n));
+        if (rt_status st = dev_alloc(&d_colours, (size_t)n, s.stream)) return st;
         colours_cap = n;
       }
       RT_CUDA_P(cudaMemcpyAsync(d_colours, colours_host + done, (size_t)n, cudaMemcpyHostToDevice, s.stream));

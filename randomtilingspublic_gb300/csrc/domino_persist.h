@@ -67,6 +67,7 @@ struct PersistEngine {
   int64_t colours_cap = 0;
   size_t xbuf_bytes = 0;
   bool pending_error_check = false;
+  cudaStream_t stream = nullptr;  // the sampler's: the buffers above are pool blocks ordered on it
 
   ~PersistEngine();
   rt_status prepare(DmSampler& s);

@@ -220,13 +220,10 @@ __global__ void k_diff(DmView v, int a, int b, unsigned long long* out) {
   } while (0)
 
 DmSampler::~DmSampler() {
-  if (tmt) cudaFree(tmt);
-  if (tmt_params) cudaFree(tmt_params);
-  if (base) cudaFree(base);
-  if (scratch) cudaFree(scratch);
-  if (counter) cudaFree(counter);
-  if (d_scan) cudaFree(d_scan);
-  if (d_cand) cudaFree(d_cand);
+  persist.reset();  // frees its plan buffers on the stream before the stream goes
+  for (void* p : {(void*)tmt, (void*)tmt_params, (void*)base, (void*)scratch, (void*)counter, (void*)d_scan,
+                  (void*)d_cand})
+    dev_free(p, stream);
   for (void* p : {(void*)d_dom, (void*)d_cls, (void*)d_h, (void*)d_hflags})
     if (p) cudaFree(p);
   if (ev0) cudaEventDestroy(ev0);
@@ -281,20 +278,22 @@ rt_status DmSampler::create(int n_side, int n_chains, const rt_walk_opts& o, std
   }
   RT_CUDA(cudaEventCreate(&s->ev0));
   RT_CUDA(cudaEventCreate(&s->ev1));
-  RT_CUDA(cudaMalloc(&s->base, s->chain_stride * n_chains));
+  // Pool allocations, ordered on the sampler's stream (device_pool.cpp).
+  if (rt_status st = dev_alloc(&s->base, s->chain_stride * n_chains, s->stream)) return st;
   RT_CUDA(cudaMemsetAsync(s->base, 0, s->chain_stride * n_chains, s->stream));
-  RT_CUDA(cudaMalloc(&s->scratch, (size_t)s->N * s->N * sizeof(int32_t)));
-  RT_CUDA(cudaMalloc(&s->counter, sizeof(unsigned long long)));
-  RT_CUDA(cudaMalloc(&s->d_scan, 3 * sizeof(unsigned long long)));
-  RT_CUDA(cudaMalloc(&s->d_cand, 2 * (size_t)s->N * sizeof(int)));
+  if (rt_status st = dev_alloc(&s->scratch, (size_t)s->N * s->N * sizeof(int32_t), s->stream)) return st;
+  if (rt_status st = dev_alloc(&s->counter, sizeof(unsigned long long), s->stream)) return st;
+  if (rt_status st = dev_alloc(&s->d_scan, 3 * sizeof(unsigned long long), s->stream)) return st;
+  if (rt_status st = dev_alloc(&s->d_cand, 2 * (size_t)s->N * sizeof(int), s->stream)) return st;
   {
     std::vector<int> init(2 * (size_t)s->N, -1);
     std::fill(init.begin(), init.begin() + s->N, INT_MAX);
-    RT_CUDA(cudaMemcpy(s->d_cand, init.data(), init.size() * sizeof(int), cudaMemcpyHostToDevice));
+    RT_CUDA(cudaMemcpyAsync(s->d_cand, init.data(), init.size() * sizeof(int), cudaMemcpyHostToDevice, s->stream));
+    RT_CUDA(cudaStreamSynchronize(s->stream));
   }
   const int64_t cells = (int64_t)(s->N - 2) * (s->N / 2 - 2);
   if (o.rng_mode == RT_RNG_TINYMT) {
-    RT_CUDA(cudaMalloc(&s->tmt, cells * sizeof(uint4)));
+    if (rt_status st = dev_alloc(&s->tmt, cells * sizeof(uint4), s->stream)) return st;
     if (o.tinymt_params) {
       // Generators beyond the table keep the default set, as the oracle does.
       std::vector<uint4> p((size_t)cells);
@@ -304,7 +303,7 @@ rt_status DmSampler::create(int n_side, int n_chains, const rt_walk_opts& o, std
         else
           p[k] = make_uint4(kTmtMat1, kTmtMat2, kTmtTmat, 0);
       }
-      RT_CUDA(cudaMalloc(&s->tmt_params, cells * sizeof(uint4)));
+      if (rt_status st = dev_alloc(&s->tmt_params, cells * sizeof(uint4), s->stream)) return st;
       RT_CUDA(cudaMemcpyAsync(s->tmt_params, p.data(), cells * sizeof(uint4), cudaMemcpyHostToDevice, s->stream));
       RT_CUDA(cudaStreamSynchronize(s->stream));
     }
@@ -718,8 +717,8 @@ RT_API rt_status rt_domino_cftp(const int32_t* tmax, const int32_t* tmin, int32_
   std::unique_ptr<DmSampler> s;
   // chains 0 (bottom) and 1 (top) are swept; 2 and 3 keep the min and max start states.
   if (rt_status st = DmSampler::create(n_side, 4, o, &s)) return st;
-  if (rt_status st = s->load(0, tmin)) return st;
-  if (rt_status st = s->load(2, tmin)) return st;
+  if (rt_status st = s->load(0, tmin)) return st;  // also counts the interior vertices
+  if (rt_status st = s->copy_chain(2, 0)) return st;
   if (rt_status st = s->load(3, tmax)) return st;
   s->active = 2;
   s->plan_dirty = true;

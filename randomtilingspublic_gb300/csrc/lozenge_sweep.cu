@@ -386,8 +386,8 @@ RT_API rt_status rt_lozenge_cftp(const int32_t* tmax, const int32_t* tmin, int32
   rt_walk_opts o = opts_or_default(opts);
   std::unique_ptr<LzSampler> s;
   if (rt_status st = LzSampler::create(n_side, 4, o, &s)) return st;
-  if (rt_status st = s->load(0, tmin)) return st;
-  if (rt_status st = s->load(2, tmin)) return st;
+  if (rt_status st = s->load(0, tmin)) return st;  // also counts the interior vertices
+  if (rt_status st = s->copy_chain(2, 0)) return st;
   if (rt_status st = s->load(3, tmax)) return st;
   s->active = 2;
   std::mt19937 drv((uint32_t)driver_seed);
