@@ -488,7 +488,9 @@ def run_ours(args) -> None:
             e2e_rates.append(stats.flip_attempts / dt)
         nbytes = n * n * 4
         e2e = {"value": _sum_over_ranks(statistics.median(e2e_rates[1:]), dist, dev), "unit": "flip attempts/s",
-               "h2d_bytes_per_step": 3 * nbytes, "d2h_bytes_per_step": nbytes + 8,
+               # the max and min tilings (the min start state is copied on the device) and the
+               # colour sequence in; the top chain and the coalescence count out
+               "h2d_bytes_per_step": 2 * nbytes + HALF_SWEEPS, "d2h_bytes_per_step": nbytes + 8,
                "api": "rt_domino_cftp (one attempt, look-back 2048 half-sweeps)"}
 
     cpu = None
