@@ -73,42 +73,71 @@ __global__ void k_lz_rotate_tmt(LzView v, int r, LzRule rule) {
   }
 }
 
+// Thread (q, i): the column quad q (one 32-bit word, columns 4q..4q+3) of row i, with the
+// quad's four draws; columns at or beyond M keep their value.
 __global__ void k_lz_rotate_fast(LzView v, int r, LzRule rule, uint64_t seed, uint32_t stream, int64_t h) {
   pdl_begin();
-  const int q = blockIdx.x * blockDim.x + threadIdx.x, i = blockIdx.y;
-  if (4 * q >= v.M) return;
+  const int q = blockIdx.x * blockDim.x + threadIdx.x, i = blockIdx.y * blockDim.y + threadIdx.y;
+  if (4 * q >= v.M || i >= v.N) return;
   const uint4 d = fast_quad(seed, stream, h, (uint32_t)i, (uint32_t)q);
   const uint32_t u4[4] = {d.x, d.y, d.z, d.w};
   for (int ch = 0; ch < v.active; ++ch) {
-    uint8_t* row = v.colour(ch, r) + (size_t)i * v.P;
+    uint32_t* word = reinterpret_cast<uint32_t*>(v.colour(ch, r) + (size_t)i * v.P) + q;
+    const uint32_t e4 = *word;
+    uint32_t n4 = e4;
 #pragma unroll
     for (int k4 = 0; k4 < 4; ++k4) {
-      const int j = 4 * q + k4;
-      if (j >= v.M) break;
-      const uint32_t e = row[j];
-      const uint8_t n = lz_flip(e, u4[k4], rule);
-      if (n != e) row[j] = n;
+      if (4 * q + k4 >= v.M) break;
+      const uint32_t e = (e4 >> (8 * k4)) & 0xffu;
+      n4 ^= (e ^ lz_flip(e, u4[k4], rule)) << (8 * k4);
     }
+    if (n4 != e4) *word = n4;
   }
 }
 
 // lozengekernel.cl:107-125: colour (r+1) mod 3 gets bits 2, 4, 32 and colour (r+2) mod 3
-// bits 1, 8, 16 from the rotated colour's neighbours; the column offsets depend on i mod 3.
-__global__ void k_lz_update(LzView v, int r) {
+// bits 1, 8, 16 from the rotated colour's neighbours; the column offsets depend on i mod 3:
+// T2 = bit 16 of up[j + p2] -> 2, bit 8 of mid[j - p4] -> 4, bit 1 of dn[j] -> 32, and
+// T3 = bit 32 of up[j] -> 1, bit 4 of mid[j + p8] -> 8, bit 2 of dn[j - p2] -> 16, with
+// p2, p4, p8 = [i mod 3 == (2r+1), (2r+2), 2r mod 3] (exactly one is set).
+// Four vertices at a time: thread (w, i) rewrites 32-bit word w (columns 4w..4w+3) of row i
+// of both passive colours.  A neighbour one column to the right or left is a funnel shift of
+// two adjacent words of the rotated colour, and every bit moves within its byte; bytes
+// outside columns [1, M-2] (and rows 0 and N-1) keep their value, as the reference rebuilds
+// only those vertices.
+__global__ void k_lz_update_w(LzView v, int r) {
   pdl_begin();
-  const int j = blockIdx.x * blockDim.x + threadIdx.x + 1, i = blockIdx.y + 1;
-  if (j > v.M - 2 || i > v.N - 2) return;
+  const int w = blockIdx.x * blockDim.x + threadIdx.x, i = blockIdx.y * blockDim.y + threadIdx.y + 1;
+  const int words = v.P / 4;
+  if (w >= words || i > v.N - 2) return;
   const int im = i % 3;
-  const int p2 = im == (2 * r + 1) % 3, p4 = im == (2 * r + 2) % 3, p8 = im == (2 * r) % 3, p16 = p2;
+  const bool p2 = im == (2 * r + 1) % 3, p4 = im == (2 * r + 2) % 3, p8 = im == (2 * r) % 3;
+  uint32_t keep = 0;
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    const int j = 4 * w + k;
+    if (j < 1 || j > v.M - 2) keep |= 0xffu << (8 * k);
+  }
+  if (keep == 0xffffffffu) return;
   for (int ch = 0; ch < v.active; ++ch) {
-    const uint8_t* A = v.colour(ch, r);
-    uint8_t* T2 = v.colour(ch, (r + 1) % 3) + (size_t)i * v.P + j;
-    uint8_t* T3 = v.colour(ch, (r + 2) % 3) + (size_t)i * v.P + j;
-    const uint8_t* up = A + (size_t)(i - 1) * v.P;
-    const uint8_t* mid = A + (size_t)i * v.P;
-    const uint8_t* dn = A + (size_t)(i + 1) * v.P;
-    *T2 = (uint8_t)((*T2 & ~(2 | 4 | 32)) | ((up[j + p2] & 16) >> 3) | ((mid[j - p4] & 8) >> 1) | ((dn[j] & 1) << 5));
-    *T3 = (uint8_t)((*T3 & ~(1 | 8 | 16)) | ((up[j] & 32) >> 5) | ((mid[j + p8] & 4) << 1) | ((dn[j - p16] & 2) << 3));
+    const uint32_t* up = reinterpret_cast<const uint32_t*>(v.colour(ch, r) + (size_t)(i - 1) * v.P);
+    const uint32_t* mid = up + words;
+    const uint32_t* dn = mid + words;
+    const uint32_t u0 = up[w], m0 = mid[w], d0 = dn[w];
+    // x[j + 1] and x[j - 1] for the word's four columns
+    const uint32_t u_r = __funnelshift_r(u0, w + 1 < words ? up[w + 1] : 0u, 8);
+    const uint32_t m_r = __funnelshift_r(m0, w + 1 < words ? mid[w + 1] : 0u, 8);
+    const uint32_t m_l = __funnelshift_l(w > 0 ? mid[w - 1] : 0u, m0, 8);
+    const uint32_t d_l = __funnelshift_l(w > 0 ? dn[w - 1] : 0u, d0, 8);
+    const uint32_t a2 = p2 ? u_r : u0, a4 = p4 ? m_l : m0, a8 = p8 ? m_r : m0, a16 = p2 ? d_l : d0;
+    const uint32_t b2 = ((a2 & 0x10101010u) >> 3) | ((a4 & 0x08080808u) >> 1) | ((d0 & 0x01010101u) << 5);
+    const uint32_t b3 = ((u0 & 0x20202020u) >> 5) | ((a8 & 0x04040404u) << 1) | ((a16 & 0x02020202u) << 3);
+    uint32_t* T2 = reinterpret_cast<uint32_t*>(v.colour(ch, (r + 1) % 3) + (size_t)i * v.P) + w;
+    uint32_t* T3 = reinterpret_cast<uint32_t*>(v.colour(ch, (r + 2) % 3) + (size_t)i * v.P) + w;
+    const uint32_t t2 = *T2, t3 = *T3;
+    const uint32_t n2 = (t2 & ~0x26262626u) | b2, n3 = (t3 & ~0x19191919u) | b3;
+    *T2 = (n2 & ~keep) | (t2 & keep);
+    *T3 = (n3 & ~keep) | (t3 & keep);
   }
 }
 
@@ -297,11 +326,11 @@ struct LzSampler {
   }
   rt_status run(const uint8_t* colours, int64_t steps) {
     const LzView v = view();
-    const dim3 gr((M + 127) / 128, N), gu((M + 127) / 128, N - 2);
+    const dim3 gr((M + 127) / 128, N), gu((P / 4 + 31) / 32, (N - 2 + 7) / 8);
     for (int64_t s = 0; s < steps; ++s) {
       const int r = colours[s];
       pdl_launch(k_lz_rotate_tmt, gr, dim3(128), stream, v, r, rule);
-      pdl_launch(k_lz_update, gu, dim3(128), stream, v, r);
+      pdl_launch(k_lz_update_w, gu, dim3(32, 8), stream, v, r);
       steps_by_colour[r]++;
     }
     return check();
@@ -309,12 +338,12 @@ struct LzSampler {
   rt_status run_fast(uint64_t seed_value, int64_t h0, int64_t steps) {
     const LzView v = view();
     const int quads = (M + 3) / 4;
-    const dim3 gr((quads + 127) / 128, N), gu((M + 127) / 128, N - 2);
+    const dim3 gr((quads + 31) / 32, (N + 7) / 8), gu((P / 4 + 31) / 32, (N - 2 + 7) / 8);
     for (int64_t s = 0; s < steps; ++s) {
       const int64_t h = h0 + s;
       const int r = (int)(((h % 3) + 3) % 3);
-      pdl_launch(k_lz_rotate_fast, gr, dim3(128), stream, v, r, rule, seed_value, opts.fast_stream, h);
-      pdl_launch(k_lz_update, gu, dim3(128), stream, v, r);
+      pdl_launch(k_lz_rotate_fast, gr, dim3(32, 8), stream, v, r, rule, seed_value, opts.fast_stream, h);
+      pdl_launch(k_lz_update_w, gu, dim3(32, 8), stream, v, r);
       steps_by_colour[r]++;
     }
     return check();
