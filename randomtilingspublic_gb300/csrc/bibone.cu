@@ -106,8 +106,8 @@ __global__ void k_td_step_tmt(uint8_t* D, uint4* tmt, int M, TdStep s) {
 // Fast mode: a thread owns columns 4q .. 4q+3 of row a and one Philox block of draws.
 __global__ void k_td_step_fast(uint8_t* D, int M, TdStep s, uint64_t seed, uint32_t stream, int64_t h) {
   pdl_begin();
-  const int q = blockIdx.x * blockDim.x + threadIdx.x, a = blockIdx.y;
-  if (4 * q >= M) return;
+  const int q = blockIdx.x * blockDim.x + threadIdx.x, a = blockIdx.y * blockDim.y + threadIdx.y;
+  if (4 * q >= M || a >= M) return;
   bool any = false;
 #pragma unroll
   for (int k = 0; k < 4; ++k) any |= (4 * q + k < M) && td_in_class(s, a, 4 * q + k);
@@ -466,12 +466,12 @@ RT_API rt_status rt_td_walk(int32_t* tiling, int32_t n_side, int64_t steps, int6
     k_td_seed<<<(unsigned)((count + 255) / 256), 256, 0, st>>>(tmt, count, (uint32_t)seed);
   }
   cudaEventRecord(e0, st);
-  const dim3 g_all((M + 127) / 128, M), g_quad(((M + 3) / 4 + 127) / 128, M);
+  const dim3 g_all((M + 127) / 128, M), g_quad(((M + 3) / 4 + 31) / 32, (M + 7) / 8);
   for (int64_t h = 0; h < steps; ++h) {
     if (o.rng_mode == RT_RNG_TINYMT)
       pdl_launch(k_td_step_tmt, g_all, dim3(128), st, dD, tmt, M, sched[(size_t)h]);
     else
-      pdl_launch(k_td_step_fast, g_quad, dim3(128), st, dD, M, sched[(size_t)h], (uint64_t)seed, o.fast_stream, h);
+      pdl_launch(k_td_step_fast, g_quad, dim3(32, 8), st, dD, M, sched[(size_t)h], (uint64_t)seed, o.fast_stream, h);
   }
   cudaEventRecord(e1, st);
   cudaError_t le = cudaGetLastError();
