@@ -420,6 +420,12 @@ RT_API rt_status rt_domino_edge_indicators(const int32_t* tiling, int32_t n_side
    persistent kernel), flip-candidate units held by the persistent kernel, CTAs (bands),
    units per thread}. */
 RT_API rt_status rt_dm_sampler_engine_info(rt_dm_sampler* s, int64_t* out4);
+/* Test hook for the resident engine's failure detection (no counterpart in the reference):
+   in the sampler's next runs band `band` publishes none of its boundary rows (band < 0:
+   none) and every wait gives up after max_spin polls (0: the default, 2^22).  The
+   neighbours' waits then run out, every CTA leaves its loop, and the run (or the next sync
+   or store) returns RT_ERR_TIMEOUT, with the CUDA context intact.  Nothing faults. */
+RT_API rt_status rt_dm_sampler_test_silent_band(rt_dm_sampler* s, int32_t band, int64_t max_spin);
 
 /* ---- allocation-free sweep -------------------------------------------------------------
    No counterpart in the reference.  For callers that cannot allocate device memory (a

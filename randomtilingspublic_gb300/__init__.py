@@ -129,6 +129,7 @@ _SIGNATURES = {
     "rt_dm_sampler_interior_vertices": (C.c_int64, [_P]),
     "rt_dm_sampler_launches": (C.c_int64, [_P]),
     "rt_dm_sampler_engine_info": (C.c_int32, [_P, _P]),
+    "rt_dm_sampler_test_silent_band": (C.c_int32, [_P, C.c_int32, C.c_int64]),
     "rt_domino_rule_table": (C.c_int32, [C.c_int32, C.c_int32, C.c_double, C.c_double, _P]),
     "rt_dm_sweep_noalloc": (C.c_int32, [_P, _P, C.c_int32, C.c_int32, _P, C.c_int64, C.c_uint64, C.c_int64, _P]),
     "rt_cftp_batch": (C.c_int32, [_P, C.c_int32, _P, _P]),

@@ -143,6 +143,7 @@ __device__ __forceinline__ uint64_t* exchange_row(const BandCtx& c, int h, int b
 // vector (four data words) per thread of the whole CTA, right after the boundary flips.
 template <int NCH>
 __device__ __forceinline__ void publish_rows(const BandCtx& c, const Planes<NCH>& pl, int t, int h) {
+  if ((int)blockIdx.x + 1 == c.a.silent_band_plus1) return;  // test hook: the neighbours' waits run out
   const int n4 = c.words >> 2;
   const uint64_t tag = (uint64_t)(uint32_t)(h + 1) << 32;
   for (int q = threadIdx.x; q < 2 * n4; q += blockDim.x) {
@@ -697,7 +698,8 @@ rt_status PersistEngine::launch(DmSampler& s, const uint8_t* colours_host, int64
     a.xbuf = d_xbuf;
     a.flags = d_flags;
     a.error = reinterpret_cast<int*>(d_flags + plan.bands.size());
-    a.max_spin = 1L << 22;
+    a.max_spin = s.test_max_spin > 0 ? s.test_max_spin : 1L << 22;
+    a.silent_band_plus1 = s.test_silent_band + 1;
     a.steps = n;
     a.h0 = h0 + done;
     a.fast_seed = fast_seed;

@@ -33,7 +33,8 @@ struct PersistArgs {
   uint8_t* xbuf;          // [2 slots][band][first, last row][P x chains / 4 tagged 64-bit words]
   unsigned* flags;        // flags[nbands] is the error word (per-band words unused)
   int* error;
-  long max_spin;
+  long max_spin;          // polls before a wait gives up
+  int silent_band_plus1;  // test hook: 1 + a band that publishes nothing (0: none)
   int64_t steps, h0;
   uint64_t fast_seed;
   uint32_t fast_stream;

@@ -632,6 +632,14 @@ RT_API int64_t rt_dm_sampler_interior_vertices(rt_dm_sampler* s) {
   return (s && s->impl) ? s->impl->interior[0] + s->impl->interior[1] : -1;
 }
 RT_API int64_t rt_dm_sampler_launches(rt_dm_sampler* s) { return (s && s->impl) ? s->impl->launches : -1; }
+RT_API rt_status rt_dm_sampler_test_silent_band(rt_dm_sampler* s, int32_t band, int64_t max_spin) {
+  RT_SAMPLER(s);
+  if (max_spin < 0) return fail(RT_ERR_INVALID_ARGUMENT, "test_silent_band: max_spin must be >= 0");
+  s->impl->test_silent_band = band < 0 ? -1 : band;
+  s->impl->test_max_spin = (long)max_spin;
+  return RT_OK;
+}
+
 RT_API rt_status rt_dm_sampler_engine_info(rt_dm_sampler* s, int64_t* out4) {
   RT_SAMPLER(s);
   if (!out4) return fail(RT_ERR_INVALID_ARGUMENT, "engine_info: out is NULL");

@@ -59,6 +59,10 @@ struct DmSampler {
   bool plan_dirty = true;
   std::unique_ptr<PersistEngine> persist;
   int last_engine = 0;  // engine of the last run: 1 per-half-sweep kernels, 2 persistent
+  // Test hook of the resident engine (rt_dm_sampler_test_silent_band): a band that
+  // publishes nothing (-1: none) and the polls after which a wait gives up (0: default).
+  int test_silent_band = -1;
+  long test_max_spin = 0;
 
   static rt_status create(int n_side, int n_chains, const rt_walk_opts& o, std::unique_ptr<DmSampler>* out);
   ~DmSampler();

@@ -229,3 +229,43 @@ def test_full_size_order_1024_properties(rt):
     inside = hmax != np.iinfo(np.int32).max
     assert (hb[inside] <= ht[inside]).all()  # monotone coupling keeps the order
     assert (hmin[inside] <= hb[inside]).all() and (ht[inside] <= hmax[inside]).all()
+
+
+@pytest.mark.gpu
+def test_resident_engine_wait_gives_up_and_the_sampler_stays_usable(rt):
+    """Failure detection without a GPU fault: band 1 of the resident kernel publishes none of
+    its boundary rows and a wait gives up after 4096 polls, so its neighbours' waits run out;
+    every CTA leaves its loop, the host reads RT_ERR_TIMEOUT, and the same sampler (same CUDA
+    context) then reproduces a fresh sampler's walk bit for bit."""
+    D = rt.DominoTiler
+    d = D.AztecDiamond(64)
+    tmax, tmin = D.MaxTiling(d), D.MinTiling(d)
+    n = rt.side_of(tmax)
+    tiler = rt.DominoTiler(rule="cftp", rng="fast", fast_stream=3, engine=2)
+
+    def fresh():
+        s = rt.DominoSampler(n, 2, tiler)
+        s.load(0, tmin)
+        s.load(1, tmax)
+        return s
+
+    s = fresh()
+    info = s.engine_info()
+    assert info["engine"] == 2 and info["bands"] >= 3
+    assert rt.lib().rt_dm_sampler_test_silent_band(s.h, 1, 4096) == rt.RT_OK
+    with pytest.raises(rt.RTError) as err:
+        s.run_fast(5, 0, 64)
+        s.sync()
+    assert err.value.status == rt.RT_ERR_TIMEOUT
+    assert rt.lib().rt_dm_sampler_test_silent_band(s.h, -1, 0) == rt.RT_OK
+    s.load(0, tmin)
+    s.load(1, tmax)
+    s.run_fast(5, 0, 64)
+    got = [s.store(0), s.store(1)]
+    s.close()
+    ref = fresh()
+    ref.run_fast(5, 0, 64)
+    want = [ref.store(0), ref.store(1)]
+    ref.close()
+    assert all(np.array_equal(a, b) for a, b in zip(got, want))
+    assert not np.array_equal(want[0], tmin)
