@@ -303,6 +303,9 @@ RT_API rt_status rt_load_matrix(const char* path, int32_t* out, int64_t cap, int
    return with rng_mode RT_RNG_FAST, fast_stream = stream and driver_seed = seed. */
 #define RT_MODEL_DOMINO 0
 #define RT_MODEL_LOZENGE 1
+#define RT_MODEL_RECTTRI 2
+#define RT_MODEL_BIBONE 3
+#define RT_MODEL_SIX_VERTEX 4
 
 typedef struct rt_cftp_instance {
   int32_t model;        /* RT_MODEL_DOMINO or RT_MODEL_LOZENGE */
@@ -333,6 +336,23 @@ typedef struct rt_batch_stats {
    persistent kernel; larger ones run after it, one at a time, through rt_domino_cftp /
    rt_lozenge_cftp on the same stream (same samples); stats->seconds adds both. */
 RT_API rt_status rt_cftp_batch(rt_cftp_instance* inst, int32_t count, void* cuda_stream, rt_batch_stats* stats);
+
+/* ---- model-generic entry points ------------------------------------------------------------
+   One signature for every model (RT_MODEL_*), dispatching to the per-model functions above,
+   for callers that bind the library once.  weights: RT_MODEL_RECTTRI the nine weights of
+   rt_recttri_walk, RT_MODEL_SIX_VERTEX {a, b, c} (NULL: all 1), unused by the other models
+   (domino and lozenge take theirs in opts).  For RT_MODEL_SIX_VERTEX the state is the height
+   function, n_side is n and steps count sweeps; for RT_MODEL_BIBONE the state is the
+   reference's tiling format of rt_td_walk.  rt_walk_epochs exists for dominoes only (the
+   reference's epoch overload), rt_cftp for dominoes, lozenges and the six-vertex model
+   (schedule is ignored there); the others return RT_ERR_INVALID_ARGUMENT. */
+RT_API rt_status rt_walk(int32_t model, int32_t* tiling, int32_t n_side, int64_t steps, int64_t seed,
+                         const double* weights, const rt_walk_opts* opts);
+RT_API rt_status rt_walk_epochs(int32_t model, int32_t* tiling, int32_t n_side, const int64_t* steps,
+                                const int64_t* seeds, int32_t n_epochs, const rt_walk_opts* opts);
+RT_API rt_status rt_cftp(int32_t model, const int32_t* tmax, const int32_t* tmin, int32_t n_side, int64_t driver_seed,
+                         int64_t first_steps, int32_t schedule, int32_t max_attempts, const double* weights,
+                         const rt_walk_opts* opts, int32_t* out, rt_cftp_stats* stats);
 
 /* ---- serving: continuous batching ----------------------------------------------------------
    No counterpart in the reference.  A request is one fast-mode CFTP instance

@@ -23,6 +23,7 @@ import numpy as np
 _PKG = Path(__file__).resolve().parent
 LIB_PATH = _PKG / "librt_tilings.so"
 
+RT_MODEL_DOMINO, RT_MODEL_LOZENGE, RT_MODEL_RECTTRI, RT_MODEL_BIBONE, RT_MODEL_SIX_VERTEX = 0, 1, 2, 3, 4
 RT_OK = 0
 RT_ERR_INVALID_ARGUMENT = 1
 RT_ERR_CUDA = 2
@@ -130,6 +131,10 @@ _SIGNATURES = {
     "rt_dm_sampler_launches": (C.c_int64, [_P]),
     "rt_dm_sampler_engine_info": (C.c_int32, [_P, _P]),
     "rt_dm_sampler_test_silent_band": (C.c_int32, [_P, C.c_int32, C.c_int64]),
+    "rt_walk": (C.c_int32, [C.c_int32, _P, C.c_int32, C.c_int64, C.c_int64, _P, _P]),
+    "rt_walk_epochs": (C.c_int32, [C.c_int32, _P, C.c_int32, _P, _P, C.c_int32, _P]),
+    "rt_cftp": (C.c_int32, [C.c_int32, _P, _P, C.c_int32, C.c_int64, C.c_int64, C.c_int32, C.c_int32, _P, _P, _P,
+                            _P]),
     "rt_domino_rule_table": (C.c_int32, [C.c_int32, C.c_int32, C.c_double, C.c_double, _P]),
     "rt_dm_sweep_noalloc": (C.c_int32, [_P, _P, C.c_int32, C.c_int32, _P, C.c_int64, C.c_uint64, C.c_int64, _P]),
     "rt_cftp_batch": (C.c_int32, [_P, C.c_int32, _P, _P]),
