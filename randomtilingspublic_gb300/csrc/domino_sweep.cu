@@ -36,16 +36,6 @@ __device__ __forceinline__ uint8_t dm_flip(uint32_t e, uint32_t u, uint32_t lo_u
   return (uint8_t)e;
 }
 
-// Passive site (i, m) rebuilt from the four active neighbours (dominokernel.cl:22-31):
-// its up edge from the site above's down edge, down from below's up, and the two
-// horizontal edges from the active sites left and right of it.
-__device__ __forceinline__ uint8_t dm_passive(const uint8_t* A, int P, int i, int m, int t) {
-  const uint8_t* row = A + (size_t)i * P;
-  const int left = m - ((i + t + 1) & 1), right = m + ((i + t) & 1);
-  return (uint8_t)(((A[(size_t)(i - 1) * P + m] & 2) >> 1) | ((A[(size_t)(i + 1) * P + m] & 1) << 1) |
-                   ((row[left] & 8) >> 1) | ((row[right] & 4) << 1));
-}
-
 __global__ void k_tmt_seed(uint4* st, const uint4* params, int64_t count, uint32_t seed) {
   int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= count) return;
@@ -97,27 +87,57 @@ __global__ void k_rotate_fast(DmView v, int t, DmRule rule, uint64_t seed, uint3
   const int c = (i & 1) | (t << 1);
   const uint32_t lo_up = rule.lo_up[c], w_up = rule.w_up[c], lo_dn = rule.lo_dn[c], w_dn = rule.w_dn[c];
   for (int ch = 0; ch < v.active; ++ch) {
-    uint8_t* A = v.colour(ch, t) + (size_t)i * v.P;
+    uint32_t* word = reinterpret_cast<uint32_t*>(v.colour(ch, t) + (size_t)i * v.P) + q;  // columns 4q..4q+3
+    const uint32_t e4 = *word;
+    uint32_t n4 = e4;
 #pragma unroll
     for (int r4 = 0; r4 < 4; ++r4) {
       const int m = 4 * q + r4;
       if (m < 1 || m > v.cols) continue;
-      const uint32_t e = A[m];
-      const uint8_t n = dm_flip(e, u4[r4], lo_up, w_up, lo_dn, w_dn);
-      if (n != e) A[m] = n;
+      const uint32_t e = (e4 >> (8 * r4)) & 0xffu;
+      n4 ^= (e ^ dm_flip(e, u4[r4], lo_up, w_up, lo_dn, w_dn)) << (8 * r4);
     }
+    if (n4 != e4) *word = n4;
   }
 }
 
-__global__ void k_update(DmView v, int t) {
+// The passive colour rebuilt from the active one (dominokernel.cl:22-31): passive site
+// (i, m) takes its up edge from the site above's down edge (bit 2 -> 1), its down edge from
+// below's up edge (1 -> 2) and its two horizontal edges from the active sites left (8 -> 4)
+// and right (4 -> 8) of it, at columns m, m+1 when i + t is odd and m-1, m otherwise.
+// Four sites at a time: thread (w, i) rewrites 32-bit word w (columns 4w..4w+3) of passive
+// row i from the active rows i-1, i, i+1; a neighbour one column over is a funnel shift of
+// two adjacent words.  Columns outside [1, cols] keep their value, as the reference rebuilds
+// only those sites.
+__global__ void k_update_w(DmView v, int t) {
   pdl_begin();
-  const int m = blockIdx.x * blockDim.x + threadIdx.x + 1;
+  const int w = blockIdx.x * blockDim.x + threadIdx.x;
   const int i = blockIdx.y * blockDim.y + threadIdx.y + 1;
-  if (m > v.cols || i > v.rows) return;
+  const int words = v.P / 4;
+  if (w >= words || i > v.rows) return;
+  uint32_t keep = 0;
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    const int m = 4 * w + k;
+    if (m < 1 || m > v.cols) keep |= 0xffu << (8 * k);
+  }
+  if (keep == 0xffffffffu) return;
+  const bool odd = ((i + t) & 1) != 0;  // left / right neighbours at columns m, m+1 (else m-1, m)
   for (int ch = 0; ch < v.active; ++ch) {
-    const uint8_t* A = v.colour(ch, t);
-    uint8_t* Pa = v.colour(ch, 1 - t);
-    Pa[(size_t)i * v.P + m] = dm_passive(A, v.P, i, m, t);
+    const uint32_t* A = reinterpret_cast<const uint32_t*>(v.colour(ch, t) + (size_t)i * v.P);
+    uint32_t* Pw = reinterpret_cast<uint32_t*>(v.colour(ch, 1 - t) + (size_t)i * v.P) + w;
+    const uint32_t cur = A[w], up = A[w - words], dn = A[w + words];
+    uint32_t left, right;
+    if (odd) {
+      left = cur;
+      right = __funnelshift_r(cur, w + 1 < words ? A[w + 1] : 0u, 8);
+    } else {
+      left = __funnelshift_l(w > 0 ? A[w - 1] : 0u, cur, 8);
+      right = cur;
+    }
+    const uint32_t val = ((up >> 1) & 0x01010101u) | ((dn & 0x01010101u) << 1) | ((left & 0x08080808u) >> 1) |
+                         ((right & 0x04040404u) << 1);
+    *Pw = (val & ~keep) | (*Pw & keep);
   }
 }
 
@@ -402,11 +422,12 @@ rt_status DmSampler::run(const uint8_t* colours, int64_t steps) {
   last_engine = 1;
   DmView v = view();
   const dim3 blk(128, 2), grd((v.cols + 127) / 128, (v.rows + 1) / 2);
+  const dim3 blk_w(32, 8), grd_w((v.P / 4 + 31) / 32, (v.rows + 7) / 8);
   for (int64_t s = 0; s < steps; ++s) {
     const int t = colours[s] ? 1 : 0;
     if (tmt_params) pdl_launch(k_rotate_tmt<true>, grd, blk, stream, v, t, rule);
     else pdl_launch(k_rotate_tmt<false>, grd, blk, stream, v, t, rule);
-    pdl_launch(k_update, grd, blk, stream, v, t);
+    pdl_launch(k_update_w, grd_w, blk_w, stream, v, t);
     launches += 2;
     half_sweeps[t]++;
   }
@@ -430,12 +451,12 @@ rt_status DmSampler::run_fast(uint64_t seed_value, int64_t h0, int64_t steps) {
   DmView v = view();
   const int quads = v.cols / 4 + 1;
   const dim3 blk(64, 4), grd_r((quads + 63) / 64, (v.rows + 3) / 4);
-  const dim3 blk_u(128, 2), grd_u((v.cols + 127) / 128, (v.rows + 1) / 2);
+  const dim3 blk_u(32, 8), grd_u((v.P / 4 + 31) / 32, (v.rows + 7) / 8);
   for (int64_t s = 0; s < steps; ++s) {
     const int64_t h = h0 + s;
     const int t = (h & 1) ? 0 : 1;
     pdl_launch(k_rotate_fast, grd_r, blk, stream, v, t, rule, seed_value, opts.fast_stream, h);
-    pdl_launch(k_update, grd_u, blk_u, stream, v, t);
+    pdl_launch(k_update_w, grd_u, blk_u, stream, v, t);
     launches += 2;
     half_sweeps[t]++;
   }
