@@ -83,38 +83,60 @@ __device__ __forceinline__ uint8_t dm_flip_b(uint32_t e, uint32_t u, uint32_t lo
 
 // One domino half-sweep of colour t on both chains held in shared memory (chain c, colour
 // k at sm + (c * 2 + k) * N * P): flips with the fast draws of half-sweep h, then the full
-// rebuild of the passive colour (dominokernel.cl:22-31 semantics).
+// rebuild of the passive colour (dominokernel.cl:22-31 semantics).  Every thread of the CTA
+// takes (row, column quad) units, one 32-bit word per chain, so that small instances keep
+// all threads busy; the rebuild writes four passive sites per word from whole words of the
+// active rows (funnel shifts for the one-column offsets) and keeps the columns outside
+// [1, cols].
 __device__ void domino_half_sweep(uint8_t* sm, const DevInstance& in, int t, int64_t h) {
   const int N = in.N, P = in.P, cols = in.cols - 1;  // sites m in [1, cols]
   const size_t plane = (size_t)N * P;
-  const int quads = cols / 4 + 1, units = (N - 2) * quads;
-  for (int k = threadIdx.x; k < units; k += kBatchThreads) {
+  const int words = P / 4, quads = cols / 4 + 1;
+  for (int k = threadIdx.x; k < (N - 2) * quads; k += kBatchThreads) {
     const int i = 1 + k / quads, q = k - (i - 1) * quads;
+    const int c = (i & 1) | (t << 1);
+    const uint32_t lo_up = in.lo_up[c], w_up = in.w_up[c], lo_dn = in.lo_dn[c], w_dn = in.w_dn[c];
     const uint4 r = fast_quad(in.seed, in.stream, h, (uint32_t)i, (uint32_t)q);
     const uint32_t rr[4] = {r.x, r.y, r.z, r.w};
-    const int c = (i & 1) | (t << 1);
     for (int ch = 0; ch < 2; ++ch) {
-      uint8_t* row = sm + (size_t)(ch * 2 + t) * plane + (size_t)i * P;
+      uint32_t* word = reinterpret_cast<uint32_t*>(sm + (size_t)(ch * 2 + t) * plane + (size_t)i * P) + q;
+      const uint32_t e4 = *word;
+      uint32_t n4 = e4;
 #pragma unroll
       for (int k4 = 0; k4 < 4; ++k4) {
         const int m = 4 * q + k4;
         if (m < 1 || m > cols) continue;
-        const uint32_t e = row[m];
-        const uint8_t n = dm_flip_b(e, rr[k4], in.lo_up[c], in.w_up[c], in.lo_dn[c], in.w_dn[c]);
-        if (n != e) row[m] = n;
+        const uint32_t e = (e4 >> (8 * k4)) & 0xffu;
+        n4 ^= (e ^ dm_flip_b(e, rr[k4], lo_up, w_up, lo_dn, w_dn)) << (8 * k4);
       }
+      if (n4 != e4) *word = n4;
     }
   }
   __syncthreads();
-  const int sites = (N - 2) * cols;
-  for (int k = threadIdx.x; k < 2 * sites; k += kBatchThreads) {
-    const int ch = k >= sites ? 1 : 0, kk = k - ch * sites;
-    const int i = 1 + kk / cols, m = 1 + kk % cols;
-    const uint8_t* A = sm + (size_t)(ch * 2 + t) * plane;
-    uint8_t* Pp = sm + (size_t)(ch * 2 + 1 - t) * plane;
-    const int left = m - ((i + t + 1) & 1), right = m + ((i + t) & 1);
-    Pp[(size_t)i * P + m] = (uint8_t)(((A[(size_t)(i - 1) * P + m] & 2) >> 1) | ((A[(size_t)(i + 1) * P + m] & 1) << 1) |
-                                      ((A[(size_t)i * P + left] & 8) >> 1) | ((A[(size_t)i * P + right] & 4) << 1));
+  for (int k = threadIdx.x; k < 2 * (N - 2) * words; k += kBatchThreads) {
+    const int rc = k / words, w = k - rc * words;
+    const int ch = rc & 1, i = 1 + (rc >> 1);
+    uint32_t keep = 0;  // columns outside [1, cols] keep their value
+#pragma unroll
+    for (int k4 = 0; k4 < 4; ++k4) {
+      const int m = 4 * w + k4;
+      if (m < 1 || m > cols) keep |= 0xffu << (8 * k4);
+    }
+    if (keep == 0xffffffffu) continue;
+    const uint32_t* A = reinterpret_cast<const uint32_t*>(sm + (size_t)(ch * 2 + t) * plane + (size_t)i * P);
+    uint32_t* Pw = reinterpret_cast<uint32_t*>(sm + (size_t)(ch * 2 + 1 - t) * plane + (size_t)i * P) + w;
+    const uint32_t cur = A[w], up = A[w - words], dn = A[w + words];
+    uint32_t left, right;  // active neighbours at columns m, m+1 when i + t is odd, else m-1, m
+    if ((i + t) & 1) {
+      left = cur;
+      right = __funnelshift_r(cur, w + 1 < words ? A[w + 1] : 0u, 8);
+    } else {
+      left = __funnelshift_l(w > 0 ? A[w - 1] : 0u, cur, 8);
+      right = cur;
+    }
+    const uint32_t val = ((up >> 1) & 0x01010101u) | ((dn & 0x01010101u) << 1) | ((left & 0x08080808u) >> 1) |
+                         ((right & 0x04040404u) << 1);
+    *Pw = (val & ~keep) | (*Pw & keep);
   }
   __syncthreads();
 }
@@ -125,40 +147,58 @@ __device__ void domino_half_sweep(uint8_t* sm, const DevInstance& in, int t, int
 __device__ void lozenge_step(uint8_t* sm, const DevInstance& in, int r, int64_t h, uint32_t c4, uint32_t c8) {
   const int N = in.N, P = in.P, M = in.cols;
   const size_t plane = (size_t)N * P;
-  const int quads = (M + 3) / 4, units = N * quads;
-  for (int k = threadIdx.x; k < units; k += kBatchThreads) {
+  const int words = P / 4, quads = (M + 3) / 4;
+  // Rotation: (row, column quad) units over every thread, one word per chain.
+  for (int k = threadIdx.x; k < N * quads; k += kBatchThreads) {
     const int i = k / quads, q = k - i * quads;
     const uint4 d = fast_quad(in.seed, in.stream, h, (uint32_t)i, (uint32_t)q);
     const uint32_t uu[4] = {d.x, d.y, d.z, d.w};
     for (int ch = 0; ch < 2; ++ch) {
-      uint8_t* row = sm + (size_t)(ch * 3 + r) * plane + (size_t)i * P;
+      uint32_t* word = reinterpret_cast<uint32_t*>(sm + (size_t)(ch * 3 + r) * plane + (size_t)i * P) + q;
+      const uint32_t e4 = *word;
+      uint32_t n4 = e4;
 #pragma unroll
       for (int k4 = 0; k4 < 4; ++k4) {
-        const int j = 4 * q + k4;
-        if (j >= M) break;
-        const uint32_t e = row[j];
-        uint8_t n = (uint8_t)e;
+        if (4 * q + k4 >= M) break;
+        const uint32_t e = (e4 >> (8 * k4)) & 0xffu;
+        uint32_t n = e;
         if (e == 25u && uu[k4] < c4) n = 38;
         else if (e == 38u && uu[k4] >= c4 && uu[k4] < c8) n = 25;
-        if (n != e) row[j] = n;
+        n4 ^= (e ^ n) << (8 * k4);
       }
+      if (n4 != e4) *word = n4;
     }
   }
   __syncthreads();
-  const int sites = (N - 2) * (M - 2);
-  for (int k = threadIdx.x; k < 2 * sites; k += kBatchThreads) {
-    const int ch = k >= sites ? 1 : 0, kk = k - ch * sites;
-    const int i = 1 + kk / (M - 2), j = 1 + kk % (M - 2);
+  // Rebuild: (chain, row, word of four vertices) units over every thread.
+  for (int k = threadIdx.x; k < 2 * (N - 2) * words; k += kBatchThreads) {
+    const int rc = k / words, w = k - rc * words;
+    const int ch = rc & 1, i = 1 + (rc >> 1);
+    uint32_t keep = 0;  // columns outside [1, M-2] keep their value
+#pragma unroll
+    for (int k4 = 0; k4 < 4; ++k4) {
+      const int j = 4 * w + k4;
+      if (j < 1 || j > M - 2) keep |= 0xffu << (8 * k4);
+    }
+    if (keep == 0xffffffffu) continue;
     const int im = i % 3;
-    const int p2 = im == (2 * r + 1) % 3, p4 = im == (2 * r + 2) % 3, p8 = im == (2 * r) % 3, p16 = p2;
-    const uint8_t* A = sm + (size_t)(ch * 3 + r) * plane;
-    uint8_t* T2 = sm + (size_t)(ch * 3 + (r + 1) % 3) * plane + (size_t)i * P + j;
-    uint8_t* T3 = sm + (size_t)(ch * 3 + (r + 2) % 3) * plane + (size_t)i * P + j;
-    const uint8_t* up = A + (size_t)(i - 1) * P;
-    const uint8_t* mid = A + (size_t)i * P;
-    const uint8_t* dn = A + (size_t)(i + 1) * P;
-    *T2 = (uint8_t)((*T2 & ~(2 | 4 | 32)) | ((up[j + p2] & 16) >> 3) | ((mid[j - p4] & 8) >> 1) | ((dn[j] & 1) << 5));
-    *T3 = (uint8_t)((*T3 & ~(1 | 8 | 16)) | ((up[j] & 32) >> 5) | ((mid[j + p8] & 4) << 1) | ((dn[j - p16] & 2) << 3));
+    const bool p2 = im == (2 * r + 1) % 3, p4 = im == (2 * r + 2) % 3, p8 = im == (2 * r) % 3;
+    const uint32_t* up = reinterpret_cast<const uint32_t*>(sm + (size_t)(ch * 3 + r) * plane + (size_t)(i - 1) * P);
+    const uint32_t* mid = up + words;
+    const uint32_t* dn = mid + words;
+    uint32_t* T2 = reinterpret_cast<uint32_t*>(sm + (size_t)(ch * 3 + (r + 1) % 3) * plane + (size_t)i * P) + w;
+    uint32_t* T3 = reinterpret_cast<uint32_t*>(sm + (size_t)(ch * 3 + (r + 2) % 3) * plane + (size_t)i * P) + w;
+    const uint32_t u0 = up[w], m0 = mid[w], d0 = dn[w];
+    const uint32_t u_r = __funnelshift_r(u0, w + 1 < words ? up[w + 1] : 0u, 8);
+    const uint32_t m_r = __funnelshift_r(m0, w + 1 < words ? mid[w + 1] : 0u, 8);
+    const uint32_t m_l = __funnelshift_l(w > 0 ? mid[w - 1] : 0u, m0, 8);
+    const uint32_t d_l = __funnelshift_l(w > 0 ? dn[w - 1] : 0u, d0, 8);
+    const uint32_t a2 = p2 ? u_r : u0, a4 = p4 ? m_l : m0, a8 = p8 ? m_r : m0, a16 = p2 ? d_l : d0;
+    const uint32_t b2 = ((a2 & 0x10101010u) >> 3) | ((a4 & 0x08080808u) >> 1) | ((d0 & 0x01010101u) << 5);
+    const uint32_t b3 = ((u0 & 0x20202020u) >> 5) | ((a8 & 0x04040404u) << 1) | ((a16 & 0x02020202u) << 3);
+    const uint32_t t2 = *T2, t3 = *T3;
+    *T2 = (((t2 & ~0x26262626u) | b2) & ~keep) | (t2 & keep);
+    *T3 = (((t3 & ~0x19191919u) | b3) & ~keep) | (t3 & keep);
   }
   __syncthreads();
 }
@@ -202,7 +242,7 @@ __device__ void run_instance(uint8_t* sm, const DevInstance& in, const uint8_t* 
   *look_out = look;
 }
 
-__global__ void __launch_bounds__(kBatchThreads) k_batch_cftp(BatchArgs a, uint32_t lz_c4, uint32_t lz_c8) {
+__global__ void __launch_bounds__(kBatchThreads, 8) k_batch_cftp(BatchArgs a, uint32_t lz_c4, uint32_t lz_c8) {
   extern __shared__ __align__(16) uint8_t sm[];
   __shared__ int s_idx;
   __shared__ uint32_t red[kBatchThreads / 32];
