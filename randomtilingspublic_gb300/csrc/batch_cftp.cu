@@ -52,11 +52,27 @@ struct DevInstance {
   int64_t final_half_sweeps;
 };
 
+// Per-instance state of a batched launch, in which an instance's attempts are separate work
+// items: the CTA that takes an instance from the queue runs its attempts in order, and CTAs
+// with nothing left to take run the next attempt of an unfinished instance beside it.
+struct InstState {
+  int next_att;             // attempts handed out
+  int best;                 // smallest attempt that coalesced (kNoAttempt: none yet)
+  unsigned long long done;  // bit j: attempt j has finished and recorded its output
+  int lock;                 // guards the instance's output
+  int finished;             // the instance's result is final
+};
+constexpr int kNoAttempt = 0x7fffffff;
+
 struct BatchArgs {
   DevInstance* inst;
+  InstState* state;
   int count;
   uint8_t* tilings;
   unsigned* queue;
+  unsigned* finished;  // instances whose result is final
+  int* error;          // set when a bounded wait for an instance's lock gave up
+  long max_spin;       // bound of that wait, and of a helper's rounds without work
 };
 
 __device__ __forceinline__ uint32_t block_sum(uint32_t v, uint32_t* red) {
@@ -242,27 +258,205 @@ __device__ void run_instance(uint8_t* sm, const DevInstance& in, const uint8_t* 
   *look_out = look;
 }
 
-__global__ void __launch_bounds__(kBatchThreads, 8) k_batch_cftp(BatchArgs a, uint32_t lz_c4, uint32_t lz_c8) {
-  extern __shared__ __align__(16) uint8_t sm[];
-  __shared__ int s_idx;
-  __shared__ uint32_t red[kBatchThreads / 32];
-  for (;;) {
-    if (threadIdx.x == 0) s_idx = (int)atomicAdd(a.queue, 1u);
-    __syncthreads();
-    const int idx = s_idx;
-    __syncthreads();
-    if (idx >= a.count) break;
-    DevInstance& g = a.inst[idx];
-    const DevInstance in = g;
-    int att;
-    int64_t look;
-    run_instance(sm, in, a.tilings + in.off_max, a.tilings + in.off_min, a.tilings + in.off_out, lz_c4, lz_c8, red, &att,
-                 &look);
+__device__ __forceinline__ int ld_volatile_i(const int* p) { return *reinterpret_cast<const volatile int*>(p); }
+__device__ __forceinline__ unsigned long long ld_volatile_u64(const unsigned long long* p) {
+  return *reinterpret_cast<const volatile unsigned long long*>(p);
+}
+
+// Attempt att of an instance in shared memory (chain 0 from the min tiling, chain 1 from the
+// max tiling, half-sweeps [-look, 0)): 1 coalesced, 0 not, -1 abandoned because a smaller
+// attempt of the instance coalesced meanwhile (checked every 256 steps).
+__device__ int run_attempt(uint8_t* sm, const DevInstance& in, const InstState* st, int att, const uint8_t* tilings,
+                           uint32_t lz_c4, uint32_t lz_c8, uint32_t* red, int* s_flag) {
+  const int ncol = in.model == 0 ? 2 : 3;
+  const int words = (int)((size_t)ncol * in.N * in.P / 4);
+  const uint32_t* gmax = reinterpret_cast<const uint32_t*>(tilings + in.off_max);
+  const uint32_t* gmin = reinterpret_cast<const uint32_t*>(tilings + in.off_min);
+  uint32_t* s32 = reinterpret_cast<uint32_t*>(sm);
+  for (int w = threadIdx.x; w < words; w += kBatchThreads) {
+    s32[w] = __ldcv(gmin + w);
+    s32[words + w] = __ldcv(gmax + w);
+  }
+  __syncthreads();
+  const int64_t look = ncol * (in.first_sweeps << att);
+  for (int64_t h = -look; h < 0; ++h) {
+    if (in.model == 0) domino_half_sweep(sm, in, (h & 1) ? 0 : 1, h);
+    else lozenge_step(sm, in, (int)(((h % 3) + 3) % 3), h, lz_c4, lz_c8);
+    if (((h + look) & 255) == 255) {  // uniform over the CTA
+      if (threadIdx.x == 0) *s_flag = ld_volatile_i(&st->best) < att;
+      __syncthreads();
+      const int stop = *s_flag;
+      __syncthreads();
+      if (stop) return -1;
+    }
+  }
+  uint32_t differ = 0;
+  for (int w = threadIdx.x; w < words; w += kBatchThreads) differ += s32[w] != s32[words + w];
+  differ = block_sum(differ, red);
+  return differ == 0 ? 1 : 0;
+}
+
+// Records attempt att (outcome of run_attempt).  A coalesced attempt smaller than any
+// recorded one, or the last attempt while none has coalesced, writes its top chain as the
+// instance's output under the instance's lock.  The CTA whose record completes the instance
+// (a coalesced attempt and every smaller one finished, or every attempt finished) writes the
+// attempt count and the look-back: the result is that of running the attempts in order.
+__device__ void record_attempt(uint8_t* sm, DevInstance* g, const DevInstance& in, InstState* st, int att, int outcome,
+                               uint8_t* tilings, const BatchArgs& a, int* s_flag) {
+  const int ncol = in.model == 0 ? 2 : 3;
+  const int words = (int)((size_t)ncol * in.N * in.P / 4);
+  if (outcome == 1 || (outcome == 0 && att == in.max_attempts - 1)) {
     if (threadIdx.x == 0) {
-      g.attempts = att;
-      g.final_half_sweeps = look;
+      int write = 0;
+      long it = 0;
+      bool locked = true;
+      while (atomicCAS(&st->lock, 0, 1) != 0) {
+        if (++it > a.max_spin) {
+          atomicExch(a.error, 1);
+          locked = false;
+          break;
+        }
+      }
+      if (locked) {
+        __threadfence();
+        const int best = ld_volatile_i(&st->best);
+        write = outcome == 1 ? att < best : best == kNoAttempt;
+        if (!write) atomicExch(&st->lock, 0);
+      }
+      *s_flag = write;
     }
     __syncthreads();
+    if (*s_flag) {
+      const uint32_t* s32 = reinterpret_cast<const uint32_t*>(sm);
+      uint32_t* gout = reinterpret_cast<uint32_t*>(tilings + in.off_out);
+      for (int w = threadIdx.x; w < words; w += kBatchThreads) __stcg(gout + w, s32[words + w]);
+      __threadfence();
+      __syncthreads();
+      if (threadIdx.x == 0) {
+        if (outcome == 1) atomicExch(&st->best, att);
+        __threadfence();
+        atomicExch(&st->lock, 0);
+      }
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    __threadfence();
+    const unsigned long long bit = 1ull << att;
+    const unsigned long long done = atomicOr(&st->done, bit) | bit;
+    const int best = ld_volatile_i(&st->best);
+    int attempts = 0, last = -1;
+    if (best != kNoAttempt) {
+      const unsigned long long need = (2ull << best) - 1;  // attempts 0 .. best (best < 40)
+      if ((done & need) == need) attempts = best + 1, last = best;
+    } else {
+      const unsigned long long all = in.max_attempts >= 64 ? ~0ull : ((1ull << in.max_attempts) - 1);
+      if ((done & all) == all) attempts = -in.max_attempts, last = in.max_attempts - 1;
+    }
+    if (last >= 0 && atomicCAS(&st->finished, 0, 1) == 0) {
+      g->attempts = attempts;
+      g->final_half_sweeps = ncol * (in.first_sweeps << last);
+      __threadfence();
+      atomicAdd(a.finished, 1u);
+    }
+  }
+  __syncthreads();
+}
+
+// Claims the next attempt of an instance if it is below limit (compare-and-swap, so that an
+// attempt handed out is always run); -1 otherwise.
+__device__ int claim_attempt(InstState* st, int limit) {
+  int cur = ld_volatile_i(&st->next_att);
+  while (cur < limit) {
+    const int prev = atomicCAS(&st->next_att, cur, cur + 1);
+    if (prev == cur) return cur;
+    cur = prev;
+  }
+  return -1;
+}
+
+// Attempts an instance's owner may still take: below max_attempts and below any attempt
+// that coalesced.  Helpers may run up to kSpeculate attempts beyond the smallest unfinished
+// one (attempt j costs 2^j units, so the deepest attempt in flight is most of the work left).
+constexpr int kSpeculate = 3;
+__device__ int owner_limit(const DevInstance& in, const InstState* st) {
+  return min(in.max_attempts, ld_volatile_i(&st->best));
+}
+__device__ int helper_limit(const DevInstance& in, const InstState* st) {
+  const unsigned long long done = ld_volatile_u64(&st->done);
+  const int lowest_unfinished = __ffsll((long long)~done) - 1;  // done < all-ones: attempts are below 64
+  return min(owner_limit(in, st), lowest_unfinished + 1 + kSpeculate);
+}
+
+__global__ void __launch_bounds__(kBatchThreads, 8) k_batch_cftp(BatchArgs a, uint32_t lz_c4, uint32_t lz_c8) {
+  extern __shared__ __align__(16) uint8_t sm[];
+  __shared__ int s_idx, s_att, s_flag, s_pick;
+  __shared__ uint32_t red[kBatchThreads / 32];
+  int own = -1;            // the instance this CTA took from the queue (thread 0's view)
+  bool drained = false;
+  long idle_rounds = 0;
+  for (;;) {
+    __syncthreads();  // every thread has read the previous round's shared picks
+    if (threadIdx.x == 0) {
+      int idx = -1, att = -1;
+      if (own >= 0) {
+        att = claim_attempt(&a.state[own], owner_limit(a.inst[own], &a.state[own]));
+        if (att >= 0) idx = own;
+        else own = -1;
+      }
+      while (idx < 0 && !drained) {
+        const int q = (int)atomicAdd(a.queue, 1u);
+        if (q >= a.count) {
+          drained = true;
+          break;
+        }
+        att = claim_attempt(&a.state[q], owner_limit(a.inst[q], &a.state[q]));
+        if (att >= 0) idx = own = q;
+      }
+      s_idx = idx;
+      s_att = att;
+      s_pick = drained && idx < 0 ? (ld_volatile_i(reinterpret_cast<const int*>(a.finished)) < a.count ? 1 : 2) : 0;
+    }
+    __syncthreads();
+    if (s_pick == 2) break;  // every instance is final
+    if (s_pick == 1) {
+      // Help: the CTA scans the unfinished instances that are under way for an attempt to take.
+      if (threadIdx.x == 0) s_idx = kNoAttempt;
+      __syncthreads();
+      const int start = (int)((blockIdx.x * 2654435761u) % (unsigned)a.count);
+      for (int k = threadIdx.x; k < a.count; k += kBatchThreads) {
+        const int i = (start + k) % a.count;
+        const InstState* st = &a.state[i];
+        if (ld_volatile_i(&st->finished) || ld_volatile_i(&st->next_att) == 0) continue;
+        if (ld_volatile_i(&st->next_att) < helper_limit(a.inst[i], st)) atomicMin(&s_idx, k);
+      }
+      __syncthreads();
+      if (threadIdx.x == 0) {
+        int idx = -1, att = -1;
+        if (s_idx != kNoAttempt) {
+          const int i = (start + s_idx) % a.count;
+          att = claim_attempt(&a.state[i], helper_limit(a.inst[i], &a.state[i]));
+          if (att >= 0) idx = i;
+        }
+        if (idx < 0) {
+          // Nothing to take now: wait and rescan.  A helper that has waited long leaves (the
+          // owners finish their instances on their own, so this bounds the wait and changes
+          // no result).
+          if (++idle_rounds > a.max_spin) s_pick = 2;
+          else __nanosleep(8000);
+        }
+        s_idx = idx;
+        s_att = att;
+      }
+      __syncthreads();
+      if (s_pick == 2) break;
+      if (s_idx < 0) continue;
+    }
+    const int idx = s_idx, att = s_att;
+    DevInstance* g = &a.inst[idx];
+    const DevInstance in = *g;
+    const int outcome = run_attempt(sm, in, &a.state[idx], att, a.tilings, lz_c4, lz_c8, red, &s_flag);
+    record_attempt(sm, g, in, &a.state[idx], att, outcome, a.tilings, a, &s_flag);
   }
 }
 
@@ -523,11 +717,13 @@ RT_API rt_status rt_cftp_batch(rt_cftp_instance* inst, int32_t count, void* cuda
   cudaStream_t stream = (cudaStream_t)cuda_stream;
   uint8_t* d_tilings = nullptr;
   DevInstance* d_inst = nullptr;
-  unsigned* d_queue = nullptr;
+  unsigned* d_queue = nullptr;  // [queue counter, finished instances, error word]
+  InstState* d_state = nullptr;
   auto cleanup = [&]() {
     if (d_tilings) cudaFree(d_tilings);
     if (d_inst) cudaFree(d_inst);
     if (d_queue) cudaFree(d_queue);
+    if (d_state) cudaFree(d_state);
   };
   cudaEvent_t e0 = nullptr, e1 = nullptr;
   rt_status status = RT_OK;
@@ -536,7 +732,8 @@ RT_API rt_status rt_cftp_batch(rt_cftp_instance* inst, int32_t count, void* cuda
   do {
     if (n_small == 0) break;
     if (cudaMalloc(&d_tilings, bytes) != cudaSuccess || cudaMalloc(&d_inst, dv.size() * sizeof(DevInstance)) != cudaSuccess ||
-        cudaMalloc(&d_queue, sizeof(unsigned)) != cudaSuccess) {
+        cudaMalloc(&d_queue, 3 * sizeof(unsigned)) != cudaSuccess ||
+        cudaMalloc(&d_state, (size_t)n_small * sizeof(InstState)) != cudaSuccess) {
       cudaGetLastError();
       status = fail(RT_ERR_OUT_OF_MEMORY, "cftp_batch: device allocation failed");
       break;
@@ -545,13 +742,19 @@ RT_API rt_status rt_cftp_batch(rt_cftp_instance* inst, int32_t count, void* cuda
     cudaEventCreate(&e1);
     cudaMemcpyAsync(d_tilings, host.data(), bytes, cudaMemcpyHostToDevice, stream);
     cudaMemcpyAsync(d_inst, dv.data(), dv.size() * sizeof(DevInstance), cudaMemcpyHostToDevice, stream);
-    cudaMemsetAsync(d_queue, 0, sizeof(unsigned), stream);
+    cudaMemsetAsync(d_queue, 0, 3 * sizeof(unsigned), stream);
+    std::vector<InstState> st0((size_t)n_small);
+    for (InstState& x : st0) {
+      std::memset(&x, 0, sizeof x);
+      x.best = kNoAttempt;
+    }
+    cudaMemcpyAsync(d_state, st0.data(), st0.size() * sizeof(InstState), cudaMemcpyHostToDevice, stream);
     cudaFuncSetAttribute(k_batch_cftp, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_max);
     int per_sm = 0;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batch_cftp, kBatchThreads, smem_max);
     grid = std::max(1, std::min(n_small, std::max(1, per_sm) * sms));
     const uint32_t c4 = (uint32_t)std::ceil(0.4 * 4294967296.0), c8 = (uint32_t)std::ceil(0.8 * 4294967296.0);
-    BatchArgs ba{d_inst, n_small, d_tilings, d_queue};
+    BatchArgs ba{d_inst, d_state, n_small, d_tilings, d_queue, d_queue + 1, reinterpret_cast<int*>(d_queue + 2), 1L << 24};
     cudaEventRecord(e0, stream);
     k_batch_cftp<<<grid, kBatchThreads, smem_max, stream>>>(ba, c4, c8);
     cudaEventRecord(e1, stream);
@@ -565,6 +768,12 @@ RT_API rt_status rt_cftp_batch(rt_cftp_instance* inst, int32_t count, void* cuda
     cudaError_t se = cudaStreamSynchronize(stream);
     if (se != cudaSuccess) {
       status = fail(RT_ERR_CUDA, std::string("cftp_batch: ") + cudaGetErrorString(se));
+      break;
+    }
+    unsigned err_word = 0;
+    cudaMemcpy(&err_word, d_queue + 2, sizeof err_word, cudaMemcpyDeviceToHost);
+    if (err_word) {
+      status = fail(RT_ERR_TIMEOUT, "cftp_batch: a bounded wait for an instance's output lock gave up");
       break;
     }
     float ms = 0.f;
