@@ -1,0 +1,147 @@
+"""Edge densities and the mean height function of exact samples on larger Aztec diamonds
+against exactly computed values.
+
+Exact edge-placement probabilities come from the Kasteleyn matrix (tests/test_edge_densities.py:
+uniform and two-periodic weights).  The height function (TilingToHeightfunc,
+DominoTiler.cpp:555-593) changes along a lattice edge u -> w by s (1 - 4 x), where
+s = +-1 is the step of the reference's walk (its axis and the colour of u) and x = 1 when a
+domino covers the edge (each square has exactly one covered side, so the three free sides'
+steps and the covered side's -3 s close up).  The height is therefore linear in the
+edge-covering indicators, and its exact mean is the path sum of s (1 - 4 P(e)).  On CPU the
+path formula is checked against TilingToHeightfunc on concrete tilings; on the GPU, batched
+CFTP samples (8000 per case) are compared with both exact quantities: every edge by its exact
+binomial tail (Bonferroni, family-wise level 1e-3), every vertex's mean height within |z| < 5
+where the height moves often enough for the normal approximation, and by a bound on the
+count of moves elsewhere."""
+from collections import deque
+
+import numpy as np
+import pytest
+
+from tests.test_edge_densities import kasteleyn_edge_probs
+
+DIRS = ((1, 0), (-1, 0), (0, 1), (0, -1))  # down, up, right, left (the reference's order)
+
+
+def _walk_order(d):
+    """Base vertex and BFS tree of the domain's lattice: (vertex, parent, direction) rows."""
+    M = int(np.sqrt(d.size))
+    N = M + 1
+    F = d.reshape(M, M)
+
+    def face(i, j):
+        return 0 <= i < M and 0 <= j < M and F[i, j] == 1
+
+    def touches(i, j, k):  # lattice edge from vertex (i, j) in direction k borders a domain face
+        if k == 0:
+            return face(i, j - 1) or face(i, j)
+        if k == 1:
+            return face(i - 1, j - 1) or face(i - 1, j)
+        if k == 2:
+            return face(i - 1, j) or face(i, j)
+        return face(i - 1, j - 1) or face(i, j - 1)
+
+    def in_domain(i, j):
+        return any(face(i - a, j - b) for a in (0, 1) for b in (0, 1))
+
+    def boundary(i, j):
+        return in_domain(i, j) and not all(face(i - a, j - b) for a in (0, 1) for b in (0, 1))
+
+    base = next((i, j) for i in range(N) for j in range(N) if boundary(i, j))
+    seen = {base}
+    order = []
+    q = deque([base])
+    while q:
+        i0, j0 = q.popleft()
+        for k, (di, dj) in enumerate(DIRS):
+            i, j = i0 + di, j0 + dj
+            if (i, j) in seen or not (0 <= i < N and 0 <= j < N) or not touches(i0, j0, k):
+                continue
+            seen.add((i, j))
+            order.append(((i, j), (i0, j0), k))
+            q.append((i, j))
+    return N, base, order
+
+
+def heights_from_edges(d, cover):
+    """Height function from edge-covering values in the [2][N][N] layout of
+    rt_domino_edge_indicators (0: the edge below a vertex, 1: the edge to its right), exact
+    0/1 for one tiling or probabilities for the mean; NaN outside the domain."""
+    N, base, order = _walk_order(d)
+    c = np.asarray(cover, np.float64).reshape(2, N, N)
+    h = np.full((N, N), np.nan)
+    h[base] = 0.0
+    for (i, j), (i0, j0), k in order:
+        if k == 0:
+            x = c[0, i0, j0]
+        elif k == 1:
+            x = c[0, i, j]
+        elif k == 2:
+            x = c[1, i0, j0]
+        else:
+            x = c[1, i, j]
+        s = (1 if k >= 2 else -1) * (1 if (i0 + j0) % 2 == 0 else -1)
+        h[i, j] = h[i0, j0] + s * (1 - 4 * x)
+    return h
+
+
+@pytest.mark.parametrize("order", [6, 20])
+def test_height_path_formula_equals_tiling_to_heightfunc(rt, order):
+    D = rt.DominoTiler
+    d = D.AztecDiamond(order)
+    for t in (D.MaxTiling(d), D.MinTiling(d)):
+        n = rt.side_of(t)
+        ref = D.TilingToHeightfunc(t, d).reshape(n, n).astype(np.float64)
+        got = heights_from_edges(d, rt.edge_indicators(t))
+        live = ~np.isnan(got)
+        assert live.sum() > 0
+        assert np.array_equal(got[live], ref[live])
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("rule,a,b", [("cftp", 1.0, 1.0), ("cftp_twoperiodic", 1.0, 0.8)])
+def test_cftp_edges_and_mean_height_match_exact_values(rt, rule, a, b):
+    D = rt.DominoTiler
+    order, samples = 32, 8000
+    d = D.AztecDiamond(order)
+    tmax, tmin = D.MaxTiling(d), D.MinTiling(d)
+    n = rt.side_of(tmax)
+    jobs = [{"model": "domino", "tmax": tmax, "tmin": tmin, "seed": 31000 + k, "stream": k, "rule": rule, "a": a,
+             "b": b, "first_steps": 64, "max_attempts": 16} for k in range(samples)]
+    outs, attempts, _ = rt.cftp_batch(jobs)
+    assert min(attempts) > 0
+    p = kasteleyn_edge_probs(d, a, b)
+    counts = np.zeros(2 * n * n, np.uint32)
+    hsum = np.zeros((n, n))
+    hsq = np.zeros((n, n))
+    for o in outs:
+        rt.edge_indicators(o, counts)
+        h = D.TilingToHeightfunc(o, d).reshape(n, n).astype(np.float64)
+        hsum += h
+        hsq += h * h
+    freq = counts / samples
+    live = (p > 1e-12) & (p < 1 - 1e-12)
+    # Exact two-sided binomial tails (edges near the frozen regions have tiny or near-one
+    # probabilities, where the normal approximation understates the tails), Bonferroni over
+    # the edges at a family-wise level of 1e-3.
+    from scipy.stats import binom
+
+    k, q = counts[live].astype(np.int64), p[live]
+    tail = 2 * np.minimum(binom.cdf(k, samples, q), binom.sf(k - 1, samples, q))
+    assert tail.min() * live.sum() > 1e-3, (float(tail.min()), int(live.sum()))
+    assert np.array_equal(freq[~live], np.round(p[~live]))
+    mean_exact = heights_from_edges(d, p)
+    mean = hsum / samples
+    var = hsq / samples - mean * mean
+    known = ~np.isnan(mean_exact)
+    # A vertex's height moves in steps of 4; where it moves in at least about 20 samples
+    # (var >= 16 * 20 / samples) the sample mean is close to normal and its z is tested.
+    # Vertices that rarely or never move (the boundary, the frozen regions) are bounded by
+    # the count of moves instead: fewer than ~25 expected, so a count off by more than 50
+    # (a mean off by 200 / samples) has a Poisson probability far below 1e-9.
+    often = known & (var * samples / 16 >= 20)
+    zh = (mean[often] - mean_exact[often]) / np.sqrt(var[often] / samples)
+    assert often.sum() > 1000
+    assert np.abs(zh).max() < 5.0, float(np.abs(zh).max())
+    rare = known & ~often
+    assert np.abs(mean[rare] - mean_exact[rare]).max() < 200 / samples
