@@ -1,5 +1,5 @@
-"""Edge densities and the mean height function of exact samples on larger Aztec diamonds
-against exactly computed values.
+"""Edge densities and the mean height function of exact samples on larger Aztec diamonds,
+and lozenge placement frequencies on a larger hexagon, against exactly computed values.
 
 Exact edge-placement probabilities come from the Kasteleyn matrix (tests/test_edge_densities.py:
 uniform and two-periodic weights).  The height function (TilingToHeightfunc,
@@ -145,3 +145,82 @@ def test_cftp_edges_and_mean_height_match_exact_values(rt, rule, a, b):
     assert np.abs(zh).max() < 5.0, float(np.abs(zh).max())
     rare = known & ~often
     assert np.abs(mean[rare] - mean_exact[rare]).max() < 200 / samples
+
+
+def lozenge_dimer_probs(d):
+    """Exact lozenge placement probabilities of a simply connected region of triangles
+    (M x 2M, even columns one colour class, odd the other), in the layout [3][N][N] of the
+    vertex bits 1, 2 and 8 (LozengeTiler.cpp:514-556: bit 1 of vertex (i, j) pairs triangles
+    (i-1, 2j-1) and (i-1, 2j), bit 2 pairs (i-1, 2j) and (i-1, 2j+1), bit 8 pairs (i-1, 2j+1)
+    and (i, 2j)).  Every inner face of the triangles' adjacency graph is a hexagon, so the
+    plain adjacency matrix is a Kasteleyn matrix and P(b, w) = K^-1(w, b)."""
+    M = int(np.sqrt(d.size // 2))
+    F = np.asarray(d).reshape(M, 2 * M)
+    N = M + 1
+    black = [(r, c) for r in range(M) for c in range(0, 2 * M, 2) if F[r, c] == 1]
+    white = [(r, c) for r in range(M) for c in range(1, 2 * M, 2) if F[r, c] == 1]
+    bi = {t: k for k, t in enumerate(black)}
+    wi = {t: k for k, t in enumerate(white)}
+    K = np.zeros((len(black), len(white)))
+    edges = []
+    for (r, c) in black:
+        for w, kind, vi, vj in (((r, c - 1), 0, r + 1, c // 2), ((r, c + 1), 1, r + 1, c // 2), ((r - 1, c + 1), 2, r, c // 2)):
+            if w in wi:
+                K[bi[(r, c)], wi[w]] = 1.0
+                edges.append(((r, c), w, kind, vi, vj))
+    Kinv = np.linalg.inv(K)
+    P = np.zeros((3, N, N))
+    for b, w, kind, vi, vj in edges:
+        P[kind, vi, vj] = Kinv[wi[w], bi[b]]
+    return P
+
+
+def lozenge_indicators(t):
+    n = int(np.sqrt(t.size))
+    x = np.asarray(t).reshape(n, n)
+    return np.stack([(x & 1) != 0, (x & 2) != 0, (x & 8) != 0]).astype(np.float64)
+
+
+@pytest.mark.parametrize("side", [3, 8])
+def test_lozenge_dimers_of_extremal_tilings_cover_each_triangle_once(rt, side):
+    L = rt.LozengeTiler
+    d = L.Hexagon(side)
+    M = int(np.sqrt(d.size // 2))
+    F = d.reshape(M, 2 * M)
+    p = lozenge_dimer_probs(d)
+    assert p.sum() == pytest.approx(F.sum() / 2, rel=1e-9)  # lozenges per tiling
+    for t in (L.MaxTiling(d), L.MinTiling(d)):
+        cover = np.zeros((M, 2 * M), int)
+        x = lozenge_indicators(t)
+        for kind in range(3):
+            for i, j in np.argwhere(x[kind] > 0):
+                pair = {0: ((i - 1, 2 * j - 1), (i - 1, 2 * j)), 1: ((i - 1, 2 * j), (i - 1, 2 * j + 1)),
+                        2: ((i - 1, 2 * j + 1), (i, 2 * j))}[kind]
+                for r, c in pair:
+                    cover[r, c] += 1
+                assert p[kind, i, j] > 0  # every placed lozenge is an edge of the exact model
+        assert np.array_equal(cover, F)
+
+
+@pytest.mark.gpu
+def test_lozenge_cftp_edge_frequencies_match_exact_probabilities(rt):
+    from scipy.stats import binom
+
+    L = rt.LozengeTiler
+    side, samples = 12, 8000
+    d = L.Hexagon(side)
+    tmax, tmin = L.MaxTiling(d), L.MinTiling(d)
+    jobs = [{"model": "lozenge", "tmax": tmax, "tmin": tmin, "seed": 52000 + k, "stream": k, "first_steps": 64,
+             "max_attempts": 16} for k in range(samples)]
+    outs, attempts, _ = rt.cftp_batch(jobs)
+    assert min(attempts) > 0
+    p = lozenge_dimer_probs(d)
+    counts = np.zeros_like(p)
+    for o in outs:
+        counts += lozenge_indicators(o)
+    live = (p > 1e-12) & (p < 1 - 1e-12)
+    k, q = counts[live].astype(np.int64), p[live]
+    tail = 2 * np.minimum(binom.cdf(k, samples, q), binom.sf(k - 1, samples, q))
+    assert live.sum() > 300
+    assert tail.min() * live.sum() > 1e-3, (float(tail.min()), int(live.sum()))
+    assert np.array_equal(counts[~live] / samples, np.round(p[~live]))
