@@ -209,6 +209,26 @@ def test_inconsistent_tiling_takes_the_per_half_sweep_path(rt, orc):
         rt.DominoTiler(rule="plain", engine=2).Walk(t0.copy(), 3, 4)
 
 
+@pytest.mark.gpu
+@pytest.mark.parametrize("rng", ["tinymt", "fast"])
+def test_arbitrary_edge_masks_sweep_as_the_reference(rt, orc, rng):
+    """Every site holding a random edge mask (no tiling at all): the per-half-sweep kernels
+    still rotate and rebuild exactly as the reference's kernels do, edges of the array
+    included."""
+    rnd = np.random.default_rng(2024)
+    for n, steps, seed in ((14, 9, 3), (30, 40, 77), (66, 25, 5)):
+        t0 = rnd.integers(0, 16, size=n * n).astype(np.int32)
+        g = t0.copy()
+        tiler = rt.DominoTiler(rule="cftp", rng=rng, fast_stream=2, engine=1)
+        tiler.Walk(g, steps, seed)
+        o = t0.copy()
+        if rng == "tinymt":
+            orc.walk_tinymt(o, n, steps, seed, rule=1)
+        else:
+            orc.walk_fast(o, n, 0, steps, seed, 2, rule=1)
+        assert np.array_equal(g, o), (rng, n)
+
+
 def test_full_size_order_1024_properties(rt):
     """Longer runs at full size: still a valid tiling of the same domain, height function
     between those of the min and max tilings, and the coupled chains stay ordered."""
