@@ -151,3 +151,22 @@ def test_lozenge_cftp_is_uniform_over_enumerated_tilings(rt, rng, n, samples):
         counts[seen[out.reshape(N, N).tobytes()]] += 1
     p = chi_square_p(counts, np.full(len(tilings), 1.0 / len(tilings)))
     assert p > 1e-3, p
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("mode", ["tinymt", "fast"])
+def test_arbitrary_edge_masks_sweep_as_the_reference(rt, orc, mode):
+    """Every vertex holding a random six-bit edge mask (no tiling at all): the per-step
+    kernels (rotation, then the word-parallel rebuild of the two other colours) still do
+    exactly what the reference's kernels do, array edges included."""
+    rnd = np.random.default_rng(99)
+    for n, steps, seed in ((12, 7, 1), (33, 40, 8), (66, 25, 3)):
+        t0 = rnd.integers(0, 64, size=n * n).astype(np.int32)
+        a = t0.copy()
+        rt.LozengeTiler(rng=mode, fast_stream=4).Walk(a, steps, seed)
+        b = t0.copy()
+        if mode == "tinymt":
+            orc.lz_walk_tinymt(b, n, steps, seed)
+        else:
+            orc.lz_walk_fast(b, n, 0, steps, seed, 4)
+        assert np.array_equal(a, b), (mode, n)
