@@ -55,11 +55,20 @@ struct SvLaunch {
   int P, n;
   int px, py, r_lo, words, rows;  // the class being updated and its interior extent
   int k_lo, k_hi;
-  uint32_t T[9];
+  uint32_t leaf[32][9];  // leaf[j][m]: all ones where bit j of threshold T[m] is set (sv_leaves)
   uint64_t seed;
   uint32_t stream;
   int64_t s;
 };
+
+// Per-plane leaf words of the nine heat-bath thresholds: leaf[j][m] is all ones where bit j
+// of T[m] is set, so that a point's threshold bit in plane j is the OR over the nine
+// vertex-weight classes m of (class mask & leaf[j][m]) - one three-input logic operation
+// each, with the leaf a constant operand once the plane loop is unrolled.
+inline void sv_leaves(const uint32_t* T, uint32_t (&leaf)[32][9]) {
+  for (int j = 0; j < 32; ++j)
+    for (int m = 0; m < 9; ++m) leaf[j][m] = ((T[m] >> j) & 1u) ? 0xffffffffu : 0u;
+}
 
 __device__ __forceinline__ uint32_t west_of(const uint32_t* row, int idx, int px) {
   return px ? row[idx] : __funnelshift_l(row[idx - 1], row[idx], 1);
@@ -84,7 +93,7 @@ __device__ __forceinline__ uint4 sv_block(uint32_t w, uint32_t r, int q, uint32_
 // Blocks q < NPRE of the draws arrive precomputed in pre[] (they do not depend on the state).
 template <int NCH, int NPRE = 0>
 __device__ __forceinline__ void sv_update_word(const SvRows (&rows)[NCH], int idx, int px, int py, uint32_t imask,
-                                               uint32_t w, uint32_t r, const uint32_t (&T)[9], uint64_t seed,
+                                               uint32_t w, uint32_t r, const uint32_t (&leaf)[32][9], uint64_t seed,
                                                uint32_t c2, uint32_t c3, const uint4* pre = nullptr) {
   uint32_t f[NCH], flip[NCH], sup[NCH], mk[NCH][9], lt[NCH], und[NCH];
   uint32_t any = 0;
@@ -121,9 +130,9 @@ __device__ __forceinline__ void sv_update_word(const SvRows (&rows)[NCH], int id
       const int j = 31 - (4 * q + t);
 #pragma unroll
       for (int c = 0; c < NCH; ++c) {
-        uint32_t Tj = 0;
+        uint32_t Tj = 0;  // bit j of each point's threshold
 #pragma unroll
-        for (int m = 0; m < 9; ++m) Tj |= ((T[m] >> j) & 1u) ? mk[c][m] : 0u;
+        for (int m = 0; m < 9; ++m) Tj |= mk[c][m] & leaf[j][m];
         lt[c] |= und[c] & ~planes[t] & Tj;
         und[c] &= ~(planes[t] ^ Tj);
       }
@@ -158,7 +167,7 @@ __global__ void __launch_bounds__(128) k_sv_sub(SvLaunch L) {
                            chain + (size_t)(cls ^ 1) * L.class_words + (size_t)r * L.P, V + (size_t)rn * L.P,
                            V + (size_t)rs * L.P, D + (size_t)rn * L.P, D + (size_t)rs * L.P}};
   const uint32_t c2 = (uint32_t)(uint64_t)L.s, c3 = ((uint32_t)((uint64_t)L.s >> 32) & 0xffffu) | (L.stream << 16);
-  sv_update_word<1>(rows, w + 1, px, py, imask, (uint32_t)w, (uint32_t)r, L.T, L.seed, c2, c3);
+  sv_update_word<1>(rows, w + 1, px, py, imask, (uint32_t)w, (uint32_t)r, L.leaf, L.seed, c2, c3);
 }
 
 // Resident engine: one thread-block cluster holds NCH chains in shared memory, CTA `rank`
@@ -169,7 +178,7 @@ struct SvClusterArgs {
   uint32_t* base;
   size_t chain_words, class_words;
   int P, n, R, rpc;
-  uint32_t T[9];
+  uint32_t leaf[32][9];  // as SvLaunch::leaf
   uint64_t seed;
   uint32_t stream;
   int64_t s0, count;
@@ -246,9 +255,9 @@ __global__ void __launch_bounds__(sv_cluster_max_threads<NCH>()) k_sv_cluster(Sv
         rows[c] = {row(c, u.cls, r), row(c, u.cls ^ 1, r), row(c, u.cls ^ 2, rn), row(c, u.cls ^ 2, rs),
                    row(c, u.cls ^ 3, rn), row(c, u.cls ^ 3, rs)};
       if (it == tid)
-        sv_update_word<NCH, kPre>(rows, w + 1, u.px, u.py, imask, (uint32_t)w, (uint32_t)r, A.T, A.seed, u.c2, u.c3, pre);
+        sv_update_word<NCH, kPre>(rows, w + 1, u.px, u.py, imask, (uint32_t)w, (uint32_t)r, A.leaf, A.seed, u.c2, u.c3, pre);
       else
-        sv_update_word<NCH>(rows, w + 1, u.px, u.py, imask, (uint32_t)w, (uint32_t)r, A.T, A.seed, u.c2, u.c3);
+        sv_update_word<NCH>(rows, w + 1, u.px, u.py, imask, (uint32_t)w, (uint32_t)r, A.leaf, A.seed, u.c2, u.c3);
     }
     // the next sub-sweep's first draws do not depend on the state: compute them while the
     // other CTAs of the cluster reach the barrier
@@ -450,7 +459,7 @@ int64_t sv_run(uint32_t* dev, int chains, const SvGeom& G, const std::vector<uin
     A.n = G.n;
     A.R = G.R;
     A.rpc = plan.rpc;
-    std::memcpy(A.T, T.data(), sizeof A.T);
+    sv_leaves(T.data(), A.leaf);
     A.seed = seed;
     A.stream = stream;
     cudaLaunchConfig_t cfg = {};
@@ -483,7 +492,7 @@ int64_t sv_run(uint32_t* dev, int chains, const SvGeom& G, const std::vector<uin
   L.class_words = G.class_words;
   L.P = G.P;
   L.n = G.n;
-  std::memcpy(L.T, T.data(), sizeof L.T);
+  sv_leaves(T.data(), L.leaf);
   L.seed = seed;
   L.stream = stream;
   for (int64_t s = s0; s < s0 + count; ++s) {
