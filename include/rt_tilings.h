@@ -49,6 +49,10 @@ typedef int32_t rt_status;
                            (src/TinyMT/tinymt32.clh, dominokernel.cl:4-40): bit-exact with it */
 #define RT_RNG_FAST 1   /* counter-based Philox4x32-10 keyed by (seed, stream, half-sweep,
                            site); no generator state in memory */
+#define RT_RNG_MTGP 2   /* cuRAND MTGP32, one generator per 8 x 8 block of sites seeded
+                           seed + block, the reference's CUDA path (DominoTiler.cpp:51-66,
+                           dominokernel*.cu): domino walks, epochs and CFTP through the
+                           per-half-sweep kernels; the same draws as the reference's build */
 
 /* Flip rules: the reference picks one by compiling one of four kernel files. */
 #define RT_DOMINO_PLAIN 0            /* src/Domino/dominokernel.cl:4-18 (propose 0.8) */
@@ -111,9 +115,11 @@ RT_API rt_status rt_domino_tiling_to_domain(const int32_t* tiling, int32_t n_sid
 /* ---- domino sweeps (GPU) ---------------------------------------------------------------- */
 
 /* DominoTiler::Walk(tiling&, long steps, long seed) (DominoTiler.cpp:18-122).  One step is
-   one half-sweep: a colour drawn from mt19937(seed) (TinyMT mode; the generators are seeded
-   with the first draw, as on the reference's OpenCL path) or alternating black/white
-   (fast mode), a flip attempt at every site of that colour, then the other colour rebuilt.
+   one half-sweep: a colour drawn from mt19937(seed) (TinyMT mode: the generators are seeded
+   with the first draw, as on the reference's OpenCL path; MTGP mode: block generator k is
+   seeded seed + k and the colours start with the first draw, as on its CUDA path) or
+   alternating black/white (fast mode), a flip attempt at every site of that colour, then
+   the other colour rebuilt.
    n_side = N must be even and >= 6; the outermost two rings must be empty (padded). */
 RT_API rt_status rt_domino_walk(int32_t* tiling, int32_t n_side, int64_t steps, int64_t seed,
                                 const rt_walk_opts* opts);
@@ -477,9 +483,17 @@ RT_API rt_status rt_dm_sweep_noalloc(uint8_t* dev_chains, void* dev_generators, 
    The acceptance intervals a rule compiles to: for c = (row & 1) | (colour << 1),
    out16[4c .. 4c+3] = {lo_up, width_up, lo_down, width_down}; a site in state 3 flips to 12
    when (u - lo_up) < width_up, a site in state 12 flips to 3 when (u - lo_down) < width_down,
-   u the 23-bit TinyMT draw or the 32-bit fast draw.  No reference counterpart: the
-   reference evaluates its float thresholds per draw (dominokernel*.cl). */
+   u the 23-bit TinyMT draw, the 32-bit fast draw or the bit pattern of the MTGP mode's float
+   draw.  No reference counterpart: the reference evaluates its float thresholds per draw
+   (dominokernel*.cl, dominokernel*.cu). */
 RT_API rt_status rt_domino_rule_table(int32_t rule, int32_t rng_mode, double a, double b, uint32_t* out16);
+
+/* The float draws RT_RNG_MTGP makes for the first `launches` half-sweeps of a domino walk on
+   an n_side tiling whose block generators are seeded seed + k: out[h][i-1][m-1] (launches x
+   (n_side-2) x (n_side/2-2) floats, host memory) is the draw of candidate site (i, m) at
+   half-sweep h, the value the reference's rotate kernel receives from curand_uniform at that
+   site (dominokernel.cu:14-15). */
+RT_API rt_status rt_domino_mtgp_draws(int32_t n_side, int64_t seed, int64_t launches, float* out);
 
 #ifdef __cplusplus
 }

@@ -12,7 +12,8 @@
 //     it is not called, every generator uses the TinyMT32 jump parameters;
 //   * failures throw rt::Error instead of printing and calling exit();
 //   * the OpenCL constructors (context, queue, devices, kernel source) are replaced by
-//     default construction; LoadTinyMT / LoadMTGP are accepted where the reference has them.
+//     default construction; LoadTinyMT / LoadMTGP are accepted where the reference has them
+//     (DominoTiler::LoadMTGP selects the cuRAND MTGP32 mode; the other tilers ignore it).
 // Header-only; link with -lrt_tilings.
 #ifndef RT_TILINGS_HPP_
 #define RT_TILINGS_HPP_
@@ -83,9 +84,10 @@ class DominoTiler {
     opts_.tinymt_params_count = size;
   }
 
-  // Present for source compatibility with the reference's CUDA build; the MTGP32
-  // generators it loads are not used by this library (see rt_tilings.h, RNG modes).
-  void LoadMTGP() {}
+  // DominoTiler::LoadMTGP (DominoTiler.cpp:239-242): as in the reference's CUDA build, the
+  // walks then draw from cuRAND MTGP32 generators, one per 8 x 8 block of sites seeded
+  // seed + block (RT_RNG_MTGP), so they see the reference's random stream.
+  void LoadMTGP() { opts_.rng_mode = RT_RNG_MTGP; }
 
   void Walk(tiling& t, long steps, long seed) {
     check(rt_domino_walk(t.data(), side_of(t), steps, seed, &opts_));

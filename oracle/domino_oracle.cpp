@@ -13,6 +13,11 @@
 //     InitTinyMT dominokernel.cl:33-40; host loop DominoTiler.cpp:50-97 (single walk: the
 //     generators are seeded with the first mt19937 draw) and :125-209 (epochs: seeded with
 //     seeds[k] itself)
+//   * the sweep as the CUDA path runs it, given its MTGP32 draws: rotate kernels
+//     dominokernel.cu:8-24, dominokernelCFTP.cu:14-33, dominokerneltwoperiodic.cu:11-43,
+//     dominokernelCFTPtwoperiodic.cu:18-47; host loop DominoTiler.cpp:51-97 (colours from
+//     the first mt19937 draw) and :155-190 (epochs).  cuRAND's MTGP32 generator itself is
+//     library code and is not restated here: its draws come in as data.
 //   * the CFTP driver    Examples/AztecDiamondCftpEx.cpp:51-77
 // plus the library's own counter-based fast mode (no reference counterpart), stated here
 // as the checker of its CUDA kernels.
@@ -330,6 +335,28 @@ inline uint8_t rotate_cl(uint8_t e, float rd, int variant, int i, int t, double 
   return e;
 }
 
+// The same decision as the reference's CUDA kernels make it, rd the float from cuRAND's
+// MTGP32 (dominokernel.cu:19-22, dominokernelCFTP.cu:26-31, dominokerneltwoperiodic.cu:23-40,
+// dominokernelCFTPtwoperiodic.cu:30-46).  Three rules read as the .cl kernels do; in the
+// two-periodic rule the CUDA kernel compares the draw with the double PROB_PROPOSE and
+// divides in double, where the .cl kernel uses a float propose.
+inline uint8_t rotate_cu(uint8_t e, float rd, int variant, int i, int t, double a, double b) {
+  if (variant != kTwoPeriodic) return rotate_cl(e, rd, variant, i, t, a, b);
+  if ((double)rd < 0.8) {
+    float thr = (double)rd / 0.8;
+    if (e == 3) {
+      float wI = b * b * ((i + t + 1) % 2) + a * a * ((i + t) % 2);
+      float wF = a * a * (i % 2) + b * b * ((i + 1) % 2);
+      if (wF / wI > thr) return 12;
+    } else if (e == 12) {
+      float wI = a * a * (i % 2) + b * b * ((i + 1) % 2);
+      float wF = b * b * ((i + t + 1) % 2) + a * a * ((i + t) % 2);
+      if (wF / wI > thr) return 3;
+    }
+  }
+  return e;
+}
+
 // The library's fast-mode acceptance rule (its own specification): the same move
 // probabilities as the reference kernels, resolved against a 32-bit uniform u by
 // u < ceil(p * 2^32) (proposal-only variants) or, for the monotone CFTP variants, by
@@ -497,6 +524,32 @@ void run_fast(SweepJob& J, uint64_t seed, uint32_t stream, int64_t h0, int64_t s
       sync();
     }
   });
+}
+
+// The reference's CUDA path with its draws supplied: step s takes draws[s][i-1][j-1] for
+// candidate (i, j) (the curand_uniform value of that thread, dominokernel.cu:14-15), rotates
+// colour[s] as the CUDA kernels decide, then rebuilds the other colour.
+void run_draws(SweepJob& J, const float* draws, const std::vector<uint8_t>& colour) {
+  const size_t per = (size_t)J.rows * J.cols;
+  for (size_t s = 0; s < colour.size(); ++s) {
+    const int t = colour[s];
+    const float* d = draws + s * per;
+    for (int i = 1; i <= J.rows; ++i)
+      for (int j = 1; j <= J.cols; ++j) {
+        const float rd = d[(size_t)(i - 1) * J.cols + (j - 1)];
+        for (Chain* c : J.chains) {
+          uint8_t* A = t ? c->B.data() : c->W.data();
+          uint8_t& e = A[(size_t)i * J.H + j];
+          e = rotate_cu(e, rd, J.variant, i, t, J.a, J.b);
+        }
+      }
+    for (Chain* c : J.chains) {
+      const uint8_t* A = t ? c->B.data() : c->W.data();
+      uint8_t* P = t ? c->W.data() : c->B.data();
+      for (int i = 1; i <= J.rows; ++i)
+        for (int j = 1; j <= J.cols; ++j) P[(size_t)i * J.H + j] = update_site(A, J.H, i, j, t);
+    }
+  }
 }
 
 void init_generators(std::vector<oracle::TinyMT32>& g, size_t count, uint32_t seed, const uint32_t* params,
@@ -669,6 +722,53 @@ int orc_dm_cftp_tinymt(const int* tmax, const int* tmin, int N, long driver_seed
   }
   if (total_steps) *total_steps = total;
   return -1;
+}
+
+// DominoTiler::Walk(t, steps, seed), CUDA path, with the MTGP32 draws supplied (steps x
+// (N-2) x (N/2-2) floats): colours from mt19937(seed) starting with its first draw
+// (DominoTiler.cpp:51, 69; no draw is spent on seeding, unlike the OpenCL path).
+int orc_dm_walk_draws(int* t, int N, const float* draws, long steps, long seed, int variant, double a, double b) {
+  if (N % 2 || N < 6) return -1;
+  Chain c;
+  split_tiling(t, N, c);
+  SweepJob J = make_job(N, variant, a, b);
+  J.chains = {&c};
+  std::mt19937 mt((uint32_t)seed);
+  run_draws(J, draws, colour_stream(mt, steps));
+  merge_tiling(c, t);
+  return 0;
+}
+
+// DominoTiler::Walk(t, steps[], seeds[]), CUDA path (DominoTiler.cpp:155-190): epoch k takes
+// its colours from mt19937(seeds[k]) and its draws from the next steps[k] blocks of draws.
+int orc_dm_walk_epochs_draws(int* t, int N, const float* draws, const long* steps, const long* seeds, int nepochs,
+                             int variant, double a, double b) {
+  if (N % 2 || N < 6) return -1;
+  Chain c;
+  split_tiling(t, N, c);
+  SweepJob J = make_job(N, variant, a, b);
+  J.chains = {&c};
+  const size_t per = (size_t)J.rows * J.cols;
+  size_t off = 0;
+  for (int k = 0; k < nepochs; ++k) {
+    std::mt19937 mt((uint32_t)seeds[k]);
+    run_draws(J, draws + off * per, colour_stream(mt, steps[k]));
+    off += (size_t)steps[k];
+  }
+  merge_tiling(c, t);
+  return 0;
+}
+
+// The CUDA kernels' decision for n draws of one (state, variant, row, colour) case.
+void orc_dm_rotate_cuda_many(const float* rd, long n, int e, int variant, int i, int t, double a, double b,
+                             uint8_t* out) {
+  for (long k = 0; k < n; ++k) out[k] = rotate_cu((uint8_t)e, rd[k], variant, i, t, a, b);
+}
+
+// n outputs of std::mt19937(seed) (the drivers' seed and colour streams).
+void orc_mt19937(uint32_t seed, long n, uint32_t* out) {
+  std::mt19937 mt(seed);
+  for (long k = 0; k < n; ++k) out[k] = (uint32_t)mt();
 }
 
 // Fast mode walk over half-sweeps [h0, h0 + steps).

@@ -34,7 +34,7 @@ RT_ERR_NOT_COALESCED = 6
 RT_ERR_BUFFER_TOO_SMALL = 7
 RT_ERR_BUSY = 8
 
-RNG_MODES = {"tinymt": 0, "fast": 1}
+RNG_MODES = {"tinymt": 0, "fast": 1, "mtgp": 2}
 RT_LOZENGE_UNIFORM, RT_LOZENGE_Q = 0, 1
 DOMINO_RULES = {"plain": 0, "cftp": 1, "twoperiodic": 2, "cftp_twoperiodic": 3}
 
@@ -136,6 +136,7 @@ _SIGNATURES = {
     "rt_cftp": (C.c_int32, [C.c_int32, _P, _P, C.c_int32, C.c_int64, C.c_int64, C.c_int32, C.c_int32, _P, _P, _P,
                             _P]),
     "rt_domino_rule_table": (C.c_int32, [C.c_int32, C.c_int32, C.c_double, C.c_double, _P]),
+    "rt_domino_mtgp_draws": (C.c_int32, [C.c_int32, C.c_int64, C.c_int64, _P]),
     "rt_dm_sweep_noalloc": (C.c_int32, [_P, _P, C.c_int32, C.c_int32, _P, C.c_int64, C.c_uint64, C.c_int64, _P]),
     "rt_cftp_batch": (C.c_int32, [_P, C.c_int32, _P, _P]),
     "rt_server_create": (C.c_int32, [_P, _P]),
@@ -255,7 +256,8 @@ class DominoTiler:
     ``rule`` selects what the reference selects by compiling one of its kernel files:
     'plain' (dominokernel), 'cftp' (dominokernelCFTP), 'twoperiodic', 'cftp_twoperiodic';
     ``a``, ``b`` are the two-periodic weights the reference hard-codes (0.7, 1.0).
-    ``rng`` is 'tinymt' (bit-exact with the reference's OpenCL path) or 'fast' (Philox).
+    ``rng`` is 'tinymt' (bit-exact with the reference's OpenCL path), 'mtgp' (cuRAND MTGP32
+    as the reference's CUDA path draws it; also selected by LoadMTGP) or 'fast' (Philox).
     """
 
     def __init__(self, rule: str = "plain", rng: str = "tinymt", a: float = 0.7, b: float = 1.0,
@@ -278,6 +280,11 @@ class DominoTiler:
             self._params = read_tinymt_params(params, size)
         else:
             self._params = np.ascontiguousarray(np.asarray(params, dtype=np.uint32).reshape(-1, 3))
+
+    def LoadMTGP(self) -> None:
+        """DominoTiler::LoadMTGP (DominoTiler.cpp:239-242): walks draw from cuRAND MTGP32, one
+        generator per 8 x 8 block of sites seeded seed + block, as the reference's CUDA build."""
+        self.rng = "mtgp"
 
     def opts(self, cuda_stream: int | None = None) -> _WalkOpts:
         o = _WalkOpts()
@@ -937,6 +944,17 @@ def mt19937_colours(seed: int, steps: int, skip: int = 0) -> np.ndarray:
     return (mt19937_draws(seed, skip + steps)[skip:] % 2).astype(np.uint8)
 
 
+def mtgp_draws(n_side: int, seed: int, launches: int) -> np.ndarray:
+    """The float draws of the 'mtgp' mode for the first ``launches`` half-sweeps of a domino
+    walk seeded ``seed`` on an n_side tiling: array (launches, n_side - 2, n_side // 2 - 2),
+    entry [h, i-1, m-1] the curand_uniform value candidate site (i, m) receives at
+    half-sweep h (dominokernel.cu:14-15)."""
+    n = int(n_side)
+    out = np.zeros((int(launches), n - 2, n // 2 - 2), np.float32)
+    _check(lib().rt_domino_mtgp_draws(n, int(seed), int(launches), _ptr(out)))
+    return out
+
+
 def SaveMatrix(a, path, rows: int | None = None, cols: int | None = None) -> None:
     """The reference's SaveMatrix (src/common/common.cpp:84-128): without rows/cols the
     square overload (floor(sqrt(size))^2 values)."""
@@ -976,4 +994,4 @@ def mt19937_draws(seed: int, count: int) -> np.ndarray:
 
 
 __all__ = ["DominoTiler", "DominoSampler", "LozengeTiler", "RectTriangleTiler", "SixVertexTiler", "TriangleDimerTiler", "cftp_batch", "Server", "RTError", "lib", "read_tinymt_params", "mt19937_colours",
-           "mt19937_draws", "CftpStats"]
+           "mt19937_draws", "mtgp_draws", "CftpStats"]

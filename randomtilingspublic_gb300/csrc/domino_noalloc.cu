@@ -89,6 +89,8 @@ extern "C" RT_API rt_status rt_dm_sweep_noalloc(uint8_t* dev_chains, void* dev_g
     return fail(RT_ERR_INVALID_ARGUMENT, "sweep_noalloc: steps must be in [0, 65536] per call");
   if (!dev_chains || ((uintptr_t)dev_chains & 15))
     return fail(RT_ERR_INVALID_ARGUMENT, "sweep_noalloc: chains must be a 16-byte aligned device pointer");
+  if (o.rng_mode != RT_RNG_TINYMT && o.rng_mode != RT_RNG_FAST)
+    return fail(RT_ERR_INVALID_ARGUMENT, "sweep_noalloc: TinyMT or fast mode only");
   if (o.rng_mode == RT_RNG_TINYMT && (!dev_generators || ((uintptr_t)dev_generators & 15) || (steps > 0 && !colours)))
     return fail(RT_ERR_INVALID_ARGUMENT, "sweep_noalloc: TinyMT mode needs generators (16-byte aligned) and colours");
   if (o.rng_mode == RT_RNG_FAST && (o.fast_stream >= 65536u || h0 < -((int64_t)1 << 47) || h0 + steps > ((int64_t)1 << 47)))

@@ -82,12 +82,42 @@ uint8_t dm_rule_reference(uint8_t e, uint32_t u23, int rule, int i, int t, doubl
   return e;
 }
 
+uint8_t dm_rule_reference_cuda(uint8_t e, float rd, int rule, int i, int t, double a, double b) {
+  switch (rule) {
+    case RT_DOMINO_PLAIN:  // dominokernel.cu:19-22 (PROB_PROPOSE 0.8, a double)
+      if ((double)rd < .8) return e == 3 ? 12 : (e == 12 ? 3 : e);
+      return e;
+    case RT_DOMINO_CFTP:  // dominokernelCFTP.cu:26-31
+      if ((double)rd < 0.5) return e == 3 ? 12 : e;
+      return e == 12 ? 3 : e;
+    case RT_DOMINO_TWOPERIODIC: {  // dominokerneltwoperiodic.cu:23-40: compare and divide in double
+      if ((double)rd < .8) {
+        float threshold = (double)rd / .8;
+        if (e == 3) return ratio_up(i, t, a, b) > threshold ? 12 : 3;
+        if (e == 12) return ratio_dn(i, t, a, b) > threshold ? 3 : 12;
+      }
+      return e;
+    }
+    case RT_DOMINO_CFTP_TWOPERIODIC: {  // dominokernelCFTPtwoperiodic.cu:30-46
+      if ((double)rd < 0.5) {
+        float threshold = (double)rd / 0.5;
+        if (e == 3) return ratio_up(i, t, a, b) > threshold ? 12 : 3;
+      } else {
+        float threshold = ((double)rd - 0.5) / 0.5;
+        if (e == 12) return ratio_dn(i, t, a, b) > threshold ? 3 : 12;
+      }
+      return e;
+    }
+  }
+  return e;
+}
+
 bool dm_rule_build(int rule, int rng_mode, double a, double b, DmRule* out, const char** err) {
   if (rule < RT_DOMINO_PLAIN || rule > RT_DOMINO_CFTP_TWOPERIODIC) {
     *err = "unknown domino rule";
     return false;
   }
-  if (rng_mode != RT_RNG_TINYMT && rng_mode != RT_RNG_FAST) {
+  if (rng_mode != RT_RNG_TINYMT && rng_mode != RT_RNG_FAST && rng_mode != RT_RNG_MTGP) {
     *err = "unknown rng mode";
     return false;
   }
@@ -101,7 +131,21 @@ bool dm_rule_build(int rule, int rng_mode, double a, double b, DmRule* out, cons
     const int ip = c & 1, t = c >> 1;
     const int i = 2 + ip;  // any row of that parity
     uint32_t lo_up = 0, w_up, lo_dn, w_dn;
-    if (rng_mode == RT_RNG_TINYMT) {
+    if (rng_mode == RT_RNG_MTGP) {
+      // MTGP mode: u is the bit pattern of the float draw in (0, 1], and positive floats
+      // order as their bit patterns, so each move's set of draws is again an interval (a
+      // prefix of [0, 1], or of [0.5, 1] for the down move of the monotone rules).
+      const uint32_t U = 0x3f800001u, half = 0x3f000000u;  // bits of 1.0f plus one; of 0.5f
+      auto rd_of = [](uint32_t u) {
+        float f;
+        std::memcpy(&f, &u, sizeof f);
+        return f;
+      };
+      w_up = first_reject(0, U, [&](uint32_t u) { return dm_rule_reference_cuda(3, rd_of(u), rule, i, t, a, b) == 12; });
+      lo_dn = monotone ? half : 0;
+      w_dn = first_reject(lo_dn, U, [&](uint32_t u) { return dm_rule_reference_cuda(12, rd_of(u), rule, i, t, a, b) == 3; }) -
+             lo_dn;
+    } else if (rng_mode == RT_RNG_TINYMT) {
       const uint32_t U = 1u << 23, half = 1u << 22;
       w_up = first_reject(0, U, [&](uint32_t u) { return dm_rule_reference(3, u, rule, i, t, a, b) == 12; });
       lo_dn = monotone ? half : 0;

@@ -5,7 +5,7 @@
 // that depends only on the row parity of the site and the colour t being rotated.  For all
 // four rules that set is one interval of the raw generator output, so the kernels test
 // (u - lo) < width on integers.  The host derives the intervals from the reference's own
-// float expressions (TinyMT mode) or from the fast mode's stated probabilities.
+// float expressions (TinyMT and MTGP modes) or from the fast mode's stated probabilities.
 #pragma once
 #include <cstdint>
 
@@ -22,5 +22,10 @@ bool dm_rule_build(int rule, int rng_mode, double a, double b, DmRule* out, cons
 // Reference decision for one site (TinyMT scale, u23 in [0, 2^23)); used to derive and to
 // check the intervals.  Returns the new state.
 uint8_t dm_rule_reference(uint8_t e, uint32_t u23, int rule, int i, int t, double a, double b);
+
+// The same decision as the reference's CUDA kernels make it (src/Domino/dominokernel*.cu,
+// float draw rd from cuRAND's MTGP32); it differs from the OpenCL kernels only in the
+// two-periodic rule, which compares and divides in double there.
+uint8_t dm_rule_reference_cuda(uint8_t e, float rd, int rule, int i, int t, double a, double b);
 
 }  // namespace rt

@@ -29,13 +29,6 @@ namespace rt {
 // Kernels
 // -----------------------------------------------------------------------------------------
 
-__device__ __forceinline__ uint8_t dm_flip(uint32_t e, uint32_t u, uint32_t lo_up, uint32_t w_up, uint32_t lo_dn,
-                                           uint32_t w_dn) {
-  if (e == 3u) return (u - lo_up) < w_up ? 12 : 3;
-  if (e == 12u) return (u - lo_dn) < w_dn ? 3 : 12;
-  return (uint8_t)e;
-}
-
 __global__ void k_tmt_seed(uint4* st, const uint4* params, int64_t count, uint32_t seed) {
   int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= count) return;
@@ -241,7 +234,7 @@ __global__ void k_diff(DmView v, int a, int b, unsigned long long* out) {
 
 DmSampler::~DmSampler() {
   persist.reset();  // frees its plan buffers on the stream before the stream goes
-  for (void* p : {(void*)tmt, (void*)tmt_params, (void*)base, (void*)scratch, (void*)counter, (void*)d_scan,
+  for (void* p : {(void*)tmt, (void*)tmt_params, mtgp, (void*)base, (void*)scratch, (void*)counter, (void*)d_scan,
                   (void*)d_cand})
     dev_free(p, stream);
   for (void* p : {(void*)d_dom, (void*)d_cls, (void*)d_h, (void*)d_hflags})
@@ -327,6 +320,9 @@ rt_status DmSampler::create(int n_side, int n_chains, const rt_walk_opts& o, std
       RT_CUDA(cudaMemcpyAsync(s->tmt_params, p.data(), cells * sizeof(uint4), cudaMemcpyHostToDevice, s->stream));
       RT_CUDA(cudaStreamSynchronize(s->stream));
     }
+  } else if (o.rng_mode == RT_RNG_MTGP) {
+    if (o.engine == 2) return fail(RT_ERR_INVALID_ARGUMENT, "MTGP mode runs on the per-half-sweep kernels only");
+    if (rt_status st = dev_alloc(&s->mtgp, mtgp_state_bytes(s->N), s->stream)) return st;
   }
   *out = std::move(s);
   return RT_OK;
@@ -400,18 +396,38 @@ rt_status DmSampler::copy_chain(int dst, int src) {
   return RT_OK;
 }
 
-rt_status DmSampler::seed(uint32_t s) {
-  if (opts.rng_mode != RT_RNG_TINYMT) return fail(RT_ERR_INVALID_ARGUMENT, "seed: sampler is not in TinyMT mode");
+rt_status DmSampler::seed(int64_t s) {
+  if (opts.rng_mode == RT_RNG_MTGP) {
+    if (rt_status st = mtgp_seed(mtgp, N, s, stream)) return st;
+    mtgp_seeded = true;
+    return RT_OK;
+  }
+  if (opts.rng_mode != RT_RNG_TINYMT) return fail(RT_ERR_INVALID_ARGUMENT, "seed: sampler is not in TinyMT or MTGP mode");
   const int64_t cells = (int64_t)(N - 2) * (N / 2 - 2);
-  k_tmt_seed<<<(unsigned)((cells + 255) / 256), 256, 0, stream>>>(tmt, tmt_params, cells, s);
+  k_tmt_seed<<<(unsigned)((cells + 255) / 256), 256, 0, stream>>>(tmt, tmt_params, cells, (uint32_t)s);
   launches++;
   return check_launch();
 }
 
 rt_status DmSampler::run(const uint8_t* colours, int64_t steps) {
-  if (opts.rng_mode != RT_RNG_TINYMT) return fail(RT_ERR_INVALID_ARGUMENT, "run: sampler is not in TinyMT mode");
+  if (opts.rng_mode == RT_RNG_FAST) return fail(RT_ERR_INVALID_ARGUMENT, "run: sampler is in fast mode (run_fast)");
   if (steps < 0 || (steps > 0 && !colours)) return fail(RT_ERR_INVALID_ARGUMENT, "run: bad colours / steps");
   if (steps == 0) return RT_OK;
+  if (opts.rng_mode == RT_RNG_MTGP) {
+    // An MTGP state holds a pointer to its parameters: none exists before the first seed.
+    if (!mtgp_seeded) return fail(RT_ERR_INVALID_ARGUMENT, "run: MTGP generators not seeded");
+    last_engine = 1;
+    DmView v = view();
+    const dim3 blk_w(32, 8), grd_w((v.P / 4 + 31) / 32, (v.rows + 7) / 8);
+    for (int64_t q = 0; q < steps; ++q) {
+      const int t = colours[q] ? 1 : 0;
+      if (rt_status st = mtgp_rotate(v, t, rule, mtgp, stream)) return st;
+      pdl_launch(k_update_w, grd_w, blk_w, stream, v, t);
+      launches += 2;
+      half_sweeps[t]++;
+    }
+    return check_launch();
+  }
   bool pers = false;
   if (rt_status st = use_persistent(&pers)) return st;
   if (pers) {
@@ -536,7 +552,7 @@ rt_status DmSampler::sync() {
 
 rt_status DmSampler::use_persistent(bool* yes) {
   *yes = false;
-  if (opts.engine == 1) return RT_OK;
+  if (opts.engine == 1 || opts.rng_mode == RT_RNG_MTGP) return RT_OK;
   if (plan_dirty) {
     if (rt_status st = fetch_candidates()) return st;
   }
@@ -699,6 +715,13 @@ RT_API rt_status rt_domino_walk(int32_t* tiling, int32_t n_side, int64_t steps, 
     if (rt_status st = s->seed((uint32_t)mt())) return st;
     std::vector<uint8_t> col = colour_draws(mt, steps);
     if (rt_status st = s->run(col.data(), steps)) return st;
+  } else if (o.rng_mode == RT_RNG_MTGP) {
+    // DominoTiler.cpp:51-66 (CUDA branch): block generator k seeded seed + k, colours from
+    // mt19937(seed) starting with its first draw (:69).
+    std::mt19937 mt((uint32_t)seed);
+    if (rt_status st = s->seed(seed)) return st;
+    std::vector<uint8_t> col = colour_draws(mt, steps);
+    if (rt_status st = s->run(col.data(), steps)) return st;
   } else {
     if (rt_status st = s->run_fast((uint64_t)seed, 0, steps)) return st;
   }
@@ -718,10 +741,11 @@ RT_API rt_status rt_domino_walk_epochs(int32_t* tiling, int32_t n_side, const in
   if (rt_status st = s->load(0, tiling)) return st;
   int64_t h = 0;
   for (int k = 0; k < n_epochs; ++k) {
-    if (o.rng_mode == RT_RNG_TINYMT) {
-      // DominoTiler.cpp:155-175: mt19937(seeds[k]) for the colours, generators from seeds[k].
+    if (o.rng_mode != RT_RNG_FAST) {
+      // DominoTiler.cpp:155-175: mt19937(seeds[k]) for the colours, generators from seeds[k]
+      // (TinyMT: generator k seeded seeds[k] + k; MTGP: block generator k seeded seeds[k] + k).
       std::mt19937 mt((uint32_t)seeds[k]);
-      if (rt_status st = s->seed((uint32_t)seeds[k])) return st;
+      if (rt_status st = s->seed(o.rng_mode == RT_RNG_MTGP ? seeds[k] : (int64_t)(uint32_t)seeds[k])) return st;
       std::vector<uint8_t> col = colour_draws(mt, steps[k]);
       if (rt_status st = s->run(col.data(), steps[k])) return st;
     } else {
@@ -763,7 +787,7 @@ RT_API rt_status rt_domino_cftp(const int32_t* tmax, const int32_t* tmin, int32_
     int64_t before0 = s->half_sweeps[0], before1 = s->half_sweeps[1];
     cudaEventRecord(s->ev0, s->stream);
     int64_t look_back = 0;
-    if (o.rng_mode == RT_RNG_TINYMT) {
+    if (o.rng_mode != RT_RNG_FAST) {
       while (colours.size() < steps.size()) colours.insert(colours.begin(), std::vector<uint8_t>());  // prepended epochs
       for (size_t k = 0; k < steps.size(); ++k) {
         if (colours[k].empty() && steps[k] > 0) {
@@ -794,7 +818,7 @@ RT_API rt_status rt_domino_cftp(const int32_t* tmax, const int32_t* tmin, int32_
       if (stats) *stats = st_out;
       return s->store(1, out);
     }
-    if (o.rng_mode == RT_RNG_TINYMT) {
+    if (o.rng_mode != RT_RNG_FAST) {
       // AztecDiamondCftpEx.cpp:76 prepends 2 * steps.back(); schedule 1 doubles the oldest.
       int64_t next = schedule == 0 ? steps.back() * 2 : steps.front() * 2;
       steps.insert(steps.begin(), next);

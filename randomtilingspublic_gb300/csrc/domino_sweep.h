@@ -24,6 +24,29 @@ struct DmView {
   }
 };
 
+#ifdef __CUDACC__
+// New state of a site in state e for draw u under one case of a rule table: the up move
+// 3 -> 12 when u lies in [lo_up, lo_up + w_up), the down move 12 -> 3 in [lo_dn, lo_dn + w_dn).
+__device__ __forceinline__ uint8_t dm_flip(uint32_t e, uint32_t u, uint32_t lo_up, uint32_t w_up, uint32_t lo_dn,
+                                           uint32_t w_dn) {
+  if (e == 3u) return (u - lo_up) < w_up ? 12 : 3;
+  if (e == 12u) return (u - lo_dn) < w_dn ? 3 : 12;
+  return (uint8_t)e;
+}
+#endif
+
+// cuRAND MTGP32 mode (domino_mtgp.cu): the reference's 8 x 8 block grid over the flip
+// candidates, one generator per block.
+struct MtgpGrid {
+  int gx = 0, gy = 0;
+};
+MtgpGrid mtgp_grid(int N);
+size_t mtgp_state_bytes(int N);
+// Seeds generator k with seed + k (drains stream first).
+rt_status mtgp_seed(void* states, int N, int64_t seed, cudaStream_t stream);
+// One half-sweep's rotation of colour t of every active chain.
+rt_status mtgp_rotate(const DmView& v, int t, const DmRule& rule, void* states, cudaStream_t stream);
+
 // Device height functions (domino_thurston.cu).
 rt_status dm_heights_device(const int32_t* d_t, const int32_t* d_cls, const int32_t* d_dom, int N, int start,
                             int32_t* d_h, unsigned* d_flags, cudaStream_t st);
@@ -39,6 +62,8 @@ struct DmSampler {
   uint8_t* base = nullptr;
   uint4* tmt = nullptr;
   uint4* tmt_params = nullptr;
+  void* mtgp = nullptr;  // RT_RNG_MTGP: the generators of the 8 x 8 blocks (curandStateMtgp32)
+  bool mtgp_seeded = false;
   int32_t* scratch = nullptr;
   unsigned long long* counter = nullptr;
   cudaStream_t stream = nullptr;
@@ -79,7 +104,8 @@ struct DmSampler {
   int hf_start = -1;
   rt_status store(int ch, int32_t* tiling);
   rt_status copy_chain(int dst, int src);
-  rt_status seed(uint32_t s);
+  // TinyMT: generator k seeded s + k on the device; MTGP: block generator k seeded s + k.
+  rt_status seed(int64_t s);
   rt_status run(const uint8_t* colours, int64_t steps);
   rt_status run_fast(uint64_t seed, int64_t h0, int64_t steps);
   rt_status diff(int a, int b, int64_t* ndiff);

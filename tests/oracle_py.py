@@ -34,6 +34,10 @@ _SIG = {
                                    C.c_int]),
     "orc_dm_cftp_fast": (C.c_int, [_P, _P, C.c_int, C.c_ulong, C.c_uint, _L, C.c_int, C.c_int, C.c_double,
                                    C.c_double, C.c_int, _P, _P]),
+    "orc_dm_walk_draws": (C.c_int, [_P, C.c_int, _P, _L, _L, C.c_int, C.c_double, C.c_double]),
+    "orc_dm_walk_epochs_draws": (C.c_int, [_P, C.c_int, _P, _P, _P, C.c_int, C.c_int, C.c_double, C.c_double]),
+    "orc_dm_rotate_cuda_many": (None, [_P, _L, C.c_int, C.c_int, C.c_int, C.c_int, C.c_double, C.c_double, _P]),
+    "orc_mt19937": (None, [C.c_uint, _L, _P]),
     "orc_tinymt_u32": (C.c_uint, [C.c_uint, C.c_uint, C.c_uint, C.c_uint, C.c_int]),
     "orc_philox4x32_10": (None, [_P, _P, _P]),
     "orc_tmt_seed_states": (None, [C.c_uint, _L, _P]),
@@ -163,6 +167,37 @@ def cftp_tinymt(tmax, tmin, n, driver_seed, first_steps, schedule, max_attempts,
     att = lib().orc_dm_cftp_tinymt(_p(tmax), _p(tmin), n, driver_seed, first_steps, schedule, max_attempts, rule, a,
                                    b, _p(p), cnt, threads, _p(out), C.addressof(total))
     return out, att, total.value
+
+
+def walk_draws(t: np.ndarray, n: int, draws: np.ndarray, steps: int, seed: int, rule: int = 0, a=0.7,
+               b=1.0) -> None:
+    """The reference's CUDA-path walk with its MTGP32 draws supplied (steps x (n-2) x (n/2-2))."""
+    d = np.ascontiguousarray(draws, np.float32)
+    assert d.size == steps * (n - 2) * (n // 2 - 2)
+    assert lib().orc_dm_walk_draws(_p(t), n, _p(d), steps, seed, rule, a, b) == 0
+
+
+def walk_epochs_draws(t: np.ndarray, n: int, draws: np.ndarray, steps, seeds, rule: int = 0, a=0.7, b=1.0) -> None:
+    """CUDA-path epochs; draws holds the epochs' draws one after another."""
+    st = np.ascontiguousarray(np.asarray(steps, np.int64))
+    sd = np.ascontiguousarray(np.asarray(seeds, np.int64))
+    d = np.ascontiguousarray(draws, np.float32)
+    assert d.size == int(st.sum()) * (n - 2) * (n // 2 - 2)
+    assert lib().orc_dm_walk_epochs_draws(_p(t), n, _p(d), _p(st), _p(sd), len(st), rule, a, b) == 0
+
+
+def rotate_cuda(rd: np.ndarray, e: int, rule: int, i: int, t: int, a=0.7, b=1.0) -> np.ndarray:
+    """The CUDA kernels' new state for state e and each float draw in rd."""
+    r = np.ascontiguousarray(rd, np.float32)
+    out = np.zeros(r.size, np.uint8)
+    lib().orc_dm_rotate_cuda_many(_p(r), r.size, e, rule, i, t, a, b, _p(out))
+    return out
+
+
+def mt19937(seed: int, n: int) -> np.ndarray:
+    out = np.zeros(n, np.uint32)
+    lib().orc_mt19937(seed & 0xFFFFFFFF, n, _p(out))
+    return out
 
 
 def walk_fast(t: np.ndarray, n: int, h0: int, steps: int, seed: int, stream: int = 0, rule: int = 0, a=0.7, b=1.0,

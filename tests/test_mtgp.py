@@ -1,0 +1,160 @@
+"""The cuRAND MTGP32 mode of the domino sweep (RT_RNG_MTGP): the random stream of the
+reference's CUDA build (DominoTiler.cpp:51-66, dominokernel*.cu).
+
+cuRAND's generator is library code: the oracle does not restate it but takes its draws as
+data (rt_domino_mtgp_draws: the curand_uniform value each candidate site receives in the
+reference's 8 x 8 block geometry) and replays the reference's CUDA rotate kernels and host
+loops on them.  On CPU, the mode's acceptance intervals over the float draw's bit pattern are
+checked against the CUDA kernels' own float/double expressions."""
+import numpy as np
+import pytest
+
+RULES = [(0, 0.7, 1.0), (1, 1.0, 1.0), (2, 0.7, 1.0), (2, 1.0, 0.5), (3, 1.0, 0.5), (3, 0.37, 2.3)]
+NAMES = {0: "plain", 1: "cftp", 2: "twoperiodic", 3: "cftp_twoperiodic"}
+ONE = 0x3F800000  # bit pattern of 1.0f; curand_uniform returns values in (0, 1]
+
+
+@pytest.mark.parametrize("rule,a,b", RULES)
+def test_mtgp_rule_intervals_decide_as_the_cuda_kernels(rt, orc, rule, a, b):
+    table = np.zeros(16, np.uint32)
+    assert rt.lib().rt_domino_rule_table(rule, rt.RNG_MODES["mtgp"], a, b, table.ctypes.data) == rt.RT_OK
+    rng = np.random.default_rng(1000 + rule)
+    for c in range(4):
+        i, t = 2 + (c & 1), c >> 1
+        lo_up, w_up, lo_dn, w_dn = (int(x) for x in table[4 * c: 4 * c + 4])
+        for e, lo, w, new in ((3, lo_up, w_up, 12), (12, lo_dn, w_dn, 3)):
+            edges = {lo - 1, lo, lo + w - 1, lo + w, 1, ONE, 0x3F000000, 0x3F4CCCCC, 0x3F4CCCCD}
+            bits = np.array(sorted(u for u in edges if 1 <= u <= ONE), np.uint32)
+            bits = np.concatenate([bits, rng.integers(1, ONE + 1, 200_000, dtype=np.uint32),
+                                   rng.integers(0x3E000000, ONE + 1, 200_000, dtype=np.uint32)])
+            want = orc.rotate_cuda(bits.view(np.float32), e, rule, i, t, a, b) == new
+            mine = ((bits.astype(np.uint64) - lo) % 2**32) < w
+            assert np.array_equal(mine, want), (rule, c, e, bits[mine != want][:4])
+
+
+def test_mtgp_two_periodic_rule_is_the_cuda_kernels_not_the_opencl_ones(orc):
+    """dominokerneltwoperiodic.cu compares the float draw with the double 0.8 and divides in
+    double; the .cl kernel uses a float 0.8.  The first float at or above 0.8 separates them."""
+    rd = np.array([np.float32(0.8)], np.float32)  # rounds to 0.800000011920929 > 0.8
+    assert orc.rotate_cuda(rd, 3, 2, 2, 0, 1.0, 1.0)[0] == 3  # double 0.8: no proposal
+    below = np.nextafter(np.float32(0.8), np.float32(0), dtype=np.float32)
+    assert orc.rotate_cuda(np.array([below], np.float32), 3, 2, 2, 0, 1.0, 1.0)[0] == 12
+
+
+def _aztec(rt, order):
+    D = rt.DominoTiler
+    d = D.AztecDiamond(order)
+    return D.MaxTiling(d), D.MinTiling(d)
+
+
+def _mixed(rt, orc, order):
+    """A tiling away from the extremal ones (which have few flippable sites): the max tiling
+    after 400 half-sweeps of the oracle's TinyMT walk."""
+    t, _ = _aztec(rt, order)
+    orc.walk_tinymt(t, rt.side_of(t), 400, 5, 1, 1.0, 1.0)
+    return t
+
+
+@pytest.mark.gpu
+def test_mtgp_draws_are_deterministic_uniforms(rt):
+    n, launches = 40, 10
+    a = rt.mtgp_draws(n, 34893, launches)
+    b = rt.mtgp_draws(n, 34893, launches)
+    c = rt.mtgp_draws(n, 34894, launches)
+    assert a.shape == (launches, n - 2, n // 2 - 2)
+    assert np.array_equal(a, b) and not np.array_equal(a, c)
+    assert a.min() > 0.0 and a.max() <= 1.0
+    assert abs(float(a.mean()) - 0.5) < 0.02
+    assert len(np.unique(a)) > 0.99 * a.size
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("rule,a,b", RULES)
+def test_mtgp_walk_equals_the_reference_cuda_path_on_its_draws(rt, orc, rule, a, b):
+    start = _mixed(rt, orc, 9)
+    n = rt.side_of(start)
+    steps, seed = 150, 34893  # Examples/MinimalDominoEx.cpp walks with seed 34893
+    want = start.copy()
+    orc.walk_draws(want, n, rt.mtgp_draws(n, seed, steps), steps, seed, rule, a, b)
+    got = start.copy()
+    rt.DominoTiler(rule=NAMES[rule], rng="mtgp", a=a, b=b).Walk(got, steps, seed)
+    assert np.array_equal(got, want)
+    assert (got != start).sum() > 8
+
+
+@pytest.mark.gpu
+def test_mtgp_epochs_and_load_mtgp_equal_the_reference_cuda_path(rt, orc):
+    start = _mixed(rt, orc, 8)
+    n = rt.side_of(start)
+    steps, seeds = [96, 48, 32], [7, 123456789, 2**31 + 5]
+    draws = np.concatenate([rt.mtgp_draws(n, s, k) for k, s in zip(steps, seeds)])
+    want = start.copy()
+    orc.walk_epochs_draws(want, n, draws, steps, seeds, 0)
+    tiler = rt.DominoTiler()
+    tiler.LoadMTGP()
+    got = start.copy()
+    tiler.Walk(got, steps, seeds)
+    assert np.array_equal(got, want)
+    assert (got != start).sum() > 8
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("rule,a,b", [(1, 1.0, 1.0), (3, 1.0, 0.5)])
+def test_mtgp_cftp_equals_the_reference_driver_on_its_draws(rt, orc, rule, a, b):
+    """Examples/AztecDiamondCftpEx.cpp:51-77: epochs prepended with doubled steps and fresh
+    seeds from mt19937(345903) until the coupled max/min chains agree."""
+    tmax, tmin = _aztec(rt, 6)
+    n = rt.side_of(tmax)
+    driver_seed, first, max_attempts = 345903, 16, 24
+    drv = iter(orc.mt19937(driver_seed, 64))
+    steps, seeds = [first], [int(next(drv))]
+    for attempt in range(1, max_attempts + 1):
+        draws = np.concatenate([rt.mtgp_draws(n, s, k) for k, s in zip(steps, seeds)])
+        top, bot = tmax.copy(), tmin.copy()
+        orc.walk_epochs_draws(top, n, draws, steps, seeds, rule, a, b)
+        orc.walk_epochs_draws(bot, n, draws, steps, seeds, rule, a, b)
+        if np.array_equal(top, bot):
+            break
+        steps.insert(0, steps[-1] * 2)
+        seeds.insert(0, int(next(drv)))
+    else:
+        pytest.fail("oracle driver did not coalesce")
+    assert attempt > 1  # the look-back grew at least once
+    got, stats = rt.DominoTiler(rule=NAMES[rule], rng="mtgp", a=a, b=b).cftp(tmax, tmin, driver_seed=driver_seed,
+                                                                             first_steps=first,
+                                                                             max_attempts=max_attempts)
+    assert stats["attempts"] == attempt
+    assert np.array_equal(got, top)
+
+
+@pytest.mark.gpu
+def test_mtgp_walk_with_host_threaded_seeding(rt, orc):
+    """Order 128: 33 x 17 = 561 block generators, seeded from several host threads."""
+    tmax, _ = _aztec(rt, 128)
+    n = rt.side_of(tmax)
+    assert ((n - 2 + 7) // 8) * ((n // 2 - 2 + 7) // 8) >= 512
+    steps, seed = 8, 99
+    orc.walk_tinymt(tmax, n, 200, 5, 1, 1.0, 1.0)
+    want = tmax.copy()
+    orc.walk_draws(want, n, rt.mtgp_draws(n, seed, steps), steps, seed, 1, 1.0, 1.0)
+    got = tmax.copy()
+    rt.DominoTiler(rule="cftp", rng="mtgp").Walk(got, steps, seed)
+    assert np.array_equal(got, want)
+    assert (got != tmax).sum() > 8
+
+
+@pytest.mark.gpu
+def test_mtgp_sampler_refuses_unseeded_runs_and_the_resident_engine(rt):
+    tmax, _ = _aztec(rt, 6)
+    n = rt.side_of(tmax)
+    s = rt.DominoSampler(n, 1, rt.DominoTiler(rng="mtgp"))
+    s.load(0, tmax)
+    colours = np.zeros(4, np.uint8)
+    assert rt.lib().rt_dm_sampler_run(s.h, colours.ctypes.data, 4) == rt.RT_ERR_INVALID_ARGUMENT
+    assert rt.lib().rt_dm_sampler_seed(s.h, 5) == rt.RT_OK
+    assert rt.lib().rt_dm_sampler_run(s.h, colours.ctypes.data, 4) == rt.RT_OK
+    s.close()
+    with pytest.raises(rt.RTError):
+        rt.DominoSampler(n, 1, rt.DominoTiler(rng="mtgp", engine=2))
+    with pytest.raises(rt.RTError):
+        rt.LozengeTiler(rng="mtgp").Walk(rt.LozengeTiler.MaxTiling(rt.LozengeTiler.Hexagon(3)), 4, 1)
