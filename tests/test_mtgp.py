@@ -158,3 +158,28 @@ def test_mtgp_sampler_refuses_unseeded_runs_and_the_resident_engine(rt):
         rt.DominoSampler(n, 1, rt.DominoTiler(rng="mtgp", engine=2))
     with pytest.raises(rt.RTError):
         rt.LozengeTiler(rng="mtgp").Walk(rt.LozengeTiler.MaxTiling(rt.LozengeTiler.Hexagon(3)), 4, 1)
+
+
+@pytest.mark.gpu
+def test_cpp_dropin_load_mtgp_walk_equals_the_reference_cuda_path(rt, orc, tmp_path):
+    """tests/cpp/dropin_walk.cpp calls LoadMTGP and Walk(T, 100, 34893) through the C++
+    header, as the reference's CUDA examples do."""
+    import shutil
+    import subprocess
+    from pathlib import Path
+
+    if not shutil.which("g++"):
+        pytest.skip("no g++")
+    root = Path(__file__).resolve().parent.parent
+    exe = tmp_path / "dropin_walk"
+    libdir = str(rt.LIB_PATH.parent)
+    subprocess.run(["g++", "-std=c++17", "-O1", f"-I{root / 'include'}", str(root / "tests/cpp/dropin_walk.cpp"),
+                    f"-L{libdir}", "-l:librt_tilings.so", f"-Wl,-rpath,{libdir}", "-o", str(exe)], check=True)
+    order = 7
+    out = subprocess.run([str(exe), str(order)], check=True, capture_output=True, text=True).stdout
+    got = np.array([int(x) for x in out.split()], np.int32)
+    tmax, _ = _aztec(rt, order)
+    n = rt.side_of(tmax)
+    want = tmax.copy()
+    orc.walk_draws(want, n, rt.mtgp_draws(n, 34893, 100), 100, 34893, 0)
+    assert np.array_equal(got, want)
