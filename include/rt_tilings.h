@@ -51,8 +51,9 @@ typedef int32_t rt_status;
                            site); no generator state in memory */
 #define RT_RNG_MTGP 2   /* cuRAND MTGP32, one generator per 8 x 8 block of sites seeded
                            seed + block, the reference's CUDA path (DominoTiler.cpp:51-66,
-                           dominokernel*.cu): domino walks, epochs and CFTP through the
-                           per-half-sweep kernels; the same draws as the reference's build */
+                           dominokernel*.cu; LozengeTiler.cpp:71-80, lozengekernel.cu):
+                           domino and uniform lozenge walks, epochs and CFTP through the
+                           per-step kernels; the same draws as the reference's build */
 
 /* Flip rules: the reference picks one by compiling one of four kernel files. */
 #define RT_DOMINO_PLAIN 0            /* src/Domino/dominokernel.cl:4-18 (propose 0.8) */
@@ -177,12 +178,18 @@ RT_API rt_status rt_lozenge_tiling_to_heightfunc(const int32_t* tiling, const in
 RT_API rt_status rt_lozenge_tiling_to_domain(const int32_t* tiling, int32_t n_side, int32_t* out);
 /* LozengeTiler::Walk(tiling&, int steps, long seed) (LozengeTiler.cpp:27-159): per step a
    colour from default_random_engine(seed) + uniform_int_distribution(0, 2) (TinyMT mode,
-   generators seeded with seed itself) or h mod 3 (fast mode), then the rotation 25 <-> 38
-   (0.4 / 0.4, lozengekernel.cl:74-105) and the rebuild of the two other colours
-   (lozengekernel.cl:107-125).  opts->rule selects RT_LOZENGE_UNIFORM or RT_LOZENGE_Q (q in
-   opts->weight_a). */
+   generators seeded with seed itself; MTGP mode, block generator k seeded seed + k as the
+   CUDA branch does, LozengeTiler.cpp:71-80) or h mod 3 (fast mode), then the rotation
+   25 <-> 38 (0.4 / 0.4, lozengekernel.cl:74-105, lozengekernel.cu:15-29) and the rebuild of
+   the two other colours (lozengekernel.cl:107-125).  opts->rule selects RT_LOZENGE_UNIFORM
+   or RT_LOZENGE_Q (q in opts->weight_a; TinyMT and fast modes only). */
 RT_API rt_status rt_lozenge_walk(int32_t* tiling, int32_t n_side, int64_t steps, int64_t seed,
                                  const rt_walk_opts* opts);
+/* The float draws RT_RNG_MTGP makes for the first `launches` steps of a lozenge walk on an
+   n_side tiling whose block generators are seeded seed + k: out[h][i][j] (launches x n_side x
+   n_side/3 floats, host memory) is the draw of slot (i, j) of the rotated colour at step h
+   (lozengekernel.cu:20-21). */
+RT_API rt_status rt_lozenge_mtgp_draws(int32_t n_side, int64_t seed, int64_t launches, float* out);
 /* Coupling from the past from the max and min tilings with the reference's primitives: each
    epoch is one Walk(t, steps_k, seed_k) of both chains on the shared stream, seeds from
    mt19937(driver_seed), look-back prepending 2*steps.back() (schedule 0) or 2*steps.front()

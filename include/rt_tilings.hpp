@@ -13,7 +13,8 @@
 //   * failures throw rt::Error instead of printing and calling exit();
 //   * the OpenCL constructors (context, queue, devices, kernel source) are replaced by
 //     default construction; LoadTinyMT / LoadMTGP are accepted where the reference has them
-//     (DominoTiler::LoadMTGP selects the cuRAND MTGP32 mode; the other tilers ignore it).
+//     (DominoTiler::LoadMTGP and LozengeTiler::LoadMTGP select the cuRAND MTGP32 mode; the
+//     other tilers ignore it).
 // Header-only; link with -lrt_tilings.
 #ifndef RT_TILINGS_HPP_
 #define RT_TILINGS_HPP_
@@ -199,7 +200,9 @@ class LozengeTiler {
  public:
   explicit LozengeTiler(int rng_mode = RT_RNG_TINYMT, uint32_t fast_stream = 0) : opts_(model_opts(rng_mode, fast_stream)) {}
   void LoadTinyMT(const std::string&, int) {}
-  void LoadMTGP() {}
+  // LozengeTiler::LoadMTGP: as in the reference's CUDA build, walks then draw from cuRAND
+  // MTGP32 block generators (RT_RNG_MTGP).
+  void LoadMTGP() { opts_.rng_mode = RT_RNG_MTGP; }
 
   void Walk(tiling& t, int steps, long seed) { check(rt_lozenge_walk(t.data(), side_of(t), steps, seed, &opts_)); }
 

@@ -8,6 +8,9 @@
 //     generators seeded with the walk seed itself (InitTinyMT, lozengekernel.cl:127-134),
 //     colours from std::default_random_engine + uniform_int_distribution(0, 2) seeded with
 //     the walk seed, RotateTiles lozengekernel.cl:74-105, UpdateTiles :107-125
+//   * Walk as the CUDA path runs it, given its MTGP32 draws (cuRAND's generator is library
+//     code and comes in as data): RotateTilesKernel lozengekernel.cu:15-29 on every slot of
+//     the N x N/3 grid, the same colour stream and UpdateTiles
 // plus the library's fast mode for lozenges (colour h mod 3, Philox draws per column quad).
 // Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg may load this.
 #include <algorithm>
@@ -259,6 +262,34 @@ void lwalk_tinymt(std::vector<LChain*>& chains, long steps, long seed, const uin
   }
 }
 
+// lozengekernel.cu:23-29: up when the float draw is below the double .4, down when it lies in
+// [.4, .8).
+inline uint8_t lrotate_cu(uint8_t e, float rd) {
+  if (rd < .4) return e == 25 ? 38 : e;
+  if (rd < .8) return e == 38 ? 25 : e;
+  return e;
+}
+
+// One reference Walk(t, steps, seed) of the CUDA path with draws[s][i][j] the curand_uniform
+// value of slot (i, j) at step s.
+void lwalk_draws(std::vector<LChain*>& chains, const float* draws, long steps, long seed) {
+  const int N = chains[0]->N, M = chains[0]->M;
+  std::default_random_engine gen;
+  std::uniform_int_distribution<int> dist(0, 2);
+  gen.seed(seed);
+  for (long s = 0; s < steps; ++s) {
+    const int r = dist(gen);
+    const float* d = draws + (size_t)s * N * M;
+    for (int i = 0; i < N; ++i)
+      for (int j = 0; j < M; ++j)
+        for (LChain* c : chains) {
+          uint8_t& e = c->X[r][(size_t)i * M + j];
+          e = lrotate_cu(e, d[(size_t)i * M + j]);
+        }
+    for (LChain* c : chains) lupdate(*c, r);
+  }
+}
+
 inline int fast_colour(long h) { return (int)(((h % 3) + 3) % 3); }
 
 void lwalk_fast(std::vector<LChain*>& chains, long h0, long steps, unsigned long seed, unsigned stream) {
@@ -387,6 +418,18 @@ int orc_lz_walk_tinymt(int* t, int N, long steps, long seed, const uint32_t* par
   lsplit(t, N, c);
   std::vector<LChain*> ch{&c};
   lwalk_tinymt(ch, steps, seed, params, nparams);
+  lmerge(c, t);
+  return 0;
+}
+
+// LozengeTiler::Walk(t, steps, seed), CUDA path, with the MTGP32 draws supplied
+// (steps x N x N/3 floats).
+int orc_lz_walk_draws(int* t, int N, const float* draws, long steps, long seed) {
+  if (N % 3 || N < 6) return -1;
+  LChain c;
+  lsplit(t, N, c);
+  std::vector<LChain*> ch{&c};
+  lwalk_draws(ch, draws, steps, seed);
   lmerge(c, t);
   return 0;
 }

@@ -137,6 +137,7 @@ _SIGNATURES = {
                             _P]),
     "rt_domino_rule_table": (C.c_int32, [C.c_int32, C.c_int32, C.c_double, C.c_double, _P]),
     "rt_domino_mtgp_draws": (C.c_int32, [C.c_int32, C.c_int64, C.c_int64, _P]),
+    "rt_lozenge_mtgp_draws": (C.c_int32, [C.c_int32, C.c_int64, C.c_int64, _P]),
     "rt_dm_sweep_noalloc": (C.c_int32, [_P, _P, C.c_int32, C.c_int32, _P, C.c_int64, C.c_uint64, C.c_int64, _P]),
     "rt_cftp_batch": (C.c_int32, [_P, C.c_int32, _P, _P]),
     "rt_server_create": (C.c_int32, [_P, _P]),
@@ -429,7 +430,8 @@ def _tri_side(d) -> int:
 
 class LozengeTiler:
     """Lozenge tilings (src/Lozenge/LozengeTiler.h:46-92).  ``rng`` is 'tinymt' (bit-exact
-    with the reference's OpenCL path) or 'fast'."""
+    with the reference's OpenCL path), 'mtgp' (its CUDA path's cuRAND MTGP32 draws, uniform
+    rule; also selected by LoadMTGP) or 'fast'."""
 
     def __init__(self, rng: str = "tinymt", fast_stream: int = 0, q: float | None = None):
         """q: None for the reference's uniform rotation (lozengekernel.cl), else the q^volume
@@ -437,6 +439,11 @@ class LozengeTiler:
         self.rng = rng
         self.fast_stream = int(fast_stream)
         self.q = q
+
+    def LoadMTGP(self) -> None:
+        """LozengeTiler::LoadMTGP: walks draw from cuRAND MTGP32 block generators, as the
+        reference's CUDA build (LozengeTiler.cpp:71-80)."""
+        self.rng = "mtgp"
 
     def opts(self) -> _WalkOpts:
         o = _WalkOpts()
@@ -955,6 +962,17 @@ def mtgp_draws(n_side: int, seed: int, launches: int) -> np.ndarray:
     return out
 
 
+def lozenge_mtgp_draws(n_side: int, seed: int, launches: int) -> np.ndarray:
+    """The float draws of the 'mtgp' mode for the first ``launches`` steps of a lozenge walk
+    seeded ``seed`` on an n_side tiling: array (launches, n_side, n_side // 3), entry [h, i, j]
+    the curand_uniform value slot (i, j) of the rotated colour receives at step h
+    (lozengekernel.cu:20-21)."""
+    n = int(n_side)
+    out = np.zeros((int(launches), n, n // 3), np.float32)
+    _check(lib().rt_lozenge_mtgp_draws(n, int(seed), int(launches), _ptr(out)))
+    return out
+
+
 def SaveMatrix(a, path, rows: int | None = None, cols: int | None = None) -> None:
     """The reference's SaveMatrix (src/common/common.cpp:84-128): without rows/cols the
     square overload (floor(sqrt(size))^2 values)."""
@@ -994,4 +1012,4 @@ def mt19937_draws(seed: int, count: int) -> np.ndarray:
 
 
 __all__ = ["DominoTiler", "DominoSampler", "LozengeTiler", "RectTriangleTiler", "SixVertexTiler", "TriangleDimerTiler", "cftp_batch", "Server", "RTError", "lib", "read_tinymt_params", "mt19937_colours",
-           "mt19937_draws", "mtgp_draws", "CftpStats"]
+           "mt19937_draws", "mtgp_draws", "lozenge_mtgp_draws", "CftpStats"]

@@ -37,8 +37,6 @@ namespace rt {
 
 namespace {
 
-constexpr int kMtgpBlock = 8;  // BLOCK_DIM of the reference (dominokernel.cuh:4)
-
 // One half-sweep's rotation of colour t: every thread of every block draws once from its
 // block's generator, then the in-range ones decide their site in every active chain.
 __global__ void __launch_bounds__(kMtgpBlock* kMtgpBlock) k_rotate_mtgp(DmView v, int t, DmRule rule,
@@ -60,15 +58,15 @@ __global__ void __launch_bounds__(kMtgpBlock* kMtgpBlock) k_rotate_mtgp(DmView v
   }
 }
 
-// The draws of one launch in the same geometry, written per candidate site (rows x cols,
-// row-major): what k_rotate_mtgp decides with.
+// The draws of one launch on a rows x cols grid, row-major (row x from the x index, column
+// y from the y index): what the rotate kernels of both tilers decide with.
 __global__ void __launch_bounds__(kMtgpBlock* kMtgpBlock) k_mtgp_draws(curandStateMtgp32* states, int rows, int cols,
                                                                         float* out) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
-  const int m = blockIdx.y * blockDim.y + threadIdx.y + 1;
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  const int y = blockIdx.y * blockDim.y + threadIdx.y;
   const float rd = curand_uniform(states + blockIdx.x * gridDim.y + blockIdx.y);
-  if (i > rows || m > cols) return;
-  out[(size_t)(i - 1) * cols + (m - 1)] = rd;
+  if (x >= rows || y >= cols) return;
+  out[(size_t)x * cols + y] = rd;
 }
 
 // The kernel parameters of the parameter set (curandMakeMTGP32Constants), made once per
@@ -95,31 +93,19 @@ rt_status kernel_params(mtgp32_kernel_params** out) {
 
 }  // namespace
 
-MtgpGrid mtgp_grid(int N) {
-  MtgpGrid g;
-  g.gx = (N - 2 + kMtgpBlock - 1) / kMtgpBlock;
-  g.gy = (N / 2 - 2 + kMtgpBlock - 1) / kMtgpBlock;
-  return g;
-}
+size_t mtgp_state_bytes(int count) { return (size_t)count * sizeof(curandStateMtgp32); }
 
-size_t mtgp_state_bytes(int N) {
-  const MtgpGrid g = mtgp_grid(N);
-  return (size_t)g.gx * g.gy * sizeof(curandStateMtgp32);
-}
-
-rt_status mtgp_seed(void* states, int N, int64_t seed, cudaStream_t stream) {
+rt_status mtgp_seed(void* states, int count, int64_t seed, cudaStream_t stream) {
   mtgp32_kernel_params* kp = nullptr;
   if (rt_status st = kernel_params(&kp)) return st;
   // curandMakeMTGP32KernelState copies each state with a blocking cudaMemcpy, which does not
   // wait for kernels still queued on a non-blocking stream: drain the stream first.
   RT_CUDA(cudaStreamSynchronize(stream));
-  const MtgpGrid g = mtgp_grid(N);
-  const int count = g.gx * g.gy;
   curandStateMtgp32* s = static_cast<curandStateMtgp32*>(states);
   int dev = 0;
   RT_CUDA(cudaGetDevice(&dev));
-  // Generator k is seeded seed + k, one state per call (DominoTiler.cpp:63-65); large grids
-  // split the calls over host threads.
+  // Generator k is seeded seed + k, one state per call (DominoTiler.cpp:63-65,
+  // LozengeTiler.cpp:78-80); large grids split the calls over host threads.
   const int nthreads = count < 512 ? 1 : (int)std::min(16u, std::max(1u, std::thread::hardware_concurrency()));
   std::vector<int> bad(nthreads, 0);
   auto work = [&](int tid) {
@@ -147,34 +133,25 @@ rt_status mtgp_seed(void* states, int N, int64_t seed, cudaStream_t stream) {
 }
 
 rt_status mtgp_rotate(const DmView& v, int t, const DmRule& rule, void* states, cudaStream_t stream) {
-  const MtgpGrid g = mtgp_grid(v.N);
+  const MtgpGrid g = mtgp_grid(v.rows, v.cols);
   const cudaError_t e = pdl_launch(k_rotate_mtgp, dim3(g.gx, g.gy), dim3(kMtgpBlock, kMtgpBlock), stream, v, t, rule,
                                    static_cast<curandStateMtgp32*>(states));
   if (e != cudaSuccess) return fail(RT_ERR_CUDA, std::string("k_rotate_mtgp: ") + cudaGetErrorString(e));
   return RT_OK;
 }
 
-}  // namespace rt
-
-using namespace rt;
-
-extern "C" {
-
-RT_API rt_status rt_domino_mtgp_draws(int32_t n_side, int64_t seed, int64_t launches, float* out) {
-  clear_error();
-  if (n_side < 6 || n_side % 2 || n_side > 32768 || launches < 0 || (launches > 0 && !out))
-    return fail(RT_ERR_INVALID_ARGUMENT, "mtgp_draws: even n_side in [6, 32768], launches >= 0, out not NULL");
-  const int rows = n_side - 2, cols = n_side / 2 - 2;
+rt_status mtgp_draws_grid(int rows, int cols, int64_t seed, int64_t launches, float* out) {
   const size_t per = (size_t)rows * cols;
+  const MtgpGrid g = mtgp_grid(rows, cols);
   cudaStream_t stream = nullptr;
   RT_CUDA(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
   void* states = nullptr;
   float* d_out = nullptr;
   rt_status st = RT_OK;
-  if (cudaMalloc(&states, mtgp_state_bytes(n_side)) != cudaSuccess || cudaMalloc(&d_out, per * sizeof(float)) != cudaSuccess)
+  if (cudaMalloc(&states, mtgp_state_bytes(g.count())) != cudaSuccess ||
+      cudaMalloc(&d_out, per * sizeof(float)) != cudaSuccess)
     st = fail(RT_ERR_OUT_OF_MEMORY, "mtgp_draws: device allocation failed");
-  if (!st) st = mtgp_seed(states, n_side, seed, stream);
-  const MtgpGrid g = mtgp_grid(n_side);
+  if (!st) st = mtgp_seed(states, g.count(), seed, stream);
   for (int64_t k = 0; !st && k < launches; ++k) {
     k_mtgp_draws<<<dim3(g.gx, g.gy), dim3(kMtgpBlock, kMtgpBlock), 0, stream>>>(
         static_cast<curandStateMtgp32*>(states), rows, cols, d_out);
@@ -187,6 +164,19 @@ RT_API rt_status rt_domino_mtgp_draws(int32_t n_side, int64_t seed, int64_t laun
   if (states) cudaFree(states);
   cudaStreamDestroy(stream);
   return st;
+}
+
+}  // namespace rt
+
+using namespace rt;
+
+extern "C" {
+
+RT_API rt_status rt_domino_mtgp_draws(int32_t n_side, int64_t seed, int64_t launches, float* out) {
+  clear_error();
+  if (n_side < 6 || n_side % 2 || n_side > 32768 || launches < 0 || (launches > 0 && !out))
+    return fail(RT_ERR_INVALID_ARGUMENT, "mtgp_draws: even n_side in [6, 32768], launches >= 0, out not NULL");
+  return mtgp_draws_grid(n_side - 2, n_side / 2 - 2, seed, launches, out);
 }
 
 }  // extern "C"

@@ -322,7 +322,8 @@ rt_status DmSampler::create(int n_side, int n_chains, const rt_walk_opts& o, std
     }
   } else if (o.rng_mode == RT_RNG_MTGP) {
     if (o.engine == 2) return fail(RT_ERR_INVALID_ARGUMENT, "MTGP mode runs on the per-half-sweep kernels only");
-    if (rt_status st = dev_alloc(&s->mtgp, mtgp_state_bytes(s->N), s->stream)) return st;
+    if (rt_status st = dev_alloc(&s->mtgp, mtgp_state_bytes(mtgp_grid(s->N - 2, s->N / 2 - 2).count()), s->stream))
+      return st;
   }
   *out = std::move(s);
   return RT_OK;
@@ -398,7 +399,7 @@ rt_status DmSampler::copy_chain(int dst, int src) {
 
 rt_status DmSampler::seed(int64_t s) {
   if (opts.rng_mode == RT_RNG_MTGP) {
-    if (rt_status st = mtgp_seed(mtgp, N, s, stream)) return st;
+    if (rt_status st = mtgp_seed(mtgp, mtgp_grid(N - 2, N / 2 - 2).count(), s, stream)) return st;
     mtgp_seeded = true;
     return RT_OK;
   }

@@ -35,16 +35,8 @@ __device__ __forceinline__ uint8_t dm_flip(uint32_t e, uint32_t u, uint32_t lo_u
 }
 #endif
 
-// cuRAND MTGP32 mode (domino_mtgp.cu): the reference's 8 x 8 block grid over the flip
-// candidates, one generator per block.
-struct MtgpGrid {
-  int gx = 0, gy = 0;
-};
-MtgpGrid mtgp_grid(int N);
-size_t mtgp_state_bytes(int N);
-// Seeds generator k with seed + k (drains stream first).
-rt_status mtgp_seed(void* states, int N, int64_t seed, cudaStream_t stream);
-// One half-sweep's rotation of colour t of every active chain.
+// cuRAND MTGP32 mode (domino_mtgp.cu): one half-sweep's rotation of colour t of every active
+// chain, on the reference's 8 x 8 block grid over the flip candidates.
 rt_status mtgp_rotate(const DmView& v, int t, const DmRule& rule, void* states, cudaStream_t stream);
 
 // Device height functions (domino_thurston.cu).

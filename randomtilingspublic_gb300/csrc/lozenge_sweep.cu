@@ -7,8 +7,11 @@
 // probability 0.4 and every 38 becomes 25 with probability 0.4 (one draw decides both, so
 // coupled chains stay ordered), then rebuilds three bits of each of the two other colours.
 // TinyMT generator k = i * (N/3) + j for every vertex slot of the N x N/3 grid, as the
-// reference's NDRange numbers them.
+// reference's NDRange numbers them.  MTGP mode: the reference's CUDA build instead (8 x 8
+// blocks over the same grid, row from the x index, one cuRAND MTGP32 generator per block
+// seeded seed + block; LozengeTiler.cpp:71-80, lozengekernel.cu:15-29).
 #include <cuda_runtime.h>
+#include <curand_kernel.h>
 
 #include <algorithm>
 #include <cmath>
@@ -65,6 +68,24 @@ __global__ void k_lz_rotate_tmt(LzView v, int r, LzRule rule) {
   uint4 s = v.tmt[k];
   const uint32_t u = tmt_next_u23(s, kTmtMat1, kTmtMat2, kTmtTmat);
   v.tmt[k] = s;
+  for (int ch = 0; ch < v.active; ++ch) {
+    uint8_t* p = v.colour(ch, r) + (size_t)i * v.P + j;
+    const uint32_t e = *p;
+    const uint8_t n = lz_flip(e, u, rule);
+    if (n != e) *p = n;
+  }
+}
+
+// MTGP mode (lozengekernel.cu:15-29): every thread of the 8 x 8 block draws from its block's
+// generator before the bounds test; u is the float draw's bit pattern.
+__global__ void __launch_bounds__(kMtgpBlock* kMtgpBlock) k_lz_rotate_mtgp(LzView v, int r, LzRule rule,
+                                                                            curandStateMtgp32* states) {
+  pdl_begin();
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int j = blockIdx.y * blockDim.y + threadIdx.y;
+  const float rd = curand_uniform(states + blockIdx.x * gridDim.y + blockIdx.y);
+  if (i >= v.N || j >= v.M) return;
+  const uint32_t u = __float_as_uint(rd);
   for (int ch = 0; ch < v.active; ++ch) {
     uint8_t* p = v.colour(ch, r) + (size_t)i * v.P + j;
     const uint32_t e = *p;
@@ -204,7 +225,19 @@ LzRule lz_rule(int rng_mode, int rule, double q) {
     }
     return r;
   }
-  if (rng_mode == RT_RNG_TINYMT) {
+  if (rng_mode == RT_RNG_MTGP) {
+    // u is the bit pattern of the float draw in (0, 1]; the kernel compares it with the
+    // doubles .4 and .8 (lozengekernel.cu:24-27).
+    auto below = [](double x) {  // float bit patterns b with float(b) < x
+      return count_below(0, 0x3f800001u, [&](uint32_t b) {
+        float f;
+        std::memcpy(&f, &b, sizeof f);
+        return (double)f < x;
+      });
+    };
+    const uint32_t c4 = below(.4), c8 = below(.8);
+    r = {0u, c4, c4, c8 - c4};
+  } else if (rng_mode == RT_RNG_TINYMT) {
     auto below = [](double x) {  // number of u23 with u23 * 2^-23 < x
       return count_below(0, 1u << 23, [&](uint32_t u) { return (double)((float)u * (1.0f / 8388608.0f)) < x; });
     };
@@ -224,6 +257,8 @@ struct LzSampler {
   LzRule rule{};
   uint8_t* base = nullptr;
   uint4* tmt = nullptr;
+  void* mtgp = nullptr;  // RT_RNG_MTGP: the block generators (curandStateMtgp32)
+  bool mtgp_seeded = false;
   int32_t* scratch = nullptr;
   unsigned long long* counter = nullptr;
   cudaStream_t stream = nullptr;
@@ -235,6 +270,7 @@ struct LzSampler {
   ~LzSampler() {
     if (base) cudaFree(base);
     if (tmt) cudaFree(tmt);
+    if (mtgp) cudaFree(mtgp);
     if (scratch) cudaFree(scratch);
     if (counter) cudaFree(counter);
     if (ev0) cudaEventDestroy(ev0);
@@ -247,7 +283,10 @@ struct LzSampler {
   static rt_status create(int n_side, int chains, const rt_walk_opts& o, std::unique_ptr<LzSampler>* out) {
     if (n_side < 9 || n_side % 3 || n_side > 32766)
       return fail(RT_ERR_INVALID_ARGUMENT, "lozenge tiling side must be a multiple of 3 in [9, 32766]");
-    if (o.rng_mode != RT_RNG_TINYMT && o.rng_mode != RT_RNG_FAST) return fail(RT_ERR_INVALID_ARGUMENT, "unknown rng mode");
+    if (o.rng_mode != RT_RNG_TINYMT && o.rng_mode != RT_RNG_FAST && o.rng_mode != RT_RNG_MTGP)
+      return fail(RT_ERR_INVALID_ARGUMENT, "unknown rng mode");
+    if (o.rng_mode == RT_RNG_MTGP && o.rule != RT_LOZENGE_UNIFORM)
+      return fail(RT_ERR_INVALID_ARGUMENT, "lozenge sweep: the MTGP mode takes the uniform rule (lozengekernel.cu)");
     if (o.rng_mode == RT_RNG_FAST && o.fast_stream >= 65536u) return fail(RT_ERR_INVALID_ARGUMENT, "fast_stream must be < 65536");
     if (o.tinymt_params) return fail(RT_ERR_INVALID_ARGUMENT, "lozenge sweep: per-generator parameter tables are not supported");
     if (o.rule != RT_LOZENGE_UNIFORM && o.rule != RT_LOZENGE_Q) return fail(RT_ERR_INVALID_ARGUMENT, "lozenge sweep: unknown rule");
@@ -280,6 +319,7 @@ struct LzSampler {
     LZ_CUDA(cudaMalloc(&s->scratch, (size_t)s->N * s->N * sizeof(int32_t)));
     LZ_CUDA(cudaMalloc(&s->counter, sizeof(unsigned long long)));
     if (o.rng_mode == RT_RNG_TINYMT) LZ_CUDA(cudaMalloc(&s->tmt, (size_t)s->N * s->M * sizeof(uint4)));
+    if (o.rng_mode == RT_RNG_MTGP) LZ_CUDA(cudaMalloc(&s->mtgp, mtgp_state_bytes(mtgp_grid(s->N, s->M).count())));
     *out = std::move(s);
     return RT_OK;
   }
@@ -319,13 +359,33 @@ struct LzSampler {
                             stream));
     return RT_OK;
   }
-  rt_status seed(uint32_t s) {
+  // TinyMT: generator k seeded s + k on the device; MTGP: block generator k seeded s + k.
+  rt_status seed(int64_t s) {
+    if (opts.rng_mode == RT_RNG_MTGP) {
+      if (rt_status st = mtgp_seed(mtgp, mtgp_grid(N, M).count(), s, stream)) return st;
+      mtgp_seeded = true;
+      return RT_OK;
+    }
     const int64_t count = (int64_t)N * M;
-    k_lz_seed<<<(unsigned)((count + 255) / 256), 256, 0, stream>>>(tmt, count, s);
+    k_lz_seed<<<(unsigned)((count + 255) / 256), 256, 0, stream>>>(tmt, count, (uint32_t)s);
     return check();
   }
   rt_status run(const uint8_t* colours, int64_t steps) {
     const LzView v = view();
+    if (opts.rng_mode == RT_RNG_MTGP) {
+      // An MTGP state holds a pointer to its parameters: none exists before the first seed.
+      if (!mtgp_seeded) return fail(RT_ERR_INVALID_ARGUMENT, "lozenge run: MTGP generators not seeded");
+      const MtgpGrid g = mtgp_grid(N, M);
+      const dim3 gu((P / 4 + 31) / 32, (N - 2 + 7) / 8);
+      for (int64_t s = 0; s < steps; ++s) {
+        const int r = colours[s];
+        pdl_launch(k_lz_rotate_mtgp, dim3(g.gx, g.gy), dim3(kMtgpBlock, kMtgpBlock), stream, v, r, rule,
+                   static_cast<curandStateMtgp32*>(mtgp));
+        pdl_launch(k_lz_update_w, gu, dim3(32, 8), stream, v, r);
+        steps_by_colour[r]++;
+      }
+      return check();
+    }
     const dim3 gr((M + 127) / 128, N), gu((P / 4 + 31) / 32, (N - 2 + 7) / 8);
     for (int64_t s = 0; s < steps; ++s) {
       const int r = colours[s];
@@ -394,15 +454,23 @@ RT_API rt_status rt_lozenge_walk(int32_t* tiling, int32_t n_side, int64_t steps,
   std::unique_ptr<LzSampler> s;
   if (rt_status st = LzSampler::create(n_side, 1, o, &s)) return st;
   if (rt_status st = s->load(0, tiling)) return st;
-  if (o.rng_mode == RT_RNG_TINYMT) {
-    // LozengeTiler.cpp:71 (OpenCL branch): generators seeded with the walk seed itself.
-    if (rt_status st = s->seed((uint32_t)seed)) return st;
+  if (o.rng_mode != RT_RNG_FAST) {
+    // LozengeTiler.cpp:71-88: TinyMT generators (OpenCL branch) or MTGP block generators
+    // (CUDA branch) seeded from the walk seed itself, colours from default_random_engine(seed).
+    if (rt_status st = s->seed(o.rng_mode == RT_RNG_MTGP ? seed : (int64_t)(uint32_t)seed)) return st;
     std::vector<uint8_t> col = lz_colours(seed, steps);
     if (rt_status st = s->run(col.data(), steps)) return st;
   } else {
     if (rt_status st = s->run_fast((uint64_t)seed, 0, steps)) return st;
   }
   return s->store(0, tiling);
+}
+
+RT_API rt_status rt_lozenge_mtgp_draws(int32_t n_side, int64_t seed, int64_t launches, float* out) {
+  clear_error();
+  if (n_side < 9 || n_side % 3 || n_side > 32766 || launches < 0 || (launches > 0 && !out))
+    return fail(RT_ERR_INVALID_ARGUMENT, "lozenge mtgp_draws: n_side a multiple of 3 in [9, 32766], launches >= 0");
+  return mtgp_draws_grid(n_side, n_side / 3, seed, launches, out);
 }
 
 RT_API rt_status rt_lozenge_cftp(const int32_t* tmax, const int32_t* tmin, int32_t n_side, int64_t driver_seed,
@@ -430,7 +498,7 @@ RT_API rt_status rt_lozenge_cftp(const int32_t* tmax, const int32_t* tmin, int32
     int64_t before[3] = {s->steps_by_colour[0], s->steps_by_colour[1], s->steps_by_colour[2]};
     cudaEventRecord(s->ev0, s->stream);
     int64_t look_back = 0;
-    if (o.rng_mode == RT_RNG_TINYMT) {
+    if (o.rng_mode != RT_RNG_FAST) {
       // Each epoch is one reference Walk(t, steps_k, seed_k) on both chains.
       for (size_t k = 0; k < steps.size(); ++k) {
         if (rt_status st = s->seed(seeds[k])) return st;
@@ -458,7 +526,7 @@ RT_API rt_status rt_lozenge_cftp(const int32_t* tmax, const int32_t* tmin, int32
       if (stats) *stats = st_out;
       return s->store(1, out);
     }
-    if (o.rng_mode == RT_RNG_TINYMT) {
+    if (o.rng_mode != RT_RNG_FAST) {
       const int64_t next = schedule == 0 ? steps.back() * 2 : steps.front() * 2;
       steps.insert(steps.begin(), next);
       seeds.insert(seeds.begin(), (uint32_t)drv());

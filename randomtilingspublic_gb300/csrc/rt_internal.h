@@ -29,6 +29,25 @@ inline rt_status dev_alloc(T** p, size_t bytes, cudaStream_t s) {
   return st;
 }
 
+// cuRAND MTGP32 generators in the reference's CUDA geometry (domino_mtgp.cu): 8 x 8 thread
+// blocks over a rows x cols grid of sites (row from the x index, column from the y index),
+// block (bx, by) drawing from generator bx * gy + by.
+struct MtgpGrid {
+  int gx = 0, gy = 0;
+  int count() const { return gx * gy; }
+};
+constexpr int kMtgpBlock = 8;  // BLOCK_DIM of the reference (dominokernel.cuh:4, lozengekernel.cuh:4)
+inline MtgpGrid mtgp_grid(int rows, int cols) {
+  return MtgpGrid{(rows + kMtgpBlock - 1) / kMtgpBlock, (cols + kMtgpBlock - 1) / kMtgpBlock};
+}
+size_t mtgp_state_bytes(int count);
+// Seeds generator k with seed + k through curandMakeMTGP32KernelState (blocking copies, so
+// the stream is drained first).
+rt_status mtgp_seed(void* states, int count, int64_t seed, cudaStream_t stream);
+// The draws of `launches` launches on a fresh grid seeded seed + k: out[h][x][y] for
+// x < rows, y < cols (host memory).
+rt_status mtgp_draws_grid(int rows, int cols, int64_t seed, int64_t launches, float* out);
+
 // Vertex classes of DomainToVertices: 0 outside, 1 interior, 2 boundary.
 void domino_vertex_classes(const int32_t* domain, int m_side, int32_t* out);
 // Interior vertices (flip candidates) of the domain a tiling covers.

@@ -244,6 +244,7 @@ _LZ_SIG = {
     "orc_lz_tiling_to_domain": (None, [_P, C.c_int, _P]),
     "orc_lz_walk_tinymt": (C.c_int, [_P, C.c_int, _L, _L, _P, _L]),
     "orc_lz_walk_fast": (C.c_int, [_P, C.c_int, _L, _L, C.c_ulong, C.c_uint]),
+    "orc_lz_walk_draws": (C.c_int, [_P, C.c_int, _P, _L, _L]),
     "orc_lz_cftp": (C.c_int, [_P, _P, C.c_int, _L, _L, C.c_int, C.c_int, C.c_int, C.c_uint, _P, _P]),
     "orc_lz_set_rule": (None, [C.c_int, C.c_double]),
 }
@@ -287,6 +288,13 @@ def lz_tiling_to_heightfunc(t, d) -> np.ndarray:
 
 def lz_walk_tinymt(t: np.ndarray, n: int, steps: int, seed: int) -> None:
     assert lz_lib().orc_lz_walk_tinymt(_p(t), n, steps, seed, None, 0) == 0
+
+
+def lz_walk_draws(t: np.ndarray, n: int, draws: np.ndarray, steps: int, seed: int) -> None:
+    """The reference's CUDA-path lozenge walk with its MTGP32 draws supplied (steps x n x n/3)."""
+    d = np.ascontiguousarray(draws, np.float32)
+    assert d.size == steps * n * (n // 3)
+    assert lz_lib().orc_lz_walk_draws(_p(t), n, _p(d), steps, seed) == 0
 
 
 def lz_walk_fast(t: np.ndarray, n: int, h0: int, steps: int, seed: int, stream: int = 0) -> None:

@@ -1,5 +1,6 @@
-"""The cuRAND MTGP32 mode of the domino sweep (RT_RNG_MTGP): the random stream of the
-reference's CUDA build (DominoTiler.cpp:51-66, dominokernel*.cu).
+"""The cuRAND MTGP32 mode of the domino and lozenge sweeps (RT_RNG_MTGP): the random stream
+of the reference's CUDA build (DominoTiler.cpp:51-66, dominokernel*.cu; LozengeTiler.cpp:71-80,
+lozengekernel.cu).
 
 cuRAND's generator is library code: the oracle does not restate it but takes its draws as
 data (rt_domino_mtgp_draws: the curand_uniform value each candidate site receives in the
@@ -156,8 +157,8 @@ def test_mtgp_sampler_refuses_unseeded_runs_and_the_resident_engine(rt):
     s.close()
     with pytest.raises(rt.RTError):
         rt.DominoSampler(n, 1, rt.DominoTiler(rng="mtgp", engine=2))
-    with pytest.raises(rt.RTError):
-        rt.LozengeTiler(rng="mtgp").Walk(rt.LozengeTiler.MaxTiling(rt.LozengeTiler.Hexagon(3)), 4, 1)
+    with pytest.raises(rt.RTError):  # the reference's q kernel has no CUDA build to match
+        rt.LozengeTiler(rng="mtgp", q=0.9).Walk(rt.LozengeTiler.MaxTiling(rt.LozengeTiler.Hexagon(3)), 4, 1)
 
 
 @pytest.mark.gpu
@@ -183,3 +184,57 @@ def test_cpp_dropin_load_mtgp_walk_equals_the_reference_cuda_path(rt, orc, tmp_p
     want = tmax.copy()
     orc.walk_draws(want, n, rt.mtgp_draws(n, 34893, 100), 100, 34893, 0)
     assert np.array_equal(got, want)
+
+
+def _lz_mixed(rt, orc, side):
+    L = rt.LozengeTiler
+    d = L.Hexagon(side)
+    tmax, tmin = L.MaxTiling(d), L.MinTiling(d)
+    t = tmax.copy()
+    orc.lz_walk_tinymt(t, rt.side_of(t), 300, 5)
+    return t, tmax, tmin
+
+
+@pytest.mark.gpu
+def test_mtgp_lozenge_walk_equals_the_reference_cuda_path_on_its_draws(rt, orc):
+    start, _, _ = _lz_mixed(rt, orc, 7)
+    n = rt.side_of(start)
+    steps, seed = 120, 2**33 + 17  # a seed beyond 32 bits: generator k gets seed + k in full
+    want = start.copy()
+    orc.lz_walk_draws(want, n, rt.lozenge_mtgp_draws(n, seed, steps), steps, seed)
+    got = start.copy()
+    tiler = rt.LozengeTiler()
+    tiler.LoadMTGP()
+    tiler.Walk(got, steps, seed)
+    assert np.array_equal(got, want)
+    assert (got != start).sum() > 8
+    draws = rt.lozenge_mtgp_draws(n, seed, 2)
+    assert draws.shape == (2, n, n // 3) and draws.min() > 0 and draws.max() <= 1
+
+
+@pytest.mark.gpu
+def test_mtgp_lozenge_cftp_equals_epochs_of_reference_walks(rt, orc):
+    """rt_lozenge_cftp: every epoch is one reference Walk(t, steps_k, seed_k) of both chains,
+    seeds from mt19937(driver_seed), look-back prepending 2 * steps.back()."""
+    _, tmax, tmin = _lz_mixed(rt, orc, 3)
+    n = rt.side_of(tmax)
+    driver_seed, first, max_attempts = 4242, 4, 30
+    drv = iter(orc.mt19937(driver_seed, 64))
+    steps, seeds = [first], [int(next(drv))]
+    for attempt in range(1, max_attempts + 1):
+        top, bot = tmax.copy(), tmin.copy()
+        for k, sd in zip(steps, seeds):
+            d = rt.lozenge_mtgp_draws(n, sd, k)
+            orc.lz_walk_draws(top, n, d, k, sd)
+            orc.lz_walk_draws(bot, n, d, k, sd)
+        if np.array_equal(top, bot):
+            break
+        steps.insert(0, steps[-1] * 2)
+        seeds.insert(0, int(next(drv)))
+    else:
+        pytest.fail("oracle driver did not coalesce")
+    assert attempt > 1
+    got, stats = rt.LozengeTiler(rng="mtgp").cftp(tmax, tmin, driver_seed=driver_seed, first_steps=first,
+                                                  max_attempts=max_attempts)
+    assert stats["attempts"] == attempt
+    assert np.array_equal(got, top)
