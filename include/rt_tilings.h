@@ -51,9 +51,10 @@ typedef int32_t rt_status;
                            site); no generator state in memory */
 #define RT_RNG_MTGP 2   /* cuRAND MTGP32, one generator per 8 x 8 block of sites seeded
                            seed + block, the reference's CUDA path (DominoTiler.cpp:51-66,
-                           dominokernel*.cu; LozengeTiler.cpp:71-80, lozengekernel.cu):
-                           domino and uniform lozenge walks, epochs and CFTP through the
-                           per-step kernels; the same draws as the reference's build */
+                           dominokernel*.cu; LozengeTiler.cpp:71-80, lozengekernel.cu;
+                           RectTriangleTiler.cpp:75-85): domino, uniform lozenge and
+                           rectangle-triangle walks, epochs and CFTP through the per-step
+                           kernels; the same draws as the reference's build */
 
 /* Flip rules: the reference picks one by compiling one of four kernel files. */
 #define RT_DOMINO_PLAIN 0            /* src/Domino/dominokernel.cl:4-18 (propose 0.8) */
@@ -217,13 +218,18 @@ RT_API rt_status rt_recttri_from_lozenge(const int32_t* lozenge, int32_t n_side,
                                          int32_t m_rows, int32_t* out);
 /* RectTriangleTiler::Walk(tiling&, int steps, long seed) (RectTriangleTiler.cpp:33-171):
    per step a colour ((i - j) mod 3) from default_random_engine(seed) +
-   uniform_int_distribution(0, 2) (TinyMT mode, generator k seeded with seed + k) or h mod 3
-   (fast mode), then flipTiles (recttrianglekernel.cl:25-118) on that colour and
+   uniform_int_distribution(0, 2) (TinyMT mode, generator k seeded with seed + k; MTGP mode,
+   block generator k seeded seed + k as the CUDA branch does, RectTriangleTiler.cpp:75-85)
+   or h mod 3 (fast mode), then flipTiles (recttrianglekernel.cl:25-118) on that colour and
    updateTiles1/2 (:120-146) on the two others.  weights9 = {wt1, wt2, wt3, wm1, wm2, wm3,
    wr1, wr2, wr3}, the compile-time constants of recttrianglekernel.cl:3-11 (NULL: all 1, the
    reference's values); float arithmetic as the reference kernel.  opts->rule is ignored. */
 RT_API rt_status rt_recttri_walk(int32_t* tiling, int32_t n_side, int64_t steps, int64_t seed,
                                  const double* weights9, const rt_walk_opts* opts);
+/* The MTGP mode's float draws of a rectangle-triangle walk: the layout of
+   rt_lozenge_mtgp_draws (launches x n_side x n_side/3; flipTilesKernel draws at
+   recttrianglekernel.cu:39-40 on the same grid). */
+RT_API rt_status rt_recttri_mtgp_draws(int32_t n_side, int64_t seed, int64_t launches, float* out);
 
 /* ---- six-vertex model ----------------------------------------------------------------------
    No counterpart in the reference (which has no six-vertex model); the entry points follow the

@@ -13,8 +13,8 @@
 //   * failures throw rt::Error instead of printing and calling exit();
 //   * the OpenCL constructors (context, queue, devices, kernel source) are replaced by
 //     default construction; LoadTinyMT / LoadMTGP are accepted where the reference has them
-//     (DominoTiler::LoadMTGP and LozengeTiler::LoadMTGP select the cuRAND MTGP32 mode; the
-//     other tilers ignore it).
+//     (the domino, lozenge and rectangle-triangle tilers' LoadMTGP selects the cuRAND MTGP32
+//     mode; TriangleDimerTiler ignores it).
 // Header-only; link with -lrt_tilings.
 #ifndef RT_TILINGS_HPP_
 #define RT_TILINGS_HPP_
@@ -275,7 +275,9 @@ class RectTriangleTiler {
     if (w_.size() != 9) throw Error(RT_ERR_INVALID_ARGUMENT, "nine weights");
   }
   void LoadTinyMT(const std::string&, int) {}
-  void LoadMTGP() {}
+  // RectTriangleTiler::LoadMTGP (RectTriangleTiler.cpp:27-30): walks then draw from cuRAND
+  // MTGP32 block generators, as in the reference's CUDA build (RT_RNG_MTGP).
+  void LoadMTGP() { opts_.rng_mode = RT_RNG_MTGP; }
 
   void Walk(tiling& t, int steps, long seed) {
     check(rt_recttri_walk(t.data(), side_of(t), steps, seed, w_.data(), &opts_));

@@ -6,6 +6,9 @@
 //     the walk seed itself, colours from default_random_engine + uniform_int_distribution(0, 2),
 //     flipTiles recttrianglekernel.cl:25-118 (with getWeightRatio :157-160), updateTiles1
 //     :120-132, updateTiles2 :134-146
+//   * Walk as the CUDA path runs it, given its MTGP32 draws (cuRAND's generator comes in as
+//     data): flipTilesKernel recttrianglekernel.cu:31-133 decides as flipTiles does, on every
+//     slot of the N x N/3 grid, with the same colour stream and updates
 // plus the library's fast mode (colour h mod 3, Philox draws per column quad).  The nine
 // weights are runtime arguments here (compile-time #defines at recttrianglekernel.cl:3-11).
 // Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg may load this.
@@ -202,6 +205,31 @@ int orc_rt_walk_tinymt(int* t, int N, long steps, long seed, const double* w9) {
         const float rd = oracle::tmt_u23_to_float(oracle::tmt_next_u23(g[(size_t)i * M + j]));
         int& e = c.X[r][(size_t)i * M + j];
         e = flip_site(e, rd, W);
+      }
+    rupdate(c, r);
+  }
+  rmerge(c, t);
+  return 0;
+}
+
+// RectTriangleTiler::Walk(t, steps, seed), CUDA path (RectTriangleTiler.cpp:75-133), with the
+// MTGP32 draws supplied: draws[s][i][j] is the curand_uniform value of slot (i, j) at step s.
+int orc_rt_walk_draws(int* t, int N, const float* draws, long steps, long seed, const double* w9) {
+  if (N % 3 || N < 9) return -1;
+  RChain c;
+  rsplit(t, N, c);
+  const Weights W = make_weights(w9);
+  const int M = c.M;
+  std::default_random_engine gen;
+  std::uniform_int_distribution<int> dist(0, 2);
+  gen.seed(seed);
+  for (long s = 0; s < steps; ++s) {
+    const int r = dist(gen);
+    const float* d = draws + (size_t)s * N * M;
+    for (int i = 0; i < N; ++i)
+      for (int j = 0; j < M; ++j) {
+        int& e = c.X[r][(size_t)i * M + j];
+        e = flip_site(e, d[(size_t)i * M + j], W);
       }
     rupdate(c, r);
   }

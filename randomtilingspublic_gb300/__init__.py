@@ -138,6 +138,7 @@ _SIGNATURES = {
     "rt_domino_rule_table": (C.c_int32, [C.c_int32, C.c_int32, C.c_double, C.c_double, _P]),
     "rt_domino_mtgp_draws": (C.c_int32, [C.c_int32, C.c_int64, C.c_int64, _P]),
     "rt_lozenge_mtgp_draws": (C.c_int32, [C.c_int32, C.c_int64, C.c_int64, _P]),
+    "rt_recttri_mtgp_draws": (C.c_int32, [C.c_int32, C.c_int64, C.c_int64, _P]),
     "rt_dm_sweep_noalloc": (C.c_int32, [_P, _P, C.c_int32, C.c_int32, _P, C.c_int64, C.c_uint64, C.c_int64, _P]),
     "rt_cftp_batch": (C.c_int32, [_P, C.c_int32, _P, _P]),
     "rt_server_create": (C.c_int32, [_P, _P]),
@@ -538,7 +539,8 @@ class RectTriangleTiler:
     """Rectangle-triangle tilings (src/RectTriangle/RectTriangleTiler.h:32-86).  ``weights``
     holds the nine tile weights {wt1, wt2, wt3, wm1, wm2, wm3, wr1, wr2, wr3}
     (recttrianglekernel.cl:3-11; all 1 by default, the reference's values).  ``rng`` is
-    'tinymt' (bit-exact with the reference's OpenCL path) or 'fast'."""
+    'tinymt' (bit-exact with the reference's OpenCL path), 'mtgp' (its CUDA path's cuRAND
+    MTGP32 draws; also selected by LoadMTGP) or 'fast'."""
 
     def __init__(self, rng: str = "tinymt", fast_stream: int = 0, weights=None):
         self.rng = rng
@@ -546,6 +548,11 @@ class RectTriangleTiler:
         self.weights = None if weights is None else np.ascontiguousarray(weights, np.float64)
         if self.weights is not None and self.weights.shape != (9,):
             raise ValueError("weights: nine values {wt1, wt2, wt3, wm1, wm2, wm3, wr1, wr2, wr3}")
+
+    def LoadMTGP(self) -> None:
+        """RectTriangleTiler::LoadMTGP (RectTriangleTiler.cpp:27-30): walks draw from cuRAND
+        MTGP32 block generators, as the reference's CUDA build."""
+        self.rng = "mtgp"
 
     def opts(self) -> _WalkOpts:
         o = _WalkOpts()
@@ -973,6 +980,15 @@ def lozenge_mtgp_draws(n_side: int, seed: int, launches: int) -> np.ndarray:
     return out
 
 
+def recttri_mtgp_draws(n_side: int, seed: int, launches: int) -> np.ndarray:
+    """The 'mtgp' mode's float draws of a rectangle-triangle walk, laid out as
+    lozenge_mtgp_draws (recttrianglekernel.cu:39-40)."""
+    n = int(n_side)
+    out = np.zeros((int(launches), n, n // 3), np.float32)
+    _check(lib().rt_recttri_mtgp_draws(n, int(seed), int(launches), _ptr(out)))
+    return out
+
+
 def SaveMatrix(a, path, rows: int | None = None, cols: int | None = None) -> None:
     """The reference's SaveMatrix (src/common/common.cpp:84-128): without rows/cols the
     square overload (floor(sqrt(size))^2 values)."""
@@ -1012,4 +1028,5 @@ def mt19937_draws(seed: int, count: int) -> np.ndarray:
 
 
 __all__ = ["DominoTiler", "DominoSampler", "LozengeTiler", "RectTriangleTiler", "SixVertexTiler", "TriangleDimerTiler", "cftp_batch", "Server", "RTError", "lib", "read_tinymt_params", "mt19937_colours",
-           "mt19937_draws", "mtgp_draws", "lozenge_mtgp_draws", "CftpStats"]
+           "mt19937_draws", "mtgp_draws", "lozenge_mtgp_draws", "recttri_mtgp_draws",
+           "CftpStats"]

@@ -10,8 +10,11 @@
 //     the quarter of the rescaled draw;
 //   * the twelve rectangle-pair hexagons toggle with their partner.
 // The nine weights are runtime arguments; the reference hard-codes them at
-// recttrianglekernel.cl:3-11.
+// recttrianglekernel.cl:3-11.  MTGP mode: the reference's CUDA build's random stream (8 x 8
+// blocks over the N x N/3 slots of the drawn colour, one cuRAND MTGP32 generator per block
+// seeded seed + block; RectTriangleTiler.cpp:75-85, recttrianglekernel.cu:31-43).
 #include <cuda_runtime.h>
+#include <curand_kernel.h>
 
 #include <algorithm>
 #include <cmath>
@@ -94,6 +97,20 @@ __global__ void k_rt_flip_tmt(RtView v, int r, RtWeights W) {
   v.tmt[k] = s;
   int32_t* p = v.colour(r) + (size_t)i * v.P + j;
   const int e = *p, n = rt_flip(e, (float)u * (1.0f / 8388608.0f), W);
+  if (n != e) *p = n;
+}
+
+// MTGP mode: every thread of the block draws before the bounds test (recttrianglekernel.cu:35-43);
+// flipTilesKernel decides as flipTiles does.
+__global__ void __launch_bounds__(kMtgpBlock* kMtgpBlock) k_rt_flip_mtgp(RtView v, int r, RtWeights W,
+                                                                          curandStateMtgp32* states) {
+  pdl_begin();
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int j = blockIdx.y * blockDim.y + threadIdx.y;
+  const float rd = curand_uniform(states + blockIdx.x * gridDim.y + blockIdx.y);
+  if (i >= v.N || j >= v.M) return;
+  int32_t* p = v.colour(r) + (size_t)i * v.P + j;
+  const int e = *p, n = rt_flip(e, rd, W);
   if (n != e) *p = n;
 }
 
@@ -337,6 +354,13 @@ RT_API rt_status rt_recttri_from_lozenge(const int32_t* lozenge, int32_t n_side,
   return RT_OK;
 }
 
+RT_API rt_status rt_recttri_mtgp_draws(int32_t n_side, int64_t seed, int64_t launches, float* out) {
+  clear_error();
+  if (n_side < 9 || n_side % 3 || n_side > 32766 || launches < 0 || (launches > 0 && !out))
+    return fail(RT_ERR_INVALID_ARGUMENT, "recttri mtgp_draws: n_side a multiple of 3 in [9, 32766], launches >= 0");
+  return mtgp_draws_grid(n_side, n_side / 3, seed, launches, out);
+}
+
 RT_API rt_status rt_recttri_walk(int32_t* tiling, int32_t n_side, int64_t steps, int64_t seed, const double* weights9,
                                  const rt_walk_opts* opts) {
   clear_error();
@@ -346,7 +370,8 @@ RT_API rt_status rt_recttri_walk(int32_t* tiling, int32_t n_side, int64_t steps,
   if (!tiling || steps < 0) return fail(RT_ERR_INVALID_ARGUMENT, "recttri walk: NULL tiling or negative steps");
   if (n_side < 9 || n_side % 3 || n_side > 32766)
     return fail(RT_ERR_INVALID_ARGUMENT, "recttri tiling side must be a multiple of 3 in [9, 32766]");
-  if (o.rng_mode != RT_RNG_TINYMT && o.rng_mode != RT_RNG_FAST) return fail(RT_ERR_INVALID_ARGUMENT, "unknown rng mode");
+  if (o.rng_mode != RT_RNG_TINYMT && o.rng_mode != RT_RNG_FAST && o.rng_mode != RT_RNG_MTGP)
+    return fail(RT_ERR_INVALID_ARGUMENT, "unknown rng mode");
   if (o.rng_mode == RT_RNG_FAST && o.fast_stream >= 65536u) return fail(RT_ERR_INVALID_ARGUMENT, "fast_stream must be < 65536");
   for (size_t p = 0; p < (size_t)n_side * n_side; ++p)
     if ((uint32_t)tiling[p] > 0xffffffu) return fail(RT_ERR_INVALID_ARGUMENT, "recttri tiling values must be six hex digits");
@@ -360,16 +385,20 @@ RT_API rt_status rt_recttri_walk(int32_t* tiling, int32_t n_side, int64_t steps,
   cudaStream_t stream = (cudaStream_t)o.cuda_stream;
   int32_t *base = nullptr, *scratch = nullptr;
   uint4* tmt = nullptr;
+  void* mtgp = nullptr;
+  const MtgpGrid mg = mtgp_grid(N, M);
   auto cleanup = [&]() {
     if (base) cudaFree(base);
     if (scratch) cudaFree(scratch);
     if (tmt) cudaFree(tmt);
+    if (mtgp) cudaFree(mtgp);
   };
   const size_t cs = (size_t)N * P;
   rt_status status = RT_OK;
   do {
     if (cudaMalloc(&base, 3 * cs * sizeof(int32_t)) != cudaSuccess || cudaMalloc(&scratch, (size_t)N * N * sizeof(int32_t)) != cudaSuccess ||
-        (o.rng_mode == RT_RNG_TINYMT && cudaMalloc(&tmt, (size_t)N * M * sizeof(uint4)) != cudaSuccess)) {
+        (o.rng_mode == RT_RNG_TINYMT && cudaMalloc(&tmt, (size_t)N * M * sizeof(uint4)) != cudaSuccess) ||
+        (o.rng_mode == RT_RNG_MTGP && cudaMalloc(&mtgp, mtgp_state_bytes(mg.count())) != cudaSuccess)) {
       cudaGetLastError();
       status = fail(RT_ERR_OUT_OF_MEMORY, "recttri walk: device allocation failed");
       break;
@@ -391,6 +420,19 @@ RT_API rt_status rt_recttri_walk(int32_t* tiling, int32_t n_side, int64_t steps,
       for (int64_t s = 0; s < steps; ++s) {
         const int r = dist(gen);
         pdl_launch(k_rt_flip_tmt, gr, dim3(128), stream, v, r, W);
+        pdl_launch(k_rt_update, gu, dim3(128), stream, v, r);
+      }
+    } else if (o.rng_mode == RT_RNG_MTGP) {
+      // RectTriangleTiler.cpp:75-85 (CUDA branch): block generator k seeded seed + k; the
+      // colours as above.
+      if ((status = mtgp_seed(mtgp, mg.count(), seed, stream)) != RT_OK) break;
+      std::default_random_engine gen;
+      std::uniform_int_distribution<int> dist(0, 2);
+      gen.seed(seed);
+      for (int64_t s = 0; s < steps; ++s) {
+        const int r = dist(gen);
+        pdl_launch(k_rt_flip_mtgp, dim3(mg.gx, mg.gy), dim3(kMtgpBlock, kMtgpBlock), stream, v, r, W,
+                   static_cast<curandStateMtgp32*>(mtgp));
         pdl_launch(k_rt_update, gu, dim3(128), stream, v, r);
       }
     } else {

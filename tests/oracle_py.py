@@ -315,6 +315,7 @@ _RT_SIG = {
     "orc_rt_hex": (C.c_int, [C.c_int, C.c_int, _P, _L]),
     "orc_rt_walk_tinymt": (C.c_int, [_P, C.c_int, _L, _L, _P]),
     "orc_rt_walk_fast": (C.c_int, [_P, C.c_int, _L, _L, C.c_ulong, C.c_uint, _P]),
+    "orc_rt_walk_draws": (C.c_int, [_P, C.c_int, _P, _L, _L, _P]),
 }
 RT_UNIT_WEIGHTS = np.ones(9, np.float64)
 
@@ -439,3 +440,11 @@ class lz_rule:
 
     def __exit__(self, *exc):
         lz_lib().orc_lz_set_rule(0, 1.0)
+
+
+def rt_walk_draws(t: np.ndarray, n: int, draws: np.ndarray, steps: int, seed: int, weights=None) -> None:
+    """The reference's CUDA-path rectangle-triangle walk with its MTGP32 draws supplied."""
+    w = _w9(weights)
+    d = np.ascontiguousarray(draws, np.float32)
+    assert d.size == steps * n * (n // 3)
+    assert rt_lib().orc_rt_walk_draws(_p(t), n, _p(d), steps, seed, _p(w)) == 0

@@ -1,6 +1,6 @@
-"""The cuRAND MTGP32 mode of the domino and lozenge sweeps (RT_RNG_MTGP): the random stream
-of the reference's CUDA build (DominoTiler.cpp:51-66, dominokernel*.cu; LozengeTiler.cpp:71-80,
-lozengekernel.cu).
+"""The cuRAND MTGP32 mode of the domino, lozenge and rectangle-triangle sweeps (RT_RNG_MTGP):
+the random stream of the reference's CUDA build (DominoTiler.cpp:51-66, dominokernel*.cu;
+LozengeTiler.cpp:71-80, lozengekernel.cu; RectTriangleTiler.cpp:75-85, recttrianglekernel.cu).
 
 cuRAND's generator is library code: the oracle does not restate it but takes its draws as
 data (rt_domino_mtgp_draws: the curand_uniform value each candidate site receives in the
@@ -238,3 +238,21 @@ def test_mtgp_lozenge_cftp_equals_epochs_of_reference_walks(rt, orc):
                                                   max_attempts=max_attempts)
     assert stats["attempts"] == attempt
     assert np.array_equal(got, top)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("weights", [None, [1.3, 0.7, 1.1, 0.9, 1.6, 0.8, 1.2, 0.5, 1.4]])
+def test_mtgp_recttri_walk_equals_the_reference_cuda_path_on_its_draws(rt, orc, weights):
+    R = rt.RectTriangleTiler
+    start = R.maxHex(6)
+    n = rt.side_of(start)
+    orc.rt_walk_tinymt(start, n, 200, 3, weights)  # away from the extremal hexagon
+    steps, seed = 90, 8675309
+    want = start.copy()
+    orc.rt_walk_draws(want, n, rt.recttri_mtgp_draws(n, seed, steps), steps, seed, weights)
+    tiler = R(weights=weights)
+    tiler.LoadMTGP()
+    got = start.copy()
+    tiler.Walk(got, steps, seed)
+    assert np.array_equal(got, want)
+    assert (got != start).sum() > 8
