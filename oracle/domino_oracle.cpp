@@ -759,6 +759,17 @@ int orc_dm_walk_epochs_draws(int* t, int N, const float* draws, const long* step
   return 0;
 }
 
+// The CUDA kernels' rotation of one colour array in the reference's layout (N rows x N/2
+// bytes), draws per candidate (N-2) x (N/2-2).
+void orc_dm_rotate_cuda_grid(uint8_t* colour, int N, int t, const float* draws, int variant, double a, double b) {
+  const int H = N / 2, cols = H - 2;
+  for (int i = 1; i <= N - 2; ++i)
+    for (int j = 1; j <= cols; ++j) {
+      uint8_t& e = colour[(size_t)i * H + j];
+      e = rotate_cu(e, draws[(size_t)(i - 1) * cols + (j - 1)], variant, i, t, a, b);
+    }
+}
+
 // The CUDA kernels' decision for n draws of one (state, variant, row, colour) case.
 void orc_dm_rotate_cuda_many(const float* rd, long n, int e, int variant, int i, int t, double a, double b,
                              uint8_t* out) {

@@ -434,6 +434,12 @@ int orc_lz_walk_draws(int* t, int N, const float* draws, long steps, long seed) 
   return 0;
 }
 
+// The CUDA kernel's rotation of one colour array (N rows x N/3 bytes), draws per slot.
+void orc_lz_rotate_cuda_grid(uint8_t* colour, int N, const float* draws) {
+  const size_t n = (size_t)N * (N / 3);
+  for (size_t k = 0; k < n; ++k) colour[k] = lrotate_cu(colour[k], draws[k]);
+}
+
 int orc_lz_walk_fast(int* t, int N, long h0, long steps, unsigned long seed, unsigned stream) {
   if (N % 3 || N < 6) return -1;
   LChain c;

@@ -237,6 +237,13 @@ int orc_rt_walk_draws(int* t, int N, const float* draws, long steps, long seed, 
   return 0;
 }
 
+// flipTiles on one colour array (N rows x N/3 ints), draws per slot.
+void orc_rt_flip_grid(int* colour, int N, const float* draws, const double* w9) {
+  const Weights W = make_weights(w9);
+  const size_t n = (size_t)N * (N / 3);
+  for (size_t k = 0; k < n; ++k) colour[k] = flip_site(colour[k], draws[k], W);
+}
+
 // Fast mode: colour h mod 3, draws u32 per site; rd = u * 2^-32 evaluated in float as
 // flipTiles does (the library's stated fast-mode rule for this model).
 int orc_rt_walk_fast(int* t, int N, long h0, long steps, unsigned long seed, unsigned stream, const double* w9) {

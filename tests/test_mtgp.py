@@ -33,13 +33,34 @@ def test_mtgp_rule_intervals_decide_as_the_cuda_kernels(rt, orc, rule, a, b):
             assert np.array_equal(mine, want), (rule, c, e, bits[mine != want][:4])
 
 
-def test_mtgp_two_periodic_rule_is_the_cuda_kernels_not_the_opencl_ones(orc):
-    """dominokerneltwoperiodic.cu compares the float draw with the double 0.8 and divides in
-    double; the .cl kernel uses a float 0.8.  The first float at or above 0.8 separates them."""
-    rd = np.array([np.float32(0.8)], np.float32)  # rounds to 0.800000011920929 > 0.8
-    assert orc.rotate_cuda(rd, 3, 2, 2, 0, 1.0, 1.0)[0] == 3  # double 0.8: no proposal
-    below = np.nextafter(np.float32(0.8), np.float32(0), dtype=np.float32)
-    assert orc.rotate_cuda(np.array([below], np.float32), 3, 2, 2, 0, 1.0, 1.0)[0] == 12
+def test_mtgp_two_periodic_rule_is_the_cuda_kernels_not_the_opencl_ones(rt, orc):
+    """dominokerneltwoperiodic.cu divides the draw by the double 0.8 and rounds to float; the
+    .cl kernel divides by the float 0.8 in float.  The two thresholds differ by an ulp for some
+    draws, which decides a flip when the weight ratio equals the larger one: with b = 1 the up
+    move at an odd row of colour 1 has ratio float(a^2), so a = sqrt(threshold) builds such a
+    case.  There the MTGP table decides as the CUDA kernel and the TinyMT table as the .cl one."""
+    u = np.arange(1 << 20, int(0.8 * 2**23), dtype=np.int64)
+    rd = (u.astype(np.float64) / 2**23).astype(np.float32)  # exact: u23 * 2^-23
+    cu = (rd.astype(np.float64) / 0.8).astype(np.float32)
+    cl = rd / np.float32(0.8)
+    for k in np.nonzero(cu != cl)[0]:
+        r = max(cu[k], cl[k])
+        a = float(np.sqrt(np.float64(r)))
+        if np.float32(a * a) == r:
+            break
+    else:
+        pytest.fail("no separating draw")
+    c = 3  # odd row, colour 1
+    tiny = np.zeros(16, np.uint32)
+    mtgp = np.zeros(16, np.uint32)
+    assert rt.lib().rt_domino_rule_table(2, rt.RNG_MODES["tinymt"], a, 1.0, tiny.ctypes.data) == 0
+    assert rt.lib().rt_domino_rule_table(2, rt.RNG_MODES["mtgp"], a, 1.0, mtgp.ctypes.data) == 0
+    flip_cl = ((int(u[k]) - int(tiny[4 * c])) % 2**32) < int(tiny[4 * c + 1])
+    bits = int(rd[k:k + 1].view(np.uint32)[0])
+    flip_cu = ((bits - int(mtgp[4 * c])) % 2**32) < int(mtgp[4 * c + 1])
+    assert flip_cu == bool(r > cu[k]) and flip_cl == bool(r > cl[k])
+    assert flip_cu != flip_cl
+    assert (orc.rotate_cuda(rd[k:k + 1], 3, 2, 3, 1, a, 1.0)[0] == 12) == flip_cu
 
 
 def _aztec(rt, order):
