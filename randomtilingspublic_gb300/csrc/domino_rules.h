@@ -25,7 +25,8 @@ uint8_t dm_rule_reference(uint8_t e, uint32_t u23, int rule, int i, int t, doubl
 
 // The same decision as the reference's CUDA kernels make it (src/Domino/dominokernel*.cu,
 // float draw rd from cuRAND's MTGP32); it differs from the OpenCL kernels only in the
-// two-periodic rule, which compares and divides in double there.
+// two-periodic rule, which divides the draw by the double 0.8 there (by a float 0.8 in the
+// .cl kernel), so a threshold can round one ulp apart.
 uint8_t dm_rule_reference_cuda(uint8_t e, float rd, int rule, int i, int t, double a, double b);
 
 }  // namespace rt
