@@ -52,9 +52,10 @@ typedef int32_t rt_status;
 #define RT_RNG_MTGP 2   /* cuRAND MTGP32, one generator per 8 x 8 block of sites seeded
                            seed + block, the reference's CUDA path (DominoTiler.cpp:51-66,
                            dominokernel*.cu; LozengeTiler.cpp:71-80, lozengekernel.cu;
-                           RectTriangleTiler.cpp:75-85): domino, uniform lozenge and
-                           rectangle-triangle walks, epochs and CFTP through the per-step
-                           kernels; the same draws as the reference's build */
+                           RectTriangleTiler.cpp:75-85, TriangleDimerTiler.cpp:279-291):
+                           domino, uniform lozenge, rectangle-triangle and bibone walks,
+                           epochs and CFTP through the per-step kernels; the same draws as
+                           the reference's build */
 
 /* Flip rules: the reference picks one by compiling one of four kernel files. */
 #define RT_DOMINO_PLAIN 0            /* src/Domino/dominokernel.cl:4-18 (propose 0.8) */
@@ -304,6 +305,10 @@ RT_API rt_status rt_td_dimer_indicator(const int32_t* tiling, int32_t n_side, in
    the chosen class on covered vertices) and the device time. */
 RT_API rt_status rt_td_walk(int32_t* tiling, int32_t n_side, int64_t steps, int64_t seed, const rt_walk_opts* opts,
                             rt_cftp_stats* stats);
+/* The MTGP mode's float draws of a bibone walk: out[h][a][b] (launches x M x M, M = n_side/2)
+   is the curand_uniform value of site (a, b) at step h, in the launch of the reference's
+   Rotate*Kernel (triangledimerkernel.cu, 8 x 8 blocks over M x M). */
+RT_API rt_status rt_td_mtgp_draws(int32_t n_side, int64_t seed, int64_t launches, float* out);
 
 /* ---- the reference's text matrix format (src/common/common.cpp:84-178) --------------------
    rt_save_matrix: rows x cols values, each followed by a space, one line per row

@@ -13,8 +13,8 @@
 //   * failures throw rt::Error instead of printing and calling exit();
 //   * the OpenCL constructors (context, queue, devices, kernel source) are replaced by
 //     default construction; LoadTinyMT / LoadMTGP are accepted where the reference has them
-//     (the domino, lozenge and rectangle-triangle tilers' LoadMTGP selects the cuRAND MTGP32
-//     mode; TriangleDimerTiler ignores it).
+//     (every tiler's LoadMTGP selects the cuRAND MTGP32 mode, as in the reference's CUDA
+//     build).
 // Header-only; link with -lrt_tilings.
 #ifndef RT_TILINGS_HPP_
 #define RT_TILINGS_HPP_
@@ -311,7 +311,9 @@ class TriangleDimerTiler {
   explicit TriangleDimerTiler(int rng_mode = RT_RNG_TINYMT, uint32_t fast_stream = 0)
       : opts_(model_opts(rng_mode, fast_stream)) {}
   void LoadTinyMT(const std::string&, int) {}
-  void LoadMTGP() {}
+  // TriangleDimerTiler::LoadMTGP (TriangleDimerTiler.cpp:29-32): walks then draw from cuRAND
+  // MTGP32 block generators, as in the reference's CUDA build (RT_RNG_MTGP).
+  void LoadMTGP() { opts_.rng_mode = RT_RNG_MTGP; }
 
   void Walk(tiling& t, int steps, long seed, rt_cftp_stats* stats = nullptr) {
     check(rt_td_walk(t.data(), side_of(t), steps, seed, &opts_, stats));

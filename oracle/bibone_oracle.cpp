@@ -9,6 +9,10 @@
 //     RotateButterflys :331-353; generator k = row * M + column, seeded seed + k, InitTinyMT
 //     :749-756); a site of the chosen class flips when rd < 0.5 and its state is one of the
 //     two flippable values (5/10, 45/54, 85/170).
+//   * Walk as the CUDA path runs it, given its MTGP32 draws (cuRAND's generator comes in as
+//     data): the same step classes, the draw of site (row a, column b) deciding as
+//     RotateLozengesKernel / RotateTrianglesKernel / RotateButterflysKernel
+//     (triangledimerkernel.cu) do, rd < 0.5
 // The reference keeps eight derived state arrays consistent through 30 update kernels; here
 // the state is the dimer configuration itself (three edge bits per vertex) and each move is
 // the toggle of its alternating cycle, which is what those kernels compute.
@@ -199,6 +203,30 @@ int orc_td_walk_tinymt(int* t, int N, long steps, long seed) {
       const float rd = oracle::tmt_u23_to_float(oracle::tmt_next_u23(g[(size_t)a * M + b]));
       return rd < .5;
     });
+  }
+  to_tiling(d, t, N);
+  return 0;
+}
+
+// TriangleDimerTiler::Walk(t, steps, seed), CUDA path (TriangleDimerTiler.cpp:279-291), with
+// the MTGP32 draws supplied: draws[s][a][b] is the curand_uniform value of site (a, b) at
+// step s.
+int orc_td_walk_draws(int* t, int N, const float* draws, long steps, long seed) {
+  if (N % 2) return -1;
+  Dimers d = from_tiling(t, N);
+  const int M = d.M;
+  std::default_random_engine gen;
+  std::uniform_int_distribution<int> d1(0, 2), d2(0, 1);
+  gen.seed(seed);
+  for (long s = 0; s < steps; ++s) {
+    Step st;
+    st.type = d1(gen);
+    st.r1 = d1(gen);
+    st.r2 = d2(gen);
+    st.p1 = st.p2 = 0;
+    if (st.type == 2) st.p1 = d1(gen), st.p2 = d2(gen);
+    const float* dr = draws + (size_t)s * M * M;
+    run_step(d, st, [&](int a, int b) { return dr[(size_t)a * M + b] < .5; });
   }
   to_tiling(d, t, N);
   return 0;

@@ -139,6 +139,7 @@ _SIGNATURES = {
     "rt_domino_mtgp_draws": (C.c_int32, [C.c_int32, C.c_int64, C.c_int64, _P]),
     "rt_lozenge_mtgp_draws": (C.c_int32, [C.c_int32, C.c_int64, C.c_int64, _P]),
     "rt_recttri_mtgp_draws": (C.c_int32, [C.c_int32, C.c_int64, C.c_int64, _P]),
+    "rt_td_mtgp_draws": (C.c_int32, [C.c_int32, C.c_int64, C.c_int64, _P]),
     "rt_dm_sweep_noalloc": (C.c_int32, [_P, _P, C.c_int32, C.c_int32, _P, C.c_int64, C.c_uint64, C.c_int64, _P]),
     "rt_cftp_batch": (C.c_int32, [_P, C.c_int32, _P, _P]),
     "rt_server_create": (C.c_int32, [_P, _P]),
@@ -600,11 +601,17 @@ class RectTriangleTiler:
 class TriangleDimerTiler:
     """Bibone tilings, i.e. dimer coverings of the triangular lattice
     (src/TriangleDimer/TriangleDimerTiler.h:84-216).  ``rng`` is 'tinymt' (bit-exact with the
-    reference's OpenCL path) or 'fast'."""
+    reference's OpenCL path), 'mtgp' (its CUDA path's cuRAND MTGP32 draws; also selected by
+    LoadMTGP) or 'fast'."""
 
     def __init__(self, rng: str = "tinymt", fast_stream: int = 0):
         self.rng = rng
         self.fast_stream = int(fast_stream)
+
+    def LoadMTGP(self) -> None:
+        """TriangleDimerTiler::LoadMTGP (TriangleDimerTiler.cpp:29-32): walks draw from cuRAND
+        MTGP32 block generators, as the reference's CUDA build."""
+        self.rng = "mtgp"
 
     def opts(self) -> _WalkOpts:
         o = _WalkOpts()
@@ -989,6 +996,15 @@ def recttri_mtgp_draws(n_side: int, seed: int, launches: int) -> np.ndarray:
     return out
 
 
+def td_mtgp_draws(n_side: int, seed: int, launches: int) -> np.ndarray:
+    """The 'mtgp' mode's float draws of a bibone walk: array (launches, M, M), M = n_side // 2,
+    entry [h, a, b] the curand_uniform value site (a, b) receives at step h."""
+    m = int(n_side) // 2
+    out = np.zeros((int(launches), m, m), np.float32)
+    _check(lib().rt_td_mtgp_draws(int(n_side), int(seed), int(launches), _ptr(out)))
+    return out
+
+
 def SaveMatrix(a, path, rows: int | None = None, cols: int | None = None) -> None:
     """The reference's SaveMatrix (src/common/common.cpp:84-128): without rows/cols the
     square overload (floor(sqrt(size))^2 values)."""
@@ -1029,4 +1045,4 @@ def mt19937_draws(seed: int, count: int) -> np.ndarray:
 
 __all__ = ["DominoTiler", "DominoSampler", "LozengeTiler", "RectTriangleTiler", "SixVertexTiler", "TriangleDimerTiler", "cftp_batch", "Server", "RTError", "lib", "read_tinymt_params", "mt19937_colours",
            "mt19937_draws", "mtgp_draws", "lozenge_mtgp_draws", "recttri_mtgp_draws",
-           "CftpStats"]
+           "td_mtgp_draws", "CftpStats"]

@@ -12,6 +12,7 @@
 // Same-class cycles are edge-disjoint (the reference's colourings), and two cycles that can
 // flip together share no vertex, so byte read-modify-writes never race.
 #include <cuda_runtime.h>
+#include <curand_kernel.h>
 
 #include <algorithm>
 #include <cmath>
@@ -101,6 +102,19 @@ __global__ void k_td_step_tmt(uint8_t* D, uint4* tmt, int M, TdStep s) {
   const uint32_t u = tmt_next_u23(g, kTmtMat1, kTmtMat2, kTmtTmat);
   tmt[k] = g;
   if (u < (1u << 22) && td_in_class(s, a, b)) td_try_flip(D, M, td_cycle_of(s), a, b);
+}
+
+// MTGP mode: the reference's CUDA launch (8 x 8 blocks over the M x M sites, row a from
+// the x index, one cuRAND MTGP32 generator per block, TriangleDimerTiler.cpp:279-291); every
+// thread draws before its tests (triangledimerkernel.cu, the three Rotate*Kernel).
+__global__ void __launch_bounds__(kMtgpBlock* kMtgpBlock) k_td_step_mtgp(uint8_t* D, int M, TdStep s,
+                                                                          curandStateMtgp32* states) {
+  pdl_begin();
+  const int a = blockIdx.x * blockDim.x + threadIdx.x;
+  const int b = blockIdx.y * blockDim.y + threadIdx.y;
+  const float rd = curand_uniform(states + blockIdx.x * gridDim.y + blockIdx.y);
+  if (a >= M || b >= M) return;
+  if (rd < 0.5f && td_in_class(s, a, b)) td_try_flip(D, M, td_cycle_of(s), a, b);
 }
 
 // Fast mode: a thread owns columns 4q .. 4q+3 of row a and one Philox block of draws.
@@ -397,6 +411,13 @@ RT_API rt_status rt_td_dimer_indicator(const int32_t* tiling, int32_t n_side, in
   return RT_OK;
 }
 
+RT_API rt_status rt_td_mtgp_draws(int32_t n_side, int64_t seed, int64_t launches, float* out) {
+  clear_error();
+  if (n_side < 8 || n_side % 2 || n_side > 2 * 32767 || launches < 0 || (launches > 0 && !out))
+    return fail(RT_ERR_INVALID_ARGUMENT, "bibone mtgp_draws: even n_side in [8, 65534], launches >= 0");
+  return mtgp_draws_grid(n_side / 2, n_side / 2, seed, launches, out);
+}
+
 RT_API rt_status rt_td_walk(int32_t* tiling, int32_t n_side, int64_t steps, int64_t seed, const rt_walk_opts* opts,
                             rt_cftp_stats* stats) {
   clear_error();
@@ -406,7 +427,8 @@ RT_API rt_status rt_td_walk(int32_t* tiling, int32_t n_side, int64_t steps, int6
   if (!tiling || steps < 0) return fail(RT_ERR_INVALID_ARGUMENT, "bibone walk: NULL tiling or negative steps");
   if (n_side < 8 || n_side % 2 || n_side > 2 * 32767)
     return fail(RT_ERR_INVALID_ARGUMENT, "bibone tiling side must be even, in [8, 65534]");
-  if (o.rng_mode != RT_RNG_TINYMT && o.rng_mode != RT_RNG_FAST) return fail(RT_ERR_INVALID_ARGUMENT, "unknown rng mode");
+  if (o.rng_mode != RT_RNG_TINYMT && o.rng_mode != RT_RNG_FAST && o.rng_mode != RT_RNG_MTGP)
+    return fail(RT_ERR_INVALID_ARGUMENT, "unknown rng mode");
   if (o.rng_mode == RT_RNG_FAST && o.fast_stream >= 65536u) return fail(RT_ERR_INVALID_ARGUMENT, "fast_stream must be < 65536");
   const int N = n_side, M = N / 2;
   std::vector<uint8_t> D((size_t)M * M);
@@ -431,19 +453,23 @@ RT_API rt_status rt_td_walk(int32_t* tiling, int32_t n_side, int64_t steps, int6
   cudaStream_t st = (cudaStream_t)o.cuda_stream;
   uint8_t* dD = nullptr;
   uint4* tmt = nullptr;
+  void* mtgp = nullptr;
+  const MtgpGrid mg = mtgp_grid(M, M);
   auto cleanup = [&]() {
     if (dD) cudaFree(dD);
     if (tmt) cudaFree(tmt);
+    if (mtgp) cudaFree(mtgp);
   };
   if (cudaMalloc(&dD, D.size()) != cudaSuccess ||
-      (o.rng_mode == RT_RNG_TINYMT && cudaMalloc(&tmt, (size_t)M * M * sizeof(uint4)) != cudaSuccess)) {
+      (o.rng_mode == RT_RNG_TINYMT && cudaMalloc(&tmt, (size_t)M * M * sizeof(uint4)) != cudaSuccess) ||
+      (o.rng_mode == RT_RNG_MTGP && cudaMalloc(&mtgp, mtgp_state_bytes(mg.count())) != cudaSuccess)) {
     cudaGetLastError();
     cleanup();
     return fail(RT_ERR_OUT_OF_MEMORY, "bibone walk: device allocation failed");
   }
   cudaMemcpyAsync(dD, D.data(), D.size(), cudaMemcpyHostToDevice, st);
   std::vector<TdStep> sched((size_t)steps);
-  if (o.rng_mode == RT_RNG_TINYMT) {
+  if (o.rng_mode != RT_RNG_FAST) {
     // TriangleDimerTiler.cpp:269-276, 459-460: type, r1, r2 (and p1, p2 for butterflies)
     std::default_random_engine gen;
     std::uniform_int_distribution<int> d1(0, 2), d2(0, 1);
@@ -464,12 +490,23 @@ RT_API rt_status rt_td_walk(int32_t* tiling, int32_t n_side, int64_t steps, int6
   if (o.rng_mode == RT_RNG_TINYMT) {
     const int64_t count = (int64_t)M * M;
     k_td_seed<<<(unsigned)((count + 255) / 256), 256, 0, st>>>(tmt, count, (uint32_t)seed);
+  } else if (o.rng_mode == RT_RNG_MTGP) {
+    // TriangleDimerTiler.cpp:287-289: block generator k seeded seed + k
+    if (rt_status ms = mtgp_seed(mtgp, mg.count(), seed, st)) {
+      cudaEventDestroy(e0);
+      cudaEventDestroy(e1);
+      cleanup();
+      return ms;
+    }
   }
   cudaEventRecord(e0, st);
   const dim3 g_all((M + 127) / 128, M), g_quad(((M + 3) / 4 + 31) / 32, (M + 7) / 8);
   for (int64_t h = 0; h < steps; ++h) {
     if (o.rng_mode == RT_RNG_TINYMT)
       pdl_launch(k_td_step_tmt, g_all, dim3(128), st, dD, tmt, M, sched[(size_t)h]);
+    else if (o.rng_mode == RT_RNG_MTGP)
+      pdl_launch(k_td_step_mtgp, dim3(mg.gx, mg.gy), dim3(kMtgpBlock, kMtgpBlock), st, dD, M, sched[(size_t)h],
+                 static_cast<curandStateMtgp32*>(mtgp));
     else
       pdl_launch(k_td_step_fast, g_quad, dim3(32, 8), st, dD, M, sched[(size_t)h], (uint64_t)seed, o.fast_stream, h);
   }

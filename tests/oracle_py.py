@@ -400,6 +400,7 @@ _TD_SIG = {
     "orc_td_icecream": (C.c_int, [C.c_int, C.c_int, _P, _L]),
     "orc_td_walk_tinymt": (C.c_int, [_P, C.c_int, _L, _L]),
     "orc_td_walk_fast": (C.c_int, [_P, C.c_int, _L, _L, C.c_ulong, C.c_uint]),
+    "orc_td_walk_draws": (C.c_int, [_P, C.c_int, _P, _L, _L]),
     "orc_td_fast_step": (None, [C.c_ulong, C.c_uint, _L, _P]),
 }
 
@@ -422,6 +423,13 @@ def td_icecream(n: int, m: int) -> np.ndarray:
 
 def td_walk_tinymt(t: np.ndarray, n_side: int, steps: int, seed: int) -> None:
     assert td_lib().orc_td_walk_tinymt(_p(t), n_side, steps, seed) == 0
+
+
+def td_walk_draws(t: np.ndarray, n_side: int, draws: np.ndarray, steps: int, seed: int) -> None:
+    """The reference's CUDA-path bibone walk with its MTGP32 draws supplied (steps x M x M)."""
+    d = np.ascontiguousarray(draws, np.float32)
+    assert d.size == steps * (n_side // 2) ** 2
+    assert td_lib().orc_td_walk_draws(_p(t), n_side, _p(d), steps, seed) == 0
 
 
 def td_walk_fast(t: np.ndarray, n_side: int, h0: int, steps: int, seed: int, stream: int = 0) -> None:

@@ -1,6 +1,7 @@
-"""The cuRAND MTGP32 mode of the domino, lozenge and rectangle-triangle sweeps (RT_RNG_MTGP):
-the random stream of the reference's CUDA build (DominoTiler.cpp:51-66, dominokernel*.cu;
-LozengeTiler.cpp:71-80, lozengekernel.cu; RectTriangleTiler.cpp:75-85, recttrianglekernel.cu).
+"""The cuRAND MTGP32 mode of the domino, lozenge, rectangle-triangle and bibone sweeps
+(RT_RNG_MTGP): the random stream of the reference's CUDA build (DominoTiler.cpp:51-66,
+dominokernel*.cu; LozengeTiler.cpp:71-80, lozengekernel.cu; RectTriangleTiler.cpp:75-85,
+recttrianglekernel.cu; TriangleDimerTiler.cpp:279-291, triangledimerkernel.cu).
 
 cuRAND's generator is library code: the oracle does not restate it but takes its draws as
 data (rt_domino_mtgp_draws: the curand_uniform value each candidate site receives in the
@@ -272,6 +273,23 @@ def test_mtgp_recttri_walk_equals_the_reference_cuda_path_on_its_draws(rt, orc, 
     want = start.copy()
     orc.rt_walk_draws(want, n, rt.recttri_mtgp_draws(n, seed, steps), steps, seed, weights)
     tiler = R(weights=weights)
+    tiler.LoadMTGP()
+    got = start.copy()
+    tiler.Walk(got, steps, seed)
+    assert np.array_equal(got, want)
+    assert (got != start).sum() > 8
+
+
+@pytest.mark.gpu
+def test_mtgp_bibone_walk_equals_the_reference_cuda_path_on_its_draws(rt, orc):
+    T = rt.TriangleDimerTiler
+    start = T.RhombusBrick(14, 14)
+    n = rt.side_of(start)
+    orc.td_walk_tinymt(start, n, 300, 3)  # away from the brick pattern
+    steps, seed = 120, 31337
+    want = start.copy()
+    orc.td_walk_draws(want, n, rt.td_mtgp_draws(n, seed, steps), steps, seed)
+    tiler = T()
     tiler.LoadMTGP()
     got = start.copy()
     tiler.Walk(got, steps, seed)
