@@ -8,6 +8,8 @@ data (rt_domino_mtgp_draws: the curand_uniform value each candidate site receive
 reference's 8 x 8 block geometry) and replays the reference's CUDA rotate kernels and host
 loops on them.  On CPU, the mode's acceptance intervals over the float draw's bit pattern are
 checked against the CUDA kernels' own float/double expressions."""
+import ctypes as C
+
 import numpy as np
 import pytest
 
@@ -295,3 +297,22 @@ def test_mtgp_bibone_walk_equals_the_reference_cuda_path_on_its_draws(rt, orc):
     tiler.Walk(got, steps, seed)
     assert np.array_equal(got, want)
     assert (got != start).sum() > 8
+
+
+def test_mtgp_entry_points_check_their_arguments_before_any_cuda_call(rt):
+    """Bad sizes are refused on the host (no device needed), and the q-weighted lozenge rule has
+    no MTGP mode: the reference's q kernel has no CUDA build to match."""
+    out = np.zeros(64, np.float32)
+    lib = rt.lib()
+    assert lib.rt_domino_mtgp_draws(7, 1, 1, out.ctypes.data) == rt.RT_ERR_INVALID_ARGUMENT  # odd side
+    assert lib.rt_domino_mtgp_draws(8, 1, -1, out.ctypes.data) == rt.RT_ERR_INVALID_ARGUMENT
+    assert lib.rt_domino_mtgp_draws(8, 1, 1, None) == rt.RT_ERR_INVALID_ARGUMENT
+    assert lib.rt_lozenge_mtgp_draws(10, 1, 1, out.ctypes.data) == rt.RT_ERR_INVALID_ARGUMENT  # not 3k
+    assert lib.rt_recttri_mtgp_draws(8, 1, 1, out.ctypes.data) == rt.RT_ERR_INVALID_ARGUMENT
+    assert lib.rt_td_mtgp_draws(9, 1, 1, out.ctypes.data) == rt.RT_ERR_INVALID_ARGUMENT
+    L = rt.LozengeTiler
+    t = L.MaxTiling(L.Hexagon(3))
+    o = rt.LozengeTiler(rng="mtgp", q=0.9).opts()
+    status = lib.rt_lozenge_walk(t.ctypes.data, rt.side_of(t), 4, 1, C.byref(o))
+    assert status == rt.RT_ERR_INVALID_ARGUMENT
+    assert "uniform rule" in lib.rt_last_error().decode()
