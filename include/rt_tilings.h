@@ -424,9 +424,11 @@ RT_API rt_status rt_dm_sampler_store(rt_dm_sampler* s, int32_t chain, int32_t* t
 RT_API rt_status rt_dm_sampler_copy_chain(rt_dm_sampler* s, int32_t dst, int32_t src);
 /* Only chains [0, k) are swept by later runs (the others keep their state), 1 <= k <= n_chains. */
 RT_API rt_status rt_dm_sampler_set_active(rt_dm_sampler* s, int32_t k);
-/* TinyMT mode: InitTinyMT (dominokernel.cl:33-40): generator k <- seed + k. */
+/* TinyMT mode: InitTinyMT (dominokernel.cl:33-40): generator k <- seed + k.  MTGP mode: block
+   generator k <- seed + k (DominoTiler.cpp:62-65), after the sampler's stream has drained. */
 RT_API rt_status rt_dm_sampler_seed(rt_dm_sampler* s, uint32_t seed);
-/* TinyMT mode: runs steps half-sweeps, colours[s] = 1 rotates black (t = 1), 0 white. */
+/* TinyMT or MTGP mode: runs steps half-sweeps, colours[s] = 1 rotates black (t = 1), 0 white.
+   MTGP mode needs a prior rt_dm_sampler_seed (RT_ERR_INVALID_ARGUMENT otherwise). */
 RT_API rt_status rt_dm_sampler_run(rt_dm_sampler* s, const uint8_t* colours, int64_t steps);
 /* Fast mode: runs half-sweeps h0 .. h0+steps-1 (even h black, odd h white). */
 RT_API rt_status rt_dm_sampler_run_fast(rt_dm_sampler* s, uint64_t seed, int64_t h0, int64_t steps);
