@@ -232,6 +232,18 @@ int orc_td_walk_draws(int* t, int N, const float* draws, long steps, long seed) 
   return 0;
 }
 
+// The step class test (in_class) for one site: 1 when site (a, b) belongs to the class of
+// move type, r1, r2, p1, p2.
+int orc_td_in_class(int type, int r1, int r2, int p1, int p2, int a, int b) {
+  Step st;
+  st.type = type;
+  st.r1 = r1;
+  st.r2 = r2;
+  st.p1 = p1;
+  st.p2 = p2;
+  return in_class(st, a, b) ? 1 : 0;
+}
+
 // Fast mode: step h's class from Philox(ctr = {~0, ~0, lo32(h), hi16(h) | stream << 16});
 // site (a, b) accepts when its fast draw (philox_ref.h fast_draw with row a, column b) is
 // below 2^31.

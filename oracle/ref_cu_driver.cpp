@@ -1,7 +1,8 @@
 // TEST INFRASTRUCTURE ONLY.  Runs the rotate kernels of the reference's CUDA build, compiled
 // as host C++ through ref_cu_shim.h (see the Makefile's ref-cu rules), over an emulated
 // launch: the grid and 8 x 8 blocks the reference's Walk launches them with
-// (DominoTiler.cpp:55-60, LozengeTiler.cpp:71-76, RectTriangleTiler.cpp:75-80), one thread
+// (DominoTiler.cpp:55-60, LozengeTiler.cpp:71-76, RectTriangleTiler.cpp:75-80,
+// TriangleDimerTiler.cpp:280-285), one thread
 // at a time (each thread touches only its own site), with the draws supplied per thread.
 #include "ref_cu_shim.h"
 
@@ -11,6 +12,11 @@ namespace ref_cu_twoperiodic { void RotateTilesKernel(curandStateMtgp32*, char*,
 namespace ref_cu_CFTPtwoperiodic { void RotateTilesKernel(curandStateMtgp32*, char*, const int, const int); }
 namespace ref_cu_lozenge { void RotateTilesKernel(curandStateMtgp32*, char*, const int); }
 namespace ref_cu_recttri { void flipTilesKernel(curandStateMtgp32*, int*, const int); }
+namespace ref_cu_tdimer {
+void RotateLozengesKernel(curandStateMtgp32*, int*, const int, const int, const int);
+void RotateTrianglesKernel(curandStateMtgp32*, int*, const int, const int);
+void RotateButterflysKernel(curandStateMtgp32*, int*, const int, const int, const int, const int);
+}  // namespace ref_cu_tdimer
 
 namespace {
 
@@ -67,6 +73,21 @@ int ref_cu_lozenge_rotate(char* colour, int N, const float* draws) {
 int ref_cu_recttri_flip(int* colour, int N, const float* draws) {
   curandStateMtgp32 st{};
   launch((N + 7) / 8, (N / 3 + 7) / 8, N, N / 3, draws, [&]() { ref_cu_recttri::flipTilesKernel(&st, colour, N); });
+  return 0;
+}
+
+// Bibone: the rotate kernel of move type 0 / 1 / 2 (RotateLozengesKernel,
+// RotateTrianglesKernel, RotateButterflysKernel of triangledimerkernel.cu) on one M x M state
+// array, with the class arguments Walk passes (TriangleDimerTiler.cpp:346, 420, 499: r1, r2,
+// p1, p2), draws per site M x M.
+int ref_cu_td_rotate(int type, int* states, int M, int r1, int r2, int p1, int p2, const float* draws) {
+  curandStateMtgp32 st{};
+  if (type < 0 || type > 2) return -1;
+  launch((M + 7) / 8, (M + 7) / 8, M, M, draws, [&]() {
+    if (type == 0) ref_cu_tdimer::RotateLozengesKernel(&st, states, M, r1, r2);
+    else if (type == 1) ref_cu_tdimer::RotateTrianglesKernel(&st, states, M, r1);
+    else ref_cu_tdimer::RotateButterflysKernel(&st, states, M, r1, p1, p2);
+  });
   return 0;
 }
 

@@ -1,6 +1,7 @@
 // TEST INFRASTRUCTURE ONLY.  Lets the rotate kernels of the reference's CUDA build
 // (src/Domino/dominokernel*.cu, src/Lozenge/lozengekernel.cu,
-// src/RectTriangle/recttrianglekernel.cu) compile as host C++, so that oracle/_ref can run
+// src/RectTriangle/recttrianglekernel.cu, src/TriangleDimer/triangledimerkernel.cu) compile
+// as host C++, so that oracle/_ref can run
 // them as a sequential loop over an emulated launch grid.  The kernel file is read through
 // a filter that drops its #include lines and its launch statements (the <<< >>> lines of
 // the host wrappers); this header stands in for what they provided: the CUDA qualifiers,

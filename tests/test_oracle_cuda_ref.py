@@ -2,7 +2,8 @@
 
 oracle/Makefile (`make ref`) compiles the rotate kernels of the reference's CUDA build
 (src/Domino/dominokernel*.cu, src/Lozenge/lozengekernel.cu,
-src/RectTriangle/recttrianglekernel.cu) as host C++ under oracle/ref_cu_shim.h, and
+src/RectTriangle/recttrianglekernel.cu, src/TriangleDimer/triangledimerkernel.cu) as host C++
+under oracle/ref_cu_shim.h, and
 oracle/ref_cu_driver.cpp runs them over the reference's launch grid with the draws supplied per
 thread.  Here they rotate random colour arrays with random draws (threshold neighbourhoods
 included), and the oracle's CUDA-path rotations, and the library's MTGP acceptance intervals,
@@ -111,3 +112,31 @@ def test_recttri_cuda_flip_equals_the_oracle(ref, orc):
         f(theirs.ctypes.data, N, draws.ctypes.data, unit.ctypes.data)
         assert np.array_equal(mine, theirs), N
         assert (mine != colour).sum() > 0
+
+
+@pytest.mark.parametrize("move_type", [0, 1, 2])
+def test_bibone_cuda_rotations_flip_exactly_the_oracle_class(ref, orc, move_type):
+    """RotateLozenges/Triangles/ButterflysKernel flip a site's state (5 <-> 10, 45 <-> 54,
+    85 <-> 170) exactly when its draw is below 0.5 and the site is in the oracle's step class
+    (in_class of oracle/bibone_oracle.cpp, which the library's td_in_class restates)."""
+    ref.ref_cu_td_rotate.argtypes = [C.c_int, C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_void_p]
+    in_class = orc.td_lib().orc_td_in_class
+    in_class.argtypes = [C.c_int] * 7
+    pair = {0: (5, 10), 1: (45, 54), 2: (85, 170)}[move_type]
+    rng = np.random.default_rng(500 + move_type)
+    for M in (11, 24, 37):
+        for _ in range(4):
+            r1, r2, p1, p2 = int(rng.integers(3)), int(rng.integers(2)), int(rng.integers(3)), int(rng.integers(2))
+            states = rng.choice(np.array([pair[0], pair[1], 0, 7, 63], np.int32), size=M * M, p=[.4, .4, .1, .05, .05])
+            states = states.astype(np.int32)
+            draws = _draws(rng, (M, M), [0.5])
+            mine = states.copy()
+            assert ref.ref_cu_td_rotate(move_type, mine.ctypes.data, M, r1, r2, p1, p2, draws.ctypes.data) == 0
+            want = states.copy()
+            for a in range(M):
+                for b in range(M):
+                    k = a * M + b
+                    if draws[a, b] < 0.5 and want[k] in pair and in_class(move_type, r1, r2, p1, p2, a, b):
+                        want[k] = pair[1] if want[k] == pair[0] else pair[0]
+            assert np.array_equal(mine, want), (move_type, M, r1, r2, p1, p2)
+            assert (mine != states).sum() > 0
