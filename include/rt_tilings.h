@@ -480,21 +480,27 @@ RT_API rt_status rt_dm_sampler_test_silent_band(rt_dm_sampler* s, int32_t band, 
    half-sweeps of the resident sweep kernel on chains the caller already holds on the
    device, and allocates nothing - no cudaMalloc, cudaFree or allocating library call.
    The kernel's scratch (neighbour exchange rows, flags, band plan, colours) is a fixed
-   static device array of about 2.2 MiB that every GPU loading the library keeps until the
-   process exits.
-   Layout: dev_chains holds n_chains chains, each two colour arrays (white then black, black
-   being the vertices with i + j even) of N rows x P bytes, P = N/2 rounded up to a multiple
-   of 16, column m of row i holding vertex (i, 2m + ((i + colour + 1) & 1))... i.e. the
-   vertex of that colour in columns 2m, 2m+1.  dev_generators (TinyMT mode) holds one uint4
-   state per site (i, m), i in [1, N-2], m in [1, N/2-2], index (i-1)*(N/2-2) + (m-1),
-   advanced in place; colours (host) gives the colour of each half-sweep (1 black, 0 white).
-   Fast mode ignores both and runs half-sweeps h0 .. h0+steps-1 keyed by fast_seed.
+   static device array of about 2.2 MiB in the library's device code module; a GPU holds it
+   from the time that module is loaded on it until the process exits.
+   Layout: dev_chains holds n_chains chains back to back, n_chains * 2 * N * P bytes in all
+   (P = N/2 rounded up to a multiple of 16).  Each chain is two colour arrays, white (colour
+   0) then black (colour 1: the vertices (i, j) with i + j even), each N rows of P bytes;
+   byte m of row i of colour c is the edge mask of the vertex of that colour in columns
+   2m, 2m+1 of row i of the N x N tiling.  The size cannot be checked, as no size is passed.
+   dev_generators (TinyMT mode) holds one uint4 state per site (i, m), i in [1, N-2], m in
+   [1, N/2-2], index (i-1)*(N/2-2) + (m-1), advanced in place; colours (host) gives the
+   colour of each half-sweep (1 black, 0 white).  Fast mode ignores both and runs
+   half-sweeps h0 .. h0+steps-1 keyed by fast_seed.
    Limits: N <= 1024, n_chains <= 2, steps <= 65536 per call; larger requests return
    RT_ERR_INVALID_ARGUMENT.  Per-generator parameter tables are not supported here.
-   The first call on a device takes the array's device address (cudaGetSymbolAddress) with
-   that device current, so make it before any stream capture.  Every call shares the array
-   and clears the flags it relies on; calls that overlap on the GPU race on it, so order them
-   (one stream, or synchronise between calls).  Synchronous: returns after the sweep ends. */
+   Set-up: every call takes the array's device address (cudaGetSymbolAddress) with the
+   current device, which under CUDA's default lazy module loading loads the module (the
+   array and the kernels) at the first call on a device.  A call with steps = 0 does all of
+   this set-up and sweeps nothing: make it first, before any stream capture and outside any
+   loop that must not see the module load (or set CUDA_MODULE_LOADING=EAGER).  Every call
+   shares the array and clears the flags it relies on; calls that overlap on the GPU race on
+   it, so order them (one stream, or synchronise between calls).  Synchronous: returns after
+   the sweep ends. */
 RT_API rt_status rt_dm_sweep_noalloc(uint8_t* dev_chains, void* dev_generators, int32_t n_side, int32_t n_chains,
                                      const uint8_t* colours, int64_t steps, uint64_t fast_seed, int64_t h0,
                                      const rt_walk_opts* opts);

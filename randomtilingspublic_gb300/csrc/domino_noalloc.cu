@@ -9,13 +9,17 @@
 // fixed size instead of memory allocated per call.  Limits: tiling side N <= 1024, at most
 // 2 chains, at most 65536 half-sweeps per call, at most 256 CTAs.
 //
-// Every GPU that loads the library holds the array (kScratchBytes, about 2.2 MiB) until the
-// process exits.  All calls share it and it keeps the last call's contents: each call clears
-// the exchange rows, flags and error word it relies on, and calls that overlap on the GPU (for example on
-// two streams at once) race on it, so callers must order them.
+// The array (kScratchBytes, about 2.2 MiB) belongs to the library's device code module, so a
+// GPU holds it from the moment that module is loaded on it until the process exits.  With
+// CUDA's lazy module loading (the default) that happens at the first call on the device, which
+// also loads the sweep kernels: a caller that must not see that happen later (inside a timed
+// loop, under a memory cap) makes one call with steps = 0 first, which does all of the set-up
+// and sweeps nothing, or sets CUDA_MODULE_LOADING=EAGER.  All calls share the array and it
+// keeps the last call's contents: each call clears the exchange rows, flags and error word it
+// relies on, and calls that overlap on the GPU (for example on two streams at once) race on
+// it, so callers must order them.
 #include <cuda_runtime.h>
 
-#include <mutex>
 #include <string>
 #include <vector>
 
@@ -45,21 +49,15 @@ constexpr size_t kScratchBytes = kOffColours + (size_t)kMaxSteps;
 
 static __device__ __align__(256) unsigned char g_sweep_scratch[kScratchBytes];
 
-// Device address of g_sweep_scratch per device, taken once with that device current.
-std::mutex g_mu;
-void* g_addr[128] = {nullptr};
-
-rt_status scratch_address(int dev, unsigned char** out) {
-  std::lock_guard<std::mutex> lock(g_mu);
-  if (dev < 0 || dev >= 128) return fail(RT_ERR_CUDA, "device ordinal out of range");
-  if (!g_addr[dev]) {
-    void* p = nullptr;
-    cudaError_t e = cudaGetSymbolAddress(&p, g_sweep_scratch);
-    if (e != cudaSuccess || !p)
-      return fail(RT_ERR_CUDA, std::string("cudaGetSymbolAddress(scratch): ") + cudaGetErrorString(e));
-    g_addr[dev] = p;
-  }
-  *out = static_cast<unsigned char*>(g_addr[dev]);
+// Device address of g_sweep_scratch on the current device.  Taken on every call, with the
+// device current: it costs nothing once the module is loaded, allocates nothing, and stays
+// right after a cudaDeviceReset, which reloads the module at another address.
+rt_status scratch_address(unsigned char** out) {
+  void* p = nullptr;
+  cudaError_t e = cudaGetSymbolAddress(&p, g_sweep_scratch);
+  if (e != cudaSuccess || !p)
+    return fail(RT_ERR_CUDA, std::string("cudaGetSymbolAddress(scratch): ") + cudaGetErrorString(e));
+  *out = static_cast<unsigned char*>(p);
   return RT_OK;
 }
 
@@ -100,8 +98,9 @@ extern "C" RT_API rt_status rt_dm_sweep_noalloc(uint8_t* dev_chains, void* dev_g
   const char* err = nullptr;
   if (!dm_rule_build(o.rule, o.rng_mode, o.weight_a, o.weight_b, &rule, &err))
     return fail(RT_ERR_INVALID_ARGUMENT, std::string("sweep_noalloc: ") + err);
-  if (steps == 0) return RT_OK;
 
+  // Set-up, also for steps = 0 (the warm-up call): the device, the scratch address (which
+  // loads the module holding the array and the kernels), the plan and the kernel attributes.
   int dev = 0, sms = 0, coop = 0, optin = 0;
   NOALLOC_CUDA(cudaGetDevice(&dev));
   NOALLOC_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
@@ -109,7 +108,7 @@ extern "C" RT_API rt_status rt_dm_sweep_noalloc(uint8_t* dev_chains, void* dev_g
   NOALLOC_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
   if (!coop) return fail(RT_ERR_CUDA, "sweep_noalloc: device lacks cooperative launch");
   unsigned char* scratch = nullptr;
-  if (rt_status st = scratch_address(dev, &scratch)) return st;
+  if (rt_status st = scratch_address(&scratch)) return st;
 
   // Plan: every site of rows 1..N-2, columns 1..N/2-2 is a unit, so windows span whole rows
   // and the sweep equals the reference's for any input.
@@ -127,6 +126,7 @@ extern "C" RT_API rt_status rt_dm_sweep_noalloc(uint8_t* dev_chains, void* dev_g
   NOALLOC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kPersistThreads, plan.smem_bytes));
   const int nbands = (int)plan.bands.size();
   if ((int64_t)per_sm * sms < nbands) return fail(RT_ERR_CUDA, "sweep_noalloc: bands cannot all be resident");
+  if (steps == 0) return RT_OK;
 
   cudaStream_t stream = (cudaStream_t)o.cuda_stream;
   std::vector<int> rows((size_t)2 * (kMaxSide + 1), 0);

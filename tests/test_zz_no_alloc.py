@@ -35,21 +35,22 @@ def _merge(a: np.ndarray, n: int) -> np.ndarray:
     return T.ravel()
 
 
-@pytest.mark.parametrize("mode", ["tinymt", "fast"])
-def test_noalloc_sweep_matches_walk_on_two_calls(rt, orc, mode):
+def _check_two_calls(rt, orc, order, mode, n_chains, s1, s2, seed=2024):
+    """A steps = 0 warm-up call (the set-up a caller that cannot allocate later makes
+    first), then two sweeping calls that continue the same chains; after each, every chain
+    must equal rt_domino_walk run for the same total number of half-sweeps."""
     import torch
 
     D = rt.DominoTiler
-    d = D.AztecDiamond(60)
+    d = D.AztecDiamond(order)
     tmax, tmin = D.MaxTiling(d), D.MinTiling(d)
     n = int(np.sqrt(tmax.size))
     pitch = (n // 2 + 15) // 16 * 16
-    seed = 2024
-    s1, s2 = 300, 457
     tiler = rt.DominoTiler(rule="cftp_twoperiodic", rng=mode, a=1.0, b=0.5)
     opts = tiler.opts()
 
-    chains = np.stack([_split(tmax, n, pitch), _split(tmin, n, pitch)])  # two coupled chains
+    starts = (tmax, tmin)[:n_chains]
+    chains = np.stack([_split(t, n, pitch) for t in starts])
     dev_chains = torch.from_numpy(chains).cuda()
     draws = rt.mt19937_draws(seed, 1 + s1 + s2)
     if mode == "tinymt":
@@ -62,17 +63,32 @@ def test_noalloc_sweep_matches_walk_on_two_calls(rt, orc, mode):
         gen_ptr = None
         colours = None
     lib = rt.lib()
+    st = lib.rt_dm_sweep_noalloc(dev_chains.data_ptr(), gen_ptr, n, n_chains, None, 0, seed, 0, C.byref(opts))
+    assert st == 0, lib.rt_last_error().decode()
+    assert np.array_equal(dev_chains.cpu().numpy(), chains), "a steps = 0 call must leave the chains alone"
     done = 0
     for steps in (s1, s2):
         cptr = colours[done:done + steps].ctypes.data if colours is not None else None
-        st = lib.rt_dm_sweep_noalloc(dev_chains.data_ptr(), gen_ptr, n, 2, cptr, steps, seed, done, C.byref(opts))
+        st = lib.rt_dm_sweep_noalloc(dev_chains.data_ptr(), gen_ptr, n, n_chains, cptr, steps, seed, done,
+                                     C.byref(opts))
         assert st == 0, lib.rt_last_error().decode()
         done += steps
         got = dev_chains.cpu().numpy()
-        for c, start in enumerate((tmax, tmin)):
+        for c, start in enumerate(starts):
             want = start.copy()
             tiler.Walk(want, done, seed)  # the existing entry point
-            assert np.array_equal(_merge(got[c], n), want), (mode, done, c)
+            assert np.array_equal(_merge(got[c], n), want), (mode, n_chains, done, c)
+
+
+@pytest.mark.parametrize("n_chains", [1, 2])
+@pytest.mark.parametrize("mode", ["tinymt", "fast"])
+def test_noalloc_sweep_matches_walk_on_two_calls(rt, orc, mode, n_chains):
+    _check_two_calls(rt, orc, 60, mode, n_chains, 300, 457)
+
+
+def test_noalloc_sweep_at_the_size_limit_matches_walk(rt, orc):
+    # Aztec order 509: tiling side 1024, the largest the static scratch holds.
+    _check_two_calls(rt, orc, 509, "fast", 2, 150, 211)
 
 
 def test_noalloc_sweep_rejects_sizes_beyond_its_limits(rt):
