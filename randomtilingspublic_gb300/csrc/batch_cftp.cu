@@ -861,6 +861,18 @@ struct rt_server {
   int64_t next_ticket = 0;
   std::vector<int64_t> owner;          // ticket held by each slot, -1 when free
   std::vector<int64_t> footprint;
+
+  // Releases whatever was set up, so that a create that fails half-way leaks nothing: a
+  // running serving kernel is told to leave and waited for first.
+  ~rt_server() {
+    if (ring) __atomic_store_n(&ring->shutdown, 1u, __ATOMIC_RELEASE);
+    if (stream) cudaStreamSynchronize(stream);
+    if (ev_exit) cudaEventDestroy(ev_exit);
+    if (own_stream && stream) cudaStreamDestroy(stream);
+    if (d_head) cudaFree(d_head);
+    for (void* p : {(void*)ring, (void*)desc, (void*)data, (void*)done})
+      if (p) cudaFreeHost(p);
+  }
 };
 
 static rt_status server_launch(rt_server* s) {
@@ -1003,17 +1015,7 @@ RT_API rt_status rt_server_wait(rt_server* s, int64_t ticket, double timeout_s, 
 
 RT_API rt_status rt_server_destroy(rt_server* s) {
   clear_error();
-  if (!s) return RT_OK;
-  if (s->ring) __atomic_store_n(&s->ring->shutdown, 1u, __ATOMIC_RELEASE);
-  if (s->stream) cudaStreamSynchronize(s->stream);
-  if (s->ev_exit) cudaEventDestroy(s->ev_exit);
-  if (s->own_stream && s->stream) cudaStreamDestroy(s->stream);
-  if (s->d_head) cudaFree(s->d_head);
-  if (s->ring) cudaFreeHost(s->ring);
-  if (s->desc) cudaFreeHost(s->desc);
-  if (s->data) cudaFreeHost(s->data);
-  if (s->done) cudaFreeHost(s->done);
-  delete s;
+  delete s;  // the destructor stops the serving kernel and frees everything
   return RT_OK;
 }
 
