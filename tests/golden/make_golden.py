@@ -9,7 +9,7 @@ noted; the reference's own table file is absent from its tree).  Also pins the c
 fixture Examples/ExampleOuts/WeightedAztecDiamond/TilingStart.txt against the reference's
 MinTiling(AztecDiamond(16)).
 
-    python tests/golden/make_golden.py [--ref /root/reference]
+    python tests/golden/make_golden.py --ref <reference tree>
 """
 from __future__ import annotations
 
@@ -28,7 +28,7 @@ RULES = ["plain", "CFTP", "twoperiodic", "CFTPtwoperiodic"]
 
 def main() -> None:
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--ref", required=True, help="path of the reference tree (its src/ and Examples/)")
     args = ap.parse_args()
     subprocess.run(["make", "-s", "-C", str(ROOT / "oracle"), "ref", f"REF={args.ref}"], check=True)
     host = C.CDLL(str(ROOT / "oracle/_ref/libref_domino_host.so"))
