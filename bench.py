@@ -46,8 +46,8 @@ def _peaks() -> dict:
     return {"hbm_gbs": 6800.0, "source": "fallback"}
 
 
-def _interior_by_colour(rt, d) -> tuple[int, int]:
-    v = rt.DominoTiler.DomainToVertices(d)
+def _interior_by_colour(v: np.ndarray) -> tuple[int, int]:
+    """Interior vertices (value 1 of DomainToVertices) of each colour: (white, black)."""
     n = int(np.sqrt(v.size))
     ii, jj = np.divmod(np.arange(v.size), n)
     inter = v == 1
@@ -146,16 +146,17 @@ def _sum_over_ranks(x: float, dist, device) -> float:
     return float(t.item())
 
 
-def cpu_leg(rt, orc, tmax, tmin, interior, steps_per_sample: int, samples: int, threads: int):
+def cpu_leg(orc, tmax, tmin, interior, steps_per_sample: int, samples: int, threads: int):
     """Oracle (the reference's sweep logic restated) on `threads` host threads: `samples`
-    coupled attempts of `steps_per_sample` TinyMT steps each; returns attempts/s per sample."""
+    coupled attempts of `steps_per_sample` TinyMT steps each; returns attempts/s per sample.
+    Uses the oracle alone (its own mt19937), so no library of this repository is loaded."""
     n = int(np.sqrt(tmax.size))
     rates = []
-    drv = rt.mt19937_draws(DRIVER_SEED, samples)
+    drv = orc.mt19937(DRIVER_SEED, samples)
     for k in range(samples):
         driver = int(drv[k]) ^ 0x5EED
-        epoch_seed = int(rt.mt19937_draws(driver, 1)[0])  # the driver's first draw seeds the epoch
-        cols = rt.mt19937_colours(epoch_seed, steps_per_sample)
+        epoch_seed = int(orc.mt19937(driver, 1)[0])  # the driver's first draw seeds the epoch
+        cols = (orc.mt19937(epoch_seed, steps_per_sample) % 2).astype(np.uint8)
         t0 = time.perf_counter()
         # One attempt (max_attempts=1) at a look-back of steps_per_sample: the same work
         # pattern as a GPU step, shortened.
@@ -164,6 +165,15 @@ def cpu_leg(rt, orc, tmax, tmin, interior, steps_per_sample: int, samples: int, 
         dt = time.perf_counter() - t0
         rates.append(_attempts(cols, interior) / dt)
     return rates
+
+
+def headline_domain_oracle(orc):
+    """The headline workload's domain, extremal tilings and interior counts from the oracle."""
+    d = orc.aztec_rectangle(ORDER)
+    rc1, tmax = orc.max_tiling(d)
+    rc2, tmin = orc.min_tiling(d)
+    assert rc1 == 0 and rc2 == 0
+    return d, tmax, tmin, _interior_by_colour(orc.domain_to_vertices(d))
 
 
 BATCH_INSTANCES = 2048
@@ -347,7 +357,7 @@ def mtgp_leg(rt, half_sweeps: int = 512) -> dict:
     d = D.AztecDiamond(ORDER)
     tmax, tmin = D.MaxTiling(d), D.MinTiling(d)
     n = int(np.sqrt(tmax.size))
-    interior = _interior_by_colour(rt, d)
+    interior = _interior_by_colour(D.DomainToVertices(d))
     stream = torch.cuda.Stream()
     tiler = rt.DominoTiler(rule="cftp_twoperiodic", rng="mtgp", a=WEIGHT_A, b=WEIGHT_B)
     s = rt.DominoSampler(n, 2, tiler, cuda_stream=stream.cuda_stream)
@@ -378,19 +388,14 @@ def run_reference(args) -> None:
     rank, ws, local, dist = _dist()
     if rank != 0:
         return
-    import randomtilingspublic_gb300 as rt
-    from tests import oracle_py as orc
+    from tests import oracle_py as orc  # the oracle alone: no library of this repository
 
-    D = rt.DominoTiler
-    d = D.AztecDiamond(ORDER)
-    tmax, tmin = D.MaxTiling(d), D.MinTiling(d)
-    interior = _interior_by_colour(rt, d)
+    _, tmax, tmin, interior = headline_domain_oracle(orc)
     threads = os.cpu_count() or 1
     sample = 32
-    orc.lib()
-    cpu_leg(rt, orc, tmax, tmin, interior, sample, max(args.warmup, 1), threads)
+    cpu_leg(orc, tmax, tmin, interior, sample, max(args.warmup, 1), threads)
     t0 = time.perf_counter()
-    rates = cpu_leg(rt, orc, tmax, tmin, interior, sample, args.steps, threads)
+    rates = cpu_leg(orc, tmax, tmin, interior, sample, args.steps, threads)
     wall = time.perf_counter() - t0
     value = statistics.mean(rates)
     line = {
@@ -408,6 +413,83 @@ def run_reference(args) -> None:
     print(json.dumps(line))
 
 
+def headline_sampler(rt, tiler, cuda_stream):
+    """The sampler a headline step runs on: chains 0 (bottom) and 1 (top) are swept, chains 2
+    and 3 keep the min and max start states; returns (sampler, tmax, tmin, interior)."""
+    D = rt.DominoTiler
+    d = D.AztecDiamond(ORDER)
+    tmax, tmin = D.MaxTiling(d), D.MinTiling(d)
+    n = int(np.sqrt(tmax.size))
+    s = rt.DominoSampler(n, 4, tiler, cuda_stream=cuda_stream)
+    s.load(0, tmin)
+    s.load(1, tmax)
+    s.load(2, tmin)
+    s.load(3, tmax)
+    s.sync()
+    s.set_active(2)
+    return s, tmax, tmin, _interior_by_colour(D.DomainToVertices(d))
+
+
+def headline_step(rt, s, seed: int, mode: str, before_run=None) -> np.ndarray:
+    """One step of the headline workload: both chains reset to the extremal tilings, then one
+    epoch of HALF_SWEEPS half-sweeps seeded `seed` (TinyMT: generators seeded seed + k and
+    colours from mt19937(seed), the reference's epoch protocol; fast: half-sweeps -2048..-1
+    keyed by seed).  Returns the colour of each half-sweep."""
+    s.copy_chain(0, 2)
+    s.copy_chain(1, 3)
+    if mode == "tinymt":
+        cols = rt.mt19937_colours(seed, HALF_SWEEPS)
+        s.seed(seed)
+        if before_run:
+            before_run()
+        s.run(cols)
+    else:
+        cols = np.array([1, 0] * (HALF_SWEEPS // 2), np.uint8)
+        if before_run:
+            before_run()
+        s.run_fast(seed, -HALF_SWEEPS, HALF_SWEEPS)
+    return cols
+
+
+def timed_seeds(rank: int, steps: int) -> np.ndarray:
+    """Seed of timed step k on a rank: draw k of mt19937(DRIVER_SEED + 7919 rank), so the
+    first timed step's chains do not depend on the warm-up count."""
+    return mt19937_host(DRIVER_SEED + 7919 * rank, steps)
+
+
+def warmup_seeds(rank: int, steps: int) -> np.ndarray:
+    return mt19937_host(DRIVER_SEED + 7919 * rank + 1, steps)
+
+
+def mt19937_host(seed: int, count: int) -> np.ndarray:
+    """First `count` outputs of std::mt19937(seed) (numpy's legacy MT19937 seeds and draws
+    the same way)."""
+    return np.random.RandomState(seed & 0xFFFFFFFF).randint(0, 2**32, size=count, dtype=np.uint32)
+
+
+def chains_sha256(top: np.ndarray, bottom: np.ndarray) -> str:
+    """Digest of a step's result: the top chain's int32 tiling, then the bottom chain's."""
+    import hashlib
+
+    h = hashlib.sha256()
+    h.update(np.ascontiguousarray(top, np.int32).tobytes())
+    h.update(np.ascontiguousarray(bottom, np.int32).tobytes())
+    return h.hexdigest()
+
+
+# The first timed step on rank 0 in TinyMT mode (seed 1791095845), as the oracle computes it:
+# tests/golden/make_bench_check.py writes it to tests/golden/bench_check.json, and
+# tests/test_bench_step.py checks both the GPU's result and this digest against the oracle.
+BENCH_CHECK_SHA256 = "b363844c09336dfecba5a174eb2a1a6b93f0091e55872316ca600e0238604f67"
+
+# DRAM bytes per launch of the resident sweep kernel (dram__bytes_read.sum +
+# dram__bytes_write.sum), from one ncu capture of the same launch of this workload:
+#   ncu --set full --clock-control none -k regex:k_persist -s 3 -c 1 \
+#       python bench.py --no-cpu --no-batch --no-single --steps 2 --warmup 3 [--mode fast]
+# Keyed by (rng mode, kernel name).  None where no capture of that kernel exists.
+NCU_TRAFFIC_BYTES = {}
+
+
 def run_ours(args) -> None:
     import torch
 
@@ -416,69 +498,49 @@ def run_ours(args) -> None:
     torch.cuda.set_device(dev)
     import randomtilingspublic_gb300 as rt
 
-    D = rt.DominoTiler
-    d = D.AztecDiamond(ORDER)
-    tmax, tmin = D.MaxTiling(d), D.MinTiling(d)
-    n = int(np.sqrt(tmax.size))
-    interior = _interior_by_colour(rt, d)
     tiler = rt.DominoTiler(rule="cftp_twoperiodic", rng=args.mode, a=WEIGHT_A, b=WEIGHT_B, fast_stream=rank,
                            engine=args.engine)
     stream = torch.cuda.Stream(device=dev)
-    s = rt.DominoSampler(n, 4, tiler, cuda_stream=stream.cuda_stream)
-    s.load(0, tmin)
-    s.load(1, tmax)
-    s.load(2, tmin)
-    s.load(3, tmax)
-    s.sync()
+    s, tmax, tmin, interior = headline_sampler(rt, tiler, stream.cuda_stream)
+    n = int(np.sqrt(tmax.size))
     lib = rt.lib()
     flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device=dev)
-    seeds = rt.mt19937_draws(DRIVER_SEED + 7919 * rank, args.warmup + args.steps)
-
-    # Chains 0, 1 are swept; chains 2, 3 keep the extremal start states.
-    s.set_active(2)
-
+    seeds = timed_seeds(rank, args.steps)
+    wseeds = warmup_seeds(rank, args.warmup)
     info = s.engine_info()
-
-    def one_step(k: int, kev=None) -> tuple[int, int]:
-        s.copy_chain(0, 2)
-        s.copy_chain(1, 3)
-        if args.mode == "tinymt":
-            cols = rt.mt19937_colours(int(seeds[k]), HALF_SWEEPS)
-            s.seed(int(seeds[k]))
-            if kev:
-                kev[0].record(stream)
-            s.run(cols)
-        else:
-            cols = np.array([1, 0] * (HALF_SWEEPS // 2), np.uint8)
-            if kev:
-                kev[0].record(stream)
-            s.run_fast(int(seeds[k]), -HALF_SWEEPS, HALF_SWEEPS)
-        if kev:
-            kev[1].record(stream)
-        return _attempts(cols, interior), int(np.count_nonzero(cols))
 
     ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
     kev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
     for k in range(args.warmup):
-        one_step(k)
+        headline_step(rt, s, int(wseeds[k]), args.mode)
         s.diff(0, 1)
     torch.cuda.synchronize()
     if dist is not None:
         dist.barrier()
     attempts = 0
-    launches0 = s.launches
+    launches = 0
+    check = None
     with Clocks(local) as clk:
         for k in range(args.steps):
             flush.zero_()  # L2 flush between timed steps (outside the events)
             torch.cuda.current_stream(dev).synchronize()
             with torch.cuda.stream(stream):
                 ev[k][0].record(stream)
-                a, _ = one_step(args.warmup + k, kev[k])
+                l0 = s.launches
+                cols = headline_step(rt, s, int(seeds[k]), args.mode, before_run=lambda: kev[k][0].record(stream))
+                launches += s.launches - l0  # this library's kernels inside the events
+                kev[k][1].record(stream)
                 ev[k][1].record(stream)
-            attempts += a
+            attempts += _attempts(cols, interior)
             s.diff(0, 1)
+            if k == 0:
+                # Self-check of the first timed step (outside the events): the digest of both
+                # chains, against the oracle's value where one is recorded.
+                digest = chains_sha256(s.store(1), s.store(0))
+                expected = BENCH_CHECK_SHA256 if (args.mode == "tinymt" and rank == 0) else None
+                check = {"step": 0, "seed": int(seeds[0]), "sha256": digest, "expected": expected,
+                         "ok": None if expected is None else digest == expected}
         torch.cuda.synchronize()
-    launches = s.launches - launches0 - args.steps  # minus the diff kernels outside the events
     ms = sum(e0.elapsed_time(e1) for e0, e1 in ev)
     sec = _max_over_ranks(ms / 1e3, dist, dev)
     total_attempts = _sum_over_ranks(attempts, dist, dev)
@@ -496,45 +558,48 @@ def run_ours(args) -> None:
     tiling_bytes_per_half = 3 * (attempts / half_sweeps)
     peaks = _peaks()
     if info["engine"] == 2:
-        kernel = "k_persist (resident cooperative sweep, one launch per step)"
+        kernel = info.get("kernel", "k_persist")
         launches_timed = args.steps
         gen = 32 * info["units"] if args.mode == "tinymt" else 0
         algo_bytes = tiling_bytes_per_half * HALF_SWEEPS + gen
+        limiter = ("on chip: integer issue and the neighbour-exchange latency; the chains stay in shared "
+                   "memory for the whole launch, so the HBM copy bandwidth is a yardstick, not the limit")
     else:
-        kernel = "k_rotate_tmt + k_update (one pair per half-sweep)"
+        kernel = "k_rotate_tmt + k_update_w (one pair per half-sweep)"
         launches_timed = half_sweeps
         gen = 32 * cells if args.mode == "tinymt" else 0
         algo_bytes = tiling_bytes_per_half + gen
+        limiter = "L2 and launch latency"
     t_launch = (kms / 1e3) / launches_timed
     achieved = algo_bytes / t_launch / 1e9
-    traffic = _traffic_from_profile(args.mode, info["engine"])
-    roofline = {"bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
-                "frac": achieved / peaks["hbm_gbs"], "traffic": traffic, "peak_source": peaks["source"],
-                "kernel": kernel, "algorithmic_bytes_per_launch": algo_bytes, "launch_us": t_launch * 1e6,
-                "half_sweep_us": (kms / 1e3) / half_sweeps * 1e6, "engine": info}
+    traffic = NCU_TRAFFIC_BYTES.get((args.mode, kernel.split(" ")[0]))
+    roofline = {"bound": "hbm", "limiter": limiter, "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
+                "frac": achieved / peaks["hbm_gbs"], "traffic": traffic,
+                "traffic_source": "ncu capture of the same launch (bench.py NCU_TRAFFIC_BYTES)" if traffic else None,
+                "peak_source": peaks["source"], "kernel": kernel, "algorithmic_bytes_per_launch": algo_bytes,
+                "launch_us": t_launch * 1e6, "half_sweep_us": (kms / 1e3) / half_sweeps * 1e6, "engine": info}
 
     # e2e: one attempt through the C ABI from pinned host buffers, copies included.
-    if True:
-        pin_max = torch.from_numpy(tmax).pin_memory()
-        pin_min = torch.from_numpy(tmin).pin_memory()
-        pin_out = torch.empty_like(pin_max).pin_memory()
-        o = tiler.opts()
-        stats = rt.CftpStats()
-        e2e_rates = []
-        for k in range(max(2, min(args.steps, 3))):
-            t0 = time.perf_counter()
-            st = lib.rt_domino_cftp(pin_max.data_ptr(), pin_min.data_ptr(), n, int(seeds[k]), HALF_SWEEPS, 0, 1,
-                                    C.byref(o), pin_out.data_ptr(), C.byref(stats))
-            dt = time.perf_counter() - t0
-            if st not in (rt.RT_OK, rt.RT_ERR_NOT_COALESCED):
-                raise rt.RTError(st, lib.rt_last_error().decode())
-            e2e_rates.append(stats.flip_attempts / dt)
-        nbytes = n * n * 4
-        e2e = {"value": _sum_over_ranks(statistics.median(e2e_rates[1:]), dist, dev), "unit": "flip attempts/s",
-               # the max and min tilings (the min start state is copied on the device) and the
-               # colour sequence in; the top chain and the coalescence count out
-               "h2d_bytes_per_step": 2 * nbytes + HALF_SWEEPS, "d2h_bytes_per_step": nbytes + 8,
-               "api": "rt_domino_cftp (one attempt, look-back 2048 half-sweeps)"}
+    pin_max = torch.from_numpy(tmax).pin_memory()
+    pin_min = torch.from_numpy(tmin).pin_memory()
+    pin_out = torch.empty_like(pin_max).pin_memory()
+    o = tiler.opts()
+    stats = rt.CftpStats()
+    e2e_rates = []
+    for k in range(max(2, min(args.steps, 3))):
+        t0 = time.perf_counter()
+        st = lib.rt_domino_cftp(pin_max.data_ptr(), pin_min.data_ptr(), n, int(seeds[k]), HALF_SWEEPS, 0, 1,
+                                C.byref(o), pin_out.data_ptr(), C.byref(stats))
+        dt = time.perf_counter() - t0
+        if st not in (rt.RT_OK, rt.RT_ERR_NOT_COALESCED):
+            raise rt.RTError(st, lib.rt_last_error().decode())
+        e2e_rates.append(stats.flip_attempts / dt)
+    nbytes = n * n * 4
+    e2e = {"value": _sum_over_ranks(statistics.median(e2e_rates[1:]), dist, dev), "unit": "flip attempts/s",
+           # the max and min tilings (the min start state is copied on the device) and the
+           # colour sequence in; the top chain and the coalescence count out
+           "h2d_bytes_per_step": 2 * nbytes + HALF_SWEEPS, "d2h_bytes_per_step": nbytes + 8,
+           "api": "rt_domino_cftp (one attempt, look-back 2048 half-sweeps)"}
 
     cpu = None
     if rank == 0 and ws == 1 and not args.no_cpu:
@@ -542,7 +607,7 @@ def run_ours(args) -> None:
 
         threads = os.cpu_count() or 1
         sample = 32
-        rates = cpu_leg(rt, orc, tmax, tmin, interior, sample, 2, threads)
+        rates = cpu_leg(orc, tmax, tmin, interior, sample, 2, threads)
         cpu = {"value": statistics.mean(rates), "unit": "flip attempts/s", "cores": threads, "kind": "port",
                "sample": f"{sample} TinyMT half-sweeps of the coupled max/min chains (order {ORDER}) per attempt, "
                          f"2 attempts, {threads} host threads"}
@@ -562,7 +627,7 @@ def run_ours(args) -> None:
                        "rng": args.mode, "engine": args.engine, "half_sweeps_per_step": HALF_SWEEPS,
                        "l2": "flushed between timed steps (256 MiB write)", "parallelism": f"replicas{ws}"},
             "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches, "clocks": clocks,
-            "batched_cftp": batched, "served_cftp": serving, "single_instance": single,
+            "check": check, "batched_cftp": batched, "served_cftp": serving, "single_instance": single,
         }
         print(json.dumps(line))
     if dist is not None:
@@ -585,20 +650,6 @@ def main() -> None:
         run_reference(args)
     else:
         run_ours(args)
-
-
-def _traffic_from_profile(mode: str, engine: int):
-    """DRAM bytes per launch of the resident sweep kernel (dram__bytes_read.sum +
-    dram__bytes_write.sum of one ncu capture of this workload), read from the committed ncu
-    summary; None for the per-half-sweep engines, which that summary does not cover."""
-    import re
-
-    p = ROOT / "profiles" / "k_persist_aztec1024.md"
-    if engine != 2 or not p.exists():
-        return None
-    m = re.search(rf"traffic per launch \(dram__bytes_read\.sum \+ dram__bytes_write\.sum\):.*?\b{mode} (\d+) B",
-                  p.read_text())
-    return int(m.group(1)) if m else None
 
 
 if __name__ == "__main__":

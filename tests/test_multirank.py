@@ -64,3 +64,19 @@ def test_reference_arm_under_torchrun_prints_one_line_from_rank_0():
     line = lines[0]
     assert line["impl"] == "reference" and line["n_gpus"] == 2 and line["value"] > 0
     assert line["e2e"]["h2d_bytes_per_step"] == 0 and line["cpu_baseline"]["kind"] == "port"
+
+
+@pytest.mark.timeout(600)
+def test_reference_arm_loads_no_library_of_this_repository():
+    """The reference arm times the oracle alone: after it ran, the process has mapped the
+    oracle's library and not librt_tilings.so."""
+    code = (
+        "import sys, argparse; sys.path.insert(0, '.'); import bench\n"
+        "bench.run_reference(argparse.Namespace(gpus=1, steps=1, warmup=1))\n"
+        "maps = open('/proc/self/maps').read()\n"
+        "print('MAPS', 'librt_tilings' in maps, 'liboracle' in maps)\n"
+    )
+    res = subprocess.run([sys.executable, "-c", code], cwd=ROOT, capture_output=True, text=True, timeout=580,
+                         env=dict(os.environ, WORLD_SIZE="1"))
+    assert res.returncode == 0, res.stderr[-2000:]
+    assert "MAPS False True" in res.stdout
