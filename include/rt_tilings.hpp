@@ -51,7 +51,48 @@ inline int side_of(const std::vector<int>& v) {
   return n;
 }
 
-class DominoTiler {
+// The options every tiler passes to the C ABI, and LoadTinyMT(params, size) of the reference's
+// tilers (DominoTiler.cpp:235-237, LozengeTiler.cpp:161-164, RectTriangleTiler.cpp:22-25,
+// TriangleDimerTiler.cpp:24-27): `size` parameter sets read from a TinyMTDC file as
+// src/TinyMT/file_reader.cpp:22-38 reads them (lines not starting with '#'; mat1, mat2, tmat
+// after the 3rd, 4th and 5th comma, in hex), set k for TinyMT generator k.
+class TinyMTOpts {
+ public:
+  void LoadTinyMT(const std::string& path, int size) {
+    std::ifstream in(path);
+    if (!in) throw Error(RT_ERR_INVALID_ARGUMENT, "cannot open " + path);
+    std::vector<uint32_t> p;
+    std::string line;
+    while ((int)p.size() < 3 * size && std::getline(in, line)) {
+      if (line.empty() || line[0] == '#') continue;
+      size_t at = 0;
+      for (int c = 0; c < 3; ++c) at = line.find(',', at) + 1;
+      for (int f = 0; f < 3; ++f) {
+        p.push_back((uint32_t)std::stoul(line.substr(at), nullptr, 16));
+        at = line.find(',', at) + 1;
+      }
+    }
+    if ((int)p.size() < 3 * size) throw Error(RT_ERR_INVALID_ARGUMENT, path + ": too few parameter sets");
+    params_ = std::move(p);
+  }
+
+  rt_walk_opts& options() { return opts_; }
+
+ protected:
+  // The options of a call, pointing at the loaded table (set on every call, so that a copied
+  // tiler points at its own copy).
+  const rt_walk_opts* wopts() {
+    if (!params_.empty()) {
+      opts_.tinymt_params = params_.data();
+      opts_.tinymt_params_count = (int64_t)(params_.size() / 3);
+    }
+    return &opts_;
+  }
+  rt_walk_opts opts_{};
+  std::vector<uint32_t> params_;
+};
+
+class DominoTiler : public TinyMTOpts {
  public:
   // rule: RT_DOMINO_PLAIN (dominokernel), RT_DOMINO_CFTP, RT_DOMINO_TWOPERIODIC,
   // RT_DOMINO_CFTP_TWOPERIODIC; rng_mode: RT_RNG_TINYMT or RT_RNG_FAST.
@@ -63,41 +104,19 @@ class DominoTiler {
     opts_.weight_b = b;
   }
 
-  // DominoTiler::LoadTinyMT(params, size) (DominoTiler.cpp:235-237): `size` parameter sets
-  // from a TinyMTDC file (lines not starting with '#'; mat1, mat2, tmat after the 3rd, 4th
-  // and 5th comma, in hex).
-  void LoadTinyMT(const std::string& path, int size) {
-    std::ifstream in(path);
-    if (!in) throw Error(RT_ERR_INVALID_ARGUMENT, "cannot open " + path);
-    params_.clear();
-    std::string line;
-    while ((int)params_.size() < 3 * size && std::getline(in, line)) {
-      if (line.empty() || line[0] == '#') continue;
-      size_t p = 0;
-      for (int c = 0; c < 3; ++c) p = line.find(',', p) + 1;
-      for (int f = 0; f < 3; ++f) {
-        params_.push_back((uint32_t)std::stoul(line.substr(p), nullptr, 16));
-        p = line.find(',', p) + 1;
-      }
-    }
-    if ((int)params_.size() < 3 * size) throw Error(RT_ERR_INVALID_ARGUMENT, path + ": too few parameter sets");
-    opts_.tinymt_params = params_.data();
-    opts_.tinymt_params_count = size;
-  }
-
   // DominoTiler::LoadMTGP (DominoTiler.cpp:239-242): as in the reference's CUDA build, the
   // walks then draw from cuRAND MTGP32 generators, one per 8 x 8 block of sites seeded
   // seed + block (RT_RNG_MTGP), so they see the reference's random stream.
   void LoadMTGP() { opts_.rng_mode = RT_RNG_MTGP; }
 
   void Walk(tiling& t, long steps, long seed) {
-    check(rt_domino_walk(t.data(), side_of(t), steps, seed, &opts_));
+    check(rt_domino_walk(t.data(), side_of(t), steps, seed, wopts()));
   }
 
   void Walk(tiling& t, std::vector<long> steps, std::vector<long> seeds) {
     if (steps.size() != seeds.size()) throw Error(RT_ERR_INVALID_ARGUMENT, "steps and seeds differ in length");
     std::vector<int64_t> st(steps.begin(), steps.end()), sd(seeds.begin(), seeds.end());
-    check(rt_domino_walk_epochs(t.data(), side_of(t), st.data(), sd.data(), (int32_t)st.size(), &opts_));
+    check(rt_domino_walk_epochs(t.data(), side_of(t), st.data(), sd.data(), (int32_t)st.size(), wopts()));
   }
 
   // Coupling from the past with the reference example's driver (AztecDiamondCftpEx.cpp).
@@ -105,7 +124,7 @@ class DominoTiler {
               int max_attempts = 30, rt_cftp_stats* stats = nullptr) {
     tiling out(tmax.size());
     check(rt_domino_cftp(tmax.data(), tmin.data(), side_of(tmax), driver_seed, first_steps, schedule, max_attempts,
-                         &opts_, out.data(), stats));
+                         wopts(), out.data(), stats));
     return out;
   }
 
@@ -171,11 +190,6 @@ class DominoTiler {
     return h;
   }
 
-  rt_walk_opts& options() { return opts_; }
-
- private:
-  rt_walk_opts opts_;
-  std::vector<uint32_t> params_;
 };
 
 
@@ -196,21 +210,22 @@ inline int tri_rows(const domain& d) {
 }
 
 // src/Lozenge/LozengeTiler.h:46-92.
-class LozengeTiler {
+class LozengeTiler : public TinyMTOpts {
  public:
-  explicit LozengeTiler(int rng_mode = RT_RNG_TINYMT, uint32_t fast_stream = 0) : opts_(model_opts(rng_mode, fast_stream)) {}
-  void LoadTinyMT(const std::string&, int) {}
+  explicit LozengeTiler(int rng_mode = RT_RNG_TINYMT, uint32_t fast_stream = 0) {
+    opts_ = model_opts(rng_mode, fast_stream);
+  }
   // LozengeTiler::LoadMTGP: as in the reference's CUDA build, walks then draw from cuRAND
   // MTGP32 block generators (RT_RNG_MTGP).
   void LoadMTGP() { opts_.rng_mode = RT_RNG_MTGP; }
 
-  void Walk(tiling& t, int steps, long seed) { check(rt_lozenge_walk(t.data(), side_of(t), steps, seed, &opts_)); }
+  void Walk(tiling& t, int steps, long seed) { check(rt_lozenge_walk(t.data(), side_of(t), steps, seed, wopts())); }
 
   tiling CFTP(const tiling& tmax, const tiling& tmin, long driver_seed, long first_steps = 128, int schedule = 0,
               int max_attempts = 30, rt_cftp_stats* stats = nullptr) {
     tiling out(tmax.size());
     check(rt_lozenge_cftp(tmax.data(), tmin.data(), side_of(tmax), driver_seed, first_steps, schedule, max_attempts,
-                          &opts_, out.data(), stats));
+                          wopts(), out.data(), stats));
     return out;
   }
 
@@ -259,28 +274,24 @@ class LozengeTiler {
     return d;
   }
 
-  rt_walk_opts& options() { return opts_; }
-
- private:
-  rt_walk_opts opts_;
 };
 
 // src/RectTriangle/RectTriangleTiler.h:32-86.  The nine weights {wt1, wt2, wt3, wm1, wm2, wm3,
 // wr1, wr2, wr3} are #defines in the reference's kernel (all 1); here a constructor argument.
-class RectTriangleTiler {
+class RectTriangleTiler : public TinyMTOpts {
  public:
   explicit RectTriangleTiler(int rng_mode = RT_RNG_TINYMT, uint32_t fast_stream = 0,
                              std::vector<double> weights = std::vector<double>(9, 1.0))
-      : opts_(model_opts(rng_mode, fast_stream)), w_(std::move(weights)) {
+      : w_(std::move(weights)) {
     if (w_.size() != 9) throw Error(RT_ERR_INVALID_ARGUMENT, "nine weights");
+    opts_ = model_opts(rng_mode, fast_stream);
   }
-  void LoadTinyMT(const std::string&, int) {}
   // RectTriangleTiler::LoadMTGP (RectTriangleTiler.cpp:27-30): walks then draw from cuRAND
   // MTGP32 block generators, as in the reference's CUDA build (RT_RNG_MTGP).
   void LoadMTGP() { opts_.rng_mode = RT_RNG_MTGP; }
 
   void Walk(tiling& t, int steps, long seed) {
-    check(rt_recttri_walk(t.data(), side_of(t), steps, seed, w_.data(), &opts_));
+    check(rt_recttri_walk(t.data(), side_of(t), steps, seed, w_.data(), wopts()));
   }
 
   static tiling maxHex(int n) { return hex(n, 1); }
@@ -301,22 +312,22 @@ class RectTriangleTiler {
     t.resize((size_t)side * side);
     return t;
   }
-  rt_walk_opts opts_;
   std::vector<double> w_;
 };
 
 // src/TriangleDimer/TriangleDimerTiler.h:84-216 (bibone tilings).
-class TriangleDimerTiler {
+class TriangleDimerTiler : public TinyMTOpts {
  public:
   explicit TriangleDimerTiler(int rng_mode = RT_RNG_TINYMT, uint32_t fast_stream = 0)
-      : opts_(model_opts(rng_mode, fast_stream)) {}
-  void LoadTinyMT(const std::string&, int) {}
+  {
+    opts_ = model_opts(rng_mode, fast_stream);
+  }
   // TriangleDimerTiler::LoadMTGP (TriangleDimerTiler.cpp:29-32): walks then draw from cuRAND
   // MTGP32 block generators, as in the reference's CUDA build (RT_RNG_MTGP).
   void LoadMTGP() { opts_.rng_mode = RT_RNG_MTGP; }
 
   void Walk(tiling& t, int steps, long seed, rt_cftp_stats* stats = nullptr) {
-    check(rt_td_walk(t.data(), side_of(t), steps, seed, &opts_, stats));
+    check(rt_td_walk(t.data(), side_of(t), steps, seed, wopts(), stats));
   }
 
   static tiling IceCreamCone(int n, int m) {
@@ -371,8 +382,6 @@ class TriangleDimerTiler {
     return v;
   }
 
- private:
-  rt_walk_opts opts_;
 };
 
 // Six-vertex model (no counterpart in the reference); the state is the height function.

@@ -180,13 +180,20 @@ int orc_td_icecream(int n, int m, int* out, long cap) {
   return T;
 }
 
-int orc_td_walk_tinymt(int* t, int N, long steps, long seed) {
+// params: nparams triples (mat1, mat2, tmat), triple k for generator k (the reference's
+// LoadTinyMT table, TriangleDimerTiler.cpp:24-27); generators beyond them keep the jump set.
+int orc_td_walk_tinymt(int* t, int N, long steps, long seed, const uint32_t* params, long nparams) {
   if (N % 2) return -1;
   Dimers d = from_tiling(t, N);
   const int M = d.M;
   std::vector<oracle::TinyMT32> g((size_t)M * M);
   for (size_t k = 0; k < g.size(); ++k) {
     g[k] = oracle::TinyMT32{0, 0, 0, 0, oracle::kTmtMat1, oracle::kTmtMat2, oracle::kTmtTmat};
+    if (params && (long)k < nparams) {
+      g[k].mat1 = params[3 * k];
+      g[k].mat2 = params[3 * k + 1];
+      g[k].tmat = params[3 * k + 2];
+    }
     oracle::tmt_init(g[k], (uint32_t)seed + (uint32_t)k);
   }
   std::default_random_engine gen;

@@ -184,7 +184,9 @@ int orc_rt_hex(int n, int top, int* out, long cap) {
   return side;
 }
 
-int orc_rt_walk_tinymt(int* t, int N, long steps, long seed, const double* w9) {
+// params: nparams triples (mat1, mat2, tmat), triple k for generator k (the reference's
+// LoadTinyMT table, RectTriangleTiler.cpp:22-25); generators beyond them keep the jump set.
+int orc_rt_walk_tinymt(int* t, int N, long steps, long seed, const double* w9, const uint32_t* params, long nparams) {
   if (N % 3 || N < 9) return -1;
   RChain c;
   rsplit(t, N, c);
@@ -193,6 +195,11 @@ int orc_rt_walk_tinymt(int* t, int N, long steps, long seed, const double* w9) {
   std::vector<oracle::TinyMT32> g((size_t)N * M);
   for (size_t k = 0; k < g.size(); ++k) {
     g[k] = oracle::TinyMT32{0, 0, 0, 0, oracle::kTmtMat1, oracle::kTmtMat2, oracle::kTmtTmat};
+    if (params && (long)k < nparams) {
+      g[k].mat1 = params[3 * k];
+      g[k].mat2 = params[3 * k + 1];
+      g[k].tmat = params[3 * k + 2];
+    }
     oracle::tmt_init(g[k], (uint32_t)seed + (uint32_t)k);
   }
   std::default_random_engine gen;

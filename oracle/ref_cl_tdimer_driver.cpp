@@ -35,7 +35,7 @@ void ndrange(F f) {
 
 }  // namespace
 
-extern "C" int ref_td_walk(int* t, int N, long steps, long seed) {
+extern "C" int ref_td_walk(int* t, int N, long steps, long seed, const uint32_t* params, long nparams) {
   const int M = N / 2;
   g_M = M;
   std::vector<int> tTri((size_t)(N / 2) * N), tB((size_t)N * N);
@@ -57,7 +57,16 @@ extern "C" int ref_td_walk(int* t, int N, long steps, long seed) {
   for (int i = 0; i < N / 2; ++i)
     for (int j = 0; j < N; ++j) (j % 2 == 0 ? tD : tU)[(size_t)i * M + j / 2] = tTri[(size_t)i * N + j];
   std::vector<reftd::tinymt32wp_t> st((size_t)M * M);
-  for (auto& s : st) s.mat1 = TINYMT32J_MAT1, s.mat2 = TINYMT32J_MAT2, s.tmat = TINYMT32J_TMAT;
+  // The parameter buffer of LoadTinyMT (file_reader.cpp: one (mat1, mat2, tmat) per
+  // generator, the rest of the buffer the jump set here).
+  for (size_t k = 0; k < st.size(); ++k) {
+    auto& s = st[k];
+    if (params && (long)k < nparams) {
+      s.mat1 = params[3 * k]; s.mat2 = params[3 * k + 1]; s.tmat = params[3 * k + 2];
+    } else {
+      s.mat1 = TINYMT32J_MAT1; s.mat2 = TINYMT32J_MAT2; s.tmat = TINYMT32J_TMAT;
+    }
+  }
   refcl::gsize[0] = (size_t)M * M; refcl::gsize[1] = 1; refcl::gsize[2] = 1; refcl::gid[1] = 0; refcl::gid[2] = 0;
   for (size_t k = 0; k < st.size(); ++k) {
     refcl::gid[0] = k;

@@ -253,7 +253,30 @@ def read_tinymt_params(path: str | os.PathLike, count: int) -> np.ndarray:
     return out
 
 
-class DominoTiler:
+class _TinyMTTable:
+    """LoadTinyMT(params, size) of every reference tiler (DominoTiler.cpp:235-237,
+    LozengeTiler.cpp:161-164, RectTriangleTiler.cpp:22-25, TriangleDimerTiler.cpp:24-27): the
+    per-generator TinyMT parameters of its OpenCL path, triple k for generator k."""
+
+    _params: np.ndarray | None = None
+
+    def LoadTinyMT(self, params, size: int | None = None) -> None:
+        """Loads per-generator TinyMT parameters: a TinyMTDC file path (with ``size`` sets)
+        or an (n, 3) array of (mat1, mat2, tmat)."""
+        if isinstance(params, (str, os.PathLike)):
+            if size is None:
+                raise ValueError("size is required with a parameter file")
+            self._params = read_tinymt_params(params, size)
+        else:
+            self._params = np.ascontiguousarray(np.asarray(params, dtype=np.uint32).reshape(-1, 3))
+
+    def _apply_params(self, o: "_WalkOpts") -> None:
+        if self._params is not None:
+            o.tinymt_params = self._params.ctypes.data
+            o.tinymt_params_count = self._params.shape[0]
+
+
+class DominoTiler(_TinyMTTable):
     """Domino tilings (src/Domino/DominoTiler.h:46-131).
 
     ``rule`` selects what the reference selects by compiling one of its kernel files:
@@ -273,17 +296,7 @@ class DominoTiler:
         self.engine = int(engine)
         self._params: np.ndarray | None = None
 
-    # -- reference: LoadTinyMT(params, size) / LoadMTGP() ----------------------------------
-    def LoadTinyMT(self, params, size: int | None = None) -> None:
-        """Loads per-generator TinyMT parameters: a TinyMTDC file path (with ``size`` sets,
-        DominoTiler.cpp:235-237) or an (n, 3) array of (mat1, mat2, tmat)."""
-        if isinstance(params, (str, os.PathLike)):
-            if size is None:
-                raise ValueError("size is required with a parameter file")
-            self._params = read_tinymt_params(params, size)
-        else:
-            self._params = np.ascontiguousarray(np.asarray(params, dtype=np.uint32).reshape(-1, 3))
-
+    # -- reference: LoadTinyMT(params, size) (the mixin) / LoadMTGP() -----------------------
     def LoadMTGP(self) -> None:
         """DominoTiler::LoadMTGP (DominoTiler.cpp:239-242): walks draw from cuRAND MTGP32, one
         generator per 8 x 8 block of sites seeded seed + block, as the reference's CUDA build."""
@@ -298,9 +311,7 @@ class DominoTiler:
         o.weight_b = self.b
         o.fast_stream = self.fast_stream
         o.engine = self.engine
-        if self._params is not None:
-            o.tinymt_params = self._params.ctypes.data
-            o.tinymt_params_count = self._params.shape[0]
+        self._apply_params(o)
         if cuda_stream:
             o.cuda_stream = cuda_stream
         return o
@@ -430,7 +441,7 @@ def _tri_side(d) -> int:
     return m
 
 
-class LozengeTiler:
+class LozengeTiler(_TinyMTTable):
     """Lozenge tilings (src/Lozenge/LozengeTiler.h:46-92).  ``rng`` is 'tinymt' (bit-exact
     with the reference's OpenCL path), 'mtgp' (its CUDA path's cuRAND MTGP32 draws, uniform
     rule; also selected by LoadMTGP) or 'fast'."""
@@ -457,6 +468,7 @@ class LozengeTiler:
             o.weight_a = float(self.q)
         else:
             o.rule = RT_LOZENGE_UNIFORM
+        self._apply_params(o)
         return o
 
     def Walk(self, t, steps: int, seed: int) -> None:
@@ -536,7 +548,7 @@ class LozengeTiler:
         return out
 
 
-class RectTriangleTiler:
+class RectTriangleTiler(_TinyMTTable):
     """Rectangle-triangle tilings (src/RectTriangle/RectTriangleTiler.h:32-86).  ``weights``
     holds the nine tile weights {wt1, wt2, wt3, wm1, wm2, wm3, wr1, wr2, wr3}
     (recttrianglekernel.cl:3-11; all 1 by default, the reference's values).  ``rng`` is
@@ -560,6 +572,7 @@ class RectTriangleTiler:
         lib().rt_walk_opts_default(C.byref(o))
         o.rng_mode = RNG_MODES[self.rng]
         o.fast_stream = self.fast_stream
+        self._apply_params(o)
         return o
 
     def Walk(self, t, steps: int, seed: int) -> None:
@@ -598,7 +611,7 @@ class RectTriangleTiler:
         return out
 
 
-class TriangleDimerTiler:
+class TriangleDimerTiler(_TinyMTTable):
     """Bibone tilings, i.e. dimer coverings of the triangular lattice
     (src/TriangleDimer/TriangleDimerTiler.h:84-216).  ``rng`` is 'tinymt' (bit-exact with the
     reference's OpenCL path), 'mtgp' (its CUDA path's cuRAND MTGP32 draws; also selected by
@@ -618,6 +631,7 @@ class TriangleDimerTiler:
         lib().rt_walk_opts_default(C.byref(o))
         o.rng_mode = RNG_MODES[self.rng]
         o.fast_stream = self.fast_stream
+        self._apply_params(o)
         return o
 
     def Walk(self, t, steps: int, seed: int) -> dict:

@@ -86,20 +86,25 @@ __device__ __forceinline__ void td_try_flip(uint8_t* D, int M, int c, int a, int
   }
 }
 
-__global__ void k_td_seed(uint4* st, int64_t count, uint32_t seed) {
+// InitTinyMT (triangledimerkernel.cl:749-756): generator k, of the work item (k / M, k mod M),
+// seeded seed + k with its own parameters when a table is loaded.
+__global__ void k_td_seed(uint4* st, const uint4* params, int64_t count, uint32_t seed) {
   const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (k < count) st[k] = tmt_seed(seed + (uint32_t)k, kTmtMat1, kTmtMat2, kTmtTmat);
+  if (k >= count) return;
+  const uint4 p = params ? params[k] : make_uint4(kTmtMat1, kTmtMat2, kTmtTmat, 0);
+  st[k] = tmt_seed(seed + (uint32_t)k, p.x, p.y, p.z);
 }
 
 // TinyMT mode: every generator draws (as every work item of the reference's rotate kernel
 // does); sites of the class flip when rd < 0.5, i.e. the 23-bit draw is below 2^22.
-__global__ void k_td_step_tmt(uint8_t* D, uint4* tmt, int M, TdStep s) {
+__global__ void k_td_step_tmt(uint8_t* D, uint4* tmt, const uint4* params, int M, TdStep s) {
   pdl_begin();
   const int b = blockIdx.x * blockDim.x + threadIdx.x, a = blockIdx.y;
   if (b >= M) return;
   const size_t k = (size_t)a * M + b;
   uint4 g = tmt[k];
-  const uint32_t u = tmt_next_u23(g, kTmtMat1, kTmtMat2, kTmtTmat);
+  const uint4 p = params ? params[k] : make_uint4(kTmtMat1, kTmtMat2, kTmtTmat, 0);
+  const uint32_t u = tmt_next_u23(g, p.x, p.y, p.z);
   tmt[k] = g;
   if (u < (1u << 22) && td_in_class(s, a, b)) td_try_flip(D, M, td_cycle_of(s), a, b);
 }
@@ -430,6 +435,8 @@ RT_API rt_status rt_td_walk(int32_t* tiling, int32_t n_side, int64_t steps, int6
   if (o.rng_mode != RT_RNG_TINYMT && o.rng_mode != RT_RNG_FAST && o.rng_mode != RT_RNG_MTGP)
     return fail(RT_ERR_INVALID_ARGUMENT, "unknown rng mode");
   if (o.rng_mode == RT_RNG_FAST && o.fast_stream >= 65536u) return fail(RT_ERR_INVALID_ARGUMENT, "fast_stream must be < 65536");
+  if (o.tinymt_params && o.rng_mode != RT_RNG_TINYMT)
+    return fail(RT_ERR_INVALID_ARGUMENT, "bibone walk: a TinyMT parameter table needs the TinyMT mode");
   const int N = n_side, M = N / 2;
   std::vector<uint8_t> D((size_t)M * M);
   td_from_tiling(tiling, N, D.data());
@@ -452,12 +459,13 @@ RT_API rt_status rt_td_walk(int32_t* tiling, int32_t n_side, int64_t steps, int6
   std::vector<int> cover = td_cover(D.data(), M);
   cudaStream_t st = (cudaStream_t)o.cuda_stream;
   uint8_t* dD = nullptr;
-  uint4* tmt = nullptr;
+  uint4 *tmt = nullptr, *tmt_params = nullptr;
   void* mtgp = nullptr;
   const MtgpGrid mg = mtgp_grid(M, M);
   auto cleanup = [&]() {
     if (dD) cudaFree(dD);
     if (tmt) cudaFree(tmt);
+    if (tmt_params) cudaFree(tmt_params);
     if (mtgp) cudaFree(mtgp);
   };
   if (cudaMalloc(&dD, D.size()) != cudaSuccess ||
@@ -468,6 +476,12 @@ RT_API rt_status rt_td_walk(int32_t* tiling, int32_t n_side, int64_t steps, int6
     return fail(RT_ERR_OUT_OF_MEMORY, "bibone walk: device allocation failed");
   }
   cudaMemcpyAsync(dD, D.data(), D.size(), cudaMemcpyHostToDevice, st);
+  if (o.rng_mode == RT_RNG_TINYMT) {
+    if (rt_status ps = tmt_param_table(o, (int64_t)M * M, &tmt_params, st)) {
+      cleanup();
+      return ps;
+    }
+  }
   std::vector<TdStep> sched((size_t)steps);
   if (o.rng_mode != RT_RNG_FAST) {
     // TriangleDimerTiler.cpp:269-276, 459-460: type, r1, r2 (and p1, p2 for butterflies)
@@ -489,7 +503,7 @@ RT_API rt_status rt_td_walk(int32_t* tiling, int32_t n_side, int64_t steps, int6
   cudaEventCreate(&e1);
   if (o.rng_mode == RT_RNG_TINYMT) {
     const int64_t count = (int64_t)M * M;
-    k_td_seed<<<(unsigned)((count + 255) / 256), 256, 0, st>>>(tmt, count, (uint32_t)seed);
+    k_td_seed<<<(unsigned)((count + 255) / 256), 256, 0, st>>>(tmt, tmt_params, count, (uint32_t)seed);
   } else if (o.rng_mode == RT_RNG_MTGP) {
     // TriangleDimerTiler.cpp:287-289: block generator k seeded seed + k
     if (rt_status ms = mtgp_seed(mtgp, mg.count(), seed, st)) {
@@ -503,7 +517,7 @@ RT_API rt_status rt_td_walk(int32_t* tiling, int32_t n_side, int64_t steps, int6
   const dim3 g_all((M + 127) / 128, M), g_quad(((M + 3) / 4 + 31) / 32, (M + 7) / 8);
   for (int64_t h = 0; h < steps; ++h) {
     if (o.rng_mode == RT_RNG_TINYMT)
-      pdl_launch(k_td_step_tmt, g_all, dim3(128), st, dD, tmt, M, sched[(size_t)h]);
+      pdl_launch(k_td_step_tmt, g_all, dim3(128), st, dD, tmt, (const uint4*)tmt_params, M, sched[(size_t)h]);
     else if (o.rng_mode == RT_RNG_MTGP)
       pdl_launch(k_td_step_mtgp, dim3(mg.gx, mg.gy), dim3(kMtgpBlock, kMtgpBlock), st, dD, M, sched[(size_t)h],
                  static_cast<curandStateMtgp32*>(mtgp));

@@ -40,6 +40,7 @@ struct LzView {
   int N, M, P, active;
   size_t colour_stride, chain_stride;
   uint4* tmt;
+  const uint4* tmt_params;  // per-generator {mat1, mat2, tmat} (LoadTinyMT), or NULL
   __host__ __device__ uint8_t* colour(int ch, int c) const {
     return base + (size_t)ch * chain_stride + (size_t)c * colour_stride;
   }
@@ -55,9 +56,13 @@ __device__ __forceinline__ uint8_t lz_flip(uint32_t e, uint32_t u, const LzRule&
   return (uint8_t)e;
 }
 
-__global__ void k_lz_seed(uint4* st, int64_t count, uint32_t seed) {
+// InitTinyMT (lozengekernel.cl:127-134): generator k, of the work item (i, j) = (k / M,
+// k mod M), seeded seed + k with its own parameters when a table is loaded.
+__global__ void k_lz_seed(uint4* st, const uint4* params, int64_t count, uint32_t seed) {
   const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (k < count) st[k] = tmt_seed(seed + (uint32_t)k, kTmtMat1, kTmtMat2, kTmtTmat);
+  if (k >= count) return;
+  const uint4 p = params ? params[k] : make_uint4(kTmtMat1, kTmtMat2, kTmtTmat, 0);
+  st[k] = tmt_seed(seed + (uint32_t)k, p.x, p.y, p.z);
 }
 
 __global__ void k_lz_rotate_tmt(LzView v, int r, LzRule rule) {
@@ -66,7 +71,8 @@ __global__ void k_lz_rotate_tmt(LzView v, int r, LzRule rule) {
   if (j >= v.M) return;
   const int64_t k = (int64_t)i * v.M + j;
   uint4 s = v.tmt[k];
-  const uint32_t u = tmt_next_u23(s, kTmtMat1, kTmtMat2, kTmtTmat);
+  const uint4 p = v.tmt_params ? v.tmt_params[k] : make_uint4(kTmtMat1, kTmtMat2, kTmtTmat, 0);
+  const uint32_t u = tmt_next_u23(s, p.x, p.y, p.z);
   v.tmt[k] = s;
   for (int ch = 0; ch < v.active; ++ch) {
     uint8_t* p = v.colour(ch, r) + (size_t)i * v.P + j;
@@ -257,6 +263,7 @@ struct LzSampler {
   LzRule rule{};
   uint8_t* base = nullptr;
   uint4* tmt = nullptr;
+  uint4* tmt_params = nullptr;  // LoadTinyMT table, or NULL
   void* mtgp = nullptr;  // RT_RNG_MTGP: the block generators (curandStateMtgp32)
   bool mtgp_seeded = false;
   int32_t* scratch = nullptr;
@@ -270,6 +277,7 @@ struct LzSampler {
   ~LzSampler() {
     if (base) cudaFree(base);
     if (tmt) cudaFree(tmt);
+    if (tmt_params) cudaFree(tmt_params);
     if (mtgp) cudaFree(mtgp);
     if (scratch) cudaFree(scratch);
     if (counter) cudaFree(counter);
@@ -278,7 +286,7 @@ struct LzSampler {
     if (own_stream && stream) cudaStreamDestroy(stream);
   }
   LzView view() const {
-    return LzView{base, N, M, P, active, colour_stride, chain_stride, tmt};
+    return LzView{base, N, M, P, active, colour_stride, chain_stride, tmt, tmt_params};
   }
   static rt_status create(int n_side, int chains, const rt_walk_opts& o, std::unique_ptr<LzSampler>* out) {
     if (n_side < 9 || n_side % 3 || n_side > 32766)
@@ -288,7 +296,8 @@ struct LzSampler {
     if (o.rng_mode == RT_RNG_MTGP && o.rule != RT_LOZENGE_UNIFORM)
       return fail(RT_ERR_INVALID_ARGUMENT, "lozenge sweep: the MTGP mode takes the uniform rule (lozengekernel.cu)");
     if (o.rng_mode == RT_RNG_FAST && o.fast_stream >= 65536u) return fail(RT_ERR_INVALID_ARGUMENT, "fast_stream must be < 65536");
-    if (o.tinymt_params) return fail(RT_ERR_INVALID_ARGUMENT, "lozenge sweep: per-generator parameter tables are not supported");
+    if (o.tinymt_params && o.rng_mode != RT_RNG_TINYMT)
+      return fail(RT_ERR_INVALID_ARGUMENT, "lozenge sweep: a TinyMT parameter table needs the TinyMT mode");
     if (o.rule != RT_LOZENGE_UNIFORM && o.rule != RT_LOZENGE_Q) return fail(RT_ERR_INVALID_ARGUMENT, "lozenge sweep: unknown rule");
     if (o.rule == RT_LOZENGE_Q && (!(o.weight_a > 0.0) || !std::isfinite(o.weight_a)))
       return fail(RT_ERR_INVALID_ARGUMENT, "lozenge sweep: q (weight_a) must be finite and > 0");
@@ -318,7 +327,10 @@ struct LzSampler {
     LZ_CUDA(cudaMemsetAsync(s->base, 0, s->chain_stride * chains, s->stream));
     LZ_CUDA(cudaMalloc(&s->scratch, (size_t)s->N * s->N * sizeof(int32_t)));
     LZ_CUDA(cudaMalloc(&s->counter, sizeof(unsigned long long)));
-    if (o.rng_mode == RT_RNG_TINYMT) LZ_CUDA(cudaMalloc(&s->tmt, (size_t)s->N * s->M * sizeof(uint4)));
+    if (o.rng_mode == RT_RNG_TINYMT) {
+      LZ_CUDA(cudaMalloc(&s->tmt, (size_t)s->N * s->M * sizeof(uint4)));
+      if (rt_status st = tmt_param_table(o, (int64_t)s->N * s->M, &s->tmt_params, s->stream)) return st;
+    }
     if (o.rng_mode == RT_RNG_MTGP) LZ_CUDA(cudaMalloc(&s->mtgp, mtgp_state_bytes(mtgp_grid(s->N, s->M).count())));
     *out = std::move(s);
     return RT_OK;
@@ -367,7 +379,7 @@ struct LzSampler {
       return RT_OK;
     }
     const int64_t count = (int64_t)N * M;
-    k_lz_seed<<<(unsigned)((count + 255) / 256), 256, 0, stream>>>(tmt, count, (uint32_t)s);
+    k_lz_seed<<<(unsigned)((count + 255) / 256), 256, 0, stream>>>(tmt, tmt_params, count, (uint32_t)s);
     return check();
   }
   rt_status run(const uint8_t* colours, int64_t steps) {

@@ -79,12 +79,17 @@ struct RtView {
   int N, M, P;
   size_t colour_stride;
   uint4* tmt;
+  const uint4* tmt_params;  // per-generator {mat1, mat2, tmat} (LoadTinyMT), or NULL
   __device__ int32_t* colour(int c) const { return base + (size_t)c * colour_stride; }
 };
 
-__global__ void k_rt_seed(uint4* st, int64_t count, uint32_t seed) {
+// InitTinyMT (recttrianglekernel.cl:148-155): generator k, of the work item (k / M, k mod M),
+// seeded seed + k with its own parameters when a table is loaded.
+__global__ void k_rt_seed(uint4* st, const uint4* params, int64_t count, uint32_t seed) {
   const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (k < count) st[k] = tmt_seed(seed + (uint32_t)k, kTmtMat1, kTmtMat2, kTmtTmat);
+  if (k >= count) return;
+  const uint4 p = params ? params[k] : make_uint4(kTmtMat1, kTmtMat2, kTmtTmat, 0);
+  st[k] = tmt_seed(seed + (uint32_t)k, p.x, p.y, p.z);
 }
 
 __global__ void k_rt_flip_tmt(RtView v, int r, RtWeights W) {
@@ -93,7 +98,8 @@ __global__ void k_rt_flip_tmt(RtView v, int r, RtWeights W) {
   if (j >= v.M) return;
   const int64_t k = (int64_t)i * v.M + j;
   uint4 s = v.tmt[k];
-  const uint32_t u = tmt_next_u23(s, kTmtMat1, kTmtMat2, kTmtTmat);
+  const uint4 pr = v.tmt_params ? v.tmt_params[k] : make_uint4(kTmtMat1, kTmtMat2, kTmtTmat, 0);
+  const uint32_t u = tmt_next_u23(s, pr.x, pr.y, pr.z);
   v.tmt[k] = s;
   int32_t* p = v.colour(r) + (size_t)i * v.P + j;
   const int e = *p, n = rt_flip(e, (float)u * (1.0f / 8388608.0f), W);
@@ -373,6 +379,8 @@ RT_API rt_status rt_recttri_walk(int32_t* tiling, int32_t n_side, int64_t steps,
   if (o.rng_mode != RT_RNG_TINYMT && o.rng_mode != RT_RNG_FAST && o.rng_mode != RT_RNG_MTGP)
     return fail(RT_ERR_INVALID_ARGUMENT, "unknown rng mode");
   if (o.rng_mode == RT_RNG_FAST && o.fast_stream >= 65536u) return fail(RT_ERR_INVALID_ARGUMENT, "fast_stream must be < 65536");
+  if (o.tinymt_params && o.rng_mode != RT_RNG_TINYMT)
+    return fail(RT_ERR_INVALID_ARGUMENT, "recttri walk: a TinyMT parameter table needs the TinyMT mode");
   for (size_t p = 0; p < (size_t)n_side * n_side; ++p)
     if ((uint32_t)tiling[p] > 0xffffffu) return fail(RT_ERR_INVALID_ARGUMENT, "recttri tiling values must be six hex digits");
   int devs = 0;
@@ -384,13 +392,14 @@ RT_API rt_status rt_recttri_walk(int32_t* tiling, int32_t n_side, int64_t steps,
   const RtWeights W = make_weights(weights9);
   cudaStream_t stream = (cudaStream_t)o.cuda_stream;
   int32_t *base = nullptr, *scratch = nullptr;
-  uint4* tmt = nullptr;
+  uint4 *tmt = nullptr, *tmt_params = nullptr;
   void* mtgp = nullptr;
   const MtgpGrid mg = mtgp_grid(N, M);
   auto cleanup = [&]() {
     if (base) cudaFree(base);
     if (scratch) cudaFree(scratch);
     if (tmt) cudaFree(tmt);
+    if (tmt_params) cudaFree(tmt_params);
     if (mtgp) cudaFree(mtgp);
   };
   const size_t cs = (size_t)N * P;
@@ -408,11 +417,12 @@ RT_API rt_status rt_recttri_walk(int32_t* tiling, int32_t n_side, int64_t steps,
     for (int i = 0; i < N; ++i)
       for (int j = 0; j < N; ++j) h[(size_t)(((i - j) % 3 + 3) % 3) * cs + (size_t)i * P + j / 3] = tiling[(size_t)i * N + j];
     cudaMemcpyAsync(base, h.data(), h.size() * sizeof(int32_t), cudaMemcpyHostToDevice, stream);
-    RtView v{base, N, M, P, cs, tmt};
+    if (o.rng_mode == RT_RNG_TINYMT && (status = tmt_param_table(o, (int64_t)N * M, &tmt_params, stream)) != RT_OK) break;
+    RtView v{base, N, M, P, cs, tmt, tmt_params};
     const dim3 gr((M + 127) / 128, N), gq(((M + 3) / 4 + 127) / 128, N), gu((M + 127) / 128, N - 2);
     if (o.rng_mode == RT_RNG_TINYMT) {
       const int64_t count = (int64_t)N * M;
-      k_rt_seed<<<(unsigned)((count + 255) / 256), 256, 0, stream>>>(tmt, count, (uint32_t)seed);
+      k_rt_seed<<<(unsigned)((count + 255) / 256), 256, 0, stream>>>(tmt, tmt_params, count, (uint32_t)seed);
       // RectTriangleTiler.cpp:74-76: colours from default_random_engine(seed)
       std::default_random_engine gen;
       std::uniform_int_distribution<int> dist(0, 2);

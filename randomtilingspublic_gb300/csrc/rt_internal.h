@@ -48,6 +48,13 @@ rt_status mtgp_seed(void* states, int count, int64_t seed, cudaStream_t stream);
 // x < rows, y < cols (host memory).
 rt_status mtgp_draws_grid(int rows, int cols, int64_t seed, int64_t launches, float* out);
 
+// Per-generator TinyMT parameters of the reference's LoadTinyMT (file_reader.cpp:22-38):
+// o.tinymt_params holds o.tinymt_params_count triples (mat1, mat2, tmat), triple k for
+// generator k.  Allocates (cudaMalloc) and fills a device table of `count` uint4
+// {mat1, mat2, tmat, 0}; generators beyond the triples keep the TinyMT32 jump set, as the
+// reference's default parameters do.  *out stays NULL when o carries no table.
+rt_status tmt_param_table(const rt_walk_opts& o, int64_t count, uint4** out, cudaStream_t s);
+
 // Vertex classes of DomainToVertices: 0 outside, 1 interior, 2 boundary.
 void domino_vertex_classes(const int32_t* domain, int m_side, int32_t* out);
 // Interior vertices (flip candidates) of the domain a tiling covers.

@@ -163,9 +163,9 @@ def lozenge(ref: str) -> None:
         getattr(lz, f"refh_lz_{which}_tiling")(P(d), rows, P(out))
         return out
 
-    def walk(t, n, steps, seed):
+    def walk(t, n, steps, seed, params=None):
         t = t.copy()
-        lz.ref_lz_walk(P(t), n, steps, seed, None, 0)
+        lz.ref_lz_walk(P(t), n, steps, seed, P(params), 0 if params is None else params.shape[0])
         return t
 
     cases, host = [], []
@@ -187,6 +187,15 @@ def lozenge(ref: str) -> None:
     start = extremal(d, rows, "max")
     cases.append({"name": "lz_walk_minimal_lozenge", "kind": "walk", "N": rows + 1, "start": start.tolist(),
                   "steps": 1000, "seed": 2018, "expected": walk(start, rows + 1, 1000, 2018).tolist()})
+    # A per-generator parameter table (synthetic, seeded; LoadTinyMT's buffer, one triple per
+    # generator of the N x N/3 grid) in place of the missing parameter file.
+    d, rows = domain(5, 0)
+    start = extremal(d, rows, "min")
+    params = np.random.default_rng(20261204).integers(0, 2**32, size=((rows + 1) * ((rows + 1) // 3), 3),
+                                                      dtype=np.uint64).astype(np.uint32)
+    cases.append({"name": "lz_walk_hex5_0_paramtable", "kind": "walk", "N": rows + 1, "start": start.tolist(),
+                  "steps": 180, "seed": 4321, "params": params.tolist(),
+                  "expected": walk(start, rows + 1, 180, 4321, params).tolist()})
     # CFTP from the reference's Walk: epochs of Walk(t, steps_k, seed_k) on both chains,
     # seeds from mt19937(driver seed), prepending 2 * steps.back().
     d, rows = domain(3, 0)
@@ -237,7 +246,7 @@ def recttri(ref: str) -> None:
     rl = C.CDLL(str(ROOT / "oracle/_ref/libref_recttri.so"))
     lz = C.CDLL(str(ROOT / "oracle/_ref/libref_lozenge.so"))
     P = lambda a: None if a is None else a.ctypes.data_as(C.c_void_p)
-    rl.ref_rt_walk.argtypes = [C.c_void_p, C.c_int, C.c_long, C.c_long]
+    rl.ref_rt_walk.argtypes = [C.c_void_p, C.c_int, C.c_long, C.c_long, C.c_void_p, C.c_long]
     rl.refh_rt_hex.argtypes = [C.c_int, C.c_int, C.c_void_p, C.c_long]
     rl.refh_rt_from_lozenge.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_int, C.c_void_p]
 
@@ -246,9 +255,9 @@ def recttri(ref: str) -> None:
         side = rl.refh_rt_hex(n, which, P(buf), buf.size)
         return buf[: side * side].copy(), side
 
-    def walk(t, n, steps, seed):
+    def walk(t, n, steps, seed, params=None):
         t = t.copy()
-        rl.ref_rt_walk(P(t), n, steps, seed)
+        rl.ref_rt_walk(P(t), n, steps, seed, P(params), 0 if params is None else params.shape[0])
         return t
 
     fixtures = Path(ref) / "Examples/ExampleOuts/RectTriangle"
@@ -266,6 +275,13 @@ def recttri(ref: str) -> None:
         start, side = hexagon(n, which)
         cases.append({"name": f"rt_walk_hex{n}_{'max' if which else 'min'}_{steps}", "N": side, "start": start.tolist(),
                       "steps": steps, "seed": seed, "expected": walk(start, side, steps, seed).tolist()})
+    # a per-generator parameter table (synthetic, seeded), one triple per generator of the
+    # N x N/3 grid, in place of the missing parameter file
+    start, side = hexagon(5, 0)
+    params = np.random.default_rng(20261205).integers(0, 2**32, size=(side * (side // 3), 3),
+                                                      dtype=np.uint64).astype(np.uint32)
+    cases.append({"name": "rt_walk_hex5_min_paramtable", "N": side, "start": start.tolist(), "steps": 400,
+                  "seed": 606, "params": params.tolist(), "expected": walk(start, side, 400, 606, params).tolist()})
     # the reference's own end state of RectTriangleEx (1000 steps from minHex(5), seed not
     # recorded) as a start state
     end = _read_matrix(fixtures / "EndTiling.txt")
@@ -303,16 +319,16 @@ def bibone(ref: str) -> None:
     td = C.CDLL(str(ROOT / "oracle/_ref/libref_tdimer.so"))
     P = lambda a: None if a is None else a.ctypes.data_as(C.c_void_p)
     td.refh_td_icecream.argtypes = [C.c_int, C.c_int, C.c_void_p, C.c_long]
-    td.ref_td_walk.argtypes = [C.c_void_p, C.c_int, C.c_long, C.c_long]
+    td.ref_td_walk.argtypes = [C.c_void_p, C.c_int, C.c_long, C.c_long, C.c_void_p, C.c_long]
 
     def cone(n, m):
         buf = np.zeros(4 * (n + 8) ** 2, np.int32)
         side = td.refh_td_icecream(n, m, P(buf), buf.size)
         return buf[: side * side].copy(), side
 
-    def walk(t, n, steps, seed):
+    def walk(t, n, steps, seed, params=None):
         t = t.copy()
-        td.ref_td_walk(P(t), n, steps, seed)
+        td.ref_td_walk(P(t), n, steps, seed, P(params), 0 if params is None else params.shape[0])
         return t
 
     fixtures = Path(ref) / "Examples/ExampleOuts/TriangleDimer"
@@ -345,6 +361,13 @@ def bibone(ref: str) -> None:
         t, side = cone(n, m)
         cases.append({"name": f"td_walk_cone{n}_{m}_{steps}", "N": side, "start": t.tolist(), "steps": steps, "seed": seed,
                       "expected": walk(t, side, steps, seed).tolist()})
+    # a per-generator parameter table (synthetic, seeded), one triple per generator of the
+    # M x M grid, in place of the missing parameter file
+    t, side = cone(7, 0)
+    params = np.random.default_rng(20261206).integers(0, 2**32, size=((side // 2) ** 2, 3),
+                                                      dtype=np.uint64).astype(np.uint32)
+    cases.append({"name": "td_walk_cone7_0_paramtable", "N": side, "start": t.tolist(), "steps": 600, "seed": 515,
+                  "params": params.tolist(), "expected": walk(t, side, 600, 515, params).tolist()})
     (HERE / "bibone_ref_cases.json").write_text(json.dumps(
         {"generator": "tests/golden/make_golden.py", "example": example, "host_cases": host, "cases": cases,
          "test_butterflies": butterflies},

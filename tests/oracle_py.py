@@ -286,8 +286,9 @@ def lz_tiling_to_heightfunc(t, d) -> np.ndarray:
     return out
 
 
-def lz_walk_tinymt(t: np.ndarray, n: int, steps: int, seed: int) -> None:
-    assert lz_lib().orc_lz_walk_tinymt(_p(t), n, steps, seed, None, 0) == 0
+def lz_walk_tinymt(t: np.ndarray, n: int, steps: int, seed: int, params=None) -> None:
+    p, cnt = _params(params)
+    assert lz_lib().orc_lz_walk_tinymt(_p(t), n, steps, seed, _p(p), cnt) == 0
 
 
 def lz_walk_draws(t: np.ndarray, n: int, draws: np.ndarray, steps: int, seed: int) -> None:
@@ -313,7 +314,7 @@ def lz_cftp(tmax, tmin, n, driver_seed, first, schedule, max_attempts, fast=Fals
 # ---- rectangle-triangle ----------------------------------------------------------------
 _RT_SIG = {
     "orc_rt_hex": (C.c_int, [C.c_int, C.c_int, _P, _L]),
-    "orc_rt_walk_tinymt": (C.c_int, [_P, C.c_int, _L, _L, _P]),
+    "orc_rt_walk_tinymt": (C.c_int, [_P, C.c_int, _L, _L, _P, _P, _L]),
     "orc_rt_walk_fast": (C.c_int, [_P, C.c_int, _L, _L, C.c_ulong, C.c_uint, _P]),
     "orc_rt_walk_draws": (C.c_int, [_P, C.c_int, _P, _L, _L, _P]),
 }
@@ -340,9 +341,10 @@ def _w9(weights) -> np.ndarray:
     return np.ascontiguousarray(RT_UNIT_WEIGHTS if weights is None else np.asarray(weights, np.float64))
 
 
-def rt_walk_tinymt(t: np.ndarray, n: int, steps: int, seed: int, weights=None) -> None:
+def rt_walk_tinymt(t: np.ndarray, n: int, steps: int, seed: int, weights=None, params=None) -> None:
     w = _w9(weights)
-    assert rt_lib().orc_rt_walk_tinymt(_p(t), n, steps, seed, _p(w)) == 0
+    p, cnt = _params(params)
+    assert rt_lib().orc_rt_walk_tinymt(_p(t), n, steps, seed, _p(w), _p(p), cnt) == 0
 
 
 def rt_walk_fast(t: np.ndarray, n: int, h0: int, steps: int, seed: int, stream: int = 0, weights=None) -> None:
@@ -398,7 +400,7 @@ def sv_cftp(hmax, hmin, n, seed, stream, first_sweeps, max_attempts, a=1.0, b=1.
 # ---- bibone (triangular-lattice dimers) -----------------------------------------------------
 _TD_SIG = {
     "orc_td_icecream": (C.c_int, [C.c_int, C.c_int, _P, _L]),
-    "orc_td_walk_tinymt": (C.c_int, [_P, C.c_int, _L, _L]),
+    "orc_td_walk_tinymt": (C.c_int, [_P, C.c_int, _L, _L, _P, _L]),
     "orc_td_walk_fast": (C.c_int, [_P, C.c_int, _L, _L, C.c_ulong, C.c_uint]),
     "orc_td_walk_draws": (C.c_int, [_P, C.c_int, _P, _L, _L]),
     "orc_td_fast_step": (None, [C.c_ulong, C.c_uint, _L, _P]),
@@ -421,8 +423,9 @@ def td_icecream(n: int, m: int) -> np.ndarray:
     return buf[: side * side].copy()
 
 
-def td_walk_tinymt(t: np.ndarray, n_side: int, steps: int, seed: int) -> None:
-    assert td_lib().orc_td_walk_tinymt(_p(t), n_side, steps, seed) == 0
+def td_walk_tinymt(t: np.ndarray, n_side: int, steps: int, seed: int, params=None) -> None:
+    p, cnt = _params(params)
+    assert td_lib().orc_td_walk_tinymt(_p(t), n_side, steps, seed, _p(p), cnt) == 0
 
 
 def td_walk_draws(t: np.ndarray, n_side: int, draws: np.ndarray, steps: int, seed: int) -> None:

@@ -96,7 +96,7 @@ def test_oracle_matches_reference_vectors(orc):
         assert np.array_equal(orc.td_icecream(hc["n"], hc["m"]), hc["tiling"])
     for case in GOLD["cases"]:
         t = np.array(case["start"], np.int32)
-        orc.td_walk_tinymt(t, case["N"], case["steps"], case["seed"])
+        orc.td_walk_tinymt(t, case["N"], case["steps"], case["seed"], params=case.get("params"))
         assert np.array_equal(t, case["expected"]), case["name"]
 
 
@@ -167,8 +167,10 @@ def test_oracle_fast_walks_keep_coverings(rt, orc):
 
 @pytest.mark.gpu
 def test_walk_matches_reference_vectors(rt):
-    T = rt.TriangleDimerTiler()
     for case in GOLD["cases"]:
+        T = rt.TriangleDimerTiler()
+        if "params" in case:  # LoadTinyMT's per-generator table (TriangleDimerTiler.cpp:24-27)
+            T.LoadTinyMT(case["params"])
         t = np.array(case["start"], np.int32)
         T.Walk(t, case["steps"], case["seed"])
         assert np.array_equal(t, case["expected"]), case["name"]

@@ -24,7 +24,7 @@ def test_oracle_matches_reference_lozenge_vectors(orc):
     for case in GOLD["cases"]:
         if case["kind"] == "walk":
             t = np.array(case["start"], np.int32)
-            orc.lz_walk_tinymt(t, case["N"], case["steps"], case["seed"])
+            orc.lz_walk_tinymt(t, case["N"], case["steps"], case["seed"], params=case.get("params"))
         else:
             t, att, _ = orc.lz_cftp(case["tmax"], case["tmin"], case["N"], case["driver_seed"], case["first_steps"],
                                     case["schedule"], 40)
@@ -91,7 +91,10 @@ def test_lozenge_walk_matches_reference_vectors(rt):
     for case in GOLD["cases"]:
         if case["kind"] == "walk":
             t = np.array(case["start"], np.int32)
-            rt.LozengeTiler().Walk(t, case["steps"], case["seed"])
+            tiler = rt.LozengeTiler()
+            if "params" in case:  # LoadTinyMT's per-generator table (LozengeTiler.cpp:161-164)
+                tiler.LoadTinyMT(case["params"])
+            tiler.Walk(t, case["steps"], case["seed"])
         else:
             t, stats = rt.LozengeTiler().cftp(case["tmax"], case["tmin"], case["driver_seed"], case["first_steps"],
                                               case["schedule"], 40)

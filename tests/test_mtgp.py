@@ -316,3 +316,54 @@ def test_mtgp_entry_points_check_their_arguments_before_any_cuda_call(rt):
     status = lib.rt_lozenge_walk(t.ctypes.data, rt.side_of(t), 4, 1, C.byref(o))
     assert status == rt.RT_ERR_INVALID_ARGUMENT
     assert "uniform rule" in lib.rt_last_error().decode()
+
+
+def _write_tinymtdc(path, params) -> None:
+    """A parameter file in the TinyMTDC text format LoadTinyMT reads (file_reader.cpp:22-38):
+    a '#' header line, then one line per set with mat1, mat2, tmat in hex after the 3rd, 4th
+    and 5th comma."""
+    lines = ["# synthetic TinyMTDC parameter sets"]
+    for k, (m1, m2, tm) in enumerate(params):
+        lines.append(f"{k:08x},32,0,{m1:08x},{m2:08x},{tm:08x},0")
+    path.write_text("\n".join(lines) + "\n")
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("model,gold,case_name", [
+    ("lozenge", "lozenge_ref_cases.json", "lz_walk_hex5_0_paramtable"),
+    ("recttri", "recttri_ref_cases.json", "rt_walk_hex5_min_paramtable"),
+    ("bibone", "bibone_ref_cases.json", "td_walk_cone7_0_paramtable"),
+])
+def test_cpp_dropin_load_tinymt_file_walk_equals_the_reference(rt, tmp_path, model, gold, case_name):
+    """tests/cpp/dropin_tinymt_file.cpp reads a TinyMTDC parameter file with LoadTinyMT and
+    walks, for the three tilers whose LoadTinyMT the reference's OpenCL path has
+    (LozengeTiler.cpp:161-164, RectTriangleTiler.cpp:22-25, TriangleDimerTiler.cpp:24-27);
+    the result equals the reference's own kernels run with the same table."""
+    import json
+    import shutil
+    import subprocess
+    from pathlib import Path
+
+    if not shutil.which("g++"):
+        pytest.skip("no g++")
+    root = Path(__file__).resolve().parent.parent
+    case = next(c for c in json.loads((root / "tests/golden" / gold).read_text())["cases"] if c["name"] == case_name)
+    exe = tmp_path / "dropin_tinymt_file"
+    libdir = str(rt.LIB_PATH.parent)
+    subprocess.run(["g++", "-std=c++17", "-O1", f"-I{root / 'include'}", str(root / "tests/cpp/dropin_tinymt_file.cpp"),
+                    f"-L{libdir}", "-l:librt_tilings.so", f"-Wl,-rpath,{libdir}", "-o", str(exe)], check=True)
+    pfile = tmp_path / "params.txt"
+    _write_tinymtdc(pfile, case["params"])
+    out = subprocess.run([str(exe), model, str(pfile), str(len(case["params"])), str(case["steps"]), str(case["seed"])],
+                         check=True, capture_output=True, text=True).stdout
+    got = np.array([int(x) for x in out.split()], np.int32)
+    assert np.array_equal(got, case["expected"])
+
+
+def test_tinymt_file_reader_reads_the_written_sets(rt, tmp_path):
+    """The Python reader of the TinyMTDC format returns the sets written (the C++ header's
+    reader follows the same rules)."""
+    params = [[0x8f7011ee, 0xfc78ff1f, 0x3793fdff], [1, 2, 3], [0xffffffff, 0, 0x10]]
+    pfile = tmp_path / "params.txt"
+    _write_tinymtdc(pfile, params)
+    assert rt.read_tinymt_params(pfile, 3).tolist() == params

@@ -37,7 +37,7 @@ def test_oracle_matches_reference_recttri_vectors(orc):
         assert np.array_equal(orc.rt_hex(hc["n"], False), hc["min"])
     for case in GOLD["cases"]:
         t = np.array(case["start"], np.int32)
-        orc.rt_walk_tinymt(t, case["N"], case["steps"], case["seed"])
+        orc.rt_walk_tinymt(t, case["N"], case["steps"], case["seed"], params=case.get("params"))
         assert np.array_equal(t, case["expected"]), case["name"]
         assert inconsistent_triangles(t) == 0
 
@@ -83,8 +83,10 @@ def test_walk_rejects_bad_arguments_before_any_device_work(rt):
 
 @pytest.mark.gpu
 def test_walk_matches_reference_vectors(rt):
-    R = rt.RectTriangleTiler()
     for case in GOLD["cases"]:
+        R = rt.RectTriangleTiler()
+        if "params" in case:  # LoadTinyMT's per-generator table (RectTriangleTiler.cpp:22-25)
+            R.LoadTinyMT(case["params"])
         t = np.array(case["start"], np.int32)
         R.Walk(t, case["steps"], case["seed"])
         assert np.array_equal(t, case["expected"]), case["name"]
