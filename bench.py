@@ -490,6 +490,9 @@ BENCH_CHECK_SHA256 = "b363844c09336dfecba5a174eb2a1a6b93f0091e55872316ca600e0238
 NCU_TRAFFIC_BYTES = {}
 
 
+TUNE_TABLE = ROOT / "randomtilingspublic_gb300" / "tune" / "gb300.txt"
+
+
 def run_ours(args) -> None:
     import torch
 
@@ -497,6 +500,13 @@ def run_ours(args) -> None:
     dev = torch.device("cuda", local)
     torch.cuda.set_device(dev)
     import randomtilingspublic_gb300 as rt
+
+    # The autotuner's measured launch shapes (randomtilingspublic_gb300/autotune.py), when a
+    # table for this GPU is present and not switched off.
+    tune = None
+    if not args.no_tune and TUNE_TABLE.exists():
+        rt.tune_load(TUNE_TABLE)
+        tune = str(TUNE_TABLE.relative_to(ROOT))
 
     tiler = rt.DominoTiler(rule="cftp_twoperiodic", rng=args.mode, a=WEIGHT_A, b=WEIGHT_B, fast_stream=rank,
                            engine=args.engine)
@@ -557,8 +567,9 @@ def run_ours(args) -> None:
     cells = (n - 2) * (n // 2 - 2)
     tiling_bytes_per_half = 3 * (attempts / half_sweeps)
     peaks = _peaks()
-    if info["engine"] == 2:
-        kernel = info.get("kernel", "k_persist")
+    if info["engine"] in (2, 3):
+        kernel = ("k_runs (run-resident cooperative sweep, one launch per step)" if info["engine"] == 2 else
+                  "k_persist (resident cooperative sweep exchanging band rows every half-sweep, one launch per step)")
         launches_timed = args.steps
         gen = 32 * info["units"] if args.mode == "tinymt" else 0
         algo_bytes = tiling_bytes_per_half * HALF_SWEEPS + gen
@@ -625,7 +636,10 @@ def run_ours(args) -> None:
             "vs_baseline": None, "dtype": "u8", "data": "synthetic",
             "config": {"workload": f"aztec{ORDER}_twoperiodic_a1.0_b0.5_cftp_coupled_maxmin",
                        "rng": args.mode, "engine": args.engine, "half_sweeps_per_step": HALF_SWEEPS,
-                       "l2": "flushed between timed steps (256 MiB write)", "parallelism": f"replicas{ws}"},
+                       "l2": "flushed between timed steps (256 MiB write)", "parallelism": f"replicas{ws}",
+                       "launch": {"tune_table": tune, "tuned": info.get("tuned"), "engine": info["engine"],
+                                  "bands": info["bands"], "threads_per_band": info.get("threads"),
+                                  "units_per_thread": info["units_per_thread"]}},
             "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches, "clocks": clocks,
             "check": check, "batched_cftp": batched, "served_cftp": serving, "single_instance": single,
         }
@@ -645,6 +659,7 @@ def main() -> None:
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-batch", action="store_true")
     ap.add_argument("--no-single", action="store_true")
+    ap.add_argument("--no-tune", action="store_true", help="ignore the autotuner's table")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

@@ -74,7 +74,10 @@ typedef struct rt_walk_opts {
   const uint32_t* tinymt_params;
   int64_t tinymt_params_count;
   uint32_t fast_stream; /* RT_RNG_FAST: stream id (< 65536), e.g. the instance number */
-  int32_t engine;       /* 0: automatic; 1: per-half-sweep kernels; 2: resident persistent kernel */
+  int32_t engine;       /* 0: automatic; 1: per-half-sweep kernels; 2: resident persistent
+                           kernel (the run kernel, which rebuilds the passive colour only where
+                           the colour switches, else k_persist); 3: k_persist, the resident
+                           kernel that exchanges band rows every half-sweep */
   void* cuda_stream;    /* cudaStream_t to run on; NULL = the library's own stream */
 } rt_walk_opts;
 
@@ -462,10 +465,35 @@ RT_API rt_status rt_dm_sampler_accumulate_heights(rt_dm_sampler* s, int32_t chai
 RT_API rt_status rt_domino_heightfunc_device(const int32_t* tiling, const int32_t* domain, int32_t n_side,
                                              int32_t* out, void* cuda_stream);
 RT_API rt_status rt_domino_edge_indicators(const int32_t* tiling, int32_t n_side, uint32_t* counts);
-/* The engine the next run will use: out4 = {engine (1 per-half-sweep kernels, 2 resident
-   persistent kernel), flip-candidate units held by the persistent kernel, CTAs (bands),
-   units per thread}. */
+/* The engine the next run will use: out4 = {engine (1 per-half-sweep kernels, 2 the
+   resident run kernel, 3 the resident k_persist), flip-candidate generators held by the
+   resident kernel (sites with a TinyMT generator: units), CTAs (bands), units per thread
+   (column quads for the run kernel, sites or quads for k_persist)}. */
 RT_API rt_status rt_dm_sampler_engine_info(rt_dm_sampler* s, int64_t* out4);
+/* Launch shape of the sampler's next runs (no counterpart in the reference: its kernels use
+   one compile-time block shape, BLOCK_DIM 8 in src/Domino/dominokernel.cuh:4): engine (0
+   automatic, 1 per-half-sweep kernels, 2 the run kernel, 3 k_persist), bands (CTAs, 0: one
+   per SM) and threads per band (a multiple of 32 up to 1024, 0: 1024) of the run kernel.
+   Results do not depend on the shape: every draw is keyed by its site.  Without this call,
+   and with rt_walk_opts.engine 0, the autotuner's table (rt_tune_load) chooses when it has an
+   entry.  out6 of rt_dm_sampler_launch_info = {engine, units, bands, units per thread,
+   threads per band, 1 when the table chose}. */
+RT_API rt_status rt_dm_sampler_set_launch(rt_dm_sampler* s, int32_t engine, int32_t bands, int32_t threads);
+RT_API rt_status rt_dm_sampler_launch_info(rt_dm_sampler* s, int64_t* out6);
+
+/* ---- autotuner table -------------------------------------------------------------------
+   No counterpart in the reference.  A text table of measured launch shapes, written by
+   `python -m randomtilingspublic_gb300.autotune`: one entry per line,
+     domino <n_lo> <n_hi> <chains> <tinymt|fast> <engine> <bands> <threads> [<us>]
+   ('#' starts a comment).  rt_tune_load replaces the process's table (also read from the
+   file named by the environment variable RT_TUNE_FILE at the first lookup); samplers with
+   engine 0 and no rt_dm_sampler_set_launch take the entry whose tiling-side range holds
+   theirs.  rt_tune_lookup returns {engine, bands, threads} of that entry, or
+   RT_ERR_INVALID_ARGUMENT when there is none. */
+RT_API rt_status rt_tune_load(const char* path);
+RT_API rt_status rt_tune_clear(void);
+RT_API rt_status rt_tune_lookup(int32_t model, int32_t n_side, int32_t chains, int32_t rng_mode, int32_t* out3);
+
 /* Test hook for the resident engine's failure detection (no counterpart in the reference):
    in the sampler's next runs band `band` publishes none of its boundary rows (band < 0:
    none) and every wait gives up after max_spin polls (0: the default, 2^22).  The

@@ -130,6 +130,11 @@ _SIGNATURES = {
     "rt_dm_sampler_interior_vertices": (C.c_int64, [_P]),
     "rt_dm_sampler_launches": (C.c_int64, [_P]),
     "rt_dm_sampler_engine_info": (C.c_int32, [_P, _P]),
+    "rt_dm_sampler_set_launch": (C.c_int32, [_P, C.c_int32, C.c_int32, C.c_int32]),
+    "rt_dm_sampler_launch_info": (C.c_int32, [_P, _P]),
+    "rt_tune_load": (C.c_int32, [C.c_char_p]),
+    "rt_tune_clear": (C.c_int32, []),
+    "rt_tune_lookup": (C.c_int32, [C.c_int32, C.c_int32, C.c_int32, C.c_int32, _P]),
     "rt_dm_sampler_test_silent_band": (C.c_int32, [_P, C.c_int32, C.c_int64]),
     "rt_walk": (C.c_int32, [C.c_int32, _P, C.c_int32, C.c_int64, C.c_int64, _P, _P]),
     "rt_walk_epochs": (C.c_int32, [C.c_int32, _P, C.c_int32, _P, _P, C.c_int32, _P]),
@@ -878,9 +883,16 @@ class DominoSampler:
         return lib().rt_dm_sampler_launches(self.h)
 
     def engine_info(self) -> dict:
-        out = np.zeros(4, np.int64)
-        _check(lib().rt_dm_sampler_engine_info(self.h, _ptr(out)))
-        return {"engine": int(out[0]), "units": int(out[1]), "bands": int(out[2]), "units_per_thread": int(out[3])}
+        out = np.zeros(6, np.int64)
+        _check(lib().rt_dm_sampler_launch_info(self.h, _ptr(out)))
+        return {"engine": int(out[0]), "units": int(out[1]), "bands": int(out[2]), "units_per_thread": int(out[3]),
+                "threads": int(out[4]), "tuned": bool(out[5])}
+
+    def set_launch(self, engine: int = 0, bands: int = 0, threads: int = 0) -> None:
+        """Launch shape of the next runs (rt_dm_sampler_set_launch): engine 0 automatic, 1
+        per-half-sweep kernels, 2 the run kernel, 3 k_persist; bands and threads per band of
+        the run kernel (0: defaults).  Results do not depend on it."""
+        _check(lib().rt_dm_sampler_set_launch(self.h, int(engine), int(bands), int(threads)))
 
 
 def cftp_batch(jobs, cuda_stream: int | None = None):
@@ -1050,6 +1062,23 @@ def edge_indicators(t, counts=None) -> np.ndarray:
     return counts
 
 
+def tune_load(path) -> None:
+    """Loads the autotuner's table of launch shapes (rt_tune_load)."""
+    _check(lib().rt_tune_load(str(path).encode()))
+
+
+def tune_clear() -> None:
+    _check(lib().rt_tune_clear())
+
+
+def tune_lookup(n_side: int, chains: int, rng: str = "tinymt", model: int = 0) -> dict | None:
+    """The table's {engine, bands, threads} for a domino sampler of that side, or None."""
+    out = np.zeros(3, np.int32)
+    if lib().rt_tune_lookup(int(model), int(n_side), int(chains), RNG_MODES[rng], _ptr(out)) != RT_OK:
+        return None
+    return {"engine": int(out[0]), "bands": int(out[1]), "threads": int(out[2])}
+
+
 def mt19937_draws(seed: int, count: int) -> np.ndarray:
     """First ``count`` outputs of std::mt19937(seed) (numpy's legacy MT19937 uses the same
     integer seeding and returns raw 32-bit outputs for the full uint32 range)."""
@@ -1058,5 +1087,5 @@ def mt19937_draws(seed: int, count: int) -> np.ndarray:
 
 
 __all__ = ["DominoTiler", "DominoSampler", "LozengeTiler", "RectTriangleTiler", "SixVertexTiler", "TriangleDimerTiler", "cftp_batch", "Server", "RTError", "lib", "read_tinymt_params", "mt19937_colours",
-           "mt19937_draws", "mtgp_draws", "lozenge_mtgp_draws", "recttri_mtgp_draws",
+           "mt19937_draws", "mtgp_draws", "tune_load", "tune_clear", "tune_lookup", "lozenge_mtgp_draws", "recttri_mtgp_draws",
            "td_mtgp_draws", "CftpStats"]

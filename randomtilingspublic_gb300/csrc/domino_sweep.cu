@@ -233,7 +233,8 @@ __global__ void k_diff(DmView v, int a, int b, unsigned long long* out) {
   } while (0)
 
 DmSampler::~DmSampler() {
-  persist.reset();  // frees its plan buffers on the stream before the stream goes
+  runs.reset();  // the engines free their plan buffers on the stream before the stream goes
+  persist.reset();
   for (void* p : {(void*)tmt, (void*)tmt_params, mtgp, (void*)base, (void*)scratch, (void*)counter, (void*)d_scan,
                   (void*)d_cand})
     dev_free(p, stream);
@@ -263,6 +264,7 @@ rt_status DmSampler::create(int n_side, int n_chains, const rt_walk_opts& o, std
   if (n_side < 6 || n_side % 2) return fail(RT_ERR_INVALID_ARGUMENT, "tiling side must be even and >= 6");
   if (n_side > 32768) return fail(RT_ERR_INVALID_ARGUMENT, "tiling side must be <= 32768");
   if (n_chains < 1 || n_chains > 64) return fail(RT_ERR_INVALID_ARGUMENT, "n_chains must be in [1, 64]");
+  if (o.engine < 0 || o.engine > 3) return fail(RT_ERR_INVALID_ARGUMENT, "engine must be 0, 1, 2 or 3");
   if (o.rng_mode == RT_RNG_FAST && o.fast_stream >= 65536u)
     return fail(RT_ERR_INVALID_ARGUMENT, "fast_stream must be < 65536");
   DmRule rule{};
@@ -321,7 +323,7 @@ rt_status DmSampler::create(int n_side, int n_chains, const rt_walk_opts& o, std
       RT_CUDA(cudaStreamSynchronize(s->stream));
     }
   } else if (o.rng_mode == RT_RNG_MTGP) {
-    if (o.engine == 2) return fail(RT_ERR_INVALID_ARGUMENT, "MTGP mode runs on the per-half-sweep kernels only");
+    if (o.engine >= 2) return fail(RT_ERR_INVALID_ARGUMENT, "MTGP mode runs on the per-half-sweep kernels only");
     if (rt_status st = dev_alloc(&s->mtgp, mtgp_state_bytes(mtgp_grid(s->N - 2, s->N / 2 - 2).count()), s->stream))
       return st;
   }
@@ -377,9 +379,7 @@ rt_status DmSampler::fetch_candidates() {
 
 rt_status DmSampler::store(int ch, int32_t* tiling) {
   if (ch < 0 || ch >= n_chains || !tiling) return fail(RT_ERR_INVALID_ARGUMENT, "store: bad chain or NULL tiling");
-  if (persist) {
-    if (rt_status st = persist->check_error(*this)) return st;
-  }
+  if (rt_status st = check_resident_error()) return st;
   DmView v = view();
   k_merge<<<dim3((N + 255) / 256, N), 256, 0, stream>>>(v, ch, scratch);
   launches++;
@@ -432,9 +432,9 @@ rt_status DmSampler::run(const uint8_t* colours, int64_t steps) {
   bool pers = false;
   if (rt_status st = use_persistent(&pers)) return st;
   if (pers) {
-    last_engine = 2;
+    last_engine = resident;
     for (int64_t q = 0; q < steps; ++q) half_sweeps[colours[q] ? 1 : 0]++;
-    return persist->launch(*this, colours, steps, 0, 0);
+    return launch_resident(colours, steps, 0, 0);
   }
   last_engine = 1;
   DmView v = view();
@@ -460,9 +460,9 @@ rt_status DmSampler::run_fast(uint64_t seed_value, int64_t h0, int64_t steps) {
   bool pers = false;
   if (rt_status st = use_persistent(&pers)) return st;
   if (pers) {
-    last_engine = 2;
+    last_engine = resident;
     for (int64_t q = 0; q < steps; ++q) half_sweeps[((h0 + q) & 1) ? 0 : 1]++;
-    return persist->launch(*this, nullptr, steps, seed_value, h0);
+    return launch_resident(nullptr, steps, seed_value, h0);
   }
   last_engine = 1;
   DmView v = view();
@@ -489,9 +489,7 @@ rt_status DmSampler::diff(int a, int b, int64_t* ndiff) {
   k_diff<<<blocks, 256, 0, stream>>>(v, a, b, counter);
   launches++;
   if (rt_status s = check_launch()) return s;
-  if (persist) {
-    if (rt_status st = persist->check_error(*this)) return st;
-  }
+  if (rt_status st = check_resident_error()) return st;
   unsigned long long h = 0;
   RT_CUDA(cudaMemcpyAsync(&h, counter, sizeof h, cudaMemcpyDeviceToHost, stream));
   RT_CUDA(cudaStreamSynchronize(stream));
@@ -547,31 +545,87 @@ rt_status DmSampler::accumulate_heights(int ch, long long* sums, int32_t* height
 
 rt_status DmSampler::sync() {
   RT_CUDA(cudaStreamSynchronize(stream));
-  if (persist) return persist->check_error(*this);
-  return RT_OK;
+  return check_resident_error();
 }
 
 rt_status DmSampler::use_persistent(bool* yes) {
   *yes = false;
-  if (opts.engine == 1 || opts.rng_mode == RT_RNG_MTGP) return RT_OK;
+  resident = 0;
+  // The engine: opts.engine when set, else the sampler's explicit launch shape, else the
+  // autotuner's entry for this side, chain count and mode, else automatic.
+  int engine = opts.engine;
+  const bool explicit_engine = engine != 0 || launch_engine != 0;
+  eff_bands = launch_bands;
+  eff_threads = launch_threads;
+  tuned = false;
+  if (engine == 0 && launch_engine != 0) {
+    engine = launch_engine;
+  } else if (engine == 0 && launch_bands == 0 && launch_threads == 0) {
+    int e = 0, b = 0, t = 0;
+    if (tune_lookup(RT_MODEL_DOMINO, N, active, opts.rng_mode, &e, &b, &t)) {
+      engine = e;
+      eff_bands = b;
+      eff_threads = t;
+      tuned = true;
+    }
+  }
+  if (engine == 1 || opts.rng_mode == RT_RNG_MTGP) return RT_OK;
   if (plan_dirty) {
     if (rt_status st = fetch_candidates()) return st;
   }
   if (!consistent || !any_candidate) {
-    if (opts.engine == 2) return fail(RT_ERR_INVALID_ARGUMENT, "persistent engine needs consistent loaded tilings");
+    if (engine >= 2 && explicit_engine)
+      return fail(RT_ERR_INVALID_ARGUMENT, "persistent engine needs consistent loaded tilings");
     return RT_OK;
   }
-  if (plan_dirty || !persist || persist->nch != active) {
-    if (!persist) persist = std::make_unique<PersistEngine>();
+  // Engine 0 and 2: the run kernel, else k_persist; engine 3: k_persist alone.
+  if (plan_dirty ||
+      (runs && (runs->nch != active || runs->bands_asked != eff_bands || runs->threads_asked != eff_threads)) ||
+      (persist && persist->nch != active)) {
+    runs.reset();
+    persist.reset();
+  }
+  plan_dirty = false;
+  std::string why;
+  if (engine != 3) {
+    if (!runs) {
+      runs = std::make_unique<RunEngine>();
+      if (rt_status st = runs->prepare(*this)) return st;
+    }
+    if (runs->ready) {
+      resident = 2;
+      *yes = true;
+      return RT_OK;
+    }
+    why = "run kernel: " + runs->plan.why + "; ";
+  }
+  if (!persist) {
+    persist = std::make_unique<PersistEngine>();
     if (rt_status st = persist->prepare(*this)) return st;
-    plan_dirty = false;
   }
-  if (!persist->ready) {
-    if (opts.engine == 2) return fail(RT_ERR_INVALID_ARGUMENT, "persistent engine unavailable: " + persist->plan.why);
+  if (persist->ready) {
+    resident = 3;
+    *yes = true;
     return RT_OK;
   }
-  *yes = true;
+  if (engine >= 2 && explicit_engine)
+    return fail(RT_ERR_INVALID_ARGUMENT, "persistent engine unavailable: " + why + "k_persist: " + persist->plan.why);
   return RT_OK;
+}
+
+rt_status DmSampler::check_resident_error() {
+  if (runs) {
+    if (rt_status st = runs->check_error(*this)) return st;
+  }
+  if (persist) {
+    if (rt_status st = persist->check_error(*this)) return st;
+  }
+  return RT_OK;
+}
+
+rt_status DmSampler::launch_resident(const uint8_t* colours, int64_t steps, uint64_t fast_seed, int64_t h0) {
+  if (resident == 2) return runs->launch(*this, colours, steps, fast_seed, h0);
+  return persist->launch(*this, colours, steps, fast_seed, h0);
 }
 
 }  // namespace rt
@@ -684,13 +738,44 @@ RT_API rt_status rt_dm_sampler_engine_info(rt_dm_sampler* s, int64_t* out4) {
   DmSampler& d = *s->impl;
   bool pers = false;
   if (rt_status st = d.use_persistent(&pers)) return st;
-  int64_t units = 0;
-  if (pers)
+  int64_t units = 0, bands = 0, k = 0;
+  if (pers && d.resident == 2) {
+    units = d.runs->plan.draw_cells;
+    bands = (int64_t)d.runs->plan.bands.size();
+    k = d.runs->plan.K;
+  } else if (pers) {
     for (const DmBand& b : d.persist->plan.bands) units += b.units;
-  out4[0] = pers ? 2 : 1;
+    bands = (int64_t)d.persist->plan.bands.size();
+    k = d.persist->plan.K;
+  }
+  out4[0] = pers ? d.resident : 1;
   out4[1] = units;
-  out4[2] = pers ? (int64_t)d.persist->plan.bands.size() : 0;
-  out4[3] = pers ? d.persist->plan.K : 0;
+  out4[2] = bands;
+  out4[3] = k;
+  return RT_OK;
+}
+
+RT_API rt_status rt_dm_sampler_set_launch(rt_dm_sampler* s, int32_t engine, int32_t bands, int32_t threads) {
+  RT_SAMPLER(s);
+  if (engine < 0 || engine > 3 || bands < 0 || threads < 0 || threads > 1024 || threads % 32)
+    return fail(RT_ERR_INVALID_ARGUMENT, "set_launch: engine 0..3, bands >= 0, threads a multiple of 32 up to 1024");
+  DmSampler& d = *s->impl;
+  d.launch_engine = engine;
+  d.launch_bands = bands;
+  d.launch_threads = threads;
+  d.plan_dirty = true;
+  return RT_OK;
+}
+
+RT_API rt_status rt_dm_sampler_launch_info(rt_dm_sampler* s, int64_t* out6) {
+  RT_SAMPLER(s);
+  if (!out6) return fail(RT_ERR_INVALID_ARGUMENT, "launch_info: out is NULL");
+  int64_t e4[4];
+  if (rt_status st = rt_dm_sampler_engine_info(s, e4)) return st;
+  DmSampler& d = *s->impl;
+  for (int k = 0; k < 4; ++k) out6[k] = e4[k];
+  out6[4] = (e4[0] == 2) ? d.runs->plan.threads : (e4[0] == 3 ? (int64_t)kPersistThreads : 0);
+  out6[5] = d.tuned ? 1 : 0;
   return RT_OK;
 }
 
@@ -776,33 +861,96 @@ RT_API rt_status rt_domino_cftp(const int32_t* tmax, const int32_t* tmin, int32_
   if (rt_status st = s->load(3, tmax)) return st;
   s->active = 2;
   s->plan_dirty = true;
-  rt_cftp_stats st_out{};
+  const bool fast = o.rng_mode == RT_RNG_FAST;
+  // The reference's epoch schedule (AztecDiamondCftpEx.cpp:54-77), drawn ahead for every
+  // attempt: epoch k is created by attempt k with the driver's k-th draw as its seed, and
+  // attempt a runs epochs a, a-1, ..., 0 in that order.  AztecDiamondCftpEx.cpp:76 gives the
+  // new epoch 2 * steps.back() half-sweeps (schedule 0); schedule 1 doubles the oldest.
   std::mt19937 drv((uint32_t)driver_seed);
-  std::vector<int64_t> steps{first_steps};
-  std::vector<uint32_t> seeds{(uint32_t)drv()};
-  std::vector<std::vector<uint8_t>> colours;  // colour draws per epoch, in the order of steps
+  std::vector<int64_t> ep_steps;
+  std::vector<uint32_t> ep_seed;
+  std::vector<std::vector<uint8_t>> ep_colours((size_t)max_attempts);
+  if (!fast) {
+    for (int k = 0; k < max_attempts; ++k) {
+      ep_seed.push_back((uint32_t)drv());
+      ep_steps.push_back(k == 0 ? first_steps : (schedule == 0 ? 2 * ep_steps[0] : 2 * ep_steps[k - 1]));
+    }
+  }
+  auto colours_of = [&](int k) -> const std::vector<uint8_t>& {
+    if (ep_colours[(size_t)k].empty() && ep_steps[(size_t)k] > 0) {
+      std::mt19937 mt(ep_seed[(size_t)k]);
+      ep_colours[(size_t)k] = colour_draws(mt, ep_steps[(size_t)k]);
+    }
+    return ep_colours[(size_t)k];
+  };
+  // Look-back of attempt a (half-sweeps) and its flip attempts over both chains.
+  auto look_back = [&](int att) -> int64_t {
+    if (fast) return 2 * (first_steps << att);
+    int64_t t = 0;
+    for (int k = 0; k <= att; ++k) t += ep_steps[(size_t)k];
+    return t;
+  };
+  auto flips_of = [&](int att) -> int64_t {
+    int64_t black = 0, total = look_back(att);
+    if (fast) {
+      black = total / 2;  // half-sweeps -2T .. -1 alternate, black at even h
+    } else {
+      for (int k = 0; k <= att; ++k)
+        for (uint8_t c : colours_of(k)) black += c ? 1 : 0;
+    }
+    return 2 * (black * s->interior[1] + (total - black) * s->interior[0]);
+  };
+  rt_cftp_stats st_out{};
   float ms_total = 0.f;
-  for (int attempt = 1; attempt <= max_attempts; ++attempt) {
+  auto account = [&](int att) {
+    st_out.attempts = att + 1;
+    st_out.total_steps += look_back(att);
+    st_out.final_steps = look_back(att);
+    st_out.flip_attempts += flips_of(att);
+  };
+  // Attempts go to the run kernel in one launch per group whose look-backs sum to at most
+  // kLaunchHalfSweeps (a launch of well under a second at order 1024); an attempt longer than
+  // that, or a sampler the run kernel does not take, runs attempt by attempt from the host.
+  const int64_t kLaunchHalfSweeps = (int64_t)1 << 21;
+  bool pers = false;
+  if (rt_status st = s->use_persistent(&pers)) return st;
+  const bool one_launch = pers && s->resident == 2 && o.rng_mode != RT_RNG_MTGP;
+  int att = 0;
+  bool coalesced = false;
+  while (att < max_attempts && !coalesced) {
+    int n = 0;
+    int64_t tot = 0;
+    while (one_launch && att + n < max_attempts && tot + look_back(att + n) <= kLaunchHalfSweeps)
+      tot += look_back(att + n++);
+    if (n > 0) {
+      std::vector<std::vector<RunEngine::Epoch>> epochs((size_t)n);
+      for (int q = 0; !fast && q < n; ++q)
+        for (int k = att + q; k >= 0; --k) epochs[(size_t)q].push_back({ep_seed[(size_t)k], &colours_of(k)});
+      cudaEventRecord(s->ev0, s->stream);
+      int ran = 0;
+      if (rt_status st = s->runs->cftp(*s, att, n, epochs, first_steps, (uint64_t)driver_seed, &ran, &coalesced))
+        return st;
+      cudaEventRecord(s->ev1, s->stream);
+      cudaEventSynchronize(s->ev1);
+      float ms = 0.f;
+      cudaEventElapsedTime(&ms, s->ev0, s->ev1);
+      ms_total += ms;
+      for (int q = 0; q < ran; ++q) account(att + q);
+      att += ran;
+      continue;
+    }
+    // One attempt from the host: reset, the attempt's half-sweeps, the coalescence count.
     if (rt_status st = s->copy_chain(0, 2)) return st;
     if (rt_status st = s->copy_chain(1, 3)) return st;
-    int64_t before0 = s->half_sweeps[0], before1 = s->half_sweeps[1];
     cudaEventRecord(s->ev0, s->stream);
-    int64_t look_back = 0;
-    if (o.rng_mode != RT_RNG_FAST) {
-      while (colours.size() < steps.size()) colours.insert(colours.begin(), std::vector<uint8_t>());  // prepended epochs
-      for (size_t k = 0; k < steps.size(); ++k) {
-        if (colours[k].empty() && steps[k] > 0) {
-          std::mt19937 mt(seeds[k]);
-          colours[k] = colour_draws(mt, steps[k]);
-        }
-        if (rt_status st = s->seed(seeds[k])) return st;
-        if (rt_status st = s->run(colours[k].data(), steps[k])) return st;
-        look_back += steps[k];
+    if (!fast) {
+      for (int k = att; k >= 0; --k) {
+        if (rt_status st = s->seed(ep_seed[(size_t)k])) return st;
+        if (rt_status st = s->run(colours_of(k).data(), ep_steps[(size_t)k])) return st;
       }
     } else {
-      const int64_t T = first_steps << (attempt - 1);
+      const int64_t T = first_steps << att;
       if (rt_status st = s->run_fast((uint64_t)driver_seed, -2 * T, 2 * T)) return st;
-      look_back = 2 * T;
     }
     cudaEventRecord(s->ev1, s->stream);
     int64_t nd = -1;
@@ -810,26 +958,16 @@ RT_API rt_status rt_domino_cftp(const int32_t* tmax, const int32_t* tmin, int32_
     float ms = 0.f;
     cudaEventElapsedTime(&ms, s->ev0, s->ev1);
     ms_total += ms;
-    st_out.attempts = attempt;
-    st_out.total_steps += look_back;
-    st_out.final_steps = look_back;
-    st_out.flip_attempts += 2 * ((s->half_sweeps[0] - before0) * s->interior[0] + (s->half_sweeps[1] - before1) * s->interior[1]);
-    st_out.seconds = ms_total * 1e-3;
-    if (nd == 0) {
-      if (stats) *stats = st_out;
-      return s->store(1, out);
-    }
-    if (o.rng_mode != RT_RNG_FAST) {
-      // AztecDiamondCftpEx.cpp:76 prepends 2 * steps.back(); schedule 1 doubles the oldest.
-      int64_t next = schedule == 0 ? steps.back() * 2 : steps.front() * 2;
-      steps.insert(steps.begin(), next);
-      seeds.insert(seeds.begin(), (uint32_t)drv());
-    }
+    account(att);
+    coalesced = nd == 0;
+    ++att;
   }
+  st_out.seconds = ms_total * 1e-3;
   if (stats) *stats = st_out;
   // out receives the top chain of the last attempt, so a caller can resume or inspect it.
   if (rt_status st = s->store(1, out)) return st;
-  return fail(RT_ERR_NOT_COALESCED, "cftp: chains did not coalesce within max_attempts");
+  if (!coalesced) return fail(RT_ERR_NOT_COALESCED, "cftp: chains did not coalesce within max_attempts");
+  return RT_OK;
 }
 
 }  // extern "C"

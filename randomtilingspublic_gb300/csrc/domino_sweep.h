@@ -6,6 +6,7 @@
 #include <memory>
 
 #include "domino_persist.h"
+#include "domino_runs.h"
 #include "domino_rules.h"
 #include "rt_internal.h"
 
@@ -74,8 +75,15 @@ struct DmSampler {
   bool any_candidate = false;
   bool consistent = true;
   bool plan_dirty = true;
-  std::unique_ptr<PersistEngine> persist;
-  int last_engine = 0;  // engine of the last run: 1 per-half-sweep kernels, 2 persistent
+  std::unique_ptr<RunEngine> runs;        // the run-resident kernel (domino_runs.cu)
+  std::unique_ptr<PersistEngine> persist;  // the per-half-sweep-exchange resident kernel
+  int resident = 0;     // the resident kernel the next run uses: 2 run kernel, 3 k_persist, 0 none
+  int last_engine = 0;  // engine of the last run: 1 per-half-sweep kernels, 2 or 3 as resident
+  // Launch shape: an explicit choice (rt_dm_sampler_set_launch; 0 = none), and the shape in
+  // force, from that choice, else the autotuner's table, else the defaults (0).
+  int launch_engine = 0, launch_bands = 0, launch_threads = 0;
+  int eff_bands = 0, eff_threads = 0;
+  bool tuned = false;
   // Test hook of the resident engine (rt_dm_sampler_test_silent_band): a band that
   // publishes nothing (-1: none) and the polls after which a wait gives up (0: default).
   int test_silent_band = -1;
@@ -103,8 +111,10 @@ struct DmSampler {
   rt_status diff(int a, int b, int64_t* ndiff);
   rt_status accumulate_edges(int ch, uint32_t* counts);
   rt_status sync();
-  // Picks the engine for the next run: true when the persistent kernel will run it.
+  // Picks the engine for the next run: true when a resident kernel (see `resident`) will run it.
   rt_status use_persistent(bool* yes);
+  rt_status check_resident_error();
+  rt_status launch_resident(const uint8_t* colours, int64_t steps, uint64_t fast_seed, int64_t h0);
 };
 
 }  // namespace rt

@@ -36,7 +36,7 @@ def _is_valid_tiling(rt, t, d) -> bool:
     return bool(np.all(cover[D == 1] == 1) and np.all(cover[D == 0] == 0))
 
 
-@pytest.mark.parametrize("engine", [1, 2])
+@pytest.mark.parametrize("engine", [1, 2, 3])
 def test_golden_reference_vectors(rt, golden, engine):
     for case in golden["cases"]:
         n = case["N"]
@@ -56,7 +56,7 @@ def test_golden_reference_vectors(rt, golden, engine):
         assert np.array_equal(t, np.array(case["expected"], np.int32)), case["name"]
 
 
-@pytest.mark.parametrize("engine", [1, 2])
+@pytest.mark.parametrize("engine", [1, 2, 3])
 def test_tinymt_walk_random_cases_match_oracle(rt, orc, engine):
     rng = np.random.default_rng(11)
     D = rt.DominoTiler
@@ -76,7 +76,7 @@ def test_tinymt_walk_random_cases_match_oracle(rt, orc, engine):
         assert np.array_equal(g, o), (order, rule, steps, seed)
 
 
-@pytest.mark.parametrize("engine", [1, 2])
+@pytest.mark.parametrize("engine", [1, 2, 3])
 def test_tinymt_walk_with_parameter_table_and_rectangles(rt, orc, engine):
     D = rt.DominoTiler
     rng = np.random.default_rng(3)
@@ -94,7 +94,7 @@ def test_tinymt_walk_with_parameter_table_and_rectangles(rt, orc, engine):
         assert np.array_equal(g, o)
 
 
-@pytest.mark.parametrize("engine", [1, 2])
+@pytest.mark.parametrize("engine", [1, 2, 3])
 def test_tinymt_epochs_match_oracle(rt, orc, engine):
     D = rt.DominoTiler
     d = D.AztecDiamond(33)
@@ -109,7 +109,7 @@ def test_tinymt_epochs_match_oracle(rt, orc, engine):
         assert np.array_equal(g, o), rule
 
 
-@pytest.mark.parametrize("engine", [1, 2])
+@pytest.mark.parametrize("engine", [1, 2, 3])
 @pytest.mark.parametrize("rule", [0, 1, 2, 3])
 def test_fast_walk_matches_oracle(rt, orc, rule, engine):
     D = rt.DominoTiler
@@ -125,7 +125,7 @@ def test_fast_walk_matches_oracle(rt, orc, rule, engine):
         assert np.array_equal(g, o), (order, steps)
 
 
-@pytest.mark.parametrize("engine", [1, 2])
+@pytest.mark.parametrize("engine", [1, 2, 3])
 @pytest.mark.parametrize("rule,a,b", [(1, 1.0, 1.0), (3, 1.0, 0.5)])
 def test_fast_cftp_matches_oracle(rt, orc, rule, a, b, engine):
     D = rt.DominoTiler
@@ -141,7 +141,7 @@ def test_fast_cftp_matches_oracle(rt, orc, rule, a, b, engine):
         assert _is_valid_tiling(rt, out, d)
 
 
-@pytest.mark.parametrize("engine", [1, 2])
+@pytest.mark.parametrize("engine", [1, 2, 3])
 def test_tinymt_cftp_doubling_schedule_matches_oracle(rt, orc, engine):
     D = rt.DominoTiler
     d = D.AztecDiamond(8)
@@ -178,7 +178,7 @@ def test_sampler_api(rt):
     s.close()
 
 
-@pytest.mark.parametrize("engine", [1, 2])
+@pytest.mark.parametrize("engine", [1, 2, 3])
 def test_full_size_order_1024_matches_threaded_oracle(rt, orc, engine):
     """Order-1024 Aztec diamond (N = 2054): 40 TinyMT steps of the two-periodic CFTP rule
     equal the oracle bit for bit."""
@@ -252,16 +252,17 @@ def test_full_size_order_1024_properties(rt):
 
 
 @pytest.mark.gpu
-def test_resident_engine_wait_gives_up_and_the_sampler_stays_usable(rt):
-    """Failure detection without a GPU fault: band 1 of the resident kernel publishes none of
-    its boundary rows and a wait gives up after 4096 polls, so its neighbours' waits run out;
-    every CTA leaves its loop, the host reads RT_ERR_TIMEOUT, and the same sampler (same CUDA
-    context) then reproduces a fresh sampler's walk bit for bit."""
+@pytest.mark.parametrize("engine", [2, 3])
+def test_resident_engine_wait_gives_up_and_the_sampler_stays_usable(rt, engine):
+    """Failure detection without a GPU fault, on both resident kernels: band 1 publishes none
+    of its boundary rows and a wait gives up after 4096 polls, so its neighbours' waits run
+    out; every CTA leaves its loop, the host reads RT_ERR_TIMEOUT, and the same sampler (same
+    CUDA context) then reproduces a fresh sampler's walk bit for bit."""
     D = rt.DominoTiler
     d = D.AztecDiamond(64)
     tmax, tmin = D.MaxTiling(d), D.MinTiling(d)
     n = rt.side_of(tmax)
-    tiler = rt.DominoTiler(rule="cftp", rng="fast", fast_stream=3, engine=2)
+    tiler = rt.DominoTiler(rule="cftp", rng="fast", fast_stream=3, engine=engine)
 
     def fresh():
         s = rt.DominoSampler(n, 2, tiler)
@@ -271,7 +272,7 @@ def test_resident_engine_wait_gives_up_and_the_sampler_stays_usable(rt):
 
     s = fresh()
     info = s.engine_info()
-    assert info["engine"] == 2 and info["bands"] >= 3
+    assert info["engine"] == engine and info["bands"] >= 3
     assert rt.lib().rt_dm_sampler_test_silent_band(s.h, 1, 4096) == rt.RT_OK
     with pytest.raises(rt.RTError) as err:
         s.run_fast(5, 0, 64)
