@@ -55,6 +55,10 @@ rt_status mtgp_draws_grid(int rows, int cols, int64_t seed, int64_t launches, fl
 // reference's default parameters do.  *out stays NULL when o carries no table.
 rt_status tmt_param_table(const rt_walk_opts& o, int64_t count, uint4** out, cudaStream_t s);
 
+// The autotuner's table (tune.cpp): the engine, bands and threads per band measured fastest
+// for a model, tiling side, chain count and random mode; false when the table has none.
+bool tune_lookup(int model, int n_side, int chains, int rng, int* engine, int* bands, int* threads);
+
 // Vertex classes of DomainToVertices: 0 outside, 1 interior, 2 boundary.
 void domino_vertex_classes(const int32_t* domain, int m_side, int32_t* out);
 // Interior vertices (flip candidates) of the domain a tiling covers.
