@@ -42,9 +42,11 @@ def _sampler(rt, n, chains, rng, tmax, tmin):
     return s
 
 
-def measure(rt, n, chains, rng, tmax, tmin, shape, half_sweeps: int = 256, reps: int = 3) -> float | None:
-    """Microseconds per half-sweep of `shape` on this domain, or None when the sampler does
-    not take it (no such plan, e.g. too many quads per thread for register generators)."""
+def measure(rt, n, chains, rng, tmax, tmin, shape, half_sweeps: int = 256, reps: int = 3):
+    """(microseconds per half-sweep, the shape the sampler used) for `shape` on this domain,
+    or None when the sampler does not take it (no such plan, e.g. too many quads per thread
+    for register generators).  A plan has at most one band per row, so on small domains the
+    bands used can be fewer than asked."""
     s = _sampler(rt, n, chains, rng, tmax, tmin)
     try:
         s.set_launch(*shape)
@@ -53,8 +55,9 @@ def measure(rt, n, chains, rng, tmax, tmin, shape, half_sweeps: int = 256, reps:
         except rt.RTError:
             return None
         engine, bands, threads = shape
-        if info["engine"] != engine or (engine == 2 and (info["bands"] != bands or info["threads"] != threads)):
+        if info["engine"] != engine or (engine == 2 and info["threads"] != threads):
             return None
+        used = (engine, info["bands"], threads) if engine == 2 else shape
         cols = rt.mt19937_colours(12345, half_sweeps)
 
         def run():
@@ -73,7 +76,7 @@ def measure(rt, n, chains, rng, tmax, tmin, shape, half_sweeps: int = 256, reps:
             run()
             s.sync()
             best = min(best, time.perf_counter() - t0)
-        return best / half_sweeps * 1e6
+        return best / half_sweeps * 1e6, used
     finally:
         s.close()
 
@@ -89,11 +92,12 @@ def tune_domino(rt, orders, chains_list=(2,), rngs=("tinymt",), half_sweeps: int
         n = rt.side_of(tmax)
         for chains in chains_list:
             for rng in rngs:
-                results = []
+                results, used_shapes = [], set()
                 for shape in candidates(sms):
-                    us = measure(rt, n, chains, rng, tmax, tmin, shape, half_sweeps)
-                    if us is not None:
-                        results.append((us, shape))
+                    got = measure(rt, n, chains, rng, tmax, tmin, shape, half_sweeps)
+                    if got is not None and got[1] not in used_shapes:
+                        used_shapes.add(got[1])
+                        results.append(got)
                 results.sort()
                 us, shape = results[0]
                 log(f"order {order} (N={n}) chains {chains} {rng}: best {shape} {us:.3f} us/half-sweep "
