@@ -15,8 +15,9 @@
 //   1. after a barrier (run j > 0): where the colour switched, each thread rebuilds its quads'
 //      colour t from colour 1 - t (rows above and below, and one neighbour cell in the row),
 //      taking the row beyond the band from the neighbour band's published quads;
-//   2. it flips each quad L times (L the run's length) in registers: 4 draws, byte-parallel
-//      state tests of all chains, no shared-memory traffic and no barrier;
+//   2. it flips each quad L times (L the run's length) in registers: 4 draws and, per 32-bit
+//      word of chains, three logic ops on byte masks (which bytes can flip, which hold
+//      state 3), no shared-memory traffic and no barrier;
 //   3. it stores the quads, and the quads of the band's first and last rows are published
 //      to the neighbour bands as tagged 64-bit words (data and tag in one single-copy-atomic
 //      element, so no fence or flag is needed).
@@ -113,15 +114,6 @@ __device__ __forceinline__ uint32_t cell_word_mask(const uint32_t (&x)[4], int j
   } else {
     return x[j];
   }
-}
-
-// Byte-parallel flip (bytes <= 15): a byte equal to 3 becomes 12 where up is all-ones, a byte
-// equal to 12 becomes 3 where dn is, both by XOR with 15.  Byte b equals v exactly when bit 4
-// of (b ^ v) + 15 is clear (the sum stays below 32, so no carry crosses a byte).
-__device__ __forceinline__ uint32_t flip_word(uint32_t x, uint32_t up, uint32_t dn) {
-  const uint32_t ne3 = (x ^ 0x03030303u) + 0x0f0f0f0fu, ne12 = (x ^ 0x0c0c0c0cu) + 0x0f0f0f0fu;
-  const uint32_t hit = ((~ne3 & up) | (~ne12 & dn)) & 0x10101010u;
-  return x ^ ((hit >> 4) * 15u);
 }
 
 // The colour-(1 - tf) quad of a row rebuilt from colour tf (dominokernel.cl:22-31): a site
@@ -372,12 +364,21 @@ __global__ void __launch_bounds__(kThreads, 1) k_runs(RunArgs a) {
     const uint32_t valid = (m >> kQuadValidShift) & 15u;
     if (valid) {
       const uint4 rl = c.rule[((m & kQuadOdd) ? 1 : 0) | (t << 1)];
-      // All-ones for the cells that draw.  Every generator of the quad advances each
-      // half-sweep, branch-free: those of cells without a candidate are never read back or
-      // written out, and their accept masks are zero.
-      uint32_t vm[4];
+      // Per word, the bytes that can flip (state 3 or 12; a flippable site is an interior
+      // vertex, so a cell without a candidate has none) and those in state 3.  A flip only
+      // toggles 3 <-> 12, so within the run the quad is tracked by its state-3 bytes and
+      // written back once: a byte flipped an odd number of times is XORed with 15.  Every
+      // generator of the quad advances each half-sweep, branch-free: those of cells without a
+      // candidate are never read back or written out.
+      uint32_t flippable[NCH], three[NCH], three0[NCH];
 #pragma unroll
-      for (int k = 0; k < 4; ++k) vm[k] = 0u - ((valid >> k) & 1u);
+      for (int jj = 0; jj < NCH; ++jj) {
+        const uint32_t x = w.w[jj];
+        const uint32_t is3 = (~((x ^ 0x03030303u) + 0x0f0f0f0fu) & 0x10101010u) >> 4;
+        const uint32_t is12 = (~((x ^ 0x0c0c0c0cu) + 0x0f0f0f0fu) & 0x10101010u) >> 4;
+        three[jj] = three0[jj] = is3 * 0xffu;
+        flippable[jj] = (is3 | is12) * 0xffu;
+      }
       for (int hh = 0; hh < L; ++hh) {
         uint32_t r[4];
         if (kMode == RT_RNG_TINYMT) {
@@ -385,11 +386,11 @@ __global__ void __launch_bounds__(kThreads, 1) k_runs(RunArgs a) {
           for (int k = 0; k < 4; ++k) {
             if (kParams) {  // per-generator parameters, reloaded (L1) to spare registers
               const int i = (int)(wh >> 16), col = 4 * (int)(wh & 0xffffu) + k;
-              const uint4 p = vm[k] ? __ldg(&a.tmt_params[(int64_t)(i - 1) * a.cols + (col - 1)])
-                                    : make_uint4(kTmtMat1, kTmtMat2, kTmtTmat, 0);
-              r[k] = tmt_next_u23(st[s][k], p.x, p.y, p.z);
+              const uint4 p = ((valid >> k) & 1u) ? __ldg(&a.tmt_params[(int64_t)(i - 1) * a.cols + (col - 1)])
+                                                  : make_uint4(kTmtMat1, kTmtMat2, kTmtTmat, 0);
+              r[k] = tmt_next_u23_mad(st[s][k], p.x, p.y, p.z);
             } else {
-              r[k] = tmt_next_u23(st[s][k], kTmtMat1, kTmtMat2, kTmtTmat);
+              r[k] = tmt_next_u23_mad(st[s][k], kTmtMat1, kTmtMat2, kTmtTmat);
             }
           }
         } else {
@@ -403,13 +404,18 @@ __global__ void __launch_bounds__(kThreads, 1) k_runs(RunArgs a) {
         uint32_t up[4], dn[4];
 #pragma unroll
         for (int k = 0; k < 4; ++k) {
-          up[k] = (r[k] - rl.x) < rl.y ? vm[k] : 0u;
-          dn[k] = (r[k] - rl.z) < rl.w ? vm[k] : 0u;
+          up[k] = (r[k] - rl.x) < rl.y ? 0xffffffffu : 0u;
+          dn[k] = (r[k] - rl.z) < rl.w ? 0xffffffffu : 0u;
         }
+        // A byte flips where it is 3 and the up move is accepted, or 12 and the down move is.
 #pragma unroll
-        for (int jj = 0; jj < NCH; ++jj)
-          w.w[jj] = flip_word(w.w[jj], cell_word_mask<NCH>(up, jj), cell_word_mask<NCH>(dn, jj));
+        for (int jj = 0; jj < NCH; ++jj) {
+          const uint32_t u = cell_word_mask<NCH>(up, jj), d = cell_word_mask<NCH>(dn, jj) & flippable[jj];
+          three[jj] ^= (three[jj] & u) | (~three[jj] & d);
+        }
       }
+#pragma unroll
+      for (int jj = 0; jj < NCH; ++jj) w.w[jj] ^= (three[jj] ^ three0[jj]) & 0x0f0f0f0fu;
     }
     st_quad<NCH>(pa + off, w);
     if (!silent) {

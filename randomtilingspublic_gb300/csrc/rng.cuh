@@ -39,6 +39,40 @@ __device__ __forceinline__ uint32_t tmt_next_u23(uint4& s, uint32_t mat1, uint32
   return t0 >> 9;
 }
 
+// The same step and tempering with the work spread over both integer pipes: the constant
+// shifts are multiplies by powers of two (x << k = x * 2^k, x >> k = the high word of
+// x * 2^(32-k)) and the parameter masks are multiplies by the parity bit, which run on the
+// multiply-add pipe, leaving the three-input logic ops to the ALU.  Identical results.
+__device__ __forceinline__ uint32_t mul_lo(uint32_t a, uint32_t b) {
+  uint32_t d;
+  asm("mul.lo.u32 %0, %1, %2;" : "=r"(d) : "r"(a), "r"(b));
+  return d;
+}
+__device__ __forceinline__ uint32_t mul_hi(uint32_t a, uint32_t b) {
+  uint32_t d;
+  asm("mul.hi.u32 %0, %1, %2;" : "=r"(d) : "r"(a), "r"(b));
+  return d;
+}
+__device__ __forceinline__ uint32_t mad_hi(uint32_t a, uint32_t b, uint32_t c) {
+  uint32_t d;
+  asm("mad.hi.u32 %0, %1, %2, %3;" : "=r"(d) : "r"(a), "r"(b), "r"(c));
+  return d;
+}
+__device__ __forceinline__ uint32_t tmt_next_u23_mad(uint4& s, uint32_t mat1, uint32_t mat2, uint32_t tmat) {
+  uint32_t x = (s.x & 0x7fffffffu) ^ s.y ^ s.z;
+  uint32_t y = s.w;
+  x ^= mul_lo(x, 2u);                   // x << 1
+  y ^= mul_hi(y, 0x80000000u) ^ x;      // y >> 1
+  const uint32_t odd = y & 1u;
+  s.x = s.y;
+  s.y = s.z ^ mul_lo(mat1, odd);
+  s.z = x ^ mul_lo(y, 1024u) ^ mul_lo(mat2, odd);  // y << 10
+  s.w = y;
+  const uint32_t t1 = mad_hi(s.z, 1u << 24, s.x);  // s.x + (s.z >> 8)
+  const uint32_t t0 = s.w ^ t1 ^ mul_lo(tmat, t1 & 1u);
+  return mul_hi(t0, 1u << 23);                     // t0 >> 9
+}
+
 __device__ __forceinline__ void tmt_plain_step(uint4& s, uint32_t mat1, uint32_t mat2) {
   uint32_t x = (s.x & 0x7fffffffu) ^ s.y ^ s.z;
   uint32_t y = s.w;

@@ -48,6 +48,62 @@ def kasteleyn_edge_probs(d: np.ndarray, a: float, b: float) -> np.ndarray:
     return P.ravel()
 
 
+def kasteleyn_edge_probs_sparse(d: np.ndarray, a: float, b: float, block: int = 2048) -> np.ndarray:
+    """The same probabilities for large domains: the Kasteleyn matrix has four entries per
+    row, so a sparse LU factorisation solved block by block against unit columns gives the
+    entries of K^-1 at the edges without forming the dense inverse."""
+    from scipy.sparse import csc_matrix
+    from scipy.sparse.linalg import splu
+
+    M = int(np.sqrt(d.size))
+    N = M + 1
+    F = d.reshape(M, M)
+    faces = [tuple(f) for f in np.argwhere(F == 1)]
+    black = [f for f in faces if (f[0] + f[1]) % 2 == 0]
+    white = [f for f in faces if (f[0] + f[1]) % 2 == 1]
+    bi = {f: k for k, f in enumerate(black)}
+    wi = {f: k for k, f in enumerate(white)}
+    rows, cols, vals, edges = [], [], [], []
+    for (r, c) in black:
+        for dr, dc in ((0, 1), (0, -1), (1, 0), (-1, 0)):
+            f2 = (r + dr, c + dc)
+            if f2 not in wi:
+                continue
+            if dr == 0:
+                left = min(c, c + dc)
+                v = a if left % 2 == 1 else b
+                edges.append((bi[(r, c)], wi[f2], v, 0, r, left + 1))
+            else:
+                top = min(r, r + dr)
+                v = 1j * (a if top % 2 == 0 else b)
+                edges.append((bi[(r, c)], wi[f2], v, 1, top + 1, c))
+            rows.append(bi[(r, c)])
+            cols.append(wi[f2])
+            vals.append(v)
+    n = len(black)
+    lu = splu(csc_matrix((np.array(vals, complex), (rows, cols)), shape=(n, n)))
+    # K^-1(w, b) = column b of K^-1 at row w: solve K X = E_b for blocks of unit columns b.
+    by_b = {}
+    for e in edges:
+        by_b.setdefault(e[0], []).append(e)
+    P = np.zeros((2, N, N))
+    for b0 in range(0, n, block):
+        b1 = min(n, b0 + block)
+        E = np.zeros((n, b1 - b0), complex)
+        E[np.arange(b0, b1), np.arange(b1 - b0)] = 1.0
+        X = lu.solve(E)
+        for bb in range(b0, b1):
+            for _, w, v, kind, i, j in by_b.get(bb, ()):
+                P[kind, i, j] = abs(v * X[w, bb - b0])
+    return P.ravel()
+
+
+@pytest.mark.parametrize("order,a,b", [(6, 1.0, 1.0), (9, 1.0, 0.8), (12, 0.7, 1.0)])
+def test_sparse_kasteleyn_equals_dense(rt, order, a, b):
+    d = rt.DominoTiler.AztecDiamond(order)
+    assert np.allclose(kasteleyn_edge_probs_sparse(d, a, b, block=37), kasteleyn_edge_probs(d, a, b), atol=1e-10)
+
+
 @pytest.mark.parametrize("order,a,b", [(3, 1.0, 1.0), (3, 1.0, 0.5), (4, 0.6, 1.0), (4, 1.0, 0.3)])
 def test_kasteleyn_equals_the_chains_stationary_edge_marginals(rt, order, a, b):
     d, n, tilings, seen = enumerate_tilings(rt, order)
