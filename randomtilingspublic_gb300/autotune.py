@@ -20,7 +20,7 @@ import argparse
 import time
 from pathlib import Path
 
-THREADS = (512, 640, 768, 896, 1024)
+THREADS = (512, 640, 768, 896, 960, 992, 1024)
 
 
 def candidates(sms: int) -> list[tuple[int, int, int]]:
