@@ -176,130 +176,160 @@ def headline_domain_oracle(orc):
     return d, tmax, tmin, _interior_by_colour(orc.domain_to_vertices(d))
 
 
-BATCH_INSTANCES = 2048
-BATCH_ORDERS = (8, 24)    # Aztec diamond orders, uniform
-BATCH_SIDES = (4, 16)     # hexagon sides, uniform
-BATCH_B = (0.7, 1.0)      # 2-periodic b of the weighted half (a = 1); smaller b couples far slower
-BATCH_FIRST, BATCH_ATTEMPTS = 16, 12
+# Batched form (config 4's shape): 8192 instances, half Aztec diamonds and half hexagons,
+# half of the diamonds 2-periodic.  The config's full size ranges (orders up to 512, sides up
+# to 256) and its b down to 0.3 would take hours for any implementation of the reference's
+# chain: the coalescence look-back grows like the order squared and, at b <= 0.6, by 8-16x per
+# doubling of the order.  The sizes are therefore truncated to orders U[16, 64] and sides
+# U[8, 32], b to U[0.8, 1.0], and the look-back capped at BATCH_ATTEMPTS doublings from
+# BATCH_FIRST sweeps (2 x 16 x 2^13 half-sweeps for dominoes).
+BATCH_INSTANCES = 8192
+BATCH_ORDERS = (16, 64)   # Aztec diamond orders, uniform
+BATCH_SIDES = (8, 32)     # hexagon sides, uniform
+BATCH_B = (0.8, 1.0)      # 2-periodic b of the weighted half (a = 1)
+BATCH_FIRST, BATCH_ATTEMPTS = 16, 14
+PLAIN_SAMPLES = 64        # instances drawn across the mix for the one-at-a-time baseline
 
 
-def batched_leg(rt, plain_samples: int = 8) -> dict:
-    """Batched fast-mode CFTP (rt_cftp_batch) on a mixed batch, against the same instances
-    run one at a time through the plain entry points (rt_domino_cftp / rt_lozenge_cftp).
-    Half the instances are Aztec diamonds, half hexagons; half of the diamonds are
-    2-periodic with a = 1, b ~ U[BATCH_B]; seed k, stream k; first look-back BATCH_FIRST
-    sweeps, at most BATCH_ATTEMPTS doublings.  Samples/s count coalesced instances."""
+def _batch_job(rt, cache, rng, k: int, log_sizes: bool = False) -> dict:
+    """Instance k of the mix: even k an Aztec diamond (every other one 2-periodic), odd k a
+    hexagon; sizes uniform (log-uniform for the served stream) in the ranges above."""
     D, L = rt.DominoTiler, rt.LozengeTiler
+
+    def draw(lo, hi):
+        if log_sizes:
+            return int(np.exp(rng.uniform(np.log(lo), np.log(hi + 1))))
+        return int(rng.integers(lo, hi + 1))
+
+    if k % 2 == 0:
+        order = draw(*BATCH_ORDERS)
+        if ("d", order) not in cache:
+            d = D.AztecDiamond(order)
+            cache[("d", order)] = (D.MaxTiling(d), D.MinTiling(d))
+        tmax, tmin = cache[("d", order)]
+        weighted = (k // 2) % 2 == 1
+        return {"model": "domino", "tmax": tmax, "tmin": tmin, "seed": k, "stream": k & 0xFFFF,
+                "rule": "cftp_twoperiodic" if weighted else "cftp", "a": 1.0,
+                "b": float(rng.uniform(*BATCH_B)) if weighted else 1.0, "first_steps": BATCH_FIRST,
+                "max_attempts": BATCH_ATTEMPTS}
+    side = draw(*BATCH_SIDES)
+    if ("l", side) not in cache:
+        d = L.Hexagon(side)
+        cache[("l", side)] = (L.MaxTiling(d), L.MinTiling(d))
+    tmax, tmin = cache[("l", side)]
+    return {"model": "lozenge", "tmax": tmax, "tmin": tmin, "seed": k, "stream": k & 0xFFFF,
+            "first_steps": BATCH_FIRST, "max_attempts": BATCH_ATTEMPTS}
+
+
+def _plain_cftp(rt, job):
+    """The one-at-a-time path: rt_domino_cftp / rt_lozenge_cftp on one instance, fast mode."""
+    tiler = (rt.DominoTiler(rule=job["rule"], rng="fast", a=job["a"], b=job["b"], fast_stream=job["stream"])
+             if job["model"] == "domino" else rt.LozengeTiler(rng="fast", fast_stream=job["stream"]))
+    try:
+        out, _ = tiler.cftp(job["tmax"], job["tmin"], job["seed"], first_steps=job["first_steps"], schedule=1,
+                            max_attempts=job["max_attempts"])
+        return out
+    except rt.RTError as e:
+        if e.status != rt.RT_ERR_NOT_COALESCED:
+            raise
+        return None
+
+
+def batched_leg(rt) -> dict:
+    """Batched fast-mode CFTP (rt_cftp_batch) on the mix above, against the same kind of
+    instances run one at a time through the plain entry points (PLAIN_SAMPLES instances drawn
+    across the mix).  Samples/s count coalesced instances; every batched sample equals the
+    plain result of its instance (tests/test_batch_cftp.py)."""
     rng = np.random.default_rng(20261203)
-    cache, jobs = {}, []
-    for k in range(BATCH_INSTANCES):
-        if k % 2 == 0:
-            order = int(rng.integers(BATCH_ORDERS[0], BATCH_ORDERS[1] + 1))
-            if ("d", order) not in cache:
-                d = D.AztecDiamond(order)
-                cache[("d", order)] = (D.MaxTiling(d), D.MinTiling(d))
-            tmax, tmin = cache[("d", order)]
-            weighted = (k // 2) % 2 == 1
-            jobs.append({"model": "domino", "tmax": tmax, "tmin": tmin, "seed": k, "stream": k,
-                         "rule": "cftp_twoperiodic" if weighted else "cftp", "a": 1.0,
-                         "b": float(rng.uniform(*BATCH_B)) if weighted else 1.0, "first_steps": BATCH_FIRST,
-                         "max_attempts": BATCH_ATTEMPTS})
-        else:
-            side = int(rng.integers(BATCH_SIDES[0], BATCH_SIDES[1] + 1))
-            if ("l", side) not in cache:
-                d = L.Hexagon(side)
-                cache[("l", side)] = (L.MaxTiling(d), L.MinTiling(d))
-            tmax, tmin = cache[("l", side)]
-            jobs.append({"model": "lozenge", "tmax": tmax, "tmin": tmin, "seed": k, "stream": k,
-                         "first_steps": BATCH_FIRST, "max_attempts": BATCH_ATTEMPTS})
+    cache = {}
+    jobs = [_batch_job(rt, cache, rng, k) for k in range(BATCH_INSTANCES)]
     rt.cftp_batch(jobs[:64])  # warm-up
     t0 = time.perf_counter()
     outs, attempts, stats = rt.cftp_batch(jobs)
     wall = time.perf_counter() - t0
-    lat = []
-    for job in jobs[:plain_samples]:
-        tiler = (rt.DominoTiler(rule=job["rule"], rng="fast", a=job["a"], b=job["b"], fast_stream=job["stream"])
-                 if job["model"] == "domino" else rt.LozengeTiler(rng="fast", fast_stream=job["stream"]))
+    pick = np.random.default_rng(7).choice(len(jobs), size=PLAIN_SAMPLES, replace=False)
+    lat, same = [], 0
+    for k in pick:
         t1 = time.perf_counter()
-        try:
-            tiler.cftp(job["tmax"], job["tmin"], job["seed"], first_steps=job["first_steps"], schedule=1,
-                       max_attempts=BATCH_ATTEMPTS)
-        except rt.RTError as e:
-            if e.status != rt.RT_ERR_NOT_COALESCED:
-                raise
+        out = _plain_cftp(rt, jobs[k])
         lat.append(time.perf_counter() - t1)
+        same += out is not None and attempts[k] > 0 and np.array_equal(out, outs[k])
     lat = np.array(lat)
     plain_rate = 1.0 / lat.mean()
-    return {"workload": f"{BATCH_INSTANCES} CFTP instances: Aztec orders U{list(BATCH_ORDERS)} and hexagon sides "
-                        f"U{list(BATCH_SIDES)}, half of the diamonds 2-periodic (a=1, b~U{list(BATCH_B)}), "
-                        f"seeds and streams 0..{BATCH_INSTANCES - 1}, look-back {BATCH_FIRST} sweeps doubling, "
-                        f"at most {BATCH_ATTEMPTS} attempts",
+    return {"workload": f"{BATCH_INSTANCES} CFTP instances (config 4's count and mix, sizes truncated): Aztec orders "
+                        f"U{list(BATCH_ORDERS)} and hexagon sides U{list(BATCH_SIDES)}, half of the diamonds 2-periodic "
+                        f"(a=1, b~U{list(BATCH_B)}), seeds and streams k, look-back {BATCH_FIRST} sweeps doubling, at "
+                        f"most {BATCH_ATTEMPTS} attempts",
             "samples_per_s": stats["coalesced"] / wall, "coalesced": stats["coalesced"], "kernel_s": stats["seconds"],
             "wall_s": wall, "ctas": stats["ctas"],
-            "plain_samples_per_s": plain_rate, "plain_sampled_instances": plain_samples,
+            "plain_samples_per_s": plain_rate, "plain_sampled_instances": PLAIN_SAMPLES,
+            "plain_equal_to_batched": int(same),
             "plain_latency_p50_s": float(np.percentile(lat, 50)), "plain_latency_p99_s": float(np.percentile(lat, 99)),
             "batched_over_plain": (stats["coalesced"] / wall) / plain_rate,
             "api": "rt_cftp_batch vs rt_domino_cftp / rt_lozenge_cftp, fast RNG mode, identical samples"}
 
 
-SERVE_RATE, SERVE_SECONDS = 2000.0, 5.0
+SERVE_RATES = (2000.0, 8000.0, 32000.0)  # offered Poisson arrival rates, per second
+SERVE_SECONDS = 3.0                       # per rate
 
 
 def serving_leg(rt) -> dict:
-    """Continuous-batching server under a Poisson request stream (mean SERVE_RATE / s for
-    SERVE_SECONDS): models domino / lozenge alternately, sizes log-uniform in the batched
-    leg's ranges, weights as there.  Latency = completion time - arrival time."""
-    D, L = rt.DominoTiler, rt.LozengeTiler
+    """Continuous-batching server under Poisson request streams at increasing offered rates
+    (SERVE_RATES, SERVE_SECONDS each): requests alternate domino / lozenge, sizes log-uniform
+    in the batched leg's ranges, weights as there.  Latency = completion time - arrival time;
+    samples/s = completions / (time until the last completes).  Where the achieved rate stops
+    following the offered one the server is saturated: that rate is its capacity."""
     rng = np.random.default_rng(20261203)
     cache = {}
-
-    def request(k):
-        if k % 2 == 0:
-            order = int(np.exp(rng.uniform(np.log(BATCH_ORDERS[0]), np.log(BATCH_ORDERS[1] + 1))))
-            if ("d", order) not in cache:
-                d = D.AztecDiamond(order)
-                cache[("d", order)] = (D.MaxTiling(d), D.MinTiling(d))
-            tmax, tmin = cache[("d", order)]
-            w = (k // 2) % 2 == 1
-            return {"model": "domino", "tmax": tmax, "tmin": tmin, "seed": k, "stream": k & 0xFFFF,
-                    "rule": "cftp_twoperiodic" if w else "cftp", "a": 1.0,
-                    "b": float(rng.uniform(*BATCH_B)) if w else 1.0, "first_steps": BATCH_FIRST,
-                    "max_attempts": BATCH_ATTEMPTS}
-        side = int(np.exp(rng.uniform(np.log(BATCH_SIDES[0]), np.log(BATCH_SIDES[1] + 1))))
-        if ("l", side) not in cache:
-            d = L.Hexagon(side)
-            cache[("l", side)] = (L.MaxTiling(d), L.MinTiling(d))
-        tmax, tmin = cache[("l", side)]
-        return {"model": "lozenge", "tmax": tmax, "tmin": tmin, "seed": k, "stream": k & 0xFFFF,
-                "first_steps": BATCH_FIRST, "max_attempts": BATCH_ATTEMPTS}
-
-    arrivals = np.cumsum(rng.exponential(1.0 / SERVE_RATE, size=int(SERVE_RATE * SERVE_SECONDS * 1.2)))
-    arrivals = arrivals[arrivals < SERVE_SECONDS]
-    reqs = [request(k) for k in range(len(arrivals))]
     srv = rt.Server(slots=1 << 16, max_side=max(2 * BATCH_ORDERS[1] + 6, 3 * ((2 * BATCH_SIDES[1] + 9) // 3 + 1)),
                     memory_budget_bytes=120 << 30, idle_seconds=0.5)
-    srv.wait(srv.submit(reqs[0]))  # warm-up
-    pending, lat, served = {}, [], 0
-    t0 = time.perf_counter()
-    k = 0
-    while k < len(reqs) or pending:
-        now = time.perf_counter() - t0
-        while k < len(reqs) and arrivals[k] <= now:
-            pending[srv.submit(reqs[k])] = arrivals[k]
-            k += 1
-        for t in list(pending):
-            if srv.poll(t):
-                srv.wait(t)
-                lat.append(time.perf_counter() - t0 - pending.pop(t))
-                served += 1
-    wall = time.perf_counter() - t0
-    srv.close()
-    lat = np.array(lat)
-    return {"workload": f"Poisson arrivals, mean {SERVE_RATE:.0f}/s for {SERVE_SECONDS:.0f} s ({len(reqs)} requests): "
+    levels = []
+    try:
+        srv.wait(srv.submit(_batch_job(rt, cache, rng, 0, True)))  # warm-up
+        base = 1
+        for rate in SERVE_RATES:
+            arrivals = np.cumsum(rng.exponential(1.0 / rate, size=int(rate * SERVE_SECONDS * 1.2) + 16))
+            arrivals = arrivals[arrivals < SERVE_SECONDS]
+            reqs = [_batch_job(rt, cache, rng, base + k, True) for k in range(len(arrivals))]
+            base += len(reqs)
+            order, lat = [], []
+            t0 = time.perf_counter()
+            k = 0
+            head = 0  # oldest request not yet collected
+            done = np.zeros(len(reqs), bool)
+            tickets = [0] * len(reqs)
+            submit_s = 0.0
+            while k < len(reqs) or head < len(reqs):
+                now = time.perf_counter() - t0
+                while k < len(reqs) and arrivals[k] <= now:
+                    ts = time.perf_counter()
+                    tickets[k] = srv.submit(reqs[k])
+                    submit_s += time.perf_counter() - ts
+                    k += 1
+                # collect finished requests among the oldest outstanding ones
+                for q in range(head, min(k, head + 512)):
+                    if not done[q] and srv.poll(tickets[q]):
+                        srv.wait(tickets[q])
+                        done[q] = True
+                        lat.append(time.perf_counter() - t0 - arrivals[q])
+                while head < k and done[head]:
+                    head += 1
+            wall = time.perf_counter() - t0
+            lat = np.array(lat)
+            levels.append({"offered_per_s": rate, "requests": len(reqs), "achieved_per_s": len(reqs) / wall,
+                           "latency_p50_s": float(np.percentile(lat, 50)), "latency_p99_s": float(np.percentile(lat, 99)),
+                           "client_submit_us": 1e6 * submit_s / max(1, len(reqs))})
+    finally:
+        srv.close()
+    capacity = max(x["achieved_per_s"] for x in levels)
+    saturated = [x["offered_per_s"] for x in levels if x["achieved_per_s"] < 0.9 * x["offered_per_s"]]
+    return {"workload": f"Poisson arrivals at {', '.join(f'{r:.0f}' for r in SERVE_RATES)}/s, {SERVE_SECONDS:.0f} s each: "
                         f"Aztec orders log-U{list(BATCH_ORDERS)} (half 2-periodic, b~U{list(BATCH_B)}) and hexagon "
-                        f"sides log-U{list(BATCH_SIDES)}",
-            "samples_per_s": served / wall, "latency_p50_s": float(np.percentile(lat, 50)),
-            "latency_p99_s": float(np.percentile(lat, 99)), "requests": len(reqs),
+                        f"sides log-U{list(BATCH_SIDES)}; config 5's 60 s at log-U[16,512] truncated as the batched leg",
+            "levels": levels, "capacity_samples_per_s": capacity,
+            "saturated_at_offered_per_s": saturated[0] if saturated else None,
+            "samples_per_s": levels[0]["achieved_per_s"], "latency_p50_s": levels[0]["latency_p50_s"],
+            "latency_p99_s": levels[0]["latency_p99_s"],
             "api": "rt_server_submit / rt_server_poll / rt_server_wait (continuous batching)"}
 
 
