@@ -271,17 +271,21 @@ def batched_leg(rt) -> dict:
 
 SERVE_RATES = (2000.0, 8000.0, 32000.0)  # offered Poisson arrival rates, per second
 SERVE_SECONDS = 3.0                       # per rate
+SERVE_SLOTS = 16384                       # ring slots: requests admitted and not yet collected
+SERVE_POLL_WINDOW = 4096                  # oldest outstanding requests polled per client loop
 
 
 def serving_leg(rt) -> dict:
     """Continuous-batching server under Poisson request streams at increasing offered rates
     (SERVE_RATES, SERVE_SECONDS each): requests alternate domino / lozenge, sizes log-uniform
     in the batched leg's ranges, weights as there.  Latency = completion time - arrival time;
-    samples/s = completions / (time until the last completes).  Where the achieved rate stops
-    following the offered one the server is saturated: that rate is its capacity."""
+    samples/s = completions / (time until the last completes).  A request that finds every
+    slot holding an uncollected one is refused (RT_ERR_BUSY) and counted as rejected.  Where
+    the achieved rate stops following the offered one the server is saturated: that rate is
+    its capacity."""
     rng = np.random.default_rng(20261203)
     cache = {}
-    srv = rt.Server(slots=1 << 16, max_side=max(2 * BATCH_ORDERS[1] + 6, 3 * ((2 * BATCH_SIDES[1] + 9) // 3 + 1)),
+    srv = rt.Server(slots=SERVE_SLOTS, max_side=max(2 * BATCH_ORDERS[1] + 6, 3 * ((2 * BATCH_SIDES[1] + 9) // 3 + 1)),
                     memory_budget_bytes=120 << 30, idle_seconds=0.5)
     levels = []
     try:
@@ -292,31 +296,38 @@ def serving_leg(rt) -> dict:
             arrivals = arrivals[arrivals < SERVE_SECONDS]
             reqs = [_batch_job(rt, cache, rng, base + k, True) for k in range(len(arrivals))]
             base += len(reqs)
-            order, lat = [], []
+            lat, rejected = [], 0
+            tickets = [0] * len(reqs)
+            outstanding = []  # submitted, not yet collected, oldest first
+            submit_s = 0.0
             t0 = time.perf_counter()
             k = 0
-            head = 0  # oldest request not yet collected
-            done = np.zeros(len(reqs), bool)
-            tickets = [0] * len(reqs)
-            submit_s = 0.0
-            while k < len(reqs) or head < len(reqs):
+            while k < len(reqs) or outstanding:
                 now = time.perf_counter() - t0
                 while k < len(reqs) and arrivals[k] <= now:
                     ts = time.perf_counter()
-                    tickets[k] = srv.submit(reqs[k])
+                    try:
+                        tickets[k] = srv.submit(reqs[k])
+                        outstanding.append(k)
+                    except rt.RTError as e:  # admission refused: every slot holds an uncollected request
+                        if e.status != rt.RT_ERR_BUSY:
+                            raise
+                        rejected += 1
                     submit_s += time.perf_counter() - ts
                     k += 1
-                # collect finished requests among the oldest outstanding ones
-                for q in range(head, min(k, head + 512)):
-                    if not done[q] and srv.poll(tickets[q]):
+                # collect the finished ones among the oldest SERVE_POLL_WINDOW outstanding requests
+                keep = []
+                for q in outstanding[:SERVE_POLL_WINDOW]:
+                    if srv.poll(tickets[q]):
                         srv.wait(tickets[q])
-                        done[q] = True
                         lat.append(time.perf_counter() - t0 - arrivals[q])
-                while head < k and done[head]:
-                    head += 1
+                    else:
+                        keep.append(q)
+                outstanding = keep + outstanding[SERVE_POLL_WINDOW:]
             wall = time.perf_counter() - t0
             lat = np.array(lat)
-            levels.append({"offered_per_s": rate, "requests": len(reqs), "achieved_per_s": len(reqs) / wall,
+            levels.append({"offered_per_s": rate, "requests": len(reqs), "served": int(len(lat)), "rejected": rejected,
+                           "achieved_per_s": len(lat) / wall, "seconds": wall,
                            "latency_p50_s": float(np.percentile(lat, 50)), "latency_p99_s": float(np.percentile(lat, 99)),
                            "client_submit_us": 1e6 * submit_s / max(1, len(reqs))})
     finally:

@@ -354,14 +354,19 @@ typedef struct rt_cftp_instance {
 
 typedef struct rt_batch_stats {
   int32_t instances, coalesced, ctas, pad;
-  double seconds;       /* device time of the batch kernel */
+  double seconds;             /* device time of the batch kernels (and of the one-at-a-time runs) */
+  int32_t cluster_instances;  /* instances held by a thread-block cluster */
+  int32_t single_instances;   /* instances run one at a time through the single-instance path */
 } rt_batch_stats;
 
 /* Runs every instance; RT_ERR_NOT_COALESCED if any instance ran out of attempts (its out
    and attempts are still written).  Instances whose two chains fit one CTA's shared memory
    (about 2 x N^2 bytes: N up to about 330 for dominoes, 340 for lozenges) run in the
-   persistent kernel; larger ones run after it, one at a time, through rt_domino_cftp /
-   rt_lozenge_cftp on the same stream (same samples); stats->seconds adds both. */
+   persistent one-CTA kernel; larger ones in a cluster kernel, each instance held by a
+   thread-block cluster of 2-16 CTAs exchanging its halo rows through distributed shared
+   memory (N up to about 1300); any larger instance runs
+   after them, one at a time, through rt_domino_cftp / rt_lozenge_cftp on the same stream.
+   All three give the same samples for the same (seed, stream). */
 RT_API rt_status rt_cftp_batch(rt_cftp_instance* inst, int32_t count, void* cuda_stream, rt_batch_stats* stats);
 
 /* ---- model-generic entry points ------------------------------------------------------------

@@ -83,7 +83,7 @@ class CftpInstance(C.Structure):
 
 class BatchStats(C.Structure):
     _fields_ = [("instances", C.c_int32), ("coalesced", C.c_int32), ("ctas", C.c_int32), ("pad", C.c_int32),
-                ("seconds", C.c_double)]
+                ("seconds", C.c_double), ("cluster_instances", C.c_int32), ("single_instances", C.c_int32)]
 
 
 class ServerOpts(C.Structure):

@@ -21,6 +21,7 @@
 #include <thread>
 #include <vector>
 
+#include "batch_cftp.cuh"
 #include "domino_rules.h"
 #include "rng.cuh"
 #include "rt_internal.h"
@@ -36,21 +37,6 @@ constexpr int kBatchThreads = 256;
     if (_e != cudaSuccess)                                                              \
       return fail(RT_ERR_CUDA, std::string(#expr) + ": " + cudaGetErrorString(_e));     \
   } while (0)
-
-// One instance as the kernel sees it.  Colour arrays are N rows x P bytes (P a multiple of
-// 16), ncol of them per chain (2 dominoes, 3 lozenges); tmax / tmin / out point at ncol
-// consecutive arrays in global memory.
-struct DevInstance {
-  int32_t model, N, P, cols;  // cols: last site column + 1 of the colour arrays (N/2 - 1 or N/3)
-  uint64_t seed;
-  uint32_t stream;
-  int32_t max_attempts;
-  int64_t first_sweeps;
-  int64_t off_max, off_min, off_out;  // byte offsets into the tiling buffer
-  uint32_t lo_up[4], w_up[4], lo_dn[4], w_dn[4];  // domino rule intervals (fast scale)
-  int32_t attempts;                                // outputs
-  int64_t final_half_sweeps;
-};
 
 // Per-instance state of a batched launch, in which an instance's attempts are separate work
 // items: the CTA that takes an instance from the queue runs its attempts in order, and CTAs
@@ -75,147 +61,24 @@ struct BatchArgs {
   long max_spin;       // bound of that wait, and of a helper's rounds without work
 };
 
-__device__ __forceinline__ uint32_t block_sum(uint32_t v, uint32_t* red) {
-  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
-  __syncthreads();
-  if (threadIdx.x < 32) {
-    v = threadIdx.x < kBatchThreads / 32 ? red[threadIdx.x] : 0;
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-    if (threadIdx.x == 0) red[0] = v;
-  }
-  __syncthreads();
-  const uint32_t r = red[0];
-  __syncthreads();
-  return r;
-}
-
-__device__ __forceinline__ uint8_t dm_flip_b(uint32_t e, uint32_t u, uint32_t lo_up, uint32_t w_up, uint32_t lo_dn,
-                                             uint32_t w_dn) {
-  if (e == 3u) return (u - lo_up) < w_up ? 12 : 3;
-  if (e == 12u) return (u - lo_dn) < w_dn ? 3 : 12;
-  return (uint8_t)e;
-}
-
-// One domino half-sweep of colour t on both chains held in shared memory (chain c, colour
-// k at sm + (c * 2 + k) * N * P): flips with the fast draws of half-sweep h, then the full
-// rebuild of the passive colour (dominokernel.cl:22-31 semantics).  Every thread of the CTA
-// takes (row, column quad) units, one 32-bit word per chain, so that small instances keep
-// all threads busy; the rebuild writes four passive sites per word from whole words of the
-// active rows (funnel shifts for the one-column offsets) and keeps the columns outside
-// [1, cols].
+// One domino half-sweep of colour t on both chains of an instance held whole in shared
+// memory (chain c, colour k at sm + (c * 2 + k) * N * P): flips on rows [1, N-1), then the
+// rebuild of the passive colour.
 __device__ void domino_half_sweep(uint8_t* sm, const DevInstance& in, int t, int64_t h) {
-  const int N = in.N, P = in.P, cols = in.cols - 1;  // sites m in [1, cols]
-  const size_t plane = (size_t)N * P;
-  const int words = P / 4, quads = cols / 4 + 1;
-  for (int k = threadIdx.x; k < (N - 2) * quads; k += kBatchThreads) {
-    const int i = 1 + k / quads, q = k - (i - 1) * quads;
-    const int c = (i & 1) | (t << 1);
-    const uint32_t lo_up = in.lo_up[c], w_up = in.w_up[c], lo_dn = in.lo_dn[c], w_dn = in.w_dn[c];
-    const uint4 r = fast_quad(in.seed, in.stream, h, (uint32_t)i, (uint32_t)q);
-    const uint32_t rr[4] = {r.x, r.y, r.z, r.w};
-    for (int ch = 0; ch < 2; ++ch) {
-      uint32_t* word = reinterpret_cast<uint32_t*>(sm + (size_t)(ch * 2 + t) * plane + (size_t)i * P) + q;
-      const uint32_t e4 = *word;
-      uint32_t n4 = e4;
-#pragma unroll
-      for (int k4 = 0; k4 < 4; ++k4) {
-        const int m = 4 * q + k4;
-        if (m < 1 || m > cols) continue;
-        const uint32_t e = (e4 >> (8 * k4)) & 0xffu;
-        n4 ^= (e ^ dm_flip_b(e, rr[k4], lo_up, w_up, lo_dn, w_dn)) << (8 * k4);
-      }
-      if (n4 != e4) *word = n4;
-    }
-  }
+  const RowView v{sm, (size_t)in.N * in.P, 0};
+  dm_flip_rows<kBatchThreads>(v, in, t, h, 1, in.N - 1, nullptr, -1, nullptr, -1);
   __syncthreads();
-  for (int k = threadIdx.x; k < 2 * (N - 2) * words; k += kBatchThreads) {
-    const int rc = k / words, w = k - rc * words;
-    const int ch = rc & 1, i = 1 + (rc >> 1);
-    uint32_t keep = 0;  // columns outside [1, cols] keep their value
-#pragma unroll
-    for (int k4 = 0; k4 < 4; ++k4) {
-      const int m = 4 * w + k4;
-      if (m < 1 || m > cols) keep |= 0xffu << (8 * k4);
-    }
-    if (keep == 0xffffffffu) continue;
-    const uint32_t* A = reinterpret_cast<const uint32_t*>(sm + (size_t)(ch * 2 + t) * plane + (size_t)i * P);
-    uint32_t* Pw = reinterpret_cast<uint32_t*>(sm + (size_t)(ch * 2 + 1 - t) * plane + (size_t)i * P) + w;
-    const uint32_t cur = A[w], up = A[w - words], dn = A[w + words];
-    uint32_t left, right;  // active neighbours at columns m, m+1 when i + t is odd, else m-1, m
-    if ((i + t) & 1) {
-      left = cur;
-      right = __funnelshift_r(cur, w + 1 < words ? A[w + 1] : 0u, 8);
-    } else {
-      left = __funnelshift_l(w > 0 ? A[w - 1] : 0u, cur, 8);
-      right = cur;
-    }
-    const uint32_t val = ((up >> 1) & 0x01010101u) | ((dn & 0x01010101u) << 1) | ((left & 0x08080808u) >> 1) |
-                         ((right & 0x04040404u) << 1);
-    *Pw = (val & ~keep) | (*Pw & keep);
-  }
+  dm_rebuild_rows<kBatchThreads>(v, in, t, 1, in.N - 1);
   __syncthreads();
 }
 
 // One lozenge step of colour r on both chains (chain c, colour k at sm + (c * 3 + k) * N * P):
-// rotation 25 <-> 38 with the fast draws of step h, then the rebuild of the two other colours
-// (lozengekernel.cl:107-125 semantics).
+// rotation on every row, then the rebuild of the two other colours on rows [1, N-1).
 __device__ void lozenge_step(uint8_t* sm, const DevInstance& in, int r, int64_t h, uint32_t c4, uint32_t c8) {
-  const int N = in.N, P = in.P, M = in.cols;
-  const size_t plane = (size_t)N * P;
-  const int words = P / 4, quads = (M + 3) / 4;
-  // Rotation: (row, column quad) units over every thread, one word per chain.
-  for (int k = threadIdx.x; k < N * quads; k += kBatchThreads) {
-    const int i = k / quads, q = k - i * quads;
-    const uint4 d = fast_quad(in.seed, in.stream, h, (uint32_t)i, (uint32_t)q);
-    const uint32_t uu[4] = {d.x, d.y, d.z, d.w};
-    for (int ch = 0; ch < 2; ++ch) {
-      uint32_t* word = reinterpret_cast<uint32_t*>(sm + (size_t)(ch * 3 + r) * plane + (size_t)i * P) + q;
-      const uint32_t e4 = *word;
-      uint32_t n4 = e4;
-#pragma unroll
-      for (int k4 = 0; k4 < 4; ++k4) {
-        if (4 * q + k4 >= M) break;
-        const uint32_t e = (e4 >> (8 * k4)) & 0xffu;
-        uint32_t n = e;
-        if (e == 25u && uu[k4] < c4) n = 38;
-        else if (e == 38u && uu[k4] >= c4 && uu[k4] < c8) n = 25;
-        n4 ^= (e ^ n) << (8 * k4);
-      }
-      if (n4 != e4) *word = n4;
-    }
-  }
+  const RowView v{sm, (size_t)in.N * in.P, 0};
+  lz_rotate_rows<kBatchThreads>(v, in, r, h, c4, c8, 0, in.N, nullptr, -1, nullptr, -1);
   __syncthreads();
-  // Rebuild: (chain, row, word of four vertices) units over every thread.
-  for (int k = threadIdx.x; k < 2 * (N - 2) * words; k += kBatchThreads) {
-    const int rc = k / words, w = k - rc * words;
-    const int ch = rc & 1, i = 1 + (rc >> 1);
-    uint32_t keep = 0;  // columns outside [1, M-2] keep their value
-#pragma unroll
-    for (int k4 = 0; k4 < 4; ++k4) {
-      const int j = 4 * w + k4;
-      if (j < 1 || j > M - 2) keep |= 0xffu << (8 * k4);
-    }
-    if (keep == 0xffffffffu) continue;
-    const int im = i % 3;
-    const bool p2 = im == (2 * r + 1) % 3, p4 = im == (2 * r + 2) % 3, p8 = im == (2 * r) % 3;
-    const uint32_t* up = reinterpret_cast<const uint32_t*>(sm + (size_t)(ch * 3 + r) * plane + (size_t)(i - 1) * P);
-    const uint32_t* mid = up + words;
-    const uint32_t* dn = mid + words;
-    uint32_t* T2 = reinterpret_cast<uint32_t*>(sm + (size_t)(ch * 3 + (r + 1) % 3) * plane + (size_t)i * P) + w;
-    uint32_t* T3 = reinterpret_cast<uint32_t*>(sm + (size_t)(ch * 3 + (r + 2) % 3) * plane + (size_t)i * P) + w;
-    const uint32_t u0 = up[w], m0 = mid[w], d0 = dn[w];
-    const uint32_t u_r = __funnelshift_r(u0, w + 1 < words ? up[w + 1] : 0u, 8);
-    const uint32_t m_r = __funnelshift_r(m0, w + 1 < words ? mid[w + 1] : 0u, 8);
-    const uint32_t m_l = __funnelshift_l(w > 0 ? mid[w - 1] : 0u, m0, 8);
-    const uint32_t d_l = __funnelshift_l(w > 0 ? dn[w - 1] : 0u, d0, 8);
-    const uint32_t a2 = p2 ? u_r : u0, a4 = p4 ? m_l : m0, a8 = p8 ? m_r : m0, a16 = p2 ? d_l : d0;
-    const uint32_t b2 = ((a2 & 0x10101010u) >> 3) | ((a4 & 0x08080808u) >> 1) | ((d0 & 0x01010101u) << 5);
-    const uint32_t b3 = ((u0 & 0x20202020u) >> 5) | ((a8 & 0x04040404u) << 1) | ((a16 & 0x02020202u) << 3);
-    const uint32_t t2 = *T2, t3 = *T3;
-    *T2 = (((t2 & ~0x26262626u) | b2) & ~keep) | (t2 & keep);
-    *T3 = (((t3 & ~0x19191919u) | b3) & ~keep) | (t3 & keep);
-  }
+  lz_rebuild_rows<kBatchThreads>(v, in, r, 1, in.N - 1);
   __syncthreads();
 }
 
@@ -248,7 +111,7 @@ __device__ void run_instance(uint8_t* sm, const DevInstance& in, const uint8_t* 
     }
     uint32_t differ = 0;
     for (int w = threadIdx.x; w < words; w += kBatchThreads) differ += s32[w] != s32[words + w];
-    differ = block_sum(differ, red);
+    differ = block_sum<kBatchThreads>(differ, red);
     attempts = att + 1;
     done = differ == 0;
   }
@@ -292,7 +155,7 @@ __device__ int run_attempt(uint8_t* sm, const DevInstance& in, const InstState* 
   }
   uint32_t differ = 0;
   for (int w = threadIdx.x; w < words; w += kBatchThreads) differ += s32[w] != s32[words + w];
-  differ = block_sum(differ, red);
+  differ = block_sum<kBatchThreads>(differ, red);
   return differ == 0 ? 1 : 0;
 }
 
@@ -627,151 +490,135 @@ RT_API rt_status rt_cftp_batch(rt_cftp_instance* inst, int32_t count, void* cuda
   }
   BT_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
   BT_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
-  // Host side: validate every instance.  Instances whose two chains fit one CTA's shared
-  // memory go to the persistent kernel (colour-split, laid out in one buffer); the others run
-  // one by one through the single-instance entry points afterwards, which draw the same
-  // (seed, stream, half-sweep) keyed randomness and so return the same samples.
+  // Host side: validate every instance and sort it by where it runs.  Instances whose two
+  // chains fit one CTA's shared memory go to the one-CTA persistent kernel; larger ones to the
+  // cluster kernel, grouped by cluster size (one launch per size); instances too large for a
+  // 16-CTA cluster run one by one through the single-instance entry points.  All three draw
+  // the same (seed, stream, half-sweep) keyed randomness and so return the same samples.
   const size_t smem_limit = (size_t)optin - 1024;
-  std::vector<DevInstance> dv;
-  std::vector<int> small_idx, large_idx;
-  dv.reserve((size_t)count);
-  size_t bytes = 0, smem_max = 0;
+  std::vector<DevInstance> dv;  // packed instances: the one-CTA ones, then the groups in order
+  std::vector<int> packed_idx, large_idx, csize((size_t)count, 0);
+  std::vector<DevInstance> all((size_t)count);
+  size_t smem_max = 0;
+  int n_small = 0;
   for (int k = 0; k < count; ++k) {
     const rt_cftp_instance& x = inst[k];
-    if (!x.tmax || !x.tmin || !x.out) return fail(RT_ERR_INVALID_ARGUMENT, "cftp_batch: NULL tiling in instance");
-    if (x.first_steps < 1 || x.max_attempts < 1 || x.max_attempts > 40)
-      return fail(RT_ERR_INVALID_ARGUMENT, "cftp_batch: first_steps >= 1 and 1 <= max_attempts <= 40");
-    if (x.stream >= 65536u) return fail(RT_ERR_INVALID_ARGUMENT, "cftp_batch: stream must be < 65536");
-    DevInstance d;
-    std::memset(&d, 0, sizeof d);
-    d.model = x.model;
-    d.N = x.n_side;
-    if (x.model == RT_MODEL_DOMINO) {
-      if (x.n_side < 6 || x.n_side % 2) return fail(RT_ERR_INVALID_ARGUMENT, "cftp_batch: domino side must be even >= 6");
-      if (x.rule != RT_DOMINO_CFTP && x.rule != RT_DOMINO_CFTP_TWOPERIODIC)
-        return fail(RT_ERR_INVALID_ARGUMENT, "cftp_batch: domino instances need a monotone rule");
-      DmRule r;
-      const char* err = nullptr;
-      if (!dm_rule_build(x.rule, RT_RNG_FAST, x.weight_a, x.weight_b, &r, &err)) return fail(RT_ERR_INVALID_ARGUMENT, err);
-      std::memcpy(d.lo_up, r.lo_up, sizeof r.lo_up);
-      std::memcpy(d.w_up, r.w_up, sizeof r.w_up);
-      std::memcpy(d.lo_dn, r.lo_dn, sizeof r.lo_dn);
-      std::memcpy(d.w_dn, r.w_dn, sizeof r.w_dn);
-      d.cols = x.n_side / 2 - 1;
-      d.P = ((x.n_side / 2) + 15) / 16 * 16;
-    } else if (x.model == RT_MODEL_LOZENGE) {
-      if (x.n_side < 9 || x.n_side % 3) return fail(RT_ERR_INVALID_ARGUMENT, "cftp_batch: lozenge side must be a multiple of 3 >= 9");
-      d.cols = x.n_side / 3;
-      d.P = ((x.n_side / 3) + 15) / 16 * 16;
+    if (!x.out) return fail(RT_ERR_INVALID_ARGUMENT, "cftp_batch: NULL output in instance");
+    size_t chain = 0;
+    if (rt_status st = pack_instance(x, &all[(size_t)k], &chain)) return st;
+    if (2 * chain <= smem_limit) {
+      smem_max = std::max(smem_max, 2 * chain);
+      packed_idx.push_back(k);
+      ++n_small;
     } else {
-      return fail(RT_ERR_INVALID_ARGUMENT, "cftp_batch: model must be RT_MODEL_DOMINO or RT_MODEL_LOZENGE");
+      csize[(size_t)k] = cluster_size_for(all[(size_t)k], smem_limit);
+      if (csize[(size_t)k] == 0) large_idx.push_back(k);
     }
-    d.seed = x.seed;
-    d.stream = x.stream;
-    d.max_attempts = x.max_attempts;
-    d.first_sweeps = x.first_steps;
-    const int ncol = x.model == RT_MODEL_DOMINO ? 2 : 3;
-    const size_t chain = (size_t)ncol * d.N * d.P;
-    if (2 * chain > smem_limit) {
-      large_idx.push_back(k);
+  }
+  std::vector<ClusterGroup> groups;
+  for (int C = 2; C <= 16; ++C) {
+    ClusterGroup g;
+    g.C = C;
+    for (int k = 0; k < count; ++k)
+      if (csize[(size_t)k] == C) {
+        g.smem = std::max(g.smem, cluster_smem_bytes(all[(size_t)k], C));
+        g.members.push_back(k);
+      }
+    if (g.members.empty()) continue;
+    const int cap = cluster_capacity(C, g.smem);
+    if (cap < 1) {  // no such cluster fits the device: the single-instance path
+      large_idx.insert(large_idx.end(), g.members.begin(), g.members.end());
       continue;
     }
-    smem_max = std::max(smem_max, 2 * chain);
+    g.clusters = std::min((int)g.members.size(), cap);
+    packed_idx.insert(packed_idx.end(), g.members.begin(), g.members.end());
+    groups.push_back(g);
+  }
+  std::sort(large_idx.begin(), large_idx.end());
+  // one tiling buffer: per packed instance its max, min and output chains
+  size_t bytes = 0;
+  for (int k : packed_idx) {
+    DevInstance d = all[(size_t)k];
+    const size_t chain = (size_t)(d.model == RT_MODEL_DOMINO ? 2 : 3) * d.N * d.P;
     d.off_max = (int64_t)bytes;
     d.off_min = (int64_t)(bytes + chain);
     d.off_out = (int64_t)(bytes + 2 * chain);
     bytes += 3 * chain;
     dv.push_back(d);
-    small_idx.push_back(k);
+  }
+  std::vector<uint8_t> host(bytes, 0);
+  for (size_t s = 0; s < dv.size(); ++s) {
+    const rt_cftp_instance& x = inst[packed_idx[s]];
+    if (rt_status st = split_into(x.tmax, dv[s], host.data() + dv[s].off_max)) return st;
+    if (rt_status st = split_into(x.tmin, dv[s], host.data() + dv[s].off_min)) return st;
   }
   for (int k : large_idx)
     for (const int32_t* t : {inst[k].tmax, inst[k].tmin})
       for (size_t v = 0; v < (size_t)inst[k].n_side * inst[k].n_side; ++v)
         if ((uint32_t)t[v] > 63u) return fail(RT_ERR_INVALID_ARGUMENT, "cftp_batch: tiling values out of range");
-  const int n_small = (int)small_idx.size();
-  std::vector<uint8_t> host(bytes, 0);
-  for (int s = 0; s < n_small; ++s) {
-    const rt_cftp_instance& x = inst[small_idx[s]];
-    const DevInstance& d = dv[s];
-    const int N = d.N, ncol = d.model == RT_MODEL_DOMINO ? 2 : 3;
-    const size_t plane = (size_t)N * d.P;
-    for (int which = 0; which < 2; ++which) {
-      const int32_t* t = which == 0 ? x.tmax : x.tmin;
-      uint8_t* dst = host.data() + (which == 0 ? d.off_max : d.off_min);
-      for (int i = 0; i < N; ++i)
-        for (int j = 0; j < N; ++j) {
-          const int32_t v = t[(size_t)i * N + j];
-          if ((uint32_t)v > 63u) return fail(RT_ERR_INVALID_ARGUMENT, "cftp_batch: tiling values out of range");
-          int c, col;
-          if (ncol == 2) {
-            c = ((i + j) & 1) == 0 ? 1 : 0;  // black (t = 1) at even i + j
-            col = j / 2;
-          } else {
-            c = ((j - i) % 3 + 3) % 3;
-            col = j / 3;
-          }
-          dst[(size_t)c * plane + (size_t)i * d.P + col] = (uint8_t)v;
-        }
-    }
-  }
   cudaStream_t stream = (cudaStream_t)cuda_stream;
+  const int n_packed = (int)dv.size();
+  const int nq = 3 + (int)groups.size();  // [queue, finished, error, one queue per cluster group]
   uint8_t* d_tilings = nullptr;
   DevInstance* d_inst = nullptr;
-  unsigned* d_queue = nullptr;  // [queue counter, finished instances, error word]
+  unsigned* d_queue = nullptr;
   InstState* d_state = nullptr;
-  auto cleanup = [&]() {
-    if (d_tilings) cudaFree(d_tilings);
-    if (d_inst) cudaFree(d_inst);
-    if (d_queue) cudaFree(d_queue);
-    if (d_state) cudaFree(d_state);
-  };
   cudaEvent_t e0 = nullptr, e1 = nullptr;
   rt_status status = RT_OK;
   int coalesced = 0, grid = 0;
   double seconds = 0.0;
   do {
-    if (n_small == 0) break;
-    if (cudaMalloc(&d_tilings, bytes) != cudaSuccess || cudaMalloc(&d_inst, dv.size() * sizeof(DevInstance)) != cudaSuccess ||
-        cudaMalloc(&d_queue, 3 * sizeof(unsigned)) != cudaSuccess ||
-        cudaMalloc(&d_state, (size_t)n_small * sizeof(InstState)) != cudaSuccess) {
-      cudaGetLastError();
-      status = fail(RT_ERR_OUT_OF_MEMORY, "cftp_batch: device allocation failed");
+    if (n_packed == 0) break;
+    if ((status = dev_alloc(&d_tilings, bytes, stream)) != RT_OK ||
+        (status = dev_alloc(&d_inst, dv.size() * sizeof(DevInstance), stream)) != RT_OK ||
+        (status = dev_alloc(&d_queue, nq * sizeof(unsigned), stream)) != RT_OK ||
+        (status = dev_alloc(&d_state, (size_t)std::max(1, n_small) * sizeof(InstState), stream)) != RT_OK)
       break;
-    }
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
     cudaMemcpyAsync(d_tilings, host.data(), bytes, cudaMemcpyHostToDevice, stream);
     cudaMemcpyAsync(d_inst, dv.data(), dv.size() * sizeof(DevInstance), cudaMemcpyHostToDevice, stream);
-    cudaMemsetAsync(d_queue, 0, 3 * sizeof(unsigned), stream);
-    std::vector<InstState> st0((size_t)n_small);
+    cudaMemsetAsync(d_queue, 0, nq * sizeof(unsigned), stream);
+    std::vector<InstState> st0((size_t)std::max(1, n_small));
     for (InstState& x : st0) {
       std::memset(&x, 0, sizeof x);
       x.best = kNoAttempt;
     }
     cudaMemcpyAsync(d_state, st0.data(), st0.size() * sizeof(InstState), cudaMemcpyHostToDevice, stream);
-    cudaFuncSetAttribute(k_batch_cftp, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_max);
-    int per_sm = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batch_cftp, kBatchThreads, smem_max);
-    grid = std::max(1, std::min(n_small, std::max(1, per_sm) * sms));
     const uint32_t c4 = (uint32_t)std::ceil(0.4 * 4294967296.0), c8 = (uint32_t)std::ceil(0.8 * 4294967296.0);
-    BatchArgs ba{d_inst, d_state, n_small, d_tilings, d_queue, d_queue + 1, reinterpret_cast<int*>(d_queue + 2), 1L << 24};
     cudaEventRecord(e0, stream);
-    k_batch_cftp<<<grid, kBatchThreads, smem_max, stream>>>(ba, c4, c8);
-    cudaEventRecord(e1, stream);
-    cudaError_t le = cudaGetLastError();
-    if (le != cudaSuccess) {
-      status = fail(RT_ERR_CUDA, std::string("cftp_batch launch: ") + cudaGetErrorString(le));
-      break;
+    if (n_small > 0) {
+      cudaFuncSetAttribute(k_batch_cftp, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_max);
+      int per_sm = 0;
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batch_cftp, kBatchThreads, smem_max);
+      grid = std::max(1, std::min(n_small, std::max(1, per_sm) * sms));
+      BatchArgs ba{d_inst, d_state, n_small, d_tilings, d_queue, d_queue + 1, reinterpret_cast<int*>(d_queue + 2),
+                   1L << 24};
+      k_batch_cftp<<<grid, kBatchThreads, smem_max, stream>>>(ba, c4, c8);
+      cudaError_t le = cudaGetLastError();
+      if (le != cudaSuccess) {
+        status = fail(RT_ERR_CUDA, std::string("cftp_batch launch: ") + cudaGetErrorString(le));
+        break;
+      }
     }
+    int first = n_small;
+    for (size_t gi = 0; gi < groups.size() && status == RT_OK; ++gi) {
+      const int n = (int)groups[gi].members.size();
+      status = launch_cluster_group(groups[gi], d_inst + first, n, d_tilings, d_queue + 3 + gi, c4, c8, stream);
+      grid += groups[gi].C * groups[gi].clusters;
+      first += n;
+    }
+    if (status != RT_OK) break;
+    cudaEventRecord(e1, stream);
     cudaMemcpyAsync(host.data(), d_tilings, bytes, cudaMemcpyDeviceToHost, stream);
     cudaMemcpyAsync(dv.data(), d_inst, dv.size() * sizeof(DevInstance), cudaMemcpyDeviceToHost, stream);
+    unsigned err_word = 0;
+    cudaMemcpyAsync(&err_word, d_queue + 2, sizeof err_word, cudaMemcpyDeviceToHost, stream);
     cudaError_t se = cudaStreamSynchronize(stream);
     if (se != cudaSuccess) {
       status = fail(RT_ERR_CUDA, std::string("cftp_batch: ") + cudaGetErrorString(se));
       break;
     }
-    unsigned err_word = 0;
-    cudaMemcpy(&err_word, d_queue + 2, sizeof err_word, cudaMemcpyDeviceToHost);
     if (err_word) {
       status = fail(RT_ERR_TIMEOUT, "cftp_batch: a bounded wait for an instance's output lock gave up");
       break;
@@ -779,17 +626,10 @@ RT_API rt_status rt_cftp_batch(rt_cftp_instance* inst, int32_t count, void* cuda
     float ms = 0.f;
     cudaEventElapsedTime(&ms, e0, e1);
     seconds += ms * 1e-3;
-    for (int s = 0; s < n_small; ++s) {
-      rt_cftp_instance& x = inst[small_idx[s]];
+    for (int s = 0; s < n_packed; ++s) {
+      rt_cftp_instance& x = inst[packed_idx[s]];
       const DevInstance& d = dv[s];
-      const int N = d.N, ncol = d.model == RT_MODEL_DOMINO ? 2 : 3;
-      const size_t plane = (size_t)N * d.P;
-      const uint8_t* src = host.data() + d.off_out;
-      for (int i = 0; i < N; ++i)
-        for (int j = 0; j < N; ++j) {
-          const int c = ncol == 2 ? (((i + j) & 1) == 0 ? 1 : 0) : ((j - i) % 3 + 3) % 3;
-          x.out[(size_t)i * N + j] = src[(size_t)c * plane + (size_t)i * d.P + (ncol == 2 ? j / 2 : j / 3)];
-        }
+      merge_from(host.data() + d.off_out, d, x.out);
       x.attempts = d.attempts;
       x.final_steps = d.final_half_sweeps;
       coalesced += d.attempts > 0;
@@ -797,9 +637,10 @@ RT_API rt_status rt_cftp_batch(rt_cftp_instance* inst, int32_t count, void* cuda
   } while (false);
   if (e0) cudaEventDestroy(e0);
   if (e1) cudaEventDestroy(e1);
-  cleanup();
+  for (void* ptr : {(void*)d_tilings, (void*)d_inst, (void*)d_queue, (void*)d_state})
+    if (ptr) dev_free(ptr, stream);
   if (status != RT_OK) return status;
-  // Instances too large for one CTA: the single-instance path (the resident engine or the
+  // Instances too large for a cluster: the single-instance path (the resident engine or the
   // per-half-sweep kernels), one at a time on the same stream.
   for (int k : large_idx) {
     rt_cftp_instance& x = inst[k];
@@ -831,6 +672,8 @@ RT_API rt_status rt_cftp_batch(rt_cftp_instance* inst, int32_t count, void* cuda
     stats->coalesced = coalesced;
     stats->seconds = seconds;
     stats->ctas = grid;
+    stats->cluster_instances = n_packed - n_small;
+    stats->single_instances = (int32_t)large_idx.size();
   }
   if (coalesced != count) return fail(RT_ERR_NOT_COALESCED, "cftp_batch: some instances did not coalesce");
   return RT_OK;

@@ -95,10 +95,31 @@ def _plain(rt, job):
     return status, out, st.attempts
 
 
-def test_oversized_instances_run_on_the_single_instance_path(rt):
+def _smem_limit():
+    import torch
+
+    return torch.cuda.get_device_properties(0).shared_memory_per_block_optin - 1024
+
+
+def _placement(rt, job, limit):
+    """Where rt_cftp_batch runs an instance: 1 (one CTA), the cluster size (2..16), or 0 (the
+    single-instance path), from the shared memory its chains need."""
+    n = rt.side_of(job["tmax"])
+    ncol = 2 if job["model"] == "domino" else 3
+    pitch = ((n // ncol) + 15) // 16 * 16
+    if 2 * ncol * n * pitch <= limit:
+        return 1
+    rows = n - 2 if job["model"] == "domino" else n
+    for c in range(2, 17):
+        if 2 * ncol * ((rows + c - 1) // c + 2) * pitch <= limit:
+            return c
+    return 0
+
+
+def test_oversized_instances_run_in_clusters(rt):
     """Instances whose two chains exceed one CTA's shared memory (an order-168 Aztec diamond,
-    a side-170 hexagon) run through the single-instance entry points inside the batch; every
-    instance of the mixed batch still equals its single-instance result, coalesced or not."""
+    a side-170 hexagon) run on thread-block clusters inside the batch; every instance of the
+    mixed batch still equals its single-instance result, coalesced or not."""
     D, L = rt.DominoTiler, rt.LozengeTiler
     jobs = _jobs(rt, 6)
     d = D.AztecDiamond(168)
@@ -109,8 +130,40 @@ def test_oversized_instances_run_on_the_single_instance_path(rt):
                  "first_steps": 64, "max_attempts": 1})
     outs, attempts, stats = rt.cftp_batch(jobs)
     assert stats["instances"] == 8
+    assert [_placement(rt, j, _smem_limit()) for j in jobs[-2:]] == [2, 2]
+    assert stats["cluster_instances"] == 2 and stats["single_instances"] == 0
     assert attempts[-1] == -1  # 64 sweeps do not coalesce a side-170 hexagon
     assert stats["coalesced"] == 8 - sum(a < 0 for a in attempts)
+    for job, out, att in zip(jobs, outs, attempts):
+        status, ref, ref_att = _plain(rt, job)
+        assert status in (rt.RT_OK, rt.RT_ERR_NOT_COALESCED)
+        assert abs(att) == ref_att and (att > 0) == (status == rt.RT_OK), job["model"]
+        assert np.array_equal(out, ref), (job["model"], rt.side_of(job["tmax"]))
+
+
+def test_cluster_sizes_up_to_sixteen_ctas_and_the_single_instance_path(rt):
+    """Aztec diamonds of orders 240-700 and hexagons of sides 300-640 beside small instances:
+    clusters of 2 to 16 CTAs (non-power-of-two sizes included), and an order-700 diamond that
+    no 16-CTA cluster holds, which runs on the single-instance path.  Short look-backs (the
+    samples need not coalesce): every output and attempt count equals the single-instance
+    entry point's."""
+    D, L = rt.DominoTiler, rt.LozengeTiler
+    jobs = _jobs(rt, 4, seed0=500)
+    for k, (order, rule, b) in enumerate(((240, "cftp_twoperiodic", 0.7), (400, "cftp", 1.0), (520, "cftp", 1.0),
+                                          (640, "cftp_twoperiodic", 0.9), (700, "cftp", 1.0))):
+        d = D.AztecDiamond(order)
+        jobs.append({"model": "domino", "tmax": D.MaxTiling(d), "tmin": D.MinTiling(d), "seed": 40 + k,
+                     "stream": 900 + k, "rule": rule, "a": 1.0, "b": b, "first_steps": 3, "max_attempts": 3})
+    for k, side in enumerate((300, 440, 640)):
+        h = L.Hexagon(side)
+        jobs.append({"model": "lozenge", "tmax": L.MaxTiling(h), "tmin": L.MinTiling(h), "seed": 70 + k,
+                     "stream": 950 + k, "first_steps": 2, "max_attempts": 3})
+    where = [_placement(rt, j, _smem_limit()) for j in jobs]
+    assert where[4:] == [where[4], where[5], where[6], where[7], 0, where[9], where[10], where[11]]
+    assert all(2 <= c <= 16 for c in where[4:8] + where[9:])
+    assert len(set(where[4:8] + where[9:])) >= 4 and max(where) >= 15
+    outs, attempts, stats = rt.cftp_batch(jobs)
+    assert stats["cluster_instances"] == 7 and stats["single_instances"] == 1, (stats, where)
     for job, out, att in zip(jobs, outs, attempts):
         status, ref, ref_att = _plain(rt, job)
         assert status in (rt.RT_OK, rt.RT_ERR_NOT_COALESCED)
