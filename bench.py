@@ -327,13 +327,14 @@ def serving_leg(rt) -> dict:
             wall = time.perf_counter() - t0
             lat = np.array(lat)
             levels.append({"offered_per_s": rate, "requests": len(reqs), "served": int(len(lat)), "rejected": rejected,
-                           "achieved_per_s": len(lat) / wall, "seconds": wall,
+                           "achieved_per_s": len(lat) / wall, "seconds": wall, "drain_s": wall - SERVE_SECONDS,
                            "latency_p50_s": float(np.percentile(lat, 50)), "latency_p99_s": float(np.percentile(lat, 99)),
                            "client_submit_us": 1e6 * submit_s / max(1, len(reqs))})
     finally:
         srv.close()
     capacity = max(x["achieved_per_s"] for x in levels)
-    saturated = [x["offered_per_s"] for x in levels if x["achieved_per_s"] < 0.9 * x["offered_per_s"]]
+    # saturated: admissions refused, or the median request waiting more than a second
+    saturated = [x["offered_per_s"] for x in levels if x["rejected"] > 0 or x["latency_p50_s"] > 1.0]
     return {"workload": f"Poisson arrivals at {', '.join(f'{r:.0f}' for r in SERVE_RATES)}/s, {SERVE_SECONDS:.0f} s each: "
                         f"Aztec orders log-U{list(BATCH_ORDERS)} (half 2-periodic, b~U{list(BATCH_B)}) and hexagon "
                         f"sides log-U{list(BATCH_SIDES)}; config 5's 60 s at log-U[16,512] truncated as the batched leg",

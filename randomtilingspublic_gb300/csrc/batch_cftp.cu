@@ -251,8 +251,9 @@ __device__ int helper_limit(const DevInstance& in, const InstState* st) {
   return min(owner_limit(in, st), lowest_unfinished + 1 + kSpeculate);
 }
 
-__global__ void __launch_bounds__(kBatchThreads, 8) k_batch_cftp(BatchArgs a, uint32_t lz_c4, uint32_t lz_c8) {
+__global__ void __launch_bounds__(kBatchThreads, 4) k_batch_cftp(BatchArgs a, uint32_t lz_c4, uint32_t lz_c8) {
   extern __shared__ __align__(16) uint8_t sm[];
+  __shared__ DevInstance s_in;
   __shared__ int s_idx, s_att, s_flag, s_pick;
   __shared__ uint32_t red[kBatchThreads / 32];
   int own = -1;            // the instance this CTA took from the queue (thread 0's view)
@@ -317,7 +318,9 @@ __global__ void __launch_bounds__(kBatchThreads, 8) k_batch_cftp(BatchArgs a, ui
     }
     const int idx = s_idx, att = s_att;
     DevInstance* g = &a.inst[idx];
-    const DevInstance in = *g;
+    if (threadIdx.x == 0) s_in = *g;  // read by every thread from shared memory
+    __syncthreads();
+    const DevInstance& in = s_in;
     const int outcome = run_attempt(sm, in, &a.state[idx], att, a.tilings, lz_c4, lz_c8, red, &s_flag);
     record_attempt(sm, g, in, &a.state[idx], att, outcome, a.tilings, a, &s_flag);
   }
@@ -360,6 +363,7 @@ __global__ void __launch_bounds__(kBatchThreads) k_serve(ServeArgs a, uint32_t l
   extern __shared__ __align__(16) uint8_t sm[];
   __shared__ long long s_ticket;
   __shared__ uint32_t red[kBatchThreads / 32];
+  __shared__ DevInstance s_in;
   for (;;) {
     if (threadIdx.x == 0) {
       long long claimed = -1;
@@ -385,12 +389,11 @@ __global__ void __launch_bounds__(kBatchThreads) k_serve(ServeArgs a, uint32_t l
     __syncthreads();
     if (ticket < 0) break;
     const int slot = (int)(ticket % a.slots);
-    DevInstance in;
-    {
-      const volatile uint32_t* src = reinterpret_cast<const volatile uint32_t*>(a.desc + slot);
-      uint32_t* dst = reinterpret_cast<uint32_t*>(&in);
-      for (int w = 0; w < (int)(sizeof(DevInstance) / 4); ++w) dst[w] = src[w];
-    }
+    if (threadIdx.x < (int)(sizeof(DevInstance) / 4))  // the request, into shared memory
+      reinterpret_cast<uint32_t*>(&s_in)[threadIdx.x] =
+          reinterpret_cast<const volatile uint32_t*>(a.desc + slot)[threadIdx.x];
+    __syncthreads();
+    const DevInstance& in = s_in;
     uint8_t* base = a.data + (size_t)slot * a.slot_bytes;
     int att;
     int64_t look;

@@ -62,6 +62,7 @@ __global__ void __launch_bounds__(kClusterThreads, 1)
   __shared__ int s_idx;
   __shared__ unsigned s_diff[64];  // CTA 0: differing words of each attempt
   __shared__ uint32_t red[kClusterThreads / 32];
+  __shared__ DevInstance s_in;
   cg::cluster_group cluster = cg::this_cluster();
   const int rank = (int)cluster.block_rank(), C = (int)cluster.num_blocks();
   const int* const idx0 = cluster.map_shared_rank(&s_idx, 0);
@@ -76,7 +77,9 @@ __global__ void __launch_bounds__(kClusterThreads, 1)
     cluster.sync();  // every CTA has its index before any CTA leaves
     if (idx >= count) break;
     DevInstance* g = &inst[idx];
-    const DevInstance in = *g;
+    if (threadIdx.x == 0) s_in = *g;  // read by every thread from shared memory
+    __syncthreads();
+    const DevInstance& in = s_in;
     const int ncol = in.model == 0 ? 2 : 3;
     const int R = cluster_rows_per_cta(in, C);
     const size_t plane = cluster_plane_bytes(in, C);
