@@ -77,7 +77,9 @@ typedef struct rt_walk_opts {
   int32_t engine;       /* 0: automatic; 1: per-half-sweep kernels; 2: resident persistent
                            kernel (the run kernel, which rebuilds the passive colour only where
                            the colour switches, else k_persist); 3: k_persist, the resident
-                           kernel that exchanges band rows every half-sweep */
+                           kernel that exchanges band rows every half-sweep.  Lozenges: 0
+                           automatic, 1 per-step kernels, 2 the resident band kernel (TinyMT
+                           without MTGP, or fast mode); the same tilings from every engine */
   void* cuda_stream;    /* cudaStream_t to run on; NULL = the library's own stream */
 } rt_walk_opts;
 

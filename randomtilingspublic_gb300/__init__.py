@@ -451,12 +451,16 @@ class LozengeTiler(_TinyMTTable):
     with the reference's OpenCL path), 'mtgp' (its CUDA path's cuRAND MTGP32 draws, uniform
     rule; also selected by LoadMTGP) or 'fast'."""
 
-    def __init__(self, rng: str = "tinymt", fast_stream: int = 0, q: float | None = None):
+    def __init__(self, rng: str = "tinymt", fast_stream: int = 0, q: float | None = None, engine: int = 0):
         """q: None for the reference's uniform rotation (lozengekernel.cl), else the q^volume
-        rotation of qlozengekernel.cl (down-move rescaling corrected)."""
+        rotation of qlozengekernel.cl (down-move rescaling corrected).  engine: 0 automatic (the
+        resident band kernel where it holds the size), 1 the per-step kernels, 2 the resident
+        band kernel (an error where it does not hold the size); every engine gives the same
+        tilings."""
         self.rng = rng
         self.fast_stream = int(fast_stream)
         self.q = q
+        self.engine = int(engine)
 
     def LoadMTGP(self) -> None:
         """LozengeTiler::LoadMTGP: walks draw from cuRAND MTGP32 block generators, as the
@@ -468,6 +472,7 @@ class LozengeTiler(_TinyMTTable):
         lib().rt_walk_opts_default(C.byref(o))
         o.rng_mode = RNG_MODES[self.rng]
         o.fast_stream = self.fast_stream
+        o.engine = self.engine
         if self.q is not None:
             o.rule = RT_LOZENGE_Q
             o.weight_a = float(self.q)

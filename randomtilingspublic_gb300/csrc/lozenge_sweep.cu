@@ -21,6 +21,7 @@
 #include <string>
 #include <vector>
 
+#include "lozenge_resident.h"
 #include "pdl.cuh"
 #include "rng.cuh"
 #include "rt_internal.h"
@@ -273,8 +274,11 @@ struct LzSampler {
   int64_t interior[3] = {0, 0, 0};
   int64_t steps_by_colour[3] = {0, 0, 0};
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  std::unique_ptr<LzResidentState> res;  // the resident engine for `res_nch` swept chains
+  int res_nch = 0;
 
   ~LzSampler() {
+    res.reset();
     if (base) cudaFree(base);
     if (tmt) cudaFree(tmt);
     if (tmt_params) cudaFree(tmt_params);
@@ -299,6 +303,10 @@ struct LzSampler {
     if (o.tinymt_params && o.rng_mode != RT_RNG_TINYMT)
       return fail(RT_ERR_INVALID_ARGUMENT, "lozenge sweep: a TinyMT parameter table needs the TinyMT mode");
     if (o.rule != RT_LOZENGE_UNIFORM && o.rule != RT_LOZENGE_Q) return fail(RT_ERR_INVALID_ARGUMENT, "lozenge sweep: unknown rule");
+    if (o.engine < 0 || o.engine > 2)
+      return fail(RT_ERR_INVALID_ARGUMENT, "lozenge sweep: engine 0 (automatic), 1 (per-step kernels) or 2 (resident)");
+    if (o.engine == 2 && o.rng_mode == RT_RNG_MTGP)
+      return fail(RT_ERR_INVALID_ARGUMENT, "lozenge sweep: the MTGP mode runs on the per-step kernels (engine 1)");
     if (o.rule == RT_LOZENGE_Q && (!(o.weight_a > 0.0) || !std::isfinite(o.weight_a)))
       return fail(RT_ERR_INVALID_ARGUMENT, "lozenge sweep: q (weight_a) must be finite and > 0");
     int devs = 0;
@@ -335,6 +343,25 @@ struct LzSampler {
     *out = std::move(s);
     return RT_OK;
   }
+  LzResidentGeom geom() const { return LzResidentGeom{N, M, P, active, colour_stride, chain_stride}; }
+  // The resident engine for the swept chains when the options allow it and a plan holds this
+  // size (engine 0: where it holds, 2: required); NULL: the per-step kernels.
+  rt_status resident(LzResidentState** out) {
+    *out = nullptr;
+    if (opts.engine == 1 || opts.rng_mode == RT_RNG_MTGP) return RT_OK;
+    if (!res || res_nch != active) {
+      res = std::make_unique<LzResidentState>();
+      res->plan = lz_resident_plan(geom(), opts.rng_mode == RT_RNG_TINYMT);
+      res_nch = active;
+    }
+    if (!res->plan.ok) {
+      if (opts.engine == 2) return fail(RT_ERR_INVALID_ARGUMENT, "lozenge sweep: the resident engine does not hold this size");
+      return RT_OK;
+    }
+    *out = res.get();
+    return RT_OK;
+  }
+  rt_status resident_error() { return res ? lz_resident_error(*res, stream) : RT_OK; }
   rt_status check() {
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return fail(RT_ERR_CUDA, std::string("kernel launch: ") + cudaGetErrorString(e));
@@ -360,6 +387,7 @@ struct LzSampler {
     return check();
   }
   rt_status store(int ch, int32_t* t) {
+    if (rt_status st = resident_error()) return st;
     k_lz_merge<<<dim3((N + 255) / 256, N), 256, 0, stream>>>(view(), ch, scratch);
     if (rt_status s = check()) return s;
     LZ_CUDA(cudaMemcpyAsync(t, scratch, (size_t)N * N * sizeof(int32_t), cudaMemcpyDeviceToHost, stream));
@@ -398,6 +426,15 @@ struct LzSampler {
       }
       return check();
     }
+    LzResidentState* rs = nullptr;
+    if (rt_status st = resident(&rs)) return st;
+    if (rs) {
+      const LzResidentRule rr{rule.lo_up, rule.w_up, rule.lo_dn, rule.w_dn};
+      if (rt_status st = lz_resident_run(*rs, geom(), base, rr, true, tmt, tmt_params, colours, steps, 0, 0, 0, stream))
+        return st;
+      for (int64_t s = 0; s < steps; ++s) steps_by_colour[colours[s]]++;
+      return RT_OK;
+    }
     const dim3 gr((M + 127) / 128, N), gu((P / 4 + 31) / 32, (N - 2 + 7) / 8);
     for (int64_t s = 0; s < steps; ++s) {
       const int r = colours[s];
@@ -408,6 +445,16 @@ struct LzSampler {
     return check();
   }
   rt_status run_fast(uint64_t seed_value, int64_t h0, int64_t steps) {
+    LzResidentState* rs = nullptr;
+    if (rt_status st = resident(&rs)) return st;
+    if (rs) {
+      const LzResidentRule rr{rule.lo_up, rule.w_up, rule.lo_dn, rule.w_dn};
+      if (rt_status st = lz_resident_run(*rs, geom(), base, rr, false, nullptr, nullptr, nullptr, steps, seed_value,
+                                         opts.fast_stream, h0, stream))
+        return st;
+      for (int64_t s = 0; s < steps; ++s) steps_by_colour[(((h0 + s) % 3) + 3) % 3]++;
+      return RT_OK;
+    }
     const LzView v = view();
     const int quads = (M + 3) / 4;
     const dim3 gr((quads + 31) / 32, (N + 7) / 8), gu((P / 4 + 31) / 32, (N - 2 + 7) / 8);
@@ -421,6 +468,7 @@ struct LzSampler {
     return check();
   }
   rt_status diff(int a, int b, int64_t* nd) {
+    if (rt_status st = resident_error()) return st;
     LZ_CUDA(cudaMemsetAsync(counter, 0, sizeof(unsigned long long), stream));
     const size_t words = chain_stride / 4;
     k_lz_diff<<<(unsigned)std::min<size_t>((words + 255) / 256, 1024), 256, 0, stream>>>(

@@ -173,3 +173,54 @@ def test_arbitrary_edge_masks_sweep_as_the_reference(rt, orc, mode):
         else:
             orc.lz_walk_fast(b, n, 0, steps, seed, 4)
         assert np.array_equal(a, b), (mode, n)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("rng,q", [("tinymt", None), ("fast", None), ("tinymt", 0.7), ("fast", 1.3)])
+def test_resident_engine_equals_per_step_kernels(rt, rng, q):
+    """The resident band kernel (engine 2) against the per-step kernels (engine 1): walks of
+    one chain and CFTP of the coupled pair give the same tilings and attempt counts, on
+    hexagons from 3 bands (side 5) to one band per SM (side 512, a short walk)."""
+    L = rt.LozengeTiler
+    for side, steps in ((5, 301), (37, 450), (150, 90), (512, 31)):
+        d = L.Hexagon(side)
+        t0 = L.MaxTiling(d)
+        out = []
+        for engine in (1, 2):
+            t = t0.copy()
+            L(rng=rng, fast_stream=11, q=q, engine=engine).Walk(t, steps, 4242 + side)
+            out.append(t)
+        assert np.array_equal(out[0], out[1]), (rng, q, side)
+        assert not np.array_equal(out[1], t0) or side == 512
+    d = L.Hexagon(9)
+    tmax, tmin = L.MaxTiling(d), L.MinTiling(d)
+    res = [L(rng=rng, fast_stream=3, q=q, engine=e).cftp(tmax, tmin, 77, first_steps=8, schedule=1, max_attempts=20)
+           for e in (1, 2)]
+    assert np.array_equal(res[0][0], res[1][0]) and res[0][1]["attempts"] == res[1][1]["attempts"]
+
+
+@pytest.mark.gpu
+def test_resident_engine_with_a_tinymt_parameter_table(rt):
+    L = rt.LozengeTiler
+    d = L.Hexagon(20)
+    t0 = L.MaxTiling(d)
+    n = int(np.sqrt(t0.size))
+    rnd = np.random.default_rng(3)
+    table = [(0x8F7011EE ^ int(x), 0xFC78FF1F ^ int(y), 0x3793FDFF ^ int(z))
+             for x, y, z in rnd.integers(0, 1 << 20, size=(n * (n // 3), 3))]
+    out = []
+    for engine in (1, 2):
+        tiler = L(engine=engine)
+        tiler.LoadTinyMT(table)
+        t = t0.copy()
+        tiler.Walk(t, 200, 9)
+        out.append(t)
+    assert np.array_equal(out[0], out[1])
+
+
+def test_resident_engine_refuses_mtgp(rt):
+    L = rt.LozengeTiler
+    t = L.MaxTiling(L.Hexagon(4))
+    with pytest.raises(rt.RTError) as e:
+        L(rng="mtgp", engine=2).Walk(t, 3, 1)
+    assert e.value.status == rt.RT_ERR_INVALID_ARGUMENT
