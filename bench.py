@@ -235,19 +235,19 @@ def _plain_cftp(rt, job):
         return None
 
 
-def batched_leg(rt) -> dict:
+def batched_leg(rt, instances: int = BATCH_INSTANCES) -> dict:
     """Batched fast-mode CFTP (rt_cftp_batch) on the mix above, against the same kind of
     instances run one at a time through the plain entry points (PLAIN_SAMPLES instances drawn
     across the mix).  Samples/s count coalesced instances; every batched sample equals the
     plain result of its instance (tests/test_batch_cftp.py)."""
     rng = np.random.default_rng(20261203)
     cache = {}
-    jobs = [_batch_job(rt, cache, rng, k) for k in range(BATCH_INSTANCES)]
+    jobs = [_batch_job(rt, cache, rng, k) for k in range(instances)]
     rt.cftp_batch(jobs[:64])  # warm-up
     t0 = time.perf_counter()
     outs, attempts, stats = rt.cftp_batch(jobs)
     wall = time.perf_counter() - t0
-    pick = np.random.default_rng(7).choice(len(jobs), size=PLAIN_SAMPLES, replace=False)
+    pick = np.random.default_rng(7).choice(len(jobs), size=min(PLAIN_SAMPLES, len(jobs)), replace=False)
     lat, same = [], 0
     for k in pick:
         t1 = time.perf_counter()
@@ -256,13 +256,13 @@ def batched_leg(rt) -> dict:
         same += out is not None and attempts[k] > 0 and np.array_equal(out, outs[k])
     lat = np.array(lat)
     plain_rate = 1.0 / lat.mean()
-    return {"workload": f"{BATCH_INSTANCES} CFTP instances (config 4's count and mix, sizes truncated): Aztec orders "
+    return {"workload": f"{instances} CFTP instances (config 4's count and mix, sizes truncated): Aztec orders "
                         f"U{list(BATCH_ORDERS)} and hexagon sides U{list(BATCH_SIDES)}, half of the diamonds 2-periodic "
                         f"(a=1, b~U{list(BATCH_B)}), seeds and streams k, look-back {BATCH_FIRST} sweeps doubling, at "
                         f"most {BATCH_ATTEMPTS} attempts",
             "samples_per_s": stats["coalesced"] / wall, "coalesced": stats["coalesced"], "kernel_s": stats["seconds"],
             "wall_s": wall, "ctas": stats["ctas"],
-            "plain_samples_per_s": plain_rate, "plain_sampled_instances": PLAIN_SAMPLES,
+            "plain_samples_per_s": plain_rate, "plain_sampled_instances": len(pick),
             "plain_equal_to_batched": int(same),
             "plain_latency_p50_s": float(np.percentile(lat, 50)), "plain_latency_p99_s": float(np.percentile(lat, 99)),
             "batched_over_plain": (stats["coalesced"] / wall) / plain_rate,
@@ -345,6 +345,61 @@ def serving_leg(rt) -> dict:
             "api": "rt_server_submit / rt_server_poll / rt_server_wait (continuous batching)"}
 
 
+MID_ORDER, MID_INSTANCES, MID_SWEEPS = 200, 152, 1024  # thread-block-cluster leg
+MID_PLAIN = 4  # of its instances also run one at a time
+
+
+def mid_batch_leg(rt) -> dict:
+    """Instances too large for one CTA (Aztec diamonds of order 200, N = 402), each held by a
+    thread-block cluster inside rt_cftp_batch: MID_INSTANCES uniform instances with a fixed
+    look-back of MID_SWEEPS sweeps (one attempt each, coalesced or not), against MID_PLAIN of
+    them run one at a time through rt_domino_cftp on the whole GPU.  Both in fast mode; the
+    samples are identical (checked here)."""
+    import ctypes as C
+
+    D = rt.DominoTiler
+    d = D.AztecDiamond(MID_ORDER)
+    tmax, tmin = D.MaxTiling(d), D.MinTiling(d)
+    n = rt.side_of(tmax)
+    jobs = [{"model": "domino", "tmax": tmax, "tmin": tmin, "seed": 7000 + k, "stream": k, "rule": "cftp", "a": 1.0,
+             "b": 1.0, "first_steps": MID_SWEEPS, "max_attempts": 1} for k in range(MID_INSTANCES)]
+    rt.cftp_batch(jobs[:2])  # warm-up
+    t0 = time.perf_counter()
+    outs, attempts, stats = rt.cftp_batch(jobs)
+    wall = time.perf_counter() - t0
+    half_sweeps = 2 * MID_SWEEPS
+    plain_s, plain_dev, same, flips = [], [], 0, 0
+    for k in range(MID_PLAIN):
+        job = jobs[k]
+        tiler = rt.DominoTiler(rule="cftp", rng="fast", fast_stream=job["stream"])
+        a_, b_ = np.ascontiguousarray(tmax, np.int32), np.ascontiguousarray(tmin, np.int32)
+        out = np.zeros_like(a_)
+        st = rt.CftpStats()
+        o = tiler.opts()
+        t1 = time.perf_counter()
+        status = rt.lib().rt_domino_cftp(rt._ptr(a_), rt._ptr(b_), n, int(job["seed"]), MID_SWEEPS, 1, 1, C.byref(o),
+                                         rt._ptr(out), C.byref(st))
+        plain_s.append(time.perf_counter() - t1)
+        if status not in (rt.RT_OK, rt.RT_ERR_NOT_COALESCED):
+            raise rt.RTError(status, rt.lib().rt_last_error().decode())
+        same += np.array_equal(out, outs[k])
+        plain_dev.append(st.seconds)
+        flips = st.flip_attempts  # both chains, every half-sweep of the attempt
+    per_instance_half_sweep_us = 1e6 * stats["seconds"] / (MID_INSTANCES * half_sweeps)
+    plain_us = 1e6 * statistics.median(plain_dev) / half_sweeps
+    out = {"workload": f"{MID_INSTANCES} uniform Aztec diamonds of order {MID_ORDER} (N = {n}), one CFTP attempt of "
+                       f"{MID_SWEEPS} sweeps each, fast mode",
+           "cluster_instances": stats["cluster_instances"], "ctas": stats["ctas"], "kernel_s": stats["seconds"],
+           "wall_s": wall, "us_per_instance_half_sweep": per_instance_half_sweep_us,
+           "plain_us_per_half_sweep": plain_us, "plain_call_s": statistics.median(plain_s),
+           "plain_instances": MID_PLAIN, "plain_equal_to_batched": int(same),
+           "batched_over_plain": plain_us / per_instance_half_sweep_us,
+           "flip_attempts_per_s": flips * MID_INSTANCES / stats["seconds"],
+           "plain_flip_attempts_per_s": flips / statistics.median(plain_dev),
+           "api": "rt_cftp_batch (thread-block clusters) vs rt_domino_cftp one at a time"}
+    return out
+
+
 def single_instance_leg(rt) -> dict:
     """The other single-instance workloads: one coupled max/min CFTP attempt on the lozenge
     hexagon of side 512, 10^5 sweeps of bibone tilings of the 512 x 512 rhombus from the brick
@@ -358,6 +413,8 @@ def single_instance_leg(rt) -> dict:
     o = L.opts()
     stats = rt.CftpStats()
     res = np.zeros_like(tmax)
+    rt.lib().rt_lozenge_cftp(tmax.ctypes.data, tmin.ctypes.data, int(np.sqrt(tmax.size)), 11, 4, 0, 1, C.byref(o),
+                             res.ctypes.data, C.byref(stats))  # warm-up: kernel loading outside the timed call
     status = rt.lib().rt_lozenge_cftp(tmax.ctypes.data, tmin.ctypes.data, int(np.sqrt(tmax.size)), 11, look_back, 0, 1,
                                       C.byref(o), res.ctypes.data, C.byref(stats))
     if status not in (rt.RT_OK, rt.RT_ERR_NOT_COALESCED):
@@ -671,9 +728,11 @@ def run_ours(args) -> None:
                          f"2 attempts, {threads} host threads"}
     s.close()
     batched = serving = single = None
+    mid = None
     if rank == 0 and not args.no_batch:
-        batched = batched_leg(rt)
-        serving = serving_leg(rt)
+        batched = batched_leg(rt, args.batch_instances)
+        serving = None if args.no_serve else serving_leg(rt)
+        mid = mid_batch_leg(rt)
     if rank == 0 and not args.no_single:
         single = single_instance_leg(rt)
     if rank == 0:
@@ -688,7 +747,8 @@ def run_ours(args) -> None:
                                   "bands": info["bands"], "threads_per_band": info.get("threads"),
                                   "units_per_thread": info["units_per_thread"]}},
             "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches, "clocks": clocks,
-            "check": check, "batched_cftp": batched, "served_cftp": serving, "single_instance": single,
+            "check": check, "batched_cftp": batched, "served_cftp": serving, "batched_cftp_clusters": mid,
+            "single_instance": single,
         }
         print(json.dumps(line))
     if dist is not None:
@@ -705,6 +765,8 @@ def main() -> None:
     ap.add_argument("--engine", type=int, default=0)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-batch", action="store_true")
+    ap.add_argument("--no-serve", action="store_true")
+    ap.add_argument("--batch-instances", type=int, default=BATCH_INSTANCES)
     ap.add_argument("--no-single", action="store_true")
     ap.add_argument("--no-tune", action="store_true", help="ignore the autotuner's table")
     args = ap.parse_args()
