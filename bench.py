@@ -671,9 +671,11 @@ def run_ours(args) -> None:
     cells = (n - 2) * (n // 2 - 2)
     tiling_bytes_per_half = 3 * (attempts / half_sweeps)
     peaks = _peaks()
-    if info["engine"] in (2, 3):
-        kernel = ("k_runs (run-resident cooperative sweep, one launch per step)" if info["engine"] == 2 else
-                  "k_persist (resident cooperative sweep exchanging band rows every half-sweep, one launch per step)")
+    if info["engine"] in (2, 3, 4):
+        kernel = {2: "k_runs (run-resident cooperative sweep, one launch per step)",
+                  3: "k_persist (resident cooperative sweep exchanging band rows every half-sweep, one launch per step)",
+                  4: "k_bits (bit-plane cooperative sweep: edge planes in shared memory, ballot-packed draws, one "
+                     "launch per step)"}[info["engine"]]
         launches_timed = args.steps
         gen = 32 * info["units"] if args.mode == "tinymt" else 0
         algo_bytes = tiling_bytes_per_half * HALF_SWEEPS + gen

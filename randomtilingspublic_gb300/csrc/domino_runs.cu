@@ -905,10 +905,6 @@ rt_status RunEngine::prepare(DmSampler& s) {
   return RT_OK;
 }
 
-namespace {
-
-// Runs of equal colour in colours[0 .. n), appended as (colour << 31) | (epoch << 30) | length,
-// the first run flagged as an epoch start when `epoch`.
 void append_runs(const uint8_t* colours, int64_t n, bool epoch, std::vector<uint32_t>* runs) {
   bool fresh = true;
   for (int64_t q = 0; q < n; ++q) {
@@ -921,6 +917,8 @@ void append_runs(const uint8_t* colours, int64_t n, bool epoch, std::vector<uint
     }
   }
 }
+
+namespace {
 
 // The launch arguments every run-kernel launch shares.
 RunArgs run_args(const RunEngine& e, DmSampler& s) {

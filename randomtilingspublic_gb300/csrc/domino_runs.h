@@ -129,6 +129,10 @@ struct RunEngine {
   rt_status check_error(DmSampler& s);
 };
 
+// Runs of equal colour in colours[0 .. n), appended as (colour << 31) | (epoch << 30) | length,
+// the first run flagged as an epoch start when `epoch`.
+void append_runs(const uint8_t* colours, int64_t n, bool epoch, std::vector<uint32_t>* runs);
+
 constexpr int kRunThreads = 1024;
 // Kernel for (rng mode, quads per thread K, parameter table, chains).
 void* dm_runs_kernel_ptr(int mode, int K, bool params, int nch);

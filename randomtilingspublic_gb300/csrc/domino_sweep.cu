@@ -156,7 +156,12 @@ __global__ void k_scan_tiling(const int32_t* t, int N, int* cand, unsigned long 
       };
       inter = sq(i - 1, j - 1) && sq(i - 1, j) && sq(i, j - 1) && sq(i, j);
       const int m = j >> 1;
-      if (inter && m >= 1 && m <= N / 2 - 2) lo = hi = m;
+      if (inter && m >= 1 && m <= N / 2 - 2) {
+        lo = hi = m;
+        // A neighbour outside rows 1 .. N-2 or columns 1 .. N/2-2: a cell the reference never
+        // rebuilds, which only the byte engines reproduce.
+        if (i < 2 || i > N - 3 || ((j - 1) >> 1) < 1 || ((j + 1) >> 1) > N / 2 - 2) f |= 4u;
+      }
     }
   }
   f = __reduce_or_sync(0xffffffffu, f);
@@ -233,7 +238,8 @@ __global__ void k_diff(DmView v, int a, int b, unsigned long long* out) {
   } while (0)
 
 DmSampler::~DmSampler() {
-  runs.reset();  // the engines free their plan buffers on the stream before the stream goes
+  bits.reset();  // the engines free their plan buffers on the stream before the stream goes
+  runs.reset();
   persist.reset();
   for (void* p : {(void*)tmt, (void*)tmt_params, mtgp, (void*)base, (void*)scratch, (void*)counter, (void*)d_scan,
                   (void*)d_cand})
@@ -264,7 +270,7 @@ rt_status DmSampler::create(int n_side, int n_chains, const rt_walk_opts& o, std
   if (n_side < 6 || n_side % 2) return fail(RT_ERR_INVALID_ARGUMENT, "tiling side must be even and >= 6");
   if (n_side > 32768) return fail(RT_ERR_INVALID_ARGUMENT, "tiling side must be <= 32768");
   if (n_chains < 1 || n_chains > 64) return fail(RT_ERR_INVALID_ARGUMENT, "n_chains must be in [1, 64]");
-  if (o.engine < 0 || o.engine > 3) return fail(RT_ERR_INVALID_ARGUMENT, "engine must be 0, 1, 2 or 3");
+  if (o.engine < 0 || o.engine > 4) return fail(RT_ERR_INVALID_ARGUMENT, "engine must be 0, 1, 2, 3 or 4");
   if (o.rng_mode == RT_RNG_FAST && o.fast_stream >= 65536u)
     return fail(RT_ERR_INVALID_ARGUMENT, "fast_stream must be < 65536");
   DmRule rule{};
@@ -350,6 +356,7 @@ rt_status DmSampler::load(int ch, const int32_t* tiling) {
   RT_CUDA(cudaStreamSynchronize(stream));
   if (h[0] & 1u) return fail(RT_ERR_INVALID_ARGUMENT, "tiling values must be edge masks in [0, 15]");
   consistent = consistent && !(h[0] & 2u);
+  border_candidates = border_candidates || (h[0] & 4u);
   if (ch == 0) {
     interior[0] = (int64_t)h[1];
     interior[1] = (int64_t)h[2];
@@ -578,15 +585,31 @@ rt_status DmSampler::use_persistent(bool* yes) {
       return fail(RT_ERR_INVALID_ARGUMENT, "persistent engine needs consistent loaded tilings");
     return RT_OK;
   }
-  // Engine 0 and 2: the run kernel, else k_persist; engine 3: k_persist alone.
+  // Engine 0: the bit-plane kernel, else the run kernel, else k_persist; 4: the bit-plane
+  // kernel alone; 2: the run kernel, else k_persist; 3: k_persist alone.
   if (plan_dirty ||
       (runs && (runs->nch != active || runs->bands_asked != eff_bands || runs->threads_asked != eff_threads)) ||
-      (persist && persist->nch != active)) {
+      (persist && persist->nch != active) || (bits && bits->nch != active)) {
+    bits.reset();
     runs.reset();
     persist.reset();
   }
   plan_dirty = false;
   std::string why;
+  if (engine == 0 || engine == 4) {
+    if (!bits) {
+      bits = std::make_unique<BitEngine>();
+      if (rt_status st = bits->prepare(*this)) return st;
+    }
+    if (bits->ready) {
+      resident = 4;
+      *yes = true;
+      return RT_OK;
+    }
+    if (engine == 4 && explicit_engine)
+      return fail(RT_ERR_INVALID_ARGUMENT, "bit-plane engine unavailable: " + bits->plan.why);
+    why = "bit-plane kernel: " + bits->plan.why + "; ";
+  }
   if (engine != 3) {
     if (!runs) {
       runs = std::make_unique<RunEngine>();
@@ -597,7 +620,7 @@ rt_status DmSampler::use_persistent(bool* yes) {
       *yes = true;
       return RT_OK;
     }
-    why = "run kernel: " + runs->plan.why + "; ";
+    why += "run kernel: " + runs->plan.why + "; ";
   }
   if (!persist) {
     persist = std::make_unique<PersistEngine>();
@@ -614,6 +637,9 @@ rt_status DmSampler::use_persistent(bool* yes) {
 }
 
 rt_status DmSampler::check_resident_error() {
+  if (bits) {
+    if (rt_status st = bits->check_error(*this)) return st;
+  }
   if (runs) {
     if (rt_status st = runs->check_error(*this)) return st;
   }
@@ -624,6 +650,7 @@ rt_status DmSampler::check_resident_error() {
 }
 
 rt_status DmSampler::launch_resident(const uint8_t* colours, int64_t steps, uint64_t fast_seed, int64_t h0) {
+  if (resident == 4) return bits->launch(*this, colours, steps);
   if (resident == 2) return runs->launch(*this, colours, steps, fast_seed, h0);
   return persist->launch(*this, colours, steps, fast_seed, h0);
 }
@@ -739,7 +766,11 @@ RT_API rt_status rt_dm_sampler_engine_info(rt_dm_sampler* s, int64_t* out4) {
   bool pers = false;
   if (rt_status st = d.use_persistent(&pers)) return st;
   int64_t units = 0, bands = 0, k = 0;
-  if (pers && d.resident == 2) {
+  if (pers && d.resident == 4) {
+    units = d.bits->plan.draw_cells;
+    bands = (int64_t)d.bits->plan.bands.size();
+    k = kBitSlots;
+  } else if (pers && d.resident == 2) {
     units = d.runs->plan.draw_cells;
     bands = (int64_t)d.runs->plan.bands.size();
     k = d.runs->plan.K;
@@ -757,8 +788,8 @@ RT_API rt_status rt_dm_sampler_engine_info(rt_dm_sampler* s, int64_t* out4) {
 
 RT_API rt_status rt_dm_sampler_set_launch(rt_dm_sampler* s, int32_t engine, int32_t bands, int32_t threads) {
   RT_SAMPLER(s);
-  if (engine < 0 || engine > 3 || bands < 0 || threads < 0 || threads > 1024 || threads % 32)
-    return fail(RT_ERR_INVALID_ARGUMENT, "set_launch: engine 0..3, bands >= 0, threads a multiple of 32 up to 1024");
+  if (engine < 0 || engine > 4 || bands < 0 || threads < 0 || threads > 1024 || threads % 32)
+    return fail(RT_ERR_INVALID_ARGUMENT, "set_launch: engine 0..4, bands >= 0, threads a multiple of 32 up to 1024");
   DmSampler& d = *s->impl;
   d.launch_engine = engine;
   d.launch_bands = bands;
@@ -774,7 +805,9 @@ RT_API rt_status rt_dm_sampler_launch_info(rt_dm_sampler* s, int64_t* out6) {
   if (rt_status st = rt_dm_sampler_engine_info(s, e4)) return st;
   DmSampler& d = *s->impl;
   for (int k = 0; k < 4; ++k) out6[k] = e4[k];
-  out6[4] = (e4[0] == 2) ? d.runs->plan.threads : (e4[0] == 3 ? (int64_t)kPersistThreads : 0);
+  out6[4] = (e4[0] == 4)   ? (int64_t)d.bits->plan.warps * 32
+            : (e4[0] == 2) ? d.runs->plan.threads
+                           : (e4[0] == 3 ? (int64_t)kPersistThreads : 0);
   out6[5] = d.tuned ? 1 : 0;
   return RT_OK;
 }
@@ -914,7 +947,7 @@ RT_API rt_status rt_domino_cftp(const int32_t* tmax, const int32_t* tmin, int32_
   const int64_t kLaunchHalfSweeps = (int64_t)1 << 21;
   bool pers = false;
   if (rt_status st = s->use_persistent(&pers)) return st;
-  const bool one_launch = pers && s->resident == 2 && o.rng_mode != RT_RNG_MTGP;
+  const bool one_launch = pers && (s->resident == 2 || s->resident == 4) && o.rng_mode != RT_RNG_MTGP;
   int att = 0;
   bool coalesced = false;
   while (att < max_attempts && !coalesced) {
@@ -928,8 +961,11 @@ RT_API rt_status rt_domino_cftp(const int32_t* tmax, const int32_t* tmin, int32_
         for (int k = att + q; k >= 0; --k) epochs[(size_t)q].push_back({ep_seed[(size_t)k], &colours_of(k)});
       cudaEventRecord(s->ev0, s->stream);
       int ran = 0;
-      if (rt_status st = s->runs->cftp(*s, att, n, epochs, first_steps, (uint64_t)driver_seed, &ran, &coalesced))
+      if (s->resident == 4) {
+        if (rt_status st = s->bits->cftp(*s, n, epochs, &ran, &coalesced)) return st;
+      } else if (rt_status st = s->runs->cftp(*s, att, n, epochs, first_steps, (uint64_t)driver_seed, &ran, &coalesced)) {
         return st;
+      }
       cudaEventRecord(s->ev1, s->stream);
       cudaEventSynchronize(s->ev1);
       float ms = 0.f;

@@ -5,6 +5,7 @@
 #include <cstdint>
 #include <memory>
 
+#include "domino_bits.h"
 #include "domino_persist.h"
 #include "domino_runs.h"
 #include "domino_rules.h"
@@ -74,11 +75,14 @@ struct DmSampler {
   std::vector<int> cand_lo, cand_hi;     // host copies (-1: no candidate)
   bool any_candidate = false;
   bool consistent = true;
+  bool border_candidates = false;  // a candidate borders a cell the reference never rebuilds
   bool plan_dirty = true;
+  std::unique_ptr<BitEngine> bits;        // the bit-plane kernel (domino_bits.cu)
   std::unique_ptr<RunEngine> runs;        // the run-resident kernel (domino_runs.cu)
   std::unique_ptr<PersistEngine> persist;  // the per-half-sweep-exchange resident kernel
-  int resident = 0;     // the resident kernel the next run uses: 2 run kernel, 3 k_persist, 0 none
-  int last_engine = 0;  // engine of the last run: 1 per-half-sweep kernels, 2 or 3 as resident
+  int resident = 0;     // the resident kernel the next run uses: 2 run kernel, 3 k_persist,
+                        // 4 bit-plane kernel, 0 none
+  int last_engine = 0;  // engine of the last run: 1 per-half-sweep kernels, 2-4 as resident
   // Launch shape: an explicit choice (rt_dm_sampler_set_launch; 0 = none), and the shape in
   // force, from that choice, else the autotuner's table, else the defaults (0).
   int launch_engine = 0, launch_bands = 0, launch_threads = 0;

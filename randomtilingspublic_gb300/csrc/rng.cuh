@@ -73,6 +73,22 @@ __device__ __forceinline__ uint32_t tmt_next_u23_mad(uint4& s, uint32_t mat1, ui
   return mul_hi(t0, 1u << 23);                     // t0 >> 9
 }
 
+// The same step returning the whole tempered word t0; the draw is t0 >> 9, so a test
+// (u - lo) < w on the draw is mad_hi(t0, 2^23, -lo) < w, one multiply-add.
+__device__ __forceinline__ uint32_t tmt_next_t0_mad(uint4& s, uint32_t mat1, uint32_t mat2, uint32_t tmat) {
+  uint32_t x = (s.x & 0x7fffffffu) ^ s.y ^ s.z;
+  uint32_t y = s.w;
+  x ^= mul_lo(x, 2u);
+  y ^= mul_hi(y, 0x80000000u) ^ x;
+  const uint32_t odd = y & 1u;
+  s.x = s.y;
+  s.y = s.z ^ mul_lo(mat1, odd);
+  s.z = x ^ mul_lo(y, 1024u) ^ mul_lo(mat2, odd);
+  s.w = y;
+  const uint32_t t1 = mad_hi(s.z, 1u << 24, s.x);
+  return s.w ^ t1 ^ mul_lo(tmat, t1 & 1u);
+}
+
 __device__ __forceinline__ void tmt_plain_step(uint4& s, uint32_t mat1, uint32_t mat2) {
   uint32_t x = (s.x & 0x7fffffffu) ^ s.y ^ s.z;
   uint32_t y = s.w;

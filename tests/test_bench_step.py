@@ -26,16 +26,17 @@ def test_bench_check_digest_is_the_golden_one():
 
 
 @pytest.mark.gpu
-def test_bench_step_tinymt_equals_oracle(rt, orc):
+@pytest.mark.parametrize("engine", [0, 2, 4])
+def test_bench_step_tinymt_equals_oracle(rt, orc, engine):
     import torch
 
     import bench
     from tests.golden.make_bench_check import oracle_step
 
-    tiler = rt.DominoTiler(rule="cftp_twoperiodic", rng="tinymt", a=bench.WEIGHT_A, b=bench.WEIGHT_B)
+    tiler = rt.DominoTiler(rule="cftp_twoperiodic", rng="tinymt", a=bench.WEIGHT_A, b=bench.WEIGHT_B, engine=engine)
     stream = torch.cuda.Stream()
     s, tmax, tmin, _ = bench.headline_sampler(rt, tiler, stream.cuda_stream)
-    assert s.engine_info()["engine"] == 2, "the bench step runs on the resident engine"
+    assert s.engine_info()["engine"] in ((2, 4) if engine == 0 else (engine,)), "the bench step runs resident"
     # A first step on other seeds, as the bench's warm-up does, then the checked one.
     bench.headline_step(rt, s, int(bench.warmup_seeds(0, 1)[0]), "tinymt")
     bench.headline_step(rt, s, GOLDEN["seed"], "tinymt")

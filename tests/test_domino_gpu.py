@@ -36,7 +36,7 @@ def _is_valid_tiling(rt, t, d) -> bool:
     return bool(np.all(cover[D == 1] == 1) and np.all(cover[D == 0] == 0))
 
 
-@pytest.mark.parametrize("engine", [1, 2, 3])
+@pytest.mark.parametrize("engine", [1, 2, 3, 4])
 def test_golden_reference_vectors(rt, golden, engine):
     for case in golden["cases"]:
         n = case["N"]
@@ -56,7 +56,7 @@ def test_golden_reference_vectors(rt, golden, engine):
         assert np.array_equal(t, np.array(case["expected"], np.int32)), case["name"]
 
 
-@pytest.mark.parametrize("engine", [1, 2, 3])
+@pytest.mark.parametrize("engine", [1, 2, 3, 4])
 def test_tinymt_walk_random_cases_match_oracle(rt, orc, engine):
     rng = np.random.default_rng(11)
     D = rt.DominoTiler
@@ -76,7 +76,7 @@ def test_tinymt_walk_random_cases_match_oracle(rt, orc, engine):
         assert np.array_equal(g, o), (order, rule, steps, seed)
 
 
-@pytest.mark.parametrize("engine", [1, 2, 3])
+@pytest.mark.parametrize("engine", [1, 2, 3, 4])
 def test_tinymt_walk_with_parameter_table_and_rectangles(rt, orc, engine):
     D = rt.DominoTiler
     rng = np.random.default_rng(3)
@@ -94,7 +94,7 @@ def test_tinymt_walk_with_parameter_table_and_rectangles(rt, orc, engine):
         assert np.array_equal(g, o)
 
 
-@pytest.mark.parametrize("engine", [1, 2, 3])
+@pytest.mark.parametrize("engine", [1, 2, 3, 4])
 def test_tinymt_epochs_match_oracle(rt, orc, engine):
     D = rt.DominoTiler
     d = D.AztecDiamond(33)
@@ -141,7 +141,7 @@ def test_fast_cftp_matches_oracle(rt, orc, rule, a, b, engine):
         assert _is_valid_tiling(rt, out, d)
 
 
-@pytest.mark.parametrize("engine", [1, 2, 3])
+@pytest.mark.parametrize("engine", [1, 2, 3, 4])
 def test_tinymt_cftp_doubling_schedule_matches_oracle(rt, orc, engine):
     D = rt.DominoTiler
     d = D.AztecDiamond(8)
@@ -178,7 +178,7 @@ def test_sampler_api(rt):
     s.close()
 
 
-@pytest.mark.parametrize("engine", [1, 2, 3])
+@pytest.mark.parametrize("engine", [1, 2, 3, 4])
 def test_full_size_order_1024_matches_threaded_oracle(rt, orc, engine):
     """Order-1024 Aztec diamond (N = 2054): 40 TinyMT steps of the two-periodic CFTP rule
     equal the oracle bit for bit."""
@@ -290,3 +290,66 @@ def test_resident_engine_wait_gives_up_and_the_sampler_stays_usable(rt, engine):
     ref.close()
     assert all(np.array_equal(a, b) for a, b in zip(got, want))
     assert not np.array_equal(want[0], tmin)
+
+
+@pytest.mark.gpu
+def test_bit_plane_engine_wait_gives_up_and_the_sampler_stays_usable(rt):
+    """The same failure detection on the bit-plane kernel (TinyMT mode): band 1 publishes none
+    of its boundary words, the neighbours' bounded waits run out, the host reads
+    RT_ERR_TIMEOUT, and the sampler then reproduces a fresh sampler's walk bit for bit."""
+    D = rt.DominoTiler
+    d = D.AztecDiamond(64)
+    tmax, tmin = D.MaxTiling(d), D.MinTiling(d)
+    n = rt.side_of(tmax)
+    tiler = rt.DominoTiler(rule="cftp", engine=4)
+    cols = rt.mt19937_colours(77, 64)
+
+    def fresh():
+        s = rt.DominoSampler(n, 2, tiler)
+        s.load(0, tmin)
+        s.load(1, tmax)
+        s.seed(5)
+        return s
+
+    s = fresh()
+    info = s.engine_info()
+    assert info["engine"] == 4 and info["bands"] >= 3
+    assert rt.lib().rt_dm_sampler_test_silent_band(s.h, 1, 4096) == rt.RT_OK
+    with pytest.raises(rt.RTError) as err:
+        s.run(cols)
+        s.sync()
+    assert err.value.status == rt.RT_ERR_TIMEOUT
+    assert rt.lib().rt_dm_sampler_test_silent_band(s.h, -1, 0) == rt.RT_OK
+    s.load(0, tmin)
+    s.load(1, tmax)
+    s.seed(5)
+    s.run(cols)
+    got = [s.store(0), s.store(1)]
+    s.close()
+    ref = fresh()
+    ref.run(cols)
+    want = [ref.store(0), ref.store(1)]
+    ref.close()
+    assert all(np.array_equal(a, b) for a, b in zip(got, want))
+    assert not np.array_equal(want[0], tmin)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("order", [1, 2, 5, 33, 130, 700])
+def test_bit_plane_engine_matches_the_run_kernel(rt, orc, order):
+    """Engine 4 (edge bit planes) against the oracle on Aztec diamonds from the smallest to
+    ones whose bands span many rows and words, from both extremal tilings, both chain counts,
+    with epochs (the in-kernel generator reseeding)."""
+    D = rt.DominoTiler
+    d = D.AztecDiamond(order)
+    tmax, tmin = D.MaxTiling(d), D.MinTiling(d)
+    n = rt.side_of(tmax)
+    steps, seeds = [37, 64], [12345 + order, 777]
+    for rule in ("cftp_twoperiodic", "plain"):
+        for start in (tmax, tmin):
+            g = start.copy()
+            rt.DominoTiler(rule=rule, a=1.0, b=0.5, engine=4).Walk(g, steps, seeds)
+            o = start.copy()
+            orc.walk_epochs_tinymt(o, n, steps, seeds, rule=3 if rule == "cftp_twoperiodic" else 0, a=1.0, b=0.5,
+                                   threads=8)
+            assert np.array_equal(g, o), (order, rule)
