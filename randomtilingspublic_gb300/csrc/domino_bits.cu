@@ -55,6 +55,7 @@ namespace {
 
 constexpr int K = kBitSlots;
 constexpr int kPhaseA = 8;  // slots of the boundary phase of a run (the plan puts boundary words there)
+constexpr int kMid = 12;     // the interior phase in two halves, the halo loads issued between
 constexpr int kGroup = 16;  // slots whose draws interleave (a warp skips empty groups)
 template <int V>
 using Int = std::integral_constant<int, V>;
@@ -138,7 +139,10 @@ __global__ void __launch_bounds__(kBitMaxWarps * 32, 1) k_bits(BitArgs a) {
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nwarps = (int)(blockDim.x >> 5);
   const int b = blockIdx.x;
   if (tid == 0) bd = a.bands[b];
-  if (tid < 4) srule[tid] = make_uint4(a.rule.lo_up[tid], a.rule.w_up[tid], a.rule.lo_dn[tid], a.rule.w_dn[tid]);
+  // Acceptance tests on the tempered word t0 (the draw is t0 >> 9): up when t0 < w_up 2^9,
+  // down when t0 - lo_dn 2^9 < w_dn 2^9 (unsigned); the host admits only intervals for which
+  // these products fit 32 bits and lo_up is 0, where the tests equal the reference's.
+  if (tid < 4) srule[tid] = make_uint4(a.rule.w_up[tid] << 9, a.rule.lo_dn[tid] << 9, a.rule.w_dn[tid] << 9, 0u);
   __syncthreads();
   const int r0 = bd.r0, r1 = bd.r1, wlo = bd.wlo;
   const int R = r1 - r0 + 2, Wn = bd.whi - wlo + 2;
@@ -247,19 +251,37 @@ __global__ void __launch_bounds__(kBitMaxWarps * 32, 1) k_bits(BitArgs a) {
   // The word's planes for colour t, the halo plane patched first with the neighbour's
   // publication tag - 1 where `patch` asks for it (the colour switched), or only waited for
   // (`wait`: so that the slot it overwrites next has been read).
-  auto word_setup = [&](int t, bool patch, bool wait, uint32_t tag, uint32_t& three, uint32_t& flip) {
+  // The exchange element a boundary word reads first (the band above's, else the band
+  // below's), loaded ahead of use: the load's round trip overlaps other work.
+  auto word_prefetch = [&](int t, uint32_t tag) -> uint64_t {
+    const uint2 e = sslot[warp * K + ws];
+    const int w = (int)(e.x & 0xffffu);
+    if (!(e.y & (kSlotHaloUp | kSlotHaloDn))) return 0ull;
+    const bool up = (e.y & kSlotHaloUp) != 0;
+    uint64_t x;
+    asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];"
+                 : "=l"(x)
+                 : "l"(xel(tag - 1, up ? b - 1 : b + 1, up ? 1 : 0, w, up ? 1 - t : t) + wc)
+                 : "memory");
+    return x;
+  };
+  auto word_setup = [&](int t, bool patch, bool wait, uint32_t tag, uint64_t pf, uint32_t& three, uint32_t& flip) {
     const uint2 e = sslot[warp * K + ws];
     const int i = (int)(e.x >> 16), w = (int)(e.x & 0xffffu);
     const int ri = i - r0 + 1, wi = w - wlo + 1;
     if ((patch || wait) && (e.y & (kSlotHaloUp | kSlotHaloDn))) {
+      const int pf_side = (e.y & kSlotHaloUp) ? 0 : 1;
 #pragma unroll
       for (int side = 0; side < 2; ++side) {  // a one-row band can have both
         const bool up = side == 0;
         if (!(e.y & (up ? kSlotHaloUp : kSlotHaloDn)) || failed) continue;
         uint32_t v[1];
-        if (!xb_wait<1>(xel(tag - 1, up ? b - 1 : b + 1, up ? 1 : 0, w, up ? 1 - t : t) + wc, tag - 1, v, a.error,
-                        a.max_spin))
+        if (side == pf_side && (uint32_t)(pf >> 32) == tag - 1) {
+          v[0] = (uint32_t)pf;  // the prefetched element already carries the tag
+        } else if (!xb_wait<1>(xel(tag - 1, up ? b - 1 : b + 1, up ? 1 : 0, w, up ? 1 - t : t) + wc, tag - 1, v,
+                               a.error, a.max_spin)) {
           failed = true;
+        }
         if (patch && !failed) {
           uint32_t* pl = up ? PL(ri - 1, 1 - t, wi) : PL(ri, t, wi);
           uint32_t* rc = up ? DL(1, 0, 1 - t, wi) : DL(1, 1, t, wi);
@@ -280,7 +302,9 @@ __global__ void __launch_bounds__(kBitMaxWarps * 32, 1) k_bits(BitArgs a) {
   };
   // L half-sweeps of slots [S0, S1) (compile-time: their draws interleave), those from nK on
   // absent; lane ℓ's word takes slot ℓ & 15's acceptance words (zero for the other slots).
-  auto draw_phase = [&](auto S0c, auto S1c, int nK, int L, uint4 rl, uint32_t& three, uint32_t flip) {
+  // `first` runs after the draws of the first half-sweep and before their update (the
+  // boundary phase sets its words up there, its halo loads overlapping those draws).
+  auto draw_phase = [&](auto S0c, auto S1c, int nK, int L, uint4 rl, uint32_t& three, uint32_t& flip, auto first) {
     constexpr int S0 = decltype(S0c)::value, S1 = decltype(S1c)::value;
     for (int hh = 0; hh < L; ++hh) {
       uint32_t up_m = 0u, dn_m = 0u;
@@ -299,36 +323,25 @@ __global__ void __launch_bounds__(kBitMaxWarps * 32, 1) k_bits(BitArgs a) {
           }
         }
         const uint32_t t0 = tmt_next_t0_mad(gen[s], m1, m2, tm);
-        const uint32_t bu = __ballot_sync(~0u, mul_hi(t0, 1u << 23) < rl.y);  // lo_up is 0 in TinyMT mode
-        const uint32_t bdn = __ballot_sync(~0u, mad_hi(t0, 1u << 23, 0u - rl.z) < rl.w);
+        const uint32_t bu = __ballot_sync(~0u, t0 < rl.x);
+        const uint32_t bdn = __ballot_sync(~0u, t0 - rl.y < rl.z);
         pick_if_lane(up_m, dn_m, bu, bdn, ws, s);
       }
+      if (hh == 0) first();
       three ^= (three & up_m) | (~three & flip & dn_m);
     }
   };
-  // The run's net toggles of lane ℓ's word back to the planes; boundary words add them to
-  // the band's own deltas and publish those under tag.
-  auto word_writeback = [&](int t, uint32_t tag, uint32_t three, uint32_t flip) {
+  // A boundary word's net toggles of the run added to the band's own deltas, which are
+  // published under tag (the planes are written back at the end of the run).
+  auto word_publish = [&](int t, uint32_t tag, uint32_t three, uint32_t flip) {
     const uint2 e = sslot[warp * K + ws];
+    if (!(e.y & (kSlotPubUp | kSlotPubDn))) return;
     const int i = (int)(e.x >> 16), w = (int)(e.x & 0xffffu);
     const int ri = i - r0 + 1, wi = w - wlo + 1;
-    const bool aligned = ((i + 1 - t) & 1) != 0;
-    uint32_t* pu = PL(ri - 1, 1 - t, wi) + wc;
-    const uint32_t T = three ^ (*pu & flip);  // cells flipped an odd number of times
-    if (T != 0u) {
-      *pu ^= T;
-      PL(ri, t, wi)[wc] ^= T;
-      PL(ri, 2, wi)[wc] ^= T;
-      if (aligned) {
-        PL(ri, 3, wi)[wc] ^= T;
-      } else {  // left edges: bit k - 1 of this word's HO, bit 31 of the previous word's
-        atomicXor(PL(ri, 3, wi) + wc, T >> 1);
-        if (T & 1u) atomicXor(PL(ri, 3, wi - 1) + wc, T << 31);
-      }
-      if (e.y & kSlotPubUp) DL(0, 0, 1 - t, wi)[wc] ^= T;
-      if (e.y & kSlotPubDn) DL(0, 1, t, wi)[wc] ^= T;
-    }
-    if (!silent && (e.y & (kSlotPubUp | kSlotPubDn))) {
+    const uint32_t T = three ^ (PL(ri - 1, 1 - t, wi)[wc] & flip);  // cells flipped an odd number of times
+    if (e.y & kSlotPubUp) DL(0, 0, 1 - t, wi)[wc] ^= T;
+    if (e.y & kSlotPubDn) DL(0, 1, t, wi)[wc] ^= T;
+    if (!silent) {
       const uint64_t tg = (uint64_t)tag << 32;
 #pragma unroll
       for (int side = 0; side < 2; ++side) {  // a one-row band can publish both ways
@@ -339,6 +352,26 @@ __global__ void __launch_bounds__(kBitMaxWarps * 32, 1) k_bits(BitArgs a) {
           asm volatile("st.relaxed.gpu.global.u64 [%0], %1;" ::"l"(g), "l"(tg | DL(0, side, colour, wi)[wc])
                        : "memory");
         }
+      }
+    }
+  };
+  // The run's net toggles of lane ℓ's word back to the planes.
+  auto word_writeback = [&](int t, uint32_t three, uint32_t flip) {
+    const uint2 e = sslot[warp * K + ws];
+    const int i = (int)(e.x >> 16), w = (int)(e.x & 0xffffu);
+    const int ri = i - r0 + 1, wi = w - wlo + 1;
+    const bool aligned = ((i + 1 - t) & 1) != 0;
+    uint32_t* pu = PL(ri - 1, 1 - t, wi) + wc;
+    const uint32_t T = three ^ (*pu & flip);
+    if (T != 0u) {
+      *pu ^= T;
+      PL(ri, t, wi)[wc] ^= T;
+      PL(ri, 2, wi)[wc] ^= T;
+      if (aligned) {
+        PL(ri, 3, wi)[wc] ^= T;
+      } else {  // left edges: bit k - 1 of this word's HO, bit 31 of the previous word's
+        atomicXor(PL(ri, 3, wi) + wc, T >> 1);
+        if (T & 1u) atomicXor(PL(ri, 3, wi - 1) + wc, T << 31);
       }
     }
   };
@@ -384,14 +417,24 @@ __global__ void __launch_bounds__(kBitMaxWarps * 32, 1) k_bits(BitArgs a) {
       const bool pull = j > 0 && t != t_last, wait = j > 0 && !pull;
       const bool mine = lane_ok && ws < nK;
       uint32_t three = 0u, flip = 0u;  // lanes without a word update zeros, branch-free
-      // Interior words first; the boundary words (slots below kPhaseA) then read the
-      // neighbours' publications of the previous run, which have had the whole interior phase
-      // to arrive.  (Boundary words the plan could not fit below kPhaseA read them at once.)
-      if (mine && ws >= kPhaseA) word_setup(t, pull, wait, tag, three, flip);
-      if (nK > kPhaseA) draw_phase(Int<kPhaseA>{}, Int<K>{}, nK, L, rl, three, flip);
-      if (mine && ws < kPhaseA) word_setup(t, pull, wait, tag, three, flip);
-      if (nK > 0) draw_phase(Int<0>{}, Int<kPhaseA>{}, nK, L, rl, three, flip);
-      if (mine) word_writeback(t, tag, three, flip);
+      // Interior words first; between their two halves the boundary words (slots below
+      // kPhaseA) load their halo elements, the neighbours' publications at the end of the
+      // previous run, which have had the first half to arrive and load in the second.  (Boundary
+      // words the plan could not fit below kPhaseA wait for theirs at once.)
+      if (mine && ws >= kPhaseA) word_setup(t, pull, wait, tag, 0ull, three, flip);
+      auto none = [] {};
+      if (nK > kPhaseA) draw_phase(Int<kPhaseA>{}, Int<kMid>{}, nK, L, rl, three, flip, none);
+      uint64_t pf = 0ull;
+      if (mine && ws < kPhaseA && (pull || wait)) pf = word_prefetch(t, tag);
+      if (nK > kMid) draw_phase(Int<kMid>{}, Int<K>{}, nK, L, rl, three, flip, none);
+      auto boundary_setup = [&] {
+        if (mine && ws < kPhaseA) word_setup(t, pull, wait, tag, pf, three, flip);
+      };
+      if (nK > 0) draw_phase(Int<0>{}, Int<kPhaseA>{}, nK, L, rl, three, flip, boundary_setup);
+      if (mine) {
+        word_publish(t, tag, three, flip);
+        word_writeback(t, three, flip);
+      }
       t_last = t;
     }
     if (__syncthreads_or(failed ? 1 : 0)) aborted = true;
@@ -536,6 +579,8 @@ rt_status BitPlan::build(const std::vector<int>& lo, const std::vector<int>& hi,
   // possible (binary search on its word count, bands filled greedily).
   const int G = std::max(1, std::min(nbands_max, cand_rows));
   auto warps_of = [](int64_t even, int64_t odd) { return (int)((even + K - 1) / K + (odd + K - 1) / K); };
+  // Rows are taken in pairs, so a band's first and last rows have different parities and its
+  // boundary words fill the warps of both parities.
   auto pack = [&](int64_t cap, std::vector<BitBand>* out) -> bool {
     out->clear();
     for (int r = 1; r <= rows;) {
@@ -543,14 +588,15 @@ rt_status BitPlan::build(const std::vector<int>& lo, const std::vector<int>& hi,
       bb.r0 = r;
       int64_t par[2] = {0, 0};
       while (r <= rows) {
+        const int take = std::min(2, rows - r + 1);
         int64_t p2[2] = {par[0], par[1]};
-        p2[r & 1] += cnt[r];
+        for (int q = 0; q < take; ++q) p2[(r + q) & 1] += cnt[r + q];
         const bool over = p2[0] + p2[1] > cap || warps_of(p2[0], p2[1]) > kBitMaxWarps;
         if (over && r > bb.r0) break;
-        if (warps_of(p2[0], p2[1]) > kBitMaxWarps) return false;  // one row alone is too wide
+        if (warps_of(p2[0], p2[1]) > kBitMaxWarps) return false;  // one row pair alone is too wide
         par[0] = p2[0];
         par[1] = p2[1];
-        ++r;
+        r += take;
       }
       bb.r1 = r;
       out->push_back(bb);
@@ -700,6 +746,13 @@ rt_status BitEngine::prepare(DmSampler& s) {
   if (s.border_candidates) {
     plan.why = "a flip candidate borders the cells the reference never rebuilds";
     return RT_OK;
+  }
+  for (int c = 0; c < 4; ++c) {  // the kernel tests the tempered word against interval ends x 2^9
+    const uint64_t lo_dn = s.rule.lo_dn[c], w_dn = s.rule.w_dn[c];
+    if (s.rule.lo_up[c] != 0 || s.rule.w_up[c] >= (1u << 23) || w_dn >= (1u << 23) || lo_dn + w_dn > (1u << 23)) {
+      plan.why = "rule intervals outside the bit-plane kernel's compare range";
+      return RT_OK;
+    }
   }
   const int nbands = s.eff_bands > 0 ? std::min(s.eff_bands, sms) : sms;
   stream = s.stream;
