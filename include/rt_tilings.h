@@ -77,7 +77,10 @@ typedef struct rt_walk_opts {
   int32_t engine;       /* 0: automatic; 1: per-half-sweep kernels; 2: resident persistent
                            kernel (the run kernel, which rebuilds the passive colour only where
                            the colour switches, else k_persist); 3: k_persist, the resident
-                           kernel that exchanges band rows every half-sweep.  Lozenges: 0
+                           kernel that exchanges band rows every half-sweep; 4: the bit-plane
+                           kernel (one bit per lattice edge, TinyMT mode, 1 or 2 swept chains,
+                           tilings whose flip candidates keep off the array's outer cells; 0
+                           prefers it where it applies).  Lozenges: 0
                            automatic, 1 per-step kernels, 2 the resident band kernel (TinyMT
                            without MTGP, or fast mode); the same tilings from every engine */
   void* cuda_stream;    /* cudaStream_t to run on; NULL = the library's own stream */
@@ -473,14 +476,16 @@ RT_API rt_status rt_domino_heightfunc_device(const int32_t* tiling, const int32_
                                              int32_t* out, void* cuda_stream);
 RT_API rt_status rt_domino_edge_indicators(const int32_t* tiling, int32_t n_side, uint32_t* counts);
 /* The engine the next run will use: out4 = {engine (1 per-half-sweep kernels, 2 the
-   resident run kernel, 3 the resident k_persist), flip-candidate generators held by the
-   resident kernel (sites with a TinyMT generator: units), CTAs (bands), units per thread
-   (column quads for the run kernel, sites or quads for k_persist)}. */
+   resident run kernel, 3 the resident k_persist, 4 the bit-plane kernel), flip-candidate
+   generators held by the resident kernel (sites with a TinyMT generator: units), CTAs
+   (bands), units per thread (column quads for the run kernel, sites or quads for k_persist,
+   32-cell words for the bit-plane kernel)}. */
 RT_API rt_status rt_dm_sampler_engine_info(rt_dm_sampler* s, int64_t* out4);
 /* Launch shape of the sampler's next runs (no counterpart in the reference: its kernels use
    one compile-time block shape, BLOCK_DIM 8 in src/Domino/dominokernel.cuh:4): engine (0
-   automatic, 1 per-half-sweep kernels, 2 the run kernel, 3 k_persist), bands (CTAs, 0: one
-   per SM) and threads per band (a multiple of 32 up to 1024, 0: 1024) of the run kernel.
+   automatic, 1 per-half-sweep kernels, 2 the run kernel, 3 k_persist, 4 the bit-plane
+   kernel), bands (CTAs, 0: one per SM) and threads per band (a multiple of 32 up to 1024,
+   0: 1024) of the run kernel.
    Results do not depend on the shape: every draw is keyed by its site.  Without this call,
    and with rt_walk_opts.engine 0, the autotuner's table (rt_tune_load) chooses when it has an
    entry.  out6 of rt_dm_sampler_launch_info = {engine, units, bands, units per thread,

@@ -289,6 +289,8 @@ class DominoTiler(_TinyMTTable):
     ``a``, ``b`` are the two-periodic weights the reference hard-codes (0.7, 1.0).
     ``rng`` is 'tinymt' (bit-exact with the reference's OpenCL path), 'mtgp' (cuRAND MTGP32
     as the reference's CUDA path draws it; also selected by LoadMTGP) or 'fast' (Philox).
+    ``engine``: 0 automatic, 1 per-half-sweep kernels, 2 the run kernel, 3 k_persist, 4 the
+    bit-plane kernel; every engine gives the same tilings.
     """
 
     def __init__(self, rule: str = "plain", rng: str = "tinymt", a: float = 0.7, b: float = 1.0,
@@ -895,8 +897,9 @@ class DominoSampler:
 
     def set_launch(self, engine: int = 0, bands: int = 0, threads: int = 0) -> None:
         """Launch shape of the next runs (rt_dm_sampler_set_launch): engine 0 automatic, 1
-        per-half-sweep kernels, 2 the run kernel, 3 k_persist; bands and threads per band of
-        the run kernel (0: defaults).  Results do not depend on it."""
+        per-half-sweep kernels, 2 the run kernel, 3 k_persist, 4 the bit-plane kernel; bands
+        (run and bit-plane kernels) and threads per band (run kernel; 0: defaults).  Results
+        do not depend on it."""
         _check(lib().rt_dm_sampler_set_launch(self.h, int(engine), int(bands), int(threads)))
 
 

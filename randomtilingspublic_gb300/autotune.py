@@ -2,9 +2,9 @@
 
 The reference launches every kernel with one compile-time block shape (BLOCK_DIM 8,
 src/Domino/dominokernel.cuh:4).  Here the shape of the resident sweep is a choice: which
-resident kernel (the run kernel, k_persist, or the per-half-sweep kernels), how many bands
-(CTAs, each a strip of rows - the tile) and how many threads per band (so how many column
-quads, four sites each, per thread).  For each Aztec-diamond order, chain count and random
+resident kernel (the bit-plane kernel, the run kernel, k_persist, or the per-half-sweep
+kernels), how many bands (CTAs, each a strip of rows - the tile) and, for the run kernel,
+how many threads per band (so how many column quads, four sites each, per thread).  For each Aztec-diamond order, chain count and random
 mode asked for, every candidate shape is timed on the GPU (CUDA-synchronised wall time of a
 fixed number of half-sweeps, best of a few repetitions) and the fastest is written to a
 table the library reads (rt_tune_load, or the RT_TUNE_FILE environment variable).  Entries
@@ -24,10 +24,12 @@ THREADS = (512, 640, 768, 896, 960, 992, 1024)
 
 
 def candidates(sms: int) -> list[tuple[int, int, int]]:
-    """(engine, bands, threads): the per-half-sweep kernels, k_persist, and the run kernel
-    over bands and threads per band."""
+    """(engine, bands, threads): the per-half-sweep kernels, k_persist, the run kernel over
+    bands and threads per band, and the bit-plane kernel (TinyMT only; its threads follow from
+    its plan) over bands."""
     out = [(1, 0, 0), (3, 0, 0)]
     for bands in sorted({sms, (3 * sms) // 4, sms // 2}, reverse=True):
+        out.append((4, bands, 0))
         for threads in THREADS:
             out.append((2, bands, threads))
     return out
@@ -57,7 +59,7 @@ def measure(rt, n, chains, rng, tmax, tmin, shape, half_sweeps: int = 256, reps:
         engine, bands, threads = shape
         if info["engine"] != engine or (engine == 2 and info["threads"] != threads):
             return None
-        used = (engine, info["bands"], threads) if engine == 2 else shape
+        used = (engine, info["bands"], threads) if engine in (2, 4) else shape
         cols = rt.mt19937_colours(12345, half_sweeps)
 
         def run():

@@ -659,23 +659,30 @@ rt_status BitPlan::build(const std::vector<int>& lo, const std::vector<int>& hi,
         cls[i & 1][edge ? 0 : 1].push_back(make_uint2(((uint32_t)i << 16) | (uint32_t)w, f));
       }
     }
-    const int base_warps = (int)((cls[0][0].size() + cls[0][1].size() + K - 1) / K) +
-                           (int)((cls[1][0].size() + cls[1][1].size() + K - 1) / K);
-    int extra = 0;
+    // Warps per parity class: enough for its words, and for its boundary words below kPhaseA
+    // where that fits; the band's remaining warps (up to kBitMaxWarps) then go one at a time to
+    // the class with the most words per warp, so that the work spreads over every warp.
+    const size_t n[2] = {cls[0][0].size() + cls[0][1].size(), cls[1][0].size() + cls[1][1].size()};
+    int cw[2];
+    for (int p = 0; p < 2; ++p) cw[p] = (int)((n[p] + K - 1) / K);
+    for (int p = 0; p < 2; ++p) {
+      const int want = (int)((cls[p][0].size() + kPhaseA - 1) / kPhaseA);
+      if (want > cw[p] && cw[0] + cw[1] + (want - cw[p]) <= kBitMaxWarps) cw[p] = want;
+    }
+    while (cw[0] + cw[1] < kBitMaxWarps) {
+      int best = -1;
+      for (int p = 0; p < 2; ++p)
+        if (n[p] > (size_t)cw[p] && (best < 0 || n[p] * cw[best] > n[best] * cw[p])) best = p;
+      if (best < 0) break;
+      ++cw[best];
+    }
     for (int p = 0; p < 2; ++p) {
       std::vector<uint2> list = cls[p][0];
       list.insert(list.end(), cls[p][1].begin(), cls[p][1].end());
       if (list.empty()) continue;
-      // Enough warps that every boundary word gets a slot below kPhaseA, when they fit.
-      int cw = (int)((list.size() + K - 1) / K);
-      const int want = (int)((cls[p][0].size() + kPhaseA - 1) / kPhaseA);
-      if (want > cw && base_warps + extra + (want - cw) <= kBitMaxWarps) {
-        extra += want - cw;
-        cw = want;
-      }
       const size_t first = per[g].size();
-      per[g].resize(first + cw, std::vector<uint2>());
-      for (size_t k = 0; k < list.size(); ++k) per[g][first + k % cw].push_back(list[k]);
+      per[g].resize(first + cw[p], std::vector<uint2>());
+      for (size_t k = 0; k < list.size(); ++k) per[g][first + k % cw[p]].push_back(list[k]);
     }
     warps = std::max(warps, (int)per[g].size());
     // Final reads: the words of the row above the band (published down by the band above)

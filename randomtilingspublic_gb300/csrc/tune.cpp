@@ -5,7 +5,7 @@
 // Text format, one entry per line ('#' starts a comment):
 //   <model> <n_lo> <n_hi> <chains> <rng> <engine> <bands> <threads> [<us per half-sweep>]
 // model: domino; rng: tinymt | fast; engine: 1 per-half-sweep kernels, 2 the run kernel,
-// 3 k_persist; bands, threads: 0 for the engine's default.
+// 3 k_persist, 4 the bit-plane kernel; bands, threads: 0 for the engine's default.
 #include <cstdlib>
 #include <fstream>
 #include <mutex>
@@ -47,7 +47,7 @@ rt_status parse_table(const std::string& path, std::vector<TuneEntry>* out) {
     if (rng == "tinymt") e.rng = RT_RNG_TINYMT;
     else if (rng == "fast") e.rng = RT_RNG_FAST;
     else return fail(RT_ERR_INVALID_ARGUMENT, where + "rng tinymt or fast");
-    if (e.n_lo > e.n_hi || e.chains < 1 || e.engine < 1 || e.engine > 3 || e.bands < 0 || e.threads < 0 ||
+    if (e.n_lo > e.n_hi || e.chains < 1 || e.engine < 1 || e.engine > 4 || e.bands < 0 || e.threads < 0 ||
         e.threads > 1024 || e.threads % 32)
       return fail(RT_ERR_INVALID_ARGUMENT, where + "field out of range");
     out->push_back(e);
