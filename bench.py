@@ -583,11 +583,12 @@ BENCH_CHECK_SHA256 = "b363844c09336dfecba5a174eb2a1a6b93f0091e55872316ca600e0238
 
 # DRAM bytes per launch of the resident sweep kernel (dram__bytes_read.sum +
 # dram__bytes_write.sum), from one ncu capture of the same launch of this workload
-# (profiles/k_runs_aztec1024.md, profiles/k_persist_aztec1024.md):
+# (profiles/k_bits_aztec1024.md, profiles/k_runs_aztec1024.md, profiles/k_persist_aztec1024.md):
 #   ncu --set full --clock-control none -k regex:<kernel> -s 3 -c 1 \
 #       python bench.py --no-cpu --no-batch --no-single --steps 2 --warmup 3 [--mode fast] [--engine 3]
 # Keyed by (rng mode, kernel name).  None where no capture of that kernel exists.
 NCU_TRAFFIC_BYTES = {
+    ("tinymt", "k_bits"): 23_789_312 + 7_424,
     ("tinymt", "k_runs"): 25_105_664 + 44_288,
     ("tinymt", "k_persist"): 23_068_672,
     ("fast", "k_persist"): 6_047_744,
