@@ -41,6 +41,8 @@
 
 #include <algorithm>
 #include <climits>
+#include <list>
+#include <mutex>
 #include <string>
 #include <type_traits>
 #include <vector>
@@ -397,8 +399,11 @@ __global__ void __launch_bounds__(kBitMaxWarps * 32, 1) k_bits(BitArgs a) {
     __syncthreads();
     const int nruns = ctl[1];
     int t_last = -1;
+    // Each run's descriptor is loaded one run ahead: its latency hides behind the run before.
+    uint32_t run_next = nruns > 0 ? __ldg(&a.runs[ctl[0]]) : 0u;
     for (int j = 0; j < nruns; ++j) {
-      const uint32_t run = __ldg(&a.runs[ctl[0] + j]);
+      const uint32_t run = run_next;
+      if (j + 1 < nruns) run_next = __ldg(&a.runs[ctl[0] + j + 1]);
       const int t = (int)(run >> 31), L = (int)(run & 0x3fffffffu);
       const bool epoch = (run >> 30) & 1u;
       if (j > 0 && __syncthreads_or(failed ? 1 : 0)) {
@@ -725,10 +730,47 @@ rt_status BitPlan::build(const std::vector<int>& lo, const std::vector<int>& hi,
   } while (0)
 
 BitEngine::~BitEngine() {
-  for (void* p : {(void*)d_bands, (void*)d_slots, (void*)d_fin, (void*)d_xbuf, (void*)d_error, (void*)d_runs,
-                  (void*)d_diff, (void*)d_epoch})
-    dev_free(p, stream);
+  for (void* p : {(void*)d_xbuf, (void*)d_error, (void*)d_runs, (void*)d_diff, (void*)d_epoch}) dev_free(p, stream);
 }
+
+BitDevPlan::~BitDevPlan() {
+  if (d_bands) cudaFree(d_bands);
+  if (d_slots) cudaFree(d_slots);
+  if (d_fin) cudaFree(d_fin);
+}
+
+namespace {
+
+// Plans of recent domains: building one is O(words) host work plus a few hundred KB of tables
+// to upload (0.7 ms at order 1024), while a CFTP or walk call creates a fresh sampler for the
+// same domain every time.  Keyed by everything the plan depends on.
+struct BitPlanKey {
+  int dev, N, P, nch, nbands;
+  size_t smem_limit;
+  std::vector<int> lo, hi;
+  bool operator==(const BitPlanKey& o) const {
+    return dev == o.dev && N == o.N && P == o.P && nch == o.nch && nbands == o.nbands && smem_limit == o.smem_limit &&
+           lo == o.lo && hi == o.hi;
+  }
+};
+struct BitPlanEntry {
+  BitPlanKey key;
+  BitPlan plan;  // without its tables
+  std::shared_ptr<BitDevPlan> dev;
+};
+std::mutex g_bit_plan_mu;
+std::list<BitPlanEntry>* g_bit_plans = new std::list<BitPlanEntry>();  // never destroyed: no CUDA calls at exit
+constexpr size_t kBitPlanCacheEntries = 8;
+
+// The cached tables are still those of the current context (a cudaDeviceReset invalidates them).
+bool bit_dev_plan_valid(const BitDevPlan& d) {
+  cudaPointerAttributes at{};
+  const bool ok = cudaPointerGetAttributes(&at, d.d_slots) == cudaSuccess && at.type == cudaMemoryTypeDevice;
+  cudaGetLastError();
+  return ok;
+}
+
+}  // namespace
 
 rt_status BitEngine::prepare(DmSampler& s) {
   ready = false;
@@ -763,8 +805,44 @@ rt_status BitEngine::prepare(DmSampler& s) {
   }
   const int nbands = s.eff_bands > 0 ? std::min(s.eff_bands, sms) : sms;
   stream = s.stream;
-  if (rt_status st = plan.build(s.cand_lo, s.cand_hi, s.N, s.P, s.active, nbands, (size_t)optin - 1024)) return st;
-  if (!plan.ok) return RT_OK;
+  BitPlanKey key{dev_id, s.N, s.P, s.active, nbands, (size_t)optin - 1024, s.cand_lo, s.cand_hi};
+  dev.reset();
+  {
+    std::lock_guard<std::mutex> lock(g_bit_plan_mu);
+    for (auto it = g_bit_plans->begin(); it != g_bit_plans->end(); ++it) {
+      if (!(it->key == key)) continue;
+      if (!bit_dev_plan_valid(*it->dev)) {
+        g_bit_plans->erase(it);
+        break;
+      }
+      plan = it->plan;
+      dev = it->dev;
+      g_bit_plans->splice(g_bit_plans->begin(), *g_bit_plans, it);  // most recent first
+      break;
+    }
+  }
+  if (!dev) {
+    if (rt_status st = plan.build(s.cand_lo, s.cand_hi, s.N, s.P, s.active, nbands, (size_t)optin - 1024)) return st;
+    if (!plan.ok) return RT_OK;
+    auto d = std::make_shared<BitDevPlan>();
+    const size_t nb = plan.bands.size(), nfin = std::max<size_t>(1, plan.fin.size());
+    RT_CUDA_B(cudaMalloc(&d->d_bands, nb * sizeof(BitBand)));
+    RT_CUDA_B(cudaMalloc(&d->d_slots, plan.slots.size() * sizeof(uint2)));
+    RT_CUDA_B(cudaMalloc(&d->d_fin, nfin * sizeof(uint32_t)));
+    RT_CUDA_B(cudaMemcpy(d->d_bands, plan.bands.data(), nb * sizeof(BitBand), cudaMemcpyHostToDevice));
+    RT_CUDA_B(cudaMemcpy(d->d_slots, plan.slots.data(), plan.slots.size() * sizeof(uint2), cudaMemcpyHostToDevice));
+    if (!plan.fin.empty())
+      RT_CUDA_B(cudaMemcpy(d->d_fin, plan.fin.data(), plan.fin.size() * sizeof(uint32_t), cudaMemcpyHostToDevice));
+    plan.slots = std::vector<uint2>();
+    plan.fin = std::vector<uint32_t>();
+    dev = d;
+    std::lock_guard<std::mutex> lock(g_bit_plan_mu);
+    g_bit_plans->push_front(BitPlanEntry{std::move(key), plan, d});
+    if (g_bit_plans->size() > kBitPlanCacheEntries) g_bit_plans->pop_back();
+  }
+  d_bands = dev->d_bands;
+  d_slots = dev->d_slots;
+  d_fin = dev->d_fin;
   kernel = dm_bits_kernel_ptr(s.tmt_params != nullptr, s.active);
   if (!kernel) {
     plan.ok = false;
@@ -779,21 +857,11 @@ rt_status BitEngine::prepare(DmSampler& s) {
     plan.why = "bands cannot all be resident";
     return RT_OK;
   }
-  for (void** p : {(void**)&d_bands, (void**)&d_slots, (void**)&d_fin, (void**)&d_xbuf, (void**)&d_error}) {
+  for (void** p : {(void**)&d_xbuf, (void**)&d_error}) {
     dev_free(*p, stream);
     *p = nullptr;
   }
   const size_t nb = plan.bands.size();
-  if (rt_status st = dev_alloc(&d_bands, nb * sizeof(BitBand), stream)) return st;
-  if (rt_status st = dev_alloc(&d_slots, plan.slots.size() * sizeof(uint2), stream)) return st;
-  if (rt_status st = dev_alloc(&d_fin, std::max<size_t>(1, plan.fin.size()) * sizeof(uint32_t), stream)) return st;
-  RT_CUDA_B(cudaMemcpyAsync(d_bands, plan.bands.data(), nb * sizeof(BitBand), cudaMemcpyHostToDevice, stream));
-  RT_CUDA_B(cudaMemcpyAsync(d_slots, plan.slots.data(), plan.slots.size() * sizeof(uint2), cudaMemcpyHostToDevice,
-                            stream));
-  if (!plan.fin.empty())
-    RT_CUDA_B(cudaMemcpyAsync(d_fin, plan.fin.data(), plan.fin.size() * sizeof(uint32_t), cudaMemcpyHostToDevice,
-                              stream));
-  // The host tables must outlive the asynchronous copies: they stay in `plan`.
   xwords = (s.P + 31) / 32 + 1;
   xbuf_bytes = (size_t)2 * nb * 2 * xwords * 2 * s.active * sizeof(uint64_t);
   if (rt_status st = dev_alloc(&d_xbuf, xbuf_bytes, stream)) return st;

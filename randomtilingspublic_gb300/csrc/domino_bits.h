@@ -76,12 +76,22 @@ struct BitPlan {
                   size_t smem_limit);
 };
 
+// A plan's device tables, shared by every engine whose domain and launch shape give the
+// same plan (domino_bits.cu keeps a small cache of recent plans).
+struct BitDevPlan {
+  BitBand* d_bands = nullptr;
+  uint2* d_slots = nullptr;
+  uint32_t* d_fin = nullptr;
+  ~BitDevPlan();
+};
+
 struct BitEngine {
-  BitPlan plan;  // slot tables live on the device
+  BitPlan plan;  // without its slot and final-read tables, which live on the device in `dev`
   bool ready = false;
   int nch = 0;
   void* kernel = nullptr;
-  BitBand* d_bands = nullptr;
+  std::shared_ptr<BitDevPlan> dev;
+  BitBand* d_bands = nullptr;  // dev's tables
   uint2* d_slots = nullptr;
   uint32_t* d_fin = nullptr;
   uint64_t* d_xbuf = nullptr;
