@@ -400,6 +400,89 @@ def mid_batch_leg(rt) -> dict:
     return out
 
 
+# Config 4's full size ranges, at a fixed look-back: 8192 instances, Aztec orders U[16, 512]
+# (half of them 2-periodic, a = 1, b ~ U[0.3, 1]) and hexagon sides U[8, 256], each run for
+# one coupled attempt of FULL_SWEEPS sweeps from the extremal tilings (coalesced or not).
+# Exact samples at these sizes take hours for any implementation of the reference's chain
+# (the look-back grows like the order squared, and 8-16x per doubling of the order at
+# b <= 0.6), so this leg measures the batch's flip-attempt throughput over the real size
+# mix, against the same attempts made one instance at a time.
+FULL_ORDERS, FULL_SIDES, FULL_B = (16, 512), (8, 256), (0.3, 1.0)
+FULL_SWEEPS = 32
+FULL_PLAIN = 64  # instances drawn across the mix for the one-at-a-time baseline
+
+
+def full_range_leg(rt, instances: int = BATCH_INSTANCES) -> dict:
+    """rt_cftp_batch over config 4's full size ranges (dominoes in clusters of CTAs where one
+    CTA is too small), one attempt per instance; against rt_domino_cftp / rt_lozenge_cftp
+    one instance at a time (FULL_PLAIN of them).  Rates count flip attempts over both chains:
+    2 x FULL_SWEEPS x the instance's interior vertices."""
+    import ctypes as C
+
+    D, L = rt.DominoTiler, rt.LozengeTiler
+    rng = np.random.default_rng(20261204)
+    cache, jobs, flips = {}, [], []
+    for k in range(instances):
+        if k % 2 == 0:
+            n = int(rng.integers(FULL_ORDERS[0], FULL_ORDERS[1] + 1))
+            if ("d", n) not in cache:
+                d = D.AztecDiamond(n)
+                cache[("d", n)] = (D.MaxTiling(d), D.MinTiling(d))
+            weighted = (k // 2) % 2 == 1
+            b = float(rng.uniform(*FULL_B)) if weighted else 1.0
+            jobs.append({"model": "domino", "tmax": cache[("d", n)][0], "tmin": cache[("d", n)][1], "seed": k,
+                         "stream": k & 0xFFFF, "rule": "cftp_twoperiodic" if weighted else "cftp", "a": 1.0, "b": b,
+                         "first_steps": FULL_SWEEPS, "max_attempts": 1})
+            flips.append(2 * FULL_SWEEPS * (2 * n * n - 2 * n + 1))
+        else:
+            sd = int(rng.integers(FULL_SIDES[0], FULL_SIDES[1] + 1))
+            if ("l", sd) not in cache:
+                d = L.Hexagon(sd)
+                cache[("l", sd)] = (L.MaxTiling(d), L.MinTiling(d))
+            jobs.append({"model": "lozenge", "tmax": cache[("l", sd)][0], "tmin": cache[("l", sd)][1], "seed": k,
+                         "stream": k & 0xFFFF, "first_steps": FULL_SWEEPS, "max_attempts": 1})
+            flips.append(2 * FULL_SWEEPS * (3 * sd * sd - 3 * sd + 1))
+    rt.cftp_batch(jobs[:2])  # warm-up
+    t0 = time.perf_counter()
+    outs, attempts, stats = rt.cftp_batch(jobs)
+    wall = time.perf_counter() - t0
+    pick = np.random.default_rng(8).choice(len(jobs), size=min(FULL_PLAIN, len(jobs)), replace=False)
+    plain_dev, plain_wall, plain_flips, same = 0.0, 0.0, 0, 0
+    for k in pick:
+        job = jobs[int(k)]
+        a_, b_ = np.ascontiguousarray(job["tmax"], np.int32), np.ascontiguousarray(job["tmin"], np.int32)
+        out, st = np.zeros_like(a_), rt.CftpStats()
+        n = rt.side_of(a_)
+        t1 = time.perf_counter()
+        if job["model"] == "domino":
+            o = rt.DominoTiler(rule=job["rule"], rng="fast", a=job["a"], b=job["b"], fast_stream=job["stream"]).opts()
+            status = rt.lib().rt_domino_cftp(rt._ptr(a_), rt._ptr(b_), n, int(job["seed"]), FULL_SWEEPS, 1, 1,
+                                             C.byref(o), rt._ptr(out), C.byref(st))
+        else:
+            o = rt.LozengeTiler(rng="fast", fast_stream=job["stream"]).opts()
+            status = rt.lib().rt_lozenge_cftp(rt._ptr(a_), rt._ptr(b_), n, int(job["seed"]), FULL_SWEEPS, 1, 1,
+                                              C.byref(o), rt._ptr(out), C.byref(st))
+        plain_wall += time.perf_counter() - t1
+        if status not in (rt.RT_OK, rt.RT_ERR_NOT_COALESCED):
+            raise rt.RTError(status, rt.lib().rt_last_error().decode())
+        plain_dev += st.seconds
+        plain_flips += flips[int(k)]
+        same += np.array_equal(out, outs[int(k)])
+    rate = float(np.sum(flips)) / stats["seconds"]
+    plain_rate = plain_flips / plain_dev
+    return {"workload": f"{instances} CFTP instances over config 4's full size ranges: Aztec orders "
+                        f"U{list(FULL_ORDERS)} (half 2-periodic, a=1, b~U{list(FULL_B)}) and hexagon sides "
+                        f"U{list(FULL_SIDES)}; one coupled attempt of {FULL_SWEEPS} sweeps each (fixed look-back: "
+                        "exact samples at these sizes take hours for any implementation), fast mode",
+            "flip_attempts": int(np.sum(flips)), "flip_attempts_per_s": rate, "kernel_s": stats["seconds"],
+            "wall_s": wall, "wall_flip_attempts_per_s": float(np.sum(flips)) / wall,
+            "plain_wall_flip_attempts_per_s": plain_flips / plain_wall, "cluster_instances": stats["cluster_instances"],
+            "single_instances": stats["single_instances"], "ctas": stats["ctas"],
+            "plain_flip_attempts_per_s": plain_rate, "plain_instances": len(pick), "plain_equal_to_batched": int(same),
+            "batched_over_plain": rate / plain_rate,
+            "api": "rt_cftp_batch vs rt_domino_cftp / rt_lozenge_cftp one at a time (device time both)"}
+
+
 def single_instance_leg(rt) -> dict:
     """The other single-instance workloads: one coupled max/min CFTP attempt on the lozenge
     hexagon of side 512, 10^5 sweeps of bibone tilings of the 512 x 512 rhombus from the brick
@@ -731,11 +814,12 @@ def run_ours(args) -> None:
                          f"2 attempts, {threads} host threads"}
     s.close()
     batched = serving = single = None
-    mid = None
+    mid = full = None
     if rank == 0 and not args.no_batch:
         batched = batched_leg(rt, args.batch_instances)
         serving = None if args.no_serve else serving_leg(rt)
         mid = mid_batch_leg(rt)
+        full = None if args.no_full else full_range_leg(rt, args.batch_instances)
     if rank == 0 and not args.no_single:
         single = single_instance_leg(rt)
     if rank == 0:
@@ -751,6 +835,7 @@ def run_ours(args) -> None:
                                   "units_per_thread": info["units_per_thread"]}},
             "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches, "clocks": clocks,
             "check": check, "batched_cftp": batched, "served_cftp": serving, "batched_cftp_clusters": mid,
+            "batched_cftp_full_range": full,
             "single_instance": single,
         }
         print(json.dumps(line))
@@ -769,6 +854,7 @@ def main() -> None:
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-batch", action="store_true")
     ap.add_argument("--no-serve", action="store_true")
+    ap.add_argument("--no-full", action="store_true", help="skip the full-size-range batch leg")
     ap.add_argument("--batch-instances", type=int, default=BATCH_INSTANCES)
     ap.add_argument("--no-single", action="store_true")
     ap.add_argument("--no-tune", action="store_true", help="ignore the autotuner's table")

@@ -14,9 +14,11 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <chrono>
 #include <cmath>
 #include <cstring>
+#include <memory>
 #include <string>
 #include <thread>
 #include <vector>
@@ -464,6 +466,46 @@ rt_status split_into(const int32_t* t, const DevInstance& d, uint8_t* dst) {
   return RT_OK;
 }
 
+// The split for the batch's host threads: false when a value is out of range.
+bool split_ok(const int32_t* t, const DevInstance& d, uint8_t* dst) {
+  const int N = d.N, ncol = d.model == RT_MODEL_DOMINO ? 2 : 3;
+  const size_t plane = (size_t)N * d.P;
+  std::memset(dst, 0, plane * ncol);
+  for (int i = 0; i < N; ++i) {
+    const int32_t* row = t + (size_t)i * N;
+    if (ncol == 2) {
+      uint8_t* b = dst + (size_t)i * d.P;  // black (i + j even) in plane 1, white in plane 0
+      for (int j = 0; j < N; ++j) {
+        const int32_t v = row[j];
+        if ((uint32_t)v > 63u) return false;
+        b[(((i + j) & 1) == 0 ? plane : 0) + (size_t)(j >> 1)] = (uint8_t)v;
+      }
+    } else {
+      for (int j = 0; j < N; ++j) {
+        const int32_t v = row[j];
+        if ((uint32_t)v > 63u) return false;
+        const int c = ((j - i) % 3 + 3) % 3;
+        dst[(size_t)c * plane + (size_t)i * d.P + j / 3] = (uint8_t)v;
+      }
+    }
+  }
+  return true;
+}
+
+size_t chain_bytes_of(const DevInstance& d) { return (size_t)(d.model == RT_MODEL_DOMINO ? 2 : 3) * d.N * d.P; }
+
+// Runs `work` (which takes items off a shared counter) on up to 32 host threads, fewer for
+// few items.
+template <class F>
+void run_on_host_threads(F work, size_t items) {
+  const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
+  const unsigned n = (unsigned)std::min<size_t>(std::min(32u, hw), std::max<size_t>(1, items / 4));
+  std::vector<std::thread> pool;
+  for (unsigned k = 1; k < n; ++k) pool.emplace_back(work);
+  work();
+  for (std::thread& th : pool) th.join();
+}
+
 void merge_from(const uint8_t* src, const DevInstance& d, int32_t* t) {
   const int N = d.N, ncol = d.model == RT_MODEL_DOMINO ? 2 : 3;
   const size_t plane = (size_t)N * d.P;
@@ -538,22 +580,36 @@ RT_API rt_status rt_cftp_batch(rt_cftp_instance* inst, int32_t count, void* cuda
     groups.push_back(g);
   }
   std::sort(large_idx.begin(), large_idx.end());
-  // one tiling buffer: per packed instance its max, min and output chains
-  size_t bytes = 0;
+  // One tiling buffer: every packed instance's max and min chains, then every output chain
+  // (so that the copy back is one contiguous region of the outputs alone).
+  size_t bytes_in = 0, bytes = 0;
+  for (int k : packed_idx) bytes_in += 2 * chain_bytes_of(all[(size_t)k]);
+  bytes = bytes_in;
   for (int k : packed_idx) {
     DevInstance d = all[(size_t)k];
-    const size_t chain = (size_t)(d.model == RT_MODEL_DOMINO ? 2 : 3) * d.N * d.P;
-    d.off_max = (int64_t)bytes;
-    d.off_min = (int64_t)(bytes + chain);
-    d.off_out = (int64_t)(bytes + 2 * chain);
-    bytes += 3 * chain;
+    const size_t chain = chain_bytes_of(d);
+    d.off_max = (int64_t)(dv.empty() ? 0 : dv.back().off_min + chain_bytes_of(dv.back()));
+    d.off_min = d.off_max + (int64_t)chain;
+    d.off_out = (int64_t)bytes;
+    bytes += chain;
     dv.push_back(d);
   }
-  std::vector<uint8_t> host(bytes, 0);
-  for (size_t s = 0; s < dv.size(); ++s) {
-    const rt_cftp_instance& x = inst[packed_idx[s]];
-    if (rt_status st = split_into(x.tmax, dv[s], host.data() + dv[s].off_max)) return st;
-    if (rt_status st = split_into(x.tmin, dv[s], host.data() + dv[s].off_min)) return st;
+  // The colour splits of all instances, on the host's cores (the staging buffer is not
+  // zero-filled first: each split writes its whole region).
+  std::unique_ptr<uint8_t[]> host_buf(new uint8_t[std::max<size_t>(bytes, 1)]);
+  uint8_t* const host = host_buf.get();
+  {
+    std::atomic<int> next{0}, bad{0};
+    auto work = [&] {
+      for (int s2 = next++; s2 < (int)dv.size(); s2 = next++) {
+        const rt_cftp_instance& x = inst[packed_idx[(size_t)s2]];
+        if (!split_ok(x.tmax, dv[(size_t)s2], host + dv[(size_t)s2].off_max) ||
+            !split_ok(x.tmin, dv[(size_t)s2], host + dv[(size_t)s2].off_min))
+          bad = 1;
+      }
+    };
+    run_on_host_threads(work, dv.size());
+    if (bad) return fail(RT_ERR_INVALID_ARGUMENT, "cftp instance: tiling values out of range");
   }
   for (int k : large_idx)
     for (const int32_t* t : {inst[k].tmax, inst[k].tmin})
@@ -579,7 +635,8 @@ RT_API rt_status rt_cftp_batch(rt_cftp_instance* inst, int32_t count, void* cuda
       break;
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
-    cudaMemcpyAsync(d_tilings, host.data(), bytes, cudaMemcpyHostToDevice, stream);
+    cudaMemcpyAsync(d_tilings, host, bytes_in, cudaMemcpyHostToDevice, stream);
+    cudaMemsetAsync(d_tilings + bytes_in, 0, bytes - bytes_in, stream);
     cudaMemcpyAsync(d_inst, dv.data(), dv.size() * sizeof(DevInstance), cudaMemcpyHostToDevice, stream);
     cudaMemsetAsync(d_queue, 0, nq * sizeof(unsigned), stream);
     std::vector<InstState> st0((size_t)std::max(1, n_small));
@@ -613,7 +670,7 @@ RT_API rt_status rt_cftp_batch(rt_cftp_instance* inst, int32_t count, void* cuda
     }
     if (status != RT_OK) break;
     cudaEventRecord(e1, stream);
-    cudaMemcpyAsync(host.data(), d_tilings, bytes, cudaMemcpyDeviceToHost, stream);
+    cudaMemcpyAsync(host + bytes_in, d_tilings + bytes_in, bytes - bytes_in, cudaMemcpyDeviceToHost, stream);
     cudaMemcpyAsync(dv.data(), d_inst, dv.size() * sizeof(DevInstance), cudaMemcpyDeviceToHost, stream);
     unsigned err_word = 0;
     cudaMemcpyAsync(&err_word, d_queue + 2, sizeof err_word, cudaMemcpyDeviceToHost, stream);
@@ -629,13 +686,18 @@ RT_API rt_status rt_cftp_batch(rt_cftp_instance* inst, int32_t count, void* cuda
     float ms = 0.f;
     cudaEventElapsedTime(&ms, e0, e1);
     seconds += ms * 1e-3;
-    for (int s = 0; s < n_packed; ++s) {
-      rt_cftp_instance& x = inst[packed_idx[s]];
-      const DevInstance& d = dv[s];
-      merge_from(host.data() + d.off_out, d, x.out);
-      x.attempts = d.attempts;
-      x.final_steps = d.final_half_sweeps;
-      coalesced += d.attempts > 0;
+    std::atomic<int> next{0};
+    run_on_host_threads(
+        [&] {
+          for (int s2 = next++; s2 < n_packed; s2 = next++)
+            merge_from(host + dv[(size_t)s2].off_out, dv[(size_t)s2], inst[packed_idx[(size_t)s2]].out);
+        },
+        (size_t)n_packed);
+    for (int s2 = 0; s2 < n_packed; ++s2) {
+      rt_cftp_instance& x = inst[packed_idx[(size_t)s2]];
+      x.attempts = dv[(size_t)s2].attempts;
+      x.final_steps = dv[(size_t)s2].final_half_sweeps;
+      coalesced += dv[(size_t)s2].attempts > 0;
     }
   } while (false);
   if (e0) cudaEventDestroy(e0);
