@@ -475,6 +475,15 @@ RT_API rt_status rt_dm_sampler_accumulate_heights(rt_dm_sampler* s, int32_t chai
 RT_API rt_status rt_domino_heightfunc_device(const int32_t* tiling, const int32_t* domain, int32_t n_side,
                                              int32_t* out, void* cuda_stream);
 RT_API rt_status rt_domino_edge_indicators(const int32_t* tiling, int32_t n_side, uint32_t* counts);
+/* Exact edge-placement probabilities of the Aztec diamond of the given order (the tiling of
+   rt_domino_aztec_diamond, N = 2 order + 6) under the reference's weights: a horizontal
+   domino weighs a when its left face's column is odd, else b; a vertical one a when its top
+   face's row is even, else b (a = b: uniform).  out (2 N^2 doubles, cap entries) receives
+   them in the layout of the edge counters above, so counts / samples estimates out.
+   Generalized domino shuffling (Propp 2003) on the device, one launch per order level, on
+   cuda_stream (NULL: the default stream); synchronous.  No counterpart in the reference. */
+RT_API rt_status rt_domino_aztec_edge_probs(int32_t order, double a, double b, double* out, int64_t cap,
+                                            void* cuda_stream);
 /* The engine the next run will use: out4 = {engine (1 per-half-sweep kernels, 2 the
    resident run kernel, 3 the resident k_persist, 4 the bit-plane kernel), flip-candidate
    generators held by the resident kernel (sites with a TinyMT generator: units), CTAs

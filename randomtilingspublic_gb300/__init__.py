@@ -125,6 +125,7 @@ _SIGNATURES = {
     "rt_dm_sampler_accumulate_heights": (C.c_int32, [_P, C.c_int32, _P, _P]),
     "rt_domino_heightfunc_device": (C.c_int32, [_P, _P, C.c_int32, _P, _P]),
     "rt_domino_edge_indicators": (C.c_int32, [_P, C.c_int32, _P]),
+    "rt_domino_aztec_edge_probs": (C.c_int32, [C.c_int32, C.c_double, C.c_double, _P, C.c_int64, _P]),
     "rt_dm_sampler_sync": (C.c_int32, [_P]),
     "rt_dm_sampler_stream": (C.c_void_p, [_P]),
     "rt_dm_sampler_interior_vertices": (C.c_int64, [_P]),
@@ -1068,6 +1069,17 @@ def edge_indicators(t, counts=None) -> np.ndarray:
         counts = np.zeros(2 * n * n, np.uint32)
     _check(lib().rt_domino_edge_indicators(_ptr(tt), n, _ptr(counts)))
     return counts
+
+
+def aztec_edge_probs(order: int, a: float = 1.0, b: float = 1.0) -> np.ndarray:
+    """Exact edge-placement probabilities of DominoTiler.AztecDiamond(order) under the weights
+    a / b of the two-periodic rule (a = b: uniform), in the layout of edge_indicators, so that
+    counts / samples estimates them (rt_domino_aztec_edge_probs: generalized domino shuffling
+    on the device)."""
+    n = 2 * int(order) + 6
+    out = np.zeros(2 * n * n, np.float64)
+    _check(lib().rt_domino_aztec_edge_probs(int(order), float(a), float(b), _ptr(out), out.size, None))
+    return out
 
 
 def tune_load(path) -> None:

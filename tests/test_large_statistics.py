@@ -2,7 +2,8 @@
 and lozenge placement frequencies on a larger hexagon, against exactly computed values.
 
 Exact edge-placement probabilities come from the Kasteleyn matrix (tests/test_edge_densities.py:
-uniform and two-periodic weights).  The height function (TilingToHeightfunc,
+uniform and two-periodic weights) up to Aztec order 44, and from generalized domino shuffling
+(shuffling_edge_probs below, equal to the Kasteleyn values where both hold) beyond.  The height function (TilingToHeightfunc,
 DominoTiler.cpp:555-593) changes along a lattice edge u -> w by s (1 - 4 x), where
 s = +-1 is the step of the reference's walk (its axis and the colour of u) and x = 1 when a
 domino covers the edge (each square has exactly one covered side, so the three free sides'
@@ -13,6 +14,7 @@ CFTP samples (8000 per case) are compared with both exact quantities: every edge
 binomial tail (Bonferroni, family-wise level 1e-3), every vertex's mean height within |z| < 5
 where the height moves often enough for the normal approximation, and by a bound on the
 count of moves elsewhere."""
+import os
 from collections import deque
 
 import numpy as np
@@ -85,6 +87,145 @@ def heights_from_edges(d, cover):
     return h
 
 
+def shuffling_edge_probs(d, a, b, dtype=np.float64):
+    """Exact placement probabilities of the two-periodic weighted Aztec diamond d (the weights
+    of kasteleyn_edge_probs) by generalized domino shuffling (J. Propp, "Generalized
+    domino-shuffling", Theoret. Comput. Sci. 303 (2003) 267-301), in the same [2][N][N] layout.
+
+    Cells of the order-n diamond are the lattice points (R, C) inside it with R + C + n odd.
+    In the rotated coordinates s = R + C, t = R - C they form an n x n grid, and a cell's four
+    edges (the grid segments meeting at its point, each crossed by one domino position) fill a
+    2 x 2 block of a 2n x 2n array: up (0, 0), left (0, 1), right (1, 0), down (1, 1), so that
+    opposite edges sit diagonally opposite.  Urban renewal at every cell gives each edge its
+    opposite's weight over D = w00 w11 + w01 w10; dropping the array's outer rows and columns
+    leaves the weights of the order n-1 diamond, whose cells are the other parity of points.
+    Probabilities go back up the way the shuffling builds a tiling: a domino of the order
+    k-1 tiling slides across its cell to the opposite edge, and a cell that nothing slides
+    into (probability 1 minus its four order k-1 probabilities, the array padded by zeros) is
+    filled by a pair, up and down with probability w00 w11 / D, left and right w01 w10 / D.
+    Every term is positive but the one complement, so the values stay accurate at any order
+    (at order 256 double and extended precision agree to 1e-14), where the Kasteleyn inverse
+    loses all digits beyond order 48."""
+    M = int(np.sqrt(d.size))
+    F = np.asarray(d).reshape(M, M)
+    rows = np.flatnonzero(F.any(axis=1))
+    cols = np.flatnonzero(F.any(axis=0))
+    n = len(rows) // 2
+    r0, c0 = int(rows[0]), int(cols[0])
+    i, j = np.meshgrid(np.arange(n), np.arange(n), indexing="ij")
+    R = (2 * i + 2 * j + 2) // 2 + r0  # s = 2i + n + 1, t = 2j - n + 1 in the diamond's frame
+    C = (2 * i - 2 * j + 2 * n) // 2 + c0
+    ref = np.zeros((M, M), np.int8)
+    ref[r0:r0 + 2 * n, c0:c0 + 2 * n] = [[1 if abs(r - n + 0.5) + abs(c - n + 0.5) <= n else 0
+                                          for c in range(2 * n)] for r in range(2 * n)]
+    assert np.array_equal(F, ref), "not an Aztec diamond"
+    W = np.empty((2 * n, 2 * n), dtype)
+    h = np.where((C - 1) % 2 == 1, a, b)  # horizontal domino: a when its left face's column is odd
+    v = np.where((R - 1) % 2 == 0, a, b)  # vertical domino: a when its top face's row is even
+    W[0::2, 0::2] = W[1::2, 1::2] = h
+    W[0::2, 1::2] = W[1::2, 0::2] = v
+    levels = [W]
+    for _ in range(n - 1):
+        w00, w01, w10, w11 = W[0::2, 0::2], W[0::2, 1::2], W[1::2, 0::2], W[1::2, 1::2]
+        D = w00 * w11 + w01 * w10
+        X = np.empty_like(W)
+        X[0::2, 0::2], X[1::2, 1::2], X[0::2, 1::2], X[1::2, 0::2] = w11 / D, w00 / D, w10 / D, w01 / D
+        W = X[1:-1, 1:-1].copy()
+        levels.append(W)
+    P = np.zeros((0, 0), dtype)
+    for W in reversed(levels):
+        Q = np.zeros(W.shape, dtype)
+        Q[1:-1, 1:-1] = P
+        w00, w01, w10, w11 = W[0::2, 0::2], W[0::2, 1::2], W[1::2, 0::2], W[1::2, 1::2]
+        D = w00 * w11 + w01 * w10
+        q00, q01, q10, q11 = Q[0::2, 0::2], Q[0::2, 1::2], Q[1::2, 0::2], Q[1::2, 1::2]
+        empty = 1 - (q00 + q01 + q10 + q11)
+        P = np.empty_like(Q)
+        P[0::2, 0::2] = q11 + w00 * w11 / D * empty
+        P[1::2, 1::2] = q00 + w00 * w11 / D * empty
+        P[0::2, 1::2] = q10 + w01 * w10 / D * empty
+        P[1::2, 0::2] = q01 + w01 * w10 / D * empty
+    out = np.zeros((2, M + 1, M + 1), dtype)
+    out[0, R - 1, C] = P[0::2, 0::2]  # up: horizontal domino on faces (R-1, C-1), (R-1, C)
+    out[0, R, C] = P[1::2, 1::2]      # down: faces (R, C-1), (R, C)
+    out[1, R, C - 1] = P[0::2, 1::2]  # left: vertical domino on faces (R-1, C-1), (R, C-1)
+    out[1, R, C] = P[1::2, 0::2]      # right: faces (R-1, C), (R, C)
+    return out.ravel()
+
+
+def face_cover(d, p):
+    """Per face of d, the summed probabilities of its four domino positions (exactly one
+    covers it in every tiling)."""
+    M = int(np.sqrt(d.size))
+    q = np.asarray(p).reshape(2, M + 1, M + 1)
+    return q[0, :M, 1:] + q[0, :M, :M] + q[1, 1:, :M] + q[1, :M, :M]
+
+
+@pytest.mark.parametrize("a,b", [(1.0, 1.0), (1.0, 0.8), (1.0, 0.5), (0.3, 1.0)])
+def test_shuffling_probabilities_equal_kasteleyn(rt, a, b):
+    from tests.test_edge_densities import kasteleyn_edge_probs
+
+    # The difference at order 24 (a few 1e-11) is the Kasteleyn inverse's rounding, which
+    # grows with the order; a misplaced edge or weight would differ by O(1).
+    for order in (1, 2, 3, 5, 8, 13, 24):
+        d = rt.DominoTiler.AztecDiamond(order)
+        assert np.abs(shuffling_edge_probs(d, a, b) - kasteleyn_edge_probs(d, a, b)).max() < 1e-9
+
+
+@pytest.mark.parametrize("order", [128, 256])
+def test_shuffling_probabilities_hold_at_large_orders(rt, order):
+    d = rt.DominoTiler.AztecDiamond(order)
+    M = int(np.sqrt(d.size))
+    F = d.reshape(M, M) == 1
+    for a, b in ((1.0, 1.0), (1.0, 0.8)):
+        p = shuffling_edge_probs(d, a, b)
+        assert np.abs(p - shuffling_edge_probs(d, a, b, np.longdouble)).max() < 1e-12
+        assert p.min() >= 0 and p.max() <= 1 + 1e-15
+        cover = face_cover(d, p)
+        assert np.abs(cover[F] - 1).max() < 1e-12 and not cover[~F].any()
+        assert abs(p.sum() - order * (order + 1)) < 1e-9
+
+
+def test_device_exact_probabilities_reject_bad_arguments(rt):
+    lib = rt.lib()
+    out = np.zeros(2 * 12 * 12)
+    for order, a, b in ((0, 1.0, 1.0), (3, 1.0, 0.0), (3, -1.0, 1.0), (3, float("nan"), 1.0), (3, 1.0, float("inf"))):
+        assert lib.rt_domino_aztec_edge_probs(order, a, b, out.ctypes.data, out.size, None) == rt.RT_ERR_INVALID_ARGUMENT
+    assert lib.rt_domino_aztec_edge_probs(4, 1.0, 1.0, out.ctypes.data, out.size, None) == rt.RT_ERR_BUFFER_TOO_SMALL
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("a,b", [(1.0, 1.0), (1.0, 0.8), (1.0, 0.5), (0.3, 1.0), (2.0, 0.7)])
+def test_device_exact_probabilities_equal_the_restatement(rt, a, b):
+    """rt_domino_aztec_edge_probs (one launch per level on the device) against
+    shuffling_edge_probs, odd and even orders, up to one past the batched kernels' CTA size."""
+    for order in (1, 2, 3, 7, 16, 33, 100, 257):
+        d = rt.DominoTiler.AztecDiamond(order)
+        got = rt.aztec_edge_probs(order, a, b)
+        assert got.shape == shuffling_edge_probs(d, a, b).shape
+        assert np.abs(got - shuffling_edge_probs(d, a, b)).max() < 1e-12, order
+
+
+@pytest.mark.gpu
+def test_device_exact_probabilities_at_order_2048(rt):
+    """Every face of the order-2048 diamond is covered with probability 1, the probabilities
+    sum to the domino count, and the uniform ones are symmetric under the diamond's mirror."""
+    order = 2048
+    d = rt.DominoTiler.AztecDiamond(order)
+    M = int(np.sqrt(d.size))
+    F = d.reshape(M, M) == 1
+    for a, b in ((1.0, 1.0), (1.0, 0.5)):
+        p = rt.aztec_edge_probs(order, a, b)
+        assert p.min() >= 0 and p.max() <= 1 + 1e-12
+        cover = face_cover(d, p)
+        assert np.abs(cover[F] - 1).max() < 1e-10 and not cover[~F].any()
+        assert abs(p.sum() - order * (order + 1)) < 1e-6 * order
+    q = rt.aztec_edge_probs(order, 1.0, 1.0).reshape(2, M + 1, M + 1)
+    # the diamond's faces fill columns 2 .. M - 3: the left-right mirror takes a vertical
+    # domino in face column C to face column M - 2 - C
+    assert np.abs(q[1][:, :M - 1] - q[1][:, M - 2::-1]).max() < 1e-12
+
+
 @pytest.mark.parametrize("order", [6, 20])
 def test_height_path_formula_equals_tiling_to_heightfunc(rt, order):
     D = rt.DominoTiler
@@ -118,16 +259,31 @@ def test_exact_values_are_exact_at_the_tested_sizes(rt):
 @pytest.mark.parametrize("order,rule,a,b", [(32, "cftp", 1.0, 1.0), (32, "cftp_twoperiodic", 1.0, 0.8),
                                             (44, "cftp", 1.0, 1.0), (44, "cftp_twoperiodic", 1.0, 0.8)])
 def test_cftp_edges_and_mean_height_match_exact_values(rt, order, rule, a, b):
+    d = rt.DominoTiler.AztecDiamond(order)
+    check_domino_cftp_samples(rt, d, order, rule, a, b, 8000, kasteleyn_edge_probs(d, a, b))
+
+
+@pytest.mark.gpu
+@pytest.mark.skipif(not os.environ.get("RT_LONG_TESTS"), reason="long test: set RT_LONG_TESTS=1")
+@pytest.mark.parametrize("order,rule,a,b", [(128, "cftp", 1.0, 1.0), (128, "cftp_twoperiodic", 1.0, 0.8)])
+def test_cftp_edges_and_mean_height_match_exact_values_at_order_128(rt, order, rule, a, b):
+    """2000 exact samples of the order-128 diamond (66 k domino positions) against the
+    shuffling probabilities.  The coupled chains coalesce after 131 K - 524 K half-sweeps of
+    look-back here, so each case takes minutes of the whole GPU."""
+    d = rt.DominoTiler.AztecDiamond(order)
+    check_domino_cftp_samples(rt, d, order, rule, a, b, 2000, shuffling_edge_probs(d, a, b))
+
+
+def check_domino_cftp_samples(rt, d, order, rule, a, b, samples, p):
+    """Batched CFTP samples of the Aztec diamond d against its exact placement probabilities
+    p: every edge frequency, and every vertex's mean height."""
     D = rt.DominoTiler
-    samples = 8000
-    d = D.AztecDiamond(order)
     tmax, tmin = D.MaxTiling(d), D.MinTiling(d)
     n = rt.side_of(tmax)
     jobs = [{"model": "domino", "tmax": tmax, "tmin": tmin, "seed": 31000 + 100000 * order + k, "stream": k,
              "rule": rule, "a": a, "b": b, "first_steps": 64, "max_attempts": 16} for k in range(samples)]
     outs, attempts, _ = rt.cftp_batch(jobs)
     assert min(attempts) > 0
-    p = kasteleyn_edge_probs(d, a, b)
     counts = np.zeros(2 * n * n, np.uint32)
     hsum = np.zeros((n, n))
     hsq = np.zeros((n, n))
