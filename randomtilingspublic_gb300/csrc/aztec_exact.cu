@@ -84,8 +84,6 @@ __global__ void k_shuffle_layout(const double* __restrict__ P, double* __restric
   out[NN + (size_t)R * N + C] = row1[0];      // right: faces (R-1, C), (R, C)
 }
 
-}  // namespace
-
 // The per-level up + down pair ratios for order n and weights a / b (host; n tiles of 4 x 4).
 std::vector<LevelRatio> aztec_level_ratios(int n, double a, double b) {
   std::vector<LevelRatio> out((size_t)n);
@@ -125,6 +123,7 @@ std::vector<LevelRatio> aztec_level_ratios(int n, double a, double b) {
   return out;
 }
 
+}  // namespace
 }  // namespace rt
 
 using namespace rt;
