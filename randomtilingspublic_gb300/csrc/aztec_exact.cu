@@ -17,12 +17,14 @@
 // both steps keep, so each level is one 4 x 4 tile, computed on the host.
 //
 // Probabilities go up, the way the shuffling grows a tiling: a domino of the order k-1
-// tiling slides across its cell to the opposite position, and a cell that nothing slides into
-// (probability 1 minus its four order k-1 probabilities, zero outside the smaller array) is
-// filled by a pair, up and down with probability w00 w11 / D, left and right w01 w10 / D.  One
-// launch per level, one thread per cell, double precision.  Every term is positive but the
-// one complement, so the values keep their accuracy at any order (the Kasteleyn inverse, the
-// other exact method, loses all its digits beyond order ~50).
+// tiling slides across its cell to the opposite position, and the cell's complement (1 minus
+// its four order k-1 probabilities, zero outside the smaller array) is filled by a pair, up
+// and down in the proportion w00 w11 / D, left and right w01 w10 / D.  The complement is not a
+// probability: a cell holding two dominoes (which the shuffling removes) counts twice, so it
+// is negative where that is common, and only the final values are clamped at 0 (against
+// rounding).  One launch per level, one thread per cell, double precision.  The values keep
+// their accuracy at any order (the Kasteleyn inverse, the other exact method, loses all its
+// digits beyond order ~50).
 #include <cuda_runtime.h>
 
 #include <cmath>
@@ -55,8 +57,8 @@ __global__ void k_shuffle_level(const double* __restrict__ prev, double* __restr
       const int I = 2 * i + dx - 1, J = 2 * j + dy - 1;
       q[dx][dy] = (I >= 0 && J >= 0 && I < Wp && J < Wp) ? prev[(size_t)I * Wp + J] : 0.0;
     }
-  // the complement is >= 0; rounding can leave it at -1e-16 where a cell is always filled
-  const double empty = fmax(0.0, 1.0 - (q[0][0] + q[0][1] + q[1][0] + q[1][1]));
+  // negative where the order k-1 tiling often holds two dominoes in the cell
+  const double empty = 1.0 - (q[0][0] + q[0][1] + q[1][0] + q[1][1]);
   const double h = ratio[k - 1].h[i & 1][j & 1];
   const double ph = h * empty, pv = (1.0 - h) * empty;
   double* row0 = cur + (size_t)(2 * i) * W + 2 * j;
@@ -78,10 +80,10 @@ __global__ void k_shuffle_layout(const double* __restrict__ P, double* __restric
   const double* row0 = P + (size_t)(2 * i) * W + 2 * j;
   const double* row1 = row0 + W;
   const size_t NN = (size_t)N * N;
-  out[(size_t)(R - 1) * N + C] = row0[0];    // up: horizontal domino on faces (R-1, C-1), (R-1, C)
-  out[(size_t)R * N + C] = row1[1];          // down: faces (R, C-1), (R, C)
-  out[NN + (size_t)R * N + C - 1] = row0[1];  // left: vertical domino on faces (R-1, C-1), (R, C-1)
-  out[NN + (size_t)R * N + C] = row1[0];      // right: faces (R-1, C), (R, C)
+  out[(size_t)(R - 1) * N + C] = fmax(0.0, row0[0]);    // up: horizontal domino on faces (R-1, C-1), (R-1, C)
+  out[(size_t)R * N + C] = fmax(0.0, row1[1]);          // down: faces (R, C-1), (R, C)
+  out[NN + (size_t)R * N + C - 1] = fmax(0.0, row0[1]);  // left: vertical domino on faces (R-1, C-1), (R, C-1)
+  out[NN + (size_t)R * N + C] = fmax(0.0, row1[0]);      // right: faces (R-1, C), (R, C)
 }
 
 // The per-level up + down pair ratios for order n and weights a / b (host; n tiles of 4 x 4).

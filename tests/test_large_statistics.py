@@ -100,12 +100,13 @@ def shuffling_edge_probs(d, a, b, dtype=np.float64):
     opposite's weight over D = w00 w11 + w01 w10; dropping the array's outer rows and columns
     leaves the weights of the order n-1 diamond, whose cells are the other parity of points.
     Probabilities go back up the way the shuffling builds a tiling: a domino of the order
-    k-1 tiling slides across its cell to the opposite edge, and a cell that nothing slides
-    into (probability 1 minus its four order k-1 probabilities, the array padded by zeros) is
-    filled by a pair, up and down with probability w00 w11 / D, left and right w01 w10 / D.
-    Every term is positive but the one complement, so the values stay accurate at any order
-    (at order 256 double and extended precision agree to 1e-14), where the Kasteleyn inverse
-    loses all digits beyond order 48."""
+    k-1 tiling slides across its cell to the opposite edge, and the cell's complement (1 minus
+    its four order k-1 probabilities, the array padded by zeros) is filled by a pair, up and
+    down in the proportion w00 w11 / D, left and right w01 w10 / D.  The complement is not a
+    probability (a cell holding two dominoes, which the shuffling removes, counts twice; it
+    is negative for two-periodic weights), but the values stay accurate at any order (at order
+    256 double and extended precision agree to 1e-14), where the Kasteleyn inverse loses all
+    digits beyond order 48."""
     M = int(np.sqrt(d.size))
     F = np.asarray(d).reshape(M, M)
     rows = np.flatnonzero(F.any(axis=1))
