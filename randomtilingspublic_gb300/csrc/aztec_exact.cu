@@ -150,17 +150,17 @@ RT_API rt_status rt_domino_aztec_edge_probs(int32_t order, double a, double b, d
   const size_t side = (size_t)2 * n;
   double *d_p0 = nullptr, *d_p1 = nullptr, *d_out = nullptr;
   LevelRatio* d_ratio = nullptr;
+  // stream-ordered blocks of the library's pool, freed on the stream after the last use
   auto cleanup = [&]() {
-    for (void* p : {(void*)d_p0, (void*)d_p1, (void*)d_out, (void*)d_ratio})
-      if (p) cudaFree(p);
+    for (void* p : {(void*)d_p0, (void*)d_p1, (void*)d_out, (void*)d_ratio}) dev_free(p, st);
   };
-  if (cudaMalloc(&d_p0, side * side * sizeof(double)) != cudaSuccess ||
-      cudaMalloc(&d_p1, side * side * sizeof(double)) != cudaSuccess ||
-      cudaMalloc(&d_out, outn * sizeof(double)) != cudaSuccess ||
-      cudaMalloc(&d_ratio, ratio.size() * sizeof(LevelRatio)) != cudaSuccess) {
-    cudaGetLastError();
+  rt_status as = dev_alloc(&d_p0, side * side * sizeof(double), st);
+  if (as == RT_OK) as = dev_alloc(&d_p1, side * side * sizeof(double), st);
+  if (as == RT_OK) as = dev_alloc(&d_out, outn * sizeof(double), st);
+  if (as == RT_OK) as = dev_alloc(&d_ratio, ratio.size() * sizeof(LevelRatio), st);
+  if (as != RT_OK) {
     cleanup();
-    return fail(RT_ERR_OUT_OF_MEMORY, "aztec_edge_probs: device allocation failed");
+    return as;
   }
   cudaMemcpyAsync(d_ratio, ratio.data(), ratio.size() * sizeof(LevelRatio), cudaMemcpyHostToDevice, st);
   cudaMemsetAsync(d_out, 0, outn * sizeof(double), st);
@@ -173,8 +173,8 @@ RT_API rt_status rt_domino_aztec_edge_probs(int32_t order, double a, double b, d
   k_shuffle_layout<<<(unsigned)(((int64_t)n * n + 255) / 256), 256, 0, st>>>(prev, d_out, n);
   cudaError_t e = cudaGetLastError();
   if (e == cudaSuccess) e = cudaMemcpyAsync(out, d_out, outn * sizeof(double), cudaMemcpyDeviceToHost, st);
-  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
   cleanup();
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
   if (e != cudaSuccess) return fail(RT_ERR_CUDA, std::string("aztec_edge_probs: ") + cudaGetErrorString(e));
   return RT_OK;
 }
