@@ -265,6 +265,14 @@ def test_cftp_edges_and_mean_height_match_exact_values(rt, order, rule, a, b):
 
 
 @pytest.mark.gpu
+def test_cftp_edges_and_mean_height_match_exact_values_at_order_128_short(rt):
+    """The order-128 check below with 400 uniform samples (about 25 s on one GB300): every
+    edge frequency and vertex mean height against the shuffling probabilities."""
+    d = rt.DominoTiler.AztecDiamond(128)
+    check_domino_cftp_samples(rt, d, 128, "cftp", 1.0, 1.0, 400, shuffling_edge_probs(d, 1.0, 1.0))
+
+
+@pytest.mark.gpu
 @pytest.mark.skipif(not os.environ.get("RT_LONG_TESTS"), reason="long test: set RT_LONG_TESTS=1")
 @pytest.mark.parametrize("order,rule,a,b", [(128, "cftp", 1.0, 1.0), (128, "cftp_twoperiodic", 1.0, 0.8)])
 def test_cftp_edges_and_mean_height_match_exact_values_at_order_128(rt, order, rule, a, b):
