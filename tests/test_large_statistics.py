@@ -265,6 +265,15 @@ def test_cftp_edges_and_mean_height_match_exact_values(rt, order, rule, a, b):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("order,samples", [(16, 4000), (24, 2000)])
+def test_cftp_at_the_benchmark_weights_matches_exact_values(rt, order, samples):
+    """The two-periodic rule at the benchmark's weights (a = 1, b = 0.5), whose coupled chains
+    coalesce far more slowly than at b = 0.8, against the shuffling probabilities."""
+    d = rt.DominoTiler.AztecDiamond(order)
+    check_domino_cftp_samples(rt, d, order, "cftp_twoperiodic", 1.0, 0.5, samples, shuffling_edge_probs(d, 1.0, 0.5))
+
+
+@pytest.mark.gpu
 def test_cftp_edges_and_mean_height_match_exact_values_at_order_128_short(rt):
     """The order-128 check below with 400 uniform samples (about 25 s on one GB300): every
     edge frequency and vertex mean height against the shuffling probabilities."""
@@ -323,7 +332,7 @@ def check_domino_cftp_samples(rt, d, order, rule, a, b, samples, p):
     # (a mean off by 200 / samples) has a Poisson probability far below 1e-9.
     often = known & (var * samples / 16 >= 20)
     zh = (mean[often] - mean_exact[often]) / np.sqrt(var[often] / samples)
-    assert often.sum() > 1000
+    assert often.sum() > min(1000, known.sum() // 4)
     assert np.abs(zh).max() < 5.0, float(np.abs(zh).max())
     rare = known & ~often
     assert np.abs(mean[rare] - mean_exact[rare]).max() < 200 / samples
