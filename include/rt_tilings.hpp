@@ -190,6 +190,15 @@ class DominoTiler : public TinyMTOpts {
     return h;
   }
 
+  // Not in the reference: the exact edge-placement probabilities of AztecDiamond(order) under
+  // the two-periodic weights a / b (a = b: uniform), in the layout of
+  // rt_domino_edge_indicators (2 N^2 values, N = 2 order + 6), computed on the device.
+  static std::vector<double> AztecEdgeProbabilities(int order, double a = 1.0, double b = 1.0) {
+    const size_t n = (size_t)2 * order + 6;
+    std::vector<double> p(2 * n * n);
+    check(rt_domino_aztec_edge_probs(order, a, b, p.data(), (int64_t)p.size(), nullptr));
+    return p;
+  }
 };
 
 
