@@ -274,6 +274,16 @@ def test_cftp_at_the_benchmark_weights_matches_exact_values(rt, order, samples):
 
 
 @pytest.mark.gpu
+@pytest.mark.skipif(not os.environ.get("RT_LONG_TESTS"), reason="long test: set RT_LONG_TESTS=1")
+def test_cftp_at_the_benchmark_weights_matches_exact_values_at_order_32(rt):
+    """As above at order 32 (2000 samples; the coupled chains need 2^20 - 2^22 half-sweeps of
+    look-back here, so up to 20 doublings from 64 sweeps)."""
+    d = rt.DominoTiler.AztecDiamond(32)
+    check_domino_cftp_samples(rt, d, 32, "cftp_twoperiodic", 1.0, 0.5, 2000, shuffling_edge_probs(d, 1.0, 0.5),
+                              max_attempts=20)
+
+
+@pytest.mark.gpu
 def test_cftp_edges_and_mean_height_match_exact_values_at_order_128_short(rt):
     """The order-128 check below with 400 uniform samples (about 25 s on one GB300): every
     edge frequency and vertex mean height against the shuffling probabilities."""
@@ -292,14 +302,14 @@ def test_cftp_edges_and_mean_height_match_exact_values_at_order_128(rt, order, r
     check_domino_cftp_samples(rt, d, order, rule, a, b, 2000, shuffling_edge_probs(d, a, b))
 
 
-def check_domino_cftp_samples(rt, d, order, rule, a, b, samples, p):
+def check_domino_cftp_samples(rt, d, order, rule, a, b, samples, p, max_attempts=16):
     """Batched CFTP samples of the Aztec diamond d against its exact placement probabilities
     p: every edge frequency, and every vertex's mean height."""
     D = rt.DominoTiler
     tmax, tmin = D.MaxTiling(d), D.MinTiling(d)
     n = rt.side_of(tmax)
     jobs = [{"model": "domino", "tmax": tmax, "tmin": tmin, "seed": 31000 + 100000 * order + k, "stream": k,
-             "rule": rule, "a": a, "b": b, "first_steps": 64, "max_attempts": 16} for k in range(samples)]
+             "rule": rule, "a": a, "b": b, "first_steps": 64, "max_attempts": max_attempts} for k in range(samples)]
     outs, attempts, _ = rt.cftp_batch(jobs)
     assert min(attempts) > 0
     counts = np.zeros(2 * n * n, np.uint32)
